@@ -1,0 +1,212 @@
+"""ctypes bindings of libgops.so (the C ABI in include/gops.h).
+
+The library is required: importing the operators without it raises, and there
+is no CPU fallback anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgops.so")
+
+GOPS_OK = 0
+GOPS_ERR_INVALID = 1
+GOPS_ERR_OOM = 2
+GOPS_ERR_CUDA = 3
+GOPS_ERR_TIMEOUT = 4
+GOPS_ERR_NO_DEVICE = 5
+GOPS_ERR_INTERNAL = 6
+
+_p = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_u64 = ctypes.c_uint64
+_dbl = ctypes.c_double
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("damping", _dbl), ("max_iterations", _u64), ("tolerance", _dbl)]
+
+
+class Run(ctypes.Structure):
+    _fields_ = [("iterations", _u64), ("diff_l1", _dbl), ("converged", _i32), ("reserved", _i32)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("solve_ms", _dbl), ("iterate_ms", _dbl), ("kernel_launches", _u64),
+                ("iterations", _u64), ("h2d_bytes", _u64), ("d2h_bytes", _u64)]
+
+
+# (name, restype, argtypes) for every symbol include/gops.h declares
+SIGNATURES = [
+    ("gops_abi_version", ctypes.c_int, []),
+    ("gops_ctx_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_p)]),
+    ("gops_ctx_destroy", None, [_p]),
+    ("gops_last_error", ctypes.c_char_p, [_p]),
+    ("gops_ctx_stats", ctypes.c_int, [_p, ctypes.POINTER(Stats)]),
+    ("gops_ctx_stream", _p, [_p]),
+    ("gops_config_validate", ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_char_p, ctypes.c_size_t]),
+    ("gops_weights_validate", ctypes.c_int, [_i64, _p, ctypes.c_char_p, ctypes.c_size_t]),
+    ("gops_personalization_validate", ctypes.c_int, [_i64, _i64, _p, ctypes.c_char_p, ctypes.c_size_t]),
+    ("gops_graph_upload", ctypes.c_int, [_p, _i64, _p, _p, _p, ctypes.POINTER(_p)]),
+    ("gops_graph_from_dense", ctypes.c_int, [_p, _i64, _p, ctypes.POINTER(_p)]),
+    ("gops_graph_destroy", None, [_p]),
+    ("gops_graph_info", ctypes.c_int, [_p, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i32)]),
+    ("gops_pagerank_run", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, ctypes.POINTER(Run)]),
+    ("gops_pagerank_weighted_run", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, ctypes.POINTER(Run)]),
+    ("gops_personalized_pagerank_run", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, _p, ctypes.POINTER(Run)]),
+    ("gops_ctx_scores_device", _p, [_p]),
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """The loaded libgops.so; raises when it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: the CUDA library must be built "
+                "(python -c 'import __graft_entry__ as g; g.build()')")
+        l = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class GopsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libgops error {code}: {msg}")
+        self.code = code
+
+
+class Context:
+    """A gops_ctx: one CUDA device, one stream.  Use from one thread at a time."""
+
+    def __init__(self, device: int = 0):
+        self._l = lib()
+        h = _p()
+        rc = self._l.gops_ctx_create(device, ctypes.byref(h))
+        if rc != GOPS_OK:
+            raise GopsError(rc, "gops_ctx_create failed (no usable CUDA device?)")
+        self.handle = h
+        self.device = device
+
+    def check(self, rc):
+        if rc != GOPS_OK:
+            raise GopsError(rc, self._l.gops_last_error(self.handle).decode())
+
+    def stats(self) -> Stats:
+        s = Stats()
+        self.check(self._l.gops_ctx_stats(self.handle, ctypes.byref(s)))
+        return s
+
+    def stream(self) -> int:
+        return self._l.gops_ctx_stream(self.handle) or 0
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._l.gops_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_tls = threading.local()
+
+
+def default_context() -> Context:
+    """A lazily created context per host thread on device 0."""
+    c = getattr(_tls, "ctx", None)
+    if c is None:
+        c = Context(int(os.environ.get("GOPS_DEVICE", "0")))
+        _tls.ctx = c
+    return c
+
+
+class DeviceGraph:
+    """A graph resident on the device (a gops_graph)."""
+
+    def __init__(self, ctx: Context, handle, n: int, m: int, weighted: bool):
+        self.ctx, self.handle, self.n, self.m, self.weighted = ctx, handle, n, m, weighted
+
+    @classmethod
+    def from_csr(cls, row_ptr, col, weights=None, ctx: Context | None = None):
+        ctx = ctx or default_context()
+        row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+        col = np.ascontiguousarray(col, dtype=np.int32)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        n = int(row_ptr.shape[0]) - 1
+        if w is not None and w.shape[0] != col.shape[0]:
+            raise ValueError("weights and col differ in length")
+        h = _p()
+        ctx.check(ctx._l.gops_graph_upload(ctx.handle, n, ptr(row_ptr), ptr(col), ptr(w), ctypes.byref(h)))
+        return cls(ctx, h, n, int(col.shape[0]), w is not None)
+
+    @classmethod
+    def from_dense(cls, matrix, ctx: Context | None = None):
+        ctx = ctx or default_context()
+        M = np.ascontiguousarray(matrix, dtype=np.float64)
+        n = int(M.shape[0]) if M.ndim == 2 else 0
+        if M.ndim != 2 or M.shape[0] != M.shape[1]:
+            raise ValueError("adjacency matrix must be square")
+        h = _p()
+        ctx.check(ctx._l.gops_graph_from_dense(ctx.handle, n, ptr(M), ctypes.byref(h)))
+        nn, mm, ww = _i64(), _i64(), _i32()
+        ctx._l.gops_graph_info(h, ctypes.byref(nn), ctypes.byref(mm), ctypes.byref(ww))
+        return cls(ctx, h, nn.value, mm.value, bool(ww.value))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.ctx._l.gops_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _solve(self, fn_name, cfg, p=None, out=True):
+        c = Config(float(cfg.damping), int(cfg.max_iterations), float(cfg.tolerance))
+        r = Run()
+        scores = np.empty(self.n, dtype=np.float64) if out else None
+        fn = getattr(self.ctx._l, fn_name)
+        if p is None:
+            rc = fn(self.ctx.handle, self.handle, ctypes.byref(c), ptr(scores), ctypes.byref(r))
+        else:
+            pp = np.ascontiguousarray(p, dtype=np.float64)
+            rc = fn(self.ctx.handle, self.handle, ctypes.byref(c), ptr(pp), ptr(scores), ctypes.byref(r))
+        self.ctx.check(rc)
+        return scores, int(r.iterations), float(r.diff_l1), bool(r.converged)
+
+    def pagerank_run(self, cfg, out=True):
+        return self._solve("gops_pagerank_run", cfg, out=out)
+
+    def pagerank_weighted_run(self, cfg, out=True):
+        return self._solve("gops_pagerank_weighted_run", cfg, out=out)
+
+    def personalized_pagerank_run(self, cfg, p, out=True):
+        return self._solve("gops_personalized_pagerank_run", cfg, p=p, out=out)

@@ -1,0 +1,292 @@
+// The extern "C" entry points declared in include/gops.h.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "objects.cuh"
+
+namespace gops {
+Status solve(Ctx *ctx, Graph *g, const gops_config *cfg, int mode, const double *p_host,
+             double *scores_host, gops_run *run);
+Status dense_to_out_csr_device(Ctx *ctx, int64_t n, const double *d_M, int64_t **d_rp,
+                               int32_t **d_col, double **d_w, int64_t *m_out);
+}  // namespace gops
+
+using namespace gops;
+
+struct gops_ctx {
+  Ctx impl;
+};
+struct gops_graph {
+  Graph impl;
+};
+
+namespace {
+
+int write_msg(char *msg, size_t cap, const char *text) {
+  if (msg && cap) std::snprintf(msg, cap, "%s", text);
+  return GOPS_ERR_INVALID;
+}
+
+void free_graph_device(Graph &g) {
+  cudaFree(g.in_rp); cudaFree(g.in_col); cudaFree(g.in_val); cudaFree(g.deg);
+  cudaFree(g.dmask_w); cudaFree(g.items);
+  workspace_free(g.ws);
+  g.in_rp = nullptr; g.in_col = nullptr; g.in_val = nullptr; g.deg = nullptr;
+  g.dmask_w = nullptr; g.items = nullptr;
+}
+
+Status check_csr_host(int64_t n, const int64_t *row_ptr, const int32_t *col) {
+  if (n < 0 || n >= INT32_MAX) return Status{GOPS_ERR_INVALID, "node count out of range"};
+  if (!row_ptr) return Status{GOPS_ERR_INVALID, "row_ptr is NULL"};
+  if (row_ptr[0] != 0) return Status{GOPS_ERR_INVALID, "row_ptr[0] must be 0"};
+  for (int64_t u = 0; u < n; ++u)
+    if (row_ptr[u + 1] < row_ptr[u]) return Status{GOPS_ERR_INVALID, "row_ptr must be non-decreasing"};
+  const int64_t m = row_ptr[n];
+  if (m >= INT32_MAX) return Status{GOPS_ERR_INVALID, "edge count out of range"};
+  if (m > 0 && !col) return Status{GOPS_ERR_INVALID, "col is NULL"};
+  for (int64_t e = 0; e < m; ++e)
+    if (col[e] < 0 || col[e] >= n) return Status{GOPS_ERR_INVALID, "neighbor index out of range"};
+  return Status::ok();
+}
+
+Status upload_impl(Ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *col,
+                   const double *w, Graph *g) {
+  GOPS_TRY(check_csr_host(n, row_ptr, col));
+  const int64_t m = row_ptr[n];
+  g->n = n;
+  g->m = m;
+  cudaStream_t s = ctx->stream;
+  int64_t *d_rp = nullptr;
+  int32_t *d_col = nullptr;
+  double *d_w = nullptr;
+  Status st;
+  auto fail = [&](cudaError_t e, const char *what) {
+    return Status{e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA,
+                  std::string(what) + ": " + cudaGetErrorString(e)};
+  };
+  cudaError_t e = cudaMallocAsync((void **)&d_rp, sizeof(int64_t) * (n + 1), s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&d_col, sizeof(int32_t) * (m > 0 ? m : 1), s);
+  if (e == cudaSuccess && w) e = cudaMallocAsync((void **)&d_w, sizeof(double) * (m > 0 ? m : 1), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_rp, row_ptr, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(d_col, col, sizeof(int32_t) * m, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && w && m > 0) e = cudaMemcpyAsync(d_w, w, sizeof(double) * m, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) st = fail(e, "graph upload");
+  else {
+    ctx->stats.h2d_bytes += sizeof(int64_t) * (n + 1) + sizeof(int32_t) * m + (w ? sizeof(double) * m : 0);
+    st = graph_build_from_out_csr_device(ctx, g, d_rp, d_col, d_w);
+  }
+  free_async(d_rp, s);
+  free_async(d_col, s);
+  free_async(d_w, s);
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  if (st.code == GOPS_OK && e2 != cudaSuccess) st = fail(e2, "graph upload");
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gops_abi_version(void) { return GOPS_ABI_VERSION; }
+
+int gops_ctx_create(int device, gops_ctx **out) {
+  if (!out) return GOPS_ERR_INVALID;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return GOPS_ERR_NO_DEVICE;
+  if (device < 0 || device >= count) return GOPS_ERR_INVALID;
+  gops_ctx *c = new (std::nothrow) gops_ctx();
+  if (!c) return GOPS_ERR_OOM;
+  Ctx &x = c->impl;
+  x.device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&x.num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&x.host_state, sizeof(SolveState));
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&x.ev[i]);
+  if (e != cudaSuccess) {
+    gops_ctx_destroy(c);
+    return e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA;
+  }
+  *out = c;
+  return GOPS_OK;
+}
+
+void gops_ctx_destroy(gops_ctx *ctx) {
+  if (!ctx) return;
+  Ctx &x = ctx->impl;
+  cudaSetDevice(x.device);
+  if (x.stream) cudaStreamSynchronize(x.stream);
+  for (int i = 0; i < 4; ++i)
+    if (x.ev[i]) cudaEventDestroy(x.ev[i]);
+  if (x.host_state) cudaFreeHost(x.host_state);
+  if (x.stream) cudaStreamDestroy(x.stream);
+  delete ctx;
+}
+
+const char *gops_last_error(const gops_ctx *ctx) {
+  return ctx ? ctx->impl.last_error.c_str() : "null context";
+}
+
+int gops_ctx_stats(const gops_ctx *ctx, gops_stats *out) {
+  if (!ctx || !out) return GOPS_ERR_INVALID;
+  *out = ctx->impl.stats;
+  return GOPS_OK;
+}
+
+void *gops_ctx_stream(gops_ctx *ctx) { return ctx ? (void *)ctx->impl.stream : nullptr; }
+
+int gops_config_validate(const gops_config *cfg, char *msg, size_t cap) {
+  if (!cfg) return write_msg(msg, cap, "config is NULL");
+  if (!std::isfinite(cfg->damping)) return write_msg(msg, cap, "damping must be finite");
+  if (!(cfg->damping >= 0.0 && cfg->damping <= 1.0)) return write_msg(msg, cap, "damping must be in [0,1]");
+  if (cfg->max_iterations == 0) return write_msg(msg, cap, "max_iterations must be > 0");
+  if (!std::isfinite(cfg->tolerance) || cfg->tolerance <= 0.0)
+    return write_msg(msg, cap, "tolerance must be finite and > 0");
+  return GOPS_OK;
+}
+
+int gops_weights_validate(int64_t m, const double *w, char *msg, size_t cap) {
+  for (int64_t e = 0; e < m; ++e) {
+    if (!std::isfinite(w[e])) return write_msg(msg, cap, "edge weights must be finite");
+    if (w[e] < 0.0) return write_msg(msg, cap, "edge weights must be non-negative");
+  }
+  return GOPS_OK;
+}
+
+int gops_personalization_validate(int64_t node_count, int64_t len, const double *p, char *msg,
+                                  size_t cap) {
+  if (len != node_count) {
+    char buf[160];
+    std::snprintf(buf, sizeof buf,
+                  "personalization length must equal node_count (len=%lld node_count=%lld)",
+                  (long long)len, (long long)node_count);
+    return write_msg(msg, cap, buf);
+  }
+  for (int64_t i = 0; i < len; ++i) {
+    if (!std::isfinite(p[i])) return write_msg(msg, cap, "personalization entries must be finite");
+    if (p[i] < 0.0) return write_msg(msg, cap, "personalization entries must be non-negative");
+  }
+  double s = 0.0;
+  for (int64_t i = 0; i < len; ++i) s += p[i];
+  if (s <= 0.0) return write_msg(msg, cap, "personalization sum must be > 0");
+  return GOPS_OK;
+}
+
+int gops_graph_upload(gops_ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *col,
+                      const double *weights, gops_graph **out) {
+  if (!ctx || !out) return GOPS_ERR_INVALID;
+  *out = nullptr;
+  Ctx &c = ctx->impl;
+  cudaSetDevice(c.device);
+  c.stats = gops_stats{};
+  gops_graph *g = new (std::nothrow) gops_graph();
+  if (!g) return c.set(Status{GOPS_ERR_OOM, "host allocation failed"});
+  g->impl.ctx = &c;
+  Status st = upload_impl(&c, n, row_ptr, col, weights, &g->impl);
+  if (st.code != GOPS_OK) {
+    free_graph_device(g->impl);
+    delete g;
+    return c.set(st);
+  }
+  *out = g;
+  return GOPS_OK;
+}
+
+int gops_graph_from_dense(gops_ctx *ctx, int64_t n, const double *matrix, gops_graph **out) {
+  if (!ctx || !out) return GOPS_ERR_INVALID;
+  *out = nullptr;
+  Ctx &c = ctx->impl;
+  cudaSetDevice(c.device);
+  c.stats = gops_stats{};
+  if (n < 0 || n >= 46341) return c.set(Status{GOPS_ERR_INVALID, "dense matrix too large"});
+  if (n > 0 && !matrix) return c.set(Status{GOPS_ERR_INVALID, "matrix is NULL"});
+  gops_graph *g = new (std::nothrow) gops_graph();
+  if (!g) return c.set(Status{GOPS_ERR_OOM, "host allocation failed"});
+  g->impl.ctx = &c;
+  cudaStream_t s = c.stream;
+  double *d_M = nullptr, *d_w = nullptr;
+  int64_t *d_rp = nullptr;
+  int32_t *d_col = nullptr;
+  int64_t m = 0;
+  Status st;
+  const size_t bytes = sizeof(double) * (size_t)std::max<int64_t>(n * n, 1);
+  cudaError_t e = cudaMallocAsync((void **)&d_M, bytes, s);
+  if (e == cudaSuccess && n > 0) e = cudaMemcpyAsync(d_M, matrix, sizeof(double) * (size_t)(n * n), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) st = Status{e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA,
+                                    std::string("dense upload: ") + cudaGetErrorString(e)};
+  if (st.code == GOPS_OK) {
+    c.stats.h2d_bytes += sizeof(double) * (size_t)(n * n);
+    st = dense_to_out_csr_device(&c, n, d_M, &d_rp, &d_col, &d_w, &m);
+  }
+  if (st.code == GOPS_OK && m >= INT32_MAX) st = Status{GOPS_ERR_INVALID, "edge count out of range"};
+  if (st.code == GOPS_OK) {
+    g->impl.n = n;
+    g->impl.m = m;
+    st = graph_build_from_out_csr_device(&c, &g->impl, d_rp, d_col, d_w);
+  }
+  free_async(d_M, s);
+  free_async(d_rp, s);
+  free_async(d_col, s);
+  free_async(d_w, s);
+  cudaStreamSynchronize(s);
+  if (st.code != GOPS_OK) {
+    free_graph_device(g->impl);
+    delete g;
+    return c.set(st);
+  }
+  *out = g;
+  return GOPS_OK;
+}
+
+void gops_graph_destroy(gops_graph *g) {
+  if (!g) return;
+  if (g->impl.ctx) {
+    cudaSetDevice(g->impl.ctx->device);
+    cudaStreamSynchronize(g->impl.ctx->stream);
+  }
+  free_graph_device(g->impl);
+  delete g;
+}
+
+int gops_graph_info(const gops_graph *g, int64_t *n, int64_t *m, int32_t *weighted) {
+  if (!g) return GOPS_ERR_INVALID;
+  if (n) *n = g->impl.n;
+  if (m) *m = g->impl.m;
+  if (weighted) *weighted = g->impl.weighted ? 1 : 0;
+  return GOPS_OK;
+}
+
+static int run_common(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int mode,
+                      const double *p, double *scores, gops_run *run) {
+  if (!ctx) return GOPS_ERR_INVALID;
+  Ctx &c = ctx->impl;
+  if (!g || !cfg || !run) return c.set(Status{GOPS_ERR_INVALID, "null argument"});
+  if (g->impl.ctx != &c) return c.set(Status{GOPS_ERR_INVALID, "graph belongs to another context"});
+  if (mode == 2 && g->impl.n > 0 && !p) return c.set(Status{GOPS_ERR_INVALID, "personalization is NULL"});
+  cudaSetDevice(c.device);
+  return c.set(solve(&c, const_cast<Graph *>(&g->impl), cfg, mode, p, scores, run));
+}
+
+int gops_pagerank_run(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, double *scores,
+                      gops_run *run) {
+  return run_common(ctx, g, cfg, 0, nullptr, scores, run);
+}
+
+int gops_pagerank_weighted_run(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg,
+                               double *scores, gops_run *run) {
+  return run_common(ctx, g, cfg, 1, nullptr, scores, run);
+}
+
+int gops_personalized_pagerank_run(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg,
+                                   const double *personalization, double *scores, gops_run *run) {
+  return run_common(ctx, g, cfg, 2, personalization, scores, run);
+}
+
+const double *gops_ctx_scores_device(const gops_ctx *ctx) {
+  return ctx ? ctx->impl.last_scores : nullptr;
+}
+
+}  // extern "C"

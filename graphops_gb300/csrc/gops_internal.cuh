@@ -1,0 +1,141 @@
+// Internal helpers shared by the libgops CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "gops.h"
+
+namespace gops {
+
+constexpr int kWarp = 32;
+
+// ---------------------------------------------------------------------------
+// Error plumbing: every entry point returns a gops status and leaves a message
+// in the context (gops_last_error).
+// ---------------------------------------------------------------------------
+struct Status {
+  int code = GOPS_OK;
+  std::string msg;
+  static Status ok() { return {}; }
+};
+
+#define GOPS_CUDA_TRY(expr)                                                      \
+  do {                                                                           \
+    cudaError_t _e = (expr);                                                     \
+    if (_e != cudaSuccess) {                                                     \
+      return ::gops::Status{_e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM       \
+                                                            : GOPS_ERR_CUDA,     \
+                            std::string(#expr) + ": " + cudaGetErrorString(_e)}; \
+    }                                                                            \
+  } while (0)
+
+#define GOPS_TRY(expr)                  \
+  do {                                  \
+    ::gops::Status _s = (expr);         \
+    if (_s.code != GOPS_OK) return _s;  \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Double-float ("DF") arithmetic: a value is hi + lo with two FP32 words,
+// about 48 significant bits, using only FP32 instructions (GB300 runs FP64 at
+// a small fraction of its FP32 rate).  Error-free transforms after Dekker
+// (1971) and Knuth (TAOCP vol. 2, 4.2.2): TwoSum, FastTwoSum, and TwoProd via
+// fused multiply-add.
+// ---------------------------------------------------------------------------
+struct df {
+  float hi, lo;
+};
+
+__device__ __forceinline__ df df_make(float h) { return {h, 0.0f}; }
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+
+__device__ __forceinline__ df fast_two_sum(float a, float b) {  // |a| >= |b|
+  float s = __fadd_rn(a, b);
+  float e = __fsub_rn(b, __fsub_rn(s, a));
+  return {s, e};
+}
+
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, e);
+}
+
+__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
+
+__device__ __forceinline__ df df_mul_f(df a, float b) {
+  float p = __fmul_rn(a.hi, b);
+  float e = __fmaf_rn(a.hi, b, -p);
+  e = __fmaf_rn(a.lo, b, e);
+  return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ df df_mul(df a, df b) {
+  float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+
+// a / b for an FP32 divisor (exact remainder through fma).
+__device__ __forceinline__ df df_div_f(df a, float b) {
+  float q = __fdiv_rn(a.hi, b);
+  float r = __fmaf_rn(-q, b, a.hi);
+  r = __fadd_rn(r, a.lo);
+  float q2 = __fdiv_rn(r, b);
+  return fast_two_sum(q, q2);
+}
+
+__host__ __device__ inline df df_from_double(double x) {
+  float h = (float)x;
+  float l = (float)(x - (double)h);
+  return {h, l};
+}
+
+__device__ __forceinline__ df shfl_xor_df(df v, int lane_mask, int width) {
+  v.hi = __shfl_xor_sync(0xffffffffu, v.hi, lane_mask, width);
+  v.lo = __shfl_xor_sync(0xffffffffu, v.lo, lane_mask, width);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Exact global sums in 64-bit fixed point.  A term x contributes
+// round(x * 2^F); integer addition is associative, so per-thread, per-block
+// and atomic accumulation give the same total in any order (deterministic),
+// and the total is exact for the rounded terms.  F is chosen per solve so
+// that every partial stays below 2^62 in magnitude.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long fx_of(float x, float scale) {
+  return __float2ll_rn(__fmul_rn(x, scale));  // power-of-two scale: exact product
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int warp_or(int v) {
+  return __reduce_or_sync(0xffffffffu, (unsigned)v);
+}
+
+// Stream-ordered free that tolerates NULL (cudaFreeAsync(NULL) is not a no-op).
+inline void free_async(void *p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+template <typename T>
+__host__ __device__ inline T ceil_div(T a, T b) {
+  return (a + b - 1) / b;
+}
+
+}  // namespace gops

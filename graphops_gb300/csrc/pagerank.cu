@@ -1,0 +1,529 @@
+// PageRank / personalized-PageRank power iteration on the in-edge CSR.
+//
+// The reference iterates x_{k+1} = F(x_k) in FP64 and stops at the first k
+// with ||x_k - x_{k-1}||_1 < tol (src/pagerank.rs:142-180, src/ppr.rs:117-149).
+// F is affine, F(x) = c + A x with
+//     A x = d * (P^T x + (sum_{u dangling} x_u) * red),
+// red = 1/n (uniform, src/pagerank.rs:150) or p (src/ppr.rs:125-128), and
+// c = (1-d) * red.  So the step r_k = x_k - x_{k-1} obeys r_{k+1} = A r_k, and
+// the library iterates on r (the "residual form"):
+//   k = 1:  r_1 = F(x_0) - x_0              (x_0 = red)
+//   k > 1:  r_k = A r_{k-1}
+//   x_k = x_0 + r_1 + ... + r_k,  diff_k = ||r_k||_1 (the reference's diff_l1)
+// Each step is one pull kernel over the in-edge CSR (K3): every row v gathers
+// the previous step's vector at its in-neighbours, and the same kernel fuses
+// the dangling sum, the L1 norm (K4) and the accumulation of x.
+//
+// Precision.  While ||r||_1 >= theta (first few steps) the gathered vector and
+// all arithmetic are double-float (two FP32 words, ~48 bits); afterwards the
+// gathered vector is FP32 and the steps are summed into an FP32 tail.  x is
+// then acc (double-float) + tail, formed in FP64 at the end.  The global sums
+// (dangling mass, L1 norm) are exact 64-bit fixed-point integer sums, so they
+// are independent of summation order and bit-reproducible.
+//
+// Convergence is decided on the device: the kernel for step k first reads
+// diff_{k-1}; if it is below tol (or k-1 == max_iterations) it records the
+// run and every block returns, so the host may launch steps ahead.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "objects.cuh"
+
+namespace gops {
+
+enum Mode : int { kPlain = 0, kWeighted = 1, kPpr = 2 };
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / kWarp;
+constexpr int kRowCapIter = 256;  // must match kRowCap of the item builder
+constexpr double kTheta = 1e-2;   // double-float phase while ||r||_1 >= kTheta
+
+struct IterParams {
+  int64_t n;
+  const int64_t *rp;
+  const int32_t *col;
+  const float *val;
+  const float *deg;
+  const uint32_t *dmask;
+  const Item *items;
+  int n_items;
+  int cap;  // stage capacity in edges (2W)
+  const float2 *gdf_in;
+  float2 *gdf_out;
+  const float *gf_in;
+  float *gf_out;
+  float2 *acc;
+  float *tail;
+  const float2 *pdf;
+  long long *sums;
+  SolveState *st;
+  float2 *lpart;
+  unsigned *lcnt;
+  df d, omd, inv_n;
+  float fx_scale;
+  double fx_inv;
+  double tol, theta;
+  unsigned long long k, max_iter;
+};
+
+// --------------------------------------------------------------------------
+// precision policies
+// --------------------------------------------------------------------------
+struct PrecDF {
+  using T = df;
+  static constexpr bool kDF = true;
+  __device__ static T zero() { return {0.0f, 0.0f}; }
+  __device__ static T add(T a, T b) { return df_add(a, b); }
+  __device__ static T shfl(T v, int m) { return shfl_xor_df(v, m, 32); }
+  __device__ static T load_g(const IterParams &p, int32_t u) {
+    float2 g = __ldg(&p.gdf_in[u]);
+    return {g.x, g.y};
+  }
+  __device__ static T scale(T g, float w) { return df_mul_f(g, w); }
+  __device__ static float2 pack(T v) { return make_float2(v.hi, v.lo); }
+  __device__ static T unpack(float2 v) { return {v.x, v.y}; }
+};
+
+struct PrecF32 {
+  using T = float;
+  static constexpr bool kDF = false;
+  __device__ static T zero() { return 0.0f; }
+  __device__ static T add(T a, T b) { return a + b; }
+  __device__ static T shfl(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+  __device__ static T load_g(const IterParams &p, int32_t u) { return __ldg(&p.gf_in[u]); }
+  __device__ static T scale(T g, float w) { return g * w; }
+  __device__ static float2 pack(T v) { return make_float2(v, 0.0f); }
+  __device__ static T unpack(float2 v) { return v.x; }
+};
+
+__device__ __forceinline__ bool dangling(const IterParams &p, int mode, int64_t v) {
+  if (mode == kWeighted) return (__ldg(&p.dmask[v >> 5]) >> (v & 31)) & 1u;
+  return __ldg(&p.deg[v]) == 0.0f;
+}
+
+struct Acc {
+  long long l1 = 0, dang = 0;
+  int bad = 0;
+};
+
+// Row v's new step value from its gathered sum s.
+template <int MODE>
+__device__ __forceinline__ void epilogue_df(const IterParams &p, int64_t v, df s, df dsum, Acc &a) {
+  const df red = (MODE == kPpr) ? PrecDF::unpack(p.pdf[v]) : p.inv_n;
+  df r = df_mul(p.d, df_add(s, df_mul(dsum, red)));
+  if (p.k == 1) r = df_add(df_add(df_mul(p.omd, red), r), df_neg(red));  // F(x_0) - x_0
+  const float2 ao = p.acc[v];
+  const df an = df_add({ao.x, ao.y}, r);
+  p.acc[v] = make_float2(an.hi, an.lo);
+  const df ar = r.hi < 0.0f ? df_neg(r) : r;
+  a.l1 += fx_of(ar.hi, p.fx_scale) + fx_of(ar.lo, p.fx_scale);
+  a.bad |= !isfinite(r.hi);
+  df g = r;
+  if (MODE != kWeighted) {
+    const float dg = __ldg(&p.deg[v]);
+    g = dg > 0.0f ? df_div_f(r, dg) : df{0.0f, 0.0f};
+    if (dg == 0.0f) a.dang += fx_of(r.hi, p.fx_scale) + fx_of(r.lo, p.fx_scale);
+  } else if (dangling(p, MODE, v)) {
+    a.dang += fx_of(r.hi, p.fx_scale) + fx_of(r.lo, p.fx_scale);
+  }
+  p.gdf_out[v] = make_float2(g.hi, g.lo);
+  p.gf_out[v] = g.hi;
+}
+
+template <int MODE>
+__device__ __forceinline__ void epilogue_f32(const IterParams &p, int64_t v, float s, float dsum,
+                                             Acc &a) {
+  const float red = (MODE == kPpr) ? p.pdf[v].x : p.inv_n.hi;
+  const float r = p.d.hi * (s + dsum * red);
+  p.tail[v] += r;
+  a.l1 += fx_of(fabsf(r), p.fx_scale);
+  a.bad |= !isfinite(r);
+  float g = r;
+  if (MODE != kWeighted) {
+    const float dg = __ldg(&p.deg[v]);
+    g = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
+    if (dg == 0.0f) a.dang += fx_of(r, p.fx_scale);
+  } else if (dangling(p, MODE, v)) {
+    a.dang += fx_of(r, p.fx_scale);
+  }
+  p.gf_out[v] = g;
+}
+
+template <class P, int MODE>
+__device__ __forceinline__ void epilogue(const IterParams &p, int64_t v, typename P::T s,
+                                         df dsum, Acc &a) {
+  if constexpr (P::kDF) epilogue_df<MODE>(p, v, s, dsum, a);
+  else epilogue_f32<MODE>(p, v, s, dsum.hi, a);
+}
+
+template <class P, int MODE>
+__device__ __forceinline__ typename P::T edge_term(const IterParams &p, int64_t e) {
+  const int32_t u = __ldg(&p.col[e]);
+  typename P::T g = P::load_g(p, u);
+  if (MODE == kWeighted) g = P::scale(g, __ldg(&p.val[e]));
+  return g;
+}
+
+// Reads diff_{k-1}; decides whether the run is over and whether this kernel's
+// precision is the active one.  Returns false when the block should exit.
+template <bool WANT_DF>
+__device__ bool prologue(const IterParams &p, df *dsum) {
+  const unsigned long long k = p.k;
+  if (*(volatile int *)&p.st->done) return false;  // recorded by an earlier step
+  const int prev = (int)((k - 1) % 3);
+  double diff = INFINITY;
+  if (k > 1) {
+    const long long raw = *(volatile long long *)&p.sums[prev * 4 + 1];
+    const long long badc = *(volatile long long *)&p.sums[prev * 4 + 2];
+    diff = badc ? NAN : (double)raw * p.fx_inv;
+  }
+  const bool conv = k > 1 && diff < p.tol;
+  if (conv || k - 1 >= p.max_iter) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      p.st->done = 1;
+      p.st->converged = conv ? 1 : 0;
+      p.st->iterations = k - 1;
+      p.st->diff_l1 = diff;
+    }
+    return false;
+  }
+  const bool f32 = k > 1 && (*(volatile int *)&p.st->f32_phase || diff < p.theta);
+  if (f32 == WANT_DF) return false;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    p.st->f32_phase = f32 ? 1 : 0;
+    const int nxt = (int)((k + 1) % 3);
+    for (int i = 0; i < 4; ++i) p.sums[nxt * 4 + i] = 0;
+  }
+  const long long draw = *(volatile long long *)&p.sums[prev * 4 + 0];
+  *dsum = df_from_double((double)draw * p.fx_inv);
+  return true;
+}
+
+template <class P, int MODE>
+__global__ void __launch_bounds__(kThreads) iterate_kernel(IterParams p) {
+  using T = typename P::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *stage = reinterpret_cast<T *>(smem_raw);
+  __shared__ int roff[kRowCapIter + 1];
+  __shared__ T rowsum[kRowCapIter];
+  __shared__ T wred[kWarps];
+  __shared__ int last_flag;
+  __shared__ long long bred[2][kWarps];
+  __shared__ int bbad[kWarps];
+
+  df dsum;
+  if (!prologue<P::kDF>(p, &dsum)) return;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  Acc a;
+
+  for (int item = blockIdx.x; item < p.n_items; item += gridDim.x) {
+    const Item it = p.items[item];
+    if (it.first < 0) {
+      // ---- a run of whole rows: stage products, reduce per row, epilogue
+      const int r0 = it.r0, nr = it.r1 - it.r0;
+      const int64_t e0 = p.rp[r0];
+      for (int i = tid; i <= nr; i += kThreads) roff[i] = (int)(p.rp[r0 + i] - e0);
+      __syncthreads();
+      const int ne = roff[nr];
+      for (int j = tid; j < ne; j += kThreads) stage[j] = edge_term<P, MODE>(p, e0 + j);
+      __syncthreads();
+      int sw = 1;
+      const int avg = nr > 0 ? (ne + nr - 1) / nr : 1;
+      while (sw < avg && sw < 32) sw <<= 1;
+      const int per_pass = kThreads / sw;
+      for (int base = 0; base < nr; base += per_pass) {
+        const int rr = base + tid / sw, li = tid & (sw - 1);
+        T s = P::zero();
+        if (rr < nr)
+          for (int j = roff[rr] + li; j < roff[rr + 1]; j += sw) s = P::add(s, stage[j]);
+        for (int o = sw >> 1; o > 0; o >>= 1) s = P::add(s, P::shfl(s, o));
+        if (rr < nr && li == 0) rowsum[rr] = s;
+      }
+      __syncthreads();
+      for (int i = tid; i < nr; i += kThreads) epilogue<P, MODE>(p, r0 + i, rowsum[i], dsum, a);
+      __syncthreads();
+    } else {
+      // ---- one chunk of a hub row; the chunk that arrives last combines
+      const int64_t v = it.r0;
+      const int c = item - it.first;
+      const int64_t cs = p.rp[v] + (int64_t)c * p.cap;
+      const int64_t ce = min(p.rp[v + 1], cs + (int64_t)p.cap);
+      T s = P::zero();
+      for (int64_t e = cs + tid; e < ce; e += kThreads) s = P::add(s, edge_term<P, MODE>(p, e));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s = P::add(s, P::shfl(s, o));
+      if (lane == 0) wred[wid] = s;
+      __syncthreads();
+      if (tid == 0) {
+        T tot = wred[0];
+        for (int w = 1; w < kWarps; ++w) tot = P::add(tot, wred[w]);
+        p.lpart[item] = P::pack(tot);
+        __threadfence();
+        const unsigned t = atomicAdd(&p.lcnt[it.first], 1u);
+        last_flag = (t == (unsigned)(it.nchunks - 1));
+        if (last_flag) {
+          __threadfence();
+          T sum = P::zero();
+          for (int j = 0; j < it.nchunks; ++j) sum = P::add(sum, P::unpack(__ldcg(&p.lpart[it.first + j])));
+          p.lcnt[it.first] = 0;
+          epilogue<P, MODE>(p, v, sum, dsum, a);
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // ---- block totals of the exact fixed-point sums -> one atomic each
+  long long l1 = warp_sum_ll(a.l1), dg = warp_sum_ll(a.dang);
+  int bad = warp_or(a.bad);
+  if (lane == 0) { bred[0][wid] = l1; bred[1][wid] = dg; bbad[wid] = bad; }
+  __syncthreads();
+  if (tid == 0) {
+    long long t1 = 0, t2 = 0;
+    int tb = 0;
+    for (int w = 0; w < kWarps; ++w) { t1 += bred[0][w]; t2 += bred[1][w]; tb |= bbad[w]; }
+    const int cur = (int)(p.k % 3);
+    atomicAdd((unsigned long long *)&p.sums[cur * 4 + 1], (unsigned long long)t1);
+    atomicAdd((unsigned long long *)&p.sums[cur * 4 + 0], (unsigned long long)t2);
+    if (tb) atomicAdd((unsigned long long *)&p.sums[cur * 4 + 2], 1ull);
+  }
+}
+
+// x_0 = red, acc = x_0, tail = 0, gathered vector for step 1, sum_dangling x_0.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) init_kernel(IterParams p) {
+  __shared__ long long bred[kWarps];
+  long long dang = 0;
+  for (int64_t v = (int64_t)blockIdx.x * kThreads + threadIdx.x; v < p.n;
+       v += (int64_t)gridDim.x * kThreads) {
+    const df red = (MODE == kPpr) ? PrecDF::unpack(p.pdf[v]) : p.inv_n;
+    p.acc[v] = make_float2(red.hi, red.lo);
+    p.tail[v] = 0.0f;
+    df g = red;
+    bool dang_v;
+    if (MODE != kWeighted) {
+      const float dg = p.deg[v];
+      dang_v = dg == 0.0f;
+      g = dang_v ? df{0.0f, 0.0f} : df_div_f(red, dg);
+    } else {
+      dang_v = (p.dmask[v >> 5] >> (v & 31)) & 1u;
+    }
+    if (dang_v) dang += fx_of(red.hi, p.fx_scale) + fx_of(red.lo, p.fx_scale);
+    p.gdf_out[v] = make_float2(g.hi, g.lo);
+    p.gf_out[v] = g.hi;
+  }
+  dang = warp_sum_ll(dang);
+  if ((threadIdx.x & 31) == 0) bred[threadIdx.x >> 5] = dang;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long t = 0;
+    for (int w = 0; w < kWarps; ++w) t += bred[w];
+    atomicAdd((unsigned long long *)&p.sums[0], (unsigned long long)t);
+  }
+}
+
+__global__ void finalize_kernel(int64_t n, const float2 *acc, const float *tail, double *x) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x)
+    x[v] = (double)acc[v].x + (double)acc[v].y + (double)tail[v];
+}
+
+// --------------------------------------------------------------------------
+// host side
+// --------------------------------------------------------------------------
+void workspace_free(Workspace &ws) {
+  cudaFree(ws.gdf[0]); cudaFree(ws.gdf[1]); cudaFree(ws.gf[0]); cudaFree(ws.gf[1]);
+  cudaFree(ws.acc); cudaFree(ws.tail); cudaFree(ws.pdf); cudaFree(ws.scores);
+  cudaFree(ws.sums); cudaFree(ws.lpart); cudaFree(ws.lcnt); cudaFree(ws.state);
+  ws = Workspace{};
+}
+
+Status workspace_ensure(Ctx *ctx, Graph *g) {
+  (void)ctx;
+  Workspace &ws = g->ws;
+  if (ws.sums) return Status::ok();
+  const size_t n = (size_t)std::max<int64_t>(g->n, 1);
+  const size_t ni = (size_t)std::max<int32_t>(g->n_items, 1);
+  GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[0], sizeof(float2) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[1], sizeof(float2) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.gf[0], sizeof(float) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.gf[1], sizeof(float) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.acc, sizeof(float2) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.tail, sizeof(float) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.pdf, sizeof(float2) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.scores, sizeof(double) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.lpart, sizeof(float2) * ni));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.lcnt, sizeof(unsigned) * ni));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.state, sizeof(SolveState)));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.sums, sizeof(long long) * 12));
+  ws.n = g->n;
+  return Status::ok();
+}
+
+namespace {
+
+template <class P, int MODE>
+int grid_for_iter(const Ctx *ctx, const Graph *g, size_t smem) {
+  int occ = 0;
+  cudaFuncSetAttribute(iterate_kernel<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, iterate_kernel<P, MODE>, kThreads, smem);
+  occ = std::max(1, occ);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g->n_items, (int64_t)ctx->num_sms * occ));
+}
+
+template <int MODE>
+Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_run *run) {
+  cudaStream_t s = ctx->stream;
+  Workspace &ws = g->ws;
+  IterParams p{};
+  p.n = g->n;
+  p.rp = g->in_rp;
+  p.col = g->in_col;
+  p.val = g->in_val;
+  p.deg = g->deg;
+  p.dmask = g->dmask_w;
+  p.items = g->items;
+  p.n_items = g->n_items;
+  p.cap = 2 * g->window;
+  p.acc = ws.acc;
+  p.tail = ws.tail;
+  p.pdf = ws.pdf;
+  p.sums = ws.sums;
+  p.st = ws.state;
+  p.lpart = ws.lpart;
+  p.lcnt = ws.lcnt;
+  p.d = df_from_double(cfg->damping);
+  p.omd = df_from_double(1.0 - cfg->damping);
+  p.inv_n = df_from_double(1.0 / (double)g->n);
+  int e = 0;
+  while (e < 20 && std::ldexp(1.0, e) < std::max(1.0, pv_l1)) ++e;
+  const int F = 58 - 2 * e;
+  p.fx_scale = std::ldexp(1.0f, F);
+  p.fx_inv = std::ldexp(1.0, -F);
+  p.tol = cfg->tolerance;
+  p.theta = kTheta;
+  p.max_iter = cfg->max_iterations;
+
+  GOPS_CUDA_TRY(cudaMemsetAsync(ws.sums, 0, sizeof(long long) * 12, s));
+  GOPS_CUDA_TRY(cudaMemsetAsync(ws.state, 0, sizeof(SolveState), s));
+  GOPS_CUDA_TRY(cudaMemsetAsync(ws.lcnt, 0, sizeof(unsigned) * std::max<int32_t>(g->n_items, 1), s));
+  GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+  uint64_t launches = 0;
+  // step 0
+  p.k = 0;
+  p.gdf_out = ws.gdf[0];
+  p.gf_out = ws.gf[0];
+  const int init_grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(g->n, kThreads),
+                                                                     (int64_t)ctx->num_sms * 8));
+  init_kernel<MODE><<<init_grid, kThreads, 0, s>>>(p);
+  GOPS_CUDA_TRY(cudaGetLastError());
+  ++launches;
+  GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+
+  const size_t smem_df = sizeof(float2) * (size_t)p.cap;
+  const size_t smem_f = sizeof(float) * (size_t)p.cap;
+  const int grid_df = grid_for_iter<PrecDF, MODE>(ctx, g, smem_df);
+  const int grid_f = grid_for_iter<PrecF32, MODE>(ctx, g, smem_f);
+  bool f32_known = false;
+  unsigned long long k = 1;
+  const int chunk = 4;
+  for (;;) {
+    for (int j = 0; j < chunk && k - 1 <= cfg->max_iterations; ++j, ++k) {
+      p.k = k;
+      p.gdf_in = ws.gdf[(k - 1) & 1];
+      p.gf_in = ws.gf[(k - 1) & 1];
+      p.gdf_out = ws.gdf[k & 1];
+      p.gf_out = ws.gf[k & 1];
+      if (!f32_known) {
+        iterate_kernel<PrecDF, MODE><<<grid_df, kThreads, smem_df, s>>>(p);
+        ++launches;
+      }
+      if (k >= 2) {
+        iterate_kernel<PrecF32, MODE><<<grid_f, kThreads, smem_f, s>>>(p);
+        ++launches;
+      }
+    }
+    GOPS_CUDA_TRY(cudaGetLastError());
+    GOPS_CUDA_TRY(cudaMemcpyAsync(ctx->host_state, ws.state, sizeof(SolveState),
+                                  cudaMemcpyDeviceToHost, s));
+    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (ctx->host_state->done) break;
+    if (ctx->host_state->f32_phase) f32_known = true;
+    if (k - 1 > cfg->max_iterations)
+      return Status{GOPS_ERR_INTERNAL, "solver did not record completion"};
+  }
+  GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
+  finalize_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(g->n, 256), 4096)),
+                    256, 0, s>>>(g->n, ws.acc, ws.tail, ws.scores);
+  GOPS_CUDA_TRY(cudaGetLastError());
+  ++launches;
+  GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
+  GOPS_CUDA_TRY(cudaEventSynchronize(ctx->ev[3]));
+  run->iterations = ctx->host_state->iterations;
+  run->diff_l1 = ctx->host_state->diff_l1;
+  run->converged = ctx->host_state->converged;
+  run->reserved = 0;
+  float t_all = 0.f, t_it = 0.f;
+  cudaEventElapsedTime(&t_all, ctx->ev[0], ctx->ev[3]);
+  cudaEventElapsedTime(&t_it, ctx->ev[1], ctx->ev[2]);
+  ctx->stats.solve_ms = t_all;
+  ctx->stats.iterate_ms = t_it;
+  ctx->stats.kernel_launches += launches;
+  ctx->stats.iterations = run->iterations;
+  return Status::ok();
+}
+
+}  // namespace
+
+// mode: 0 plain, 1 weighted, 2 personalized (p_host: n raw entries)
+Status solve(Ctx *ctx, Graph *g, const gops_config *cfg, int mode, const double *p_host,
+             double *scores_host, gops_run *run) {
+  ctx->stats = gops_stats{};
+  if (g->n == 0) {  // src/pagerank.rs:123-131, src/ppr.rs:96-103
+    run->iterations = 0;
+    run->diff_l1 = 0.0;
+    run->converged = 1;
+    run->reserved = 0;
+    return Status::ok();
+  }
+  if (mode == kWeighted && !g->weighted)
+    return Status{GOPS_ERR_INVALID, "graph was uploaded without weights"};
+  GOPS_TRY(workspace_ensure(ctx, g));
+  double pv_l1 = 1.0;
+  if (mode == kPpr) {
+    // normalisation of src/ppr.rs:104-109, sequential FP64 like the reference
+    const int64_t n = g->n;
+    double psum = 0.0;
+    for (int64_t i = 0; i < n; ++i) psum += p_host[i];
+    std::vector<float2> pdf((size_t)n);
+    pv_l1 = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+      const double v = psum > 0.0 ? p_host[i] / psum : 1.0 / (double)n;
+      pv_l1 += std::fabs(v);
+      const df d = df_from_double(v);
+      pdf[(size_t)i] = make_float2(d.hi, d.lo);
+    }
+    GOPS_CUDA_TRY(cudaMemcpyAsync(g->ws.pdf, pdf.data(), sizeof(float2) * (size_t)n,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    ctx->stats.h2d_bytes += sizeof(float2) * (size_t)n;
+    GOPS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (!std::isfinite(pv_l1)) pv_l1 = 1.0;
+  }
+  Status st;
+  if (mode == kPlain) st = run_mode<kPlain>(ctx, g, cfg, pv_l1, run);
+  else if (mode == kWeighted) st = run_mode<kWeighted>(ctx, g, cfg, pv_l1, run);
+  else st = run_mode<kPpr>(ctx, g, cfg, pv_l1, run);
+  GOPS_TRY(st);
+  ctx->last_scores = g->ws.scores;
+  if (scores_host) {
+    GOPS_CUDA_TRY(cudaMemcpyAsync(scores_host, g->ws.scores, sizeof(double) * (size_t)g->n,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    GOPS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->stats.d2h_bytes += sizeof(double) * (size_t)g->n;
+  }
+  return Status::ok();
+}
+
+}  // namespace gops

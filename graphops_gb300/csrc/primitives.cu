@@ -1,0 +1,214 @@
+// Exclusive scan and stable LSD radix sort (see primitives.cuh).
+#include "primitives.cuh"
+
+namespace gops {
+namespace {
+
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+// Block-wide exclusive scan of one value per thread; returns the block total
+// through *total.
+template <typename T>
+__device__ T block_exclusive_scan(T v, T *total) {
+  __shared__ T warp_tot[kScanThreads / kWarp];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  T incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    T w = (lane < kScanThreads / kWarp) ? warp_tot[lane] : T(0);
+    T wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < kScanThreads / kWarp) warp_tot[lane] = wi - w;  // exclusive warp offsets
+    if (lane == kScanThreads / kWarp - 1) warp_tot[kScanThreads / kWarp - 1] = wi - w, *total = wi;
+  }
+  __syncthreads();
+  T r = warp_tot[wid] + incl - v;
+  __syncthreads();
+  return r;
+}
+
+template <typename T>
+__global__ void scan_tile_sums(const T *in, int64_t n, T *tile_sums) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  T s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)
+    if (base + i < n) s += in[base + i];
+  __shared__ T tot;
+  block_exclusive_scan<T>(s, &tot);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+}
+
+template <typename T>
+__global__ void scan_tiles(const T *in, T *out, int64_t n, const T *tile_offsets) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  T v[kScanItems];
+  T s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = (base + i < n) ? in[base + i] : T(0);
+    s += v[i];
+  }
+  __shared__ T tot;
+  T run = block_exclusive_scan<T>(s, &tot) + (tile_offsets ? tile_offsets[blockIdx.x] : T(0));
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+  }
+}
+
+template <typename T>
+Status exclusive_scan(const T *in, T *out, int64_t n, cudaStream_t s) {
+  if (n <= 0) return Status::ok();
+  const int64_t tiles = ceil_div<int64_t>(n, kScanTile);
+  if (tiles == 1) {
+    scan_tiles<T><<<1, kScanThreads, 0, s>>>(in, out, n, nullptr);
+    GOPS_CUDA_TRY(cudaGetLastError());
+    return Status::ok();
+  }
+  T *sums = nullptr;
+  GOPS_CUDA_TRY(cudaMallocAsync((void **)&sums, sizeof(T) * tiles, s));
+  scan_tile_sums<T><<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, sums);
+  Status st = exclusive_scan<T>(sums, sums, tiles, s);
+  if (st.code == GOPS_OK) {
+    scan_tiles<T><<<(unsigned)tiles, kScanThreads, 0, s>>>(in, out, n, sums);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) st = Status{GOPS_ERR_CUDA, std::string("scan: ") + cudaGetErrorString(e)};
+  }
+  free_async(sums, s);
+  return st;
+}
+
+// ---------------------------------------------------------------------------
+// Radix sort: 8-bit digits, tiles of 4096 items (8 warps x 512 consecutive
+// items each).  Per pass: (1) per-tile digit histogram, (2) exclusive scan of
+// the histogram in digit-major order, (3) stable scatter.  Inside a tile the
+// rank of an item among equal digits comes from __match_any_sync within a
+// 32-item chunk plus warp-private running counters, so the order of equal keys
+// is preserved exactly.
+// ---------------------------------------------------------------------------
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / kWarp;
+constexpr int kPerWarp = 512;
+constexpr int kSortTile = kSortWarps * kPerWarp;
+constexpr int kRadix = 256;
+
+__global__ void radix_upsweep(const uint32_t *keys, int64_t n, int shift, uint32_t *hist,
+                              int64_t tiles) {
+  __shared__ uint32_t cnt[kRadix];
+  for (int i = threadIdx.x; i < kRadix; i += kSortThreads) cnt[i] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kSortTile;
+  for (int i = threadIdx.x; i < kSortTile; i += kSortThreads) {
+    int64_t idx = base + i;
+    if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & 0xFF], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < kRadix; d += kSortThreads) hist[(int64_t)d * tiles + blockIdx.x] = cnt[d];
+}
+
+__global__ void radix_downsweep(const uint32_t *keys, const uint32_t *vals, uint32_t *okeys,
+                                uint32_t *ovals, int64_t n, int shift, const uint32_t *offs,
+                                int64_t tiles) {
+  __shared__ uint32_t wcnt[kSortWarps][kRadix];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) (&wcnt[0][0])[i] = 0;
+  __syncthreads();
+  const int64_t wbase = (int64_t)blockIdx.x * kSortTile + (int64_t)w * kPerWarp;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  // (a) warp-private digit counts
+  for (int c = 0; c < kPerWarp; c += 32) {
+    int64_t idx = wbase + c + lane;
+    bool valid = idx < n;
+    unsigned dig = valid ? ((keys[idx] >> shift) & 0xFF) : 0x100u;
+    unsigned peers = __match_any_sync(0xffffffffu, dig);
+    int leader = __ffs(peers) - 1;
+    if (valid && lane == leader) wcnt[w][dig] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // (b) turn counts into global positions: tile offset for the digit plus the
+  //     counts of earlier warps of this tile
+  for (int d = threadIdx.x; d < kRadix; d += kSortThreads) {
+    uint32_t run = offs[(int64_t)d * tiles + blockIdx.x];
+    for (int ww = 0; ww < kSortWarps; ++ww) {
+      uint32_t c = wcnt[ww][d];
+      wcnt[ww][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  // (c) stable scatter
+  for (int c = 0; c < kPerWarp; c += 32) {
+    int64_t idx = wbase + c + lane;
+    bool valid = idx < n;
+    uint32_t k = valid ? keys[idx] : 0u;
+    uint32_t v = valid ? vals[idx] : 0u;
+    unsigned dig = valid ? ((k >> shift) & 0xFF) : 0x100u;
+    unsigned peers = __match_any_sync(0xffffffffu, dig);
+    int leader = __ffs(peers) - 1;
+    uint32_t pos = valid ? wcnt[w][dig] + __popc(peers & lt_mask) : 0u;
+    __syncwarp();
+    if (valid) {
+      okeys[pos] = k;
+      ovals[pos] = v;
+      if (lane == leader) wcnt[w][dig] += __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace
+
+Status exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s) {
+  return exclusive_scan<long long>((const long long *)in, (long long *)out, n, s);
+}
+
+Status exclusive_scan_u32(const uint32_t *in, uint32_t *out, int64_t n, cudaStream_t s) {
+  return exclusive_scan<uint32_t>(in, out, n, s);
+}
+
+Status radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt,
+                            uint32_t *vals_alt, int64_t n, int key_bits,
+                            bool *result_in_alt, cudaStream_t s) {
+  *result_in_alt = false;
+  if (n <= 1 || key_bits <= 0) return Status::ok();
+  if (n >= (int64_t)UINT32_MAX) return Status{GOPS_ERR_INVALID, "radix sort: too many items"};
+  const int64_t tiles = ceil_div<int64_t>(n, kSortTile);
+  uint32_t *hist = nullptr;
+  GOPS_CUDA_TRY(cudaMallocAsync((void **)&hist, sizeof(uint32_t) * tiles * kRadix, s));
+  uint32_t *k_in = keys, *v_in = vals, *k_out = keys_alt, *v_out = vals_alt;
+  Status st;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    radix_upsweep<<<(unsigned)tiles, kSortThreads, 0, s>>>(k_in, n, shift, hist, tiles);
+    st = exclusive_scan_u32(hist, hist, tiles * kRadix, s);
+    if (st.code != GOPS_OK) break;
+    radix_downsweep<<<(unsigned)tiles, kSortThreads, 0, s>>>(k_in, v_in, k_out, v_out, n, shift,
+                                                             hist, tiles);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      st = Status{GOPS_ERR_CUDA, std::string("radix sort: ") + cudaGetErrorString(e)};
+      break;
+    }
+    std::swap(k_in, k_out);
+    std::swap(v_in, v_out);
+    *result_in_alt = !*result_in_alt;
+  }
+  free_async(hist, s);
+  return st;
+}
+
+}  // namespace gops

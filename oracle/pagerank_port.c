@@ -1,0 +1,318 @@
+/*
+ * CPU restatement of graphops' PageRank / personalized-PageRank power
+ * iteration, in FP64, with the reference's loop order and summation order.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: tests, the smoke check
+ * and the CPU-baseline leg of bench.py load it to check or time against.  The
+ * product path (libgops.so) never links or calls it.
+ *
+ * Parity is pinned by the reference's own known-answer tests (invariants,
+ * doctests, the 4-node example) and by closed forms; the reference crate
+ * holds no golden vectors and cannot be built here (it is Rust; no cargo).
+ *
+ * Graph input is the out-adjacency in ADAPTER order: row u of (row_ptr, col)
+ * lists graph.neighbors(u) exactly as the reference's `Graph` adapter returns
+ * it (duplicates allowed).  For the weighted variant w[e] is the value of
+ * graph.edge_weight(u, col[e]) for that neighbor entry (raw, unclamped).
+ *
+ * Build: oracle/build_oracle.py (gcc -O2 -ffp-contract=off, so x86 and Arm
+ * give bit-identical FP64 results).
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct {
+    double damping;
+    uint64_t max_iterations;
+    double tolerance;
+} orc_config;
+
+typedef struct {
+    uint64_t iterations;
+    double diff_l1;
+    int32_t converged;
+} orc_run;
+
+/* Rust's f64::max: if one argument is NaN the other is returned; fmax has the
+ * same rule.  Used for `edge_weight(..).max(0.0)` (src/pagerank.rs:231,257). */
+static double rust_max(double a, double b) { return fmax(a, b); }
+
+/* Result of the `n == 0` early return (src/pagerank.rs:123-131). */
+static void empty_run(orc_run *r) {
+    r->iterations = 0;
+    r->diff_l1 = 0.0;
+    r->converged = 1;
+}
+
+/* Sequential L1 residual, old-new (src/pagerank.rs:169-173). */
+static double l1_seq(const double *a, const double *b, int64_t n) {
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += fabs(a[i] - b[i]);
+    return s;
+}
+
+/*
+ * pagerank_run, src/pagerank.rs:122-187.
+ * scores: caller buffer of n doubles; receives the returned (new) vector.
+ */
+int orc_pagerank_run(int64_t n, const int64_t *row_ptr, const int32_t *col,
+                     orc_config cfg, double *scores, orc_run *run) {
+    if (n == 0) { empty_run(run); return 0; }
+    const double n_f64 = (double)n;
+    double *x = scores;
+    double *nx = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!nx) return -1;
+    for (int64_t i = 0; i < n; ++i) x[i] = 1.0 / n_f64;          /* :133 */
+    uint64_t iters = 0;
+    double last_diff = INFINITY;
+    int converged = 0;
+    for (uint64_t it = 0; it < cfg.max_iterations; ++it) {       /* :142 */
+        iters += 1;
+        double dangling_sum = 0.0;                               /* :144-149 */
+        for (int64_t i = 0; i < n; ++i)
+            if (row_ptr[i + 1] == row_ptr[i]) dangling_sum += x[i];
+        const double dangling_contrib = cfg.damping * dangling_sum / n_f64;
+        const double teleport = (1.0 - cfg.damping) / n_f64;
+        const double fill = teleport + dangling_contrib;          /* :152 */
+        for (int64_t i = 0; i < n; ++i) nx[i] = fill;
+        for (int64_t u = 0; u < n; ++u) {                        /* :154-162 */
+            const int64_t deg = row_ptr[u + 1] - row_ptr[u];
+            if (deg > 0) {
+                const double share = cfg.damping * x[u] / (double)deg;
+                for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e)
+                    nx[col[e]] += share;
+            }
+        }
+        const double diff = l1_seq(x, nx, n);                    /* :169-173 */
+        last_diff = diff;
+        double *t = x; x = nx; nx = t;                           /* :175 */
+        if (diff < cfg.tolerance) { converged = 1; break; }      /* :176 */
+    }
+    if (x != scores) { memcpy(scores, x, sizeof(double) * (size_t)n); free(x); }
+    else free(nx);
+    run->iterations = iters;
+    run->diff_l1 = last_diff;
+    run->converged = converged;
+    return 0;
+}
+
+/*
+ * pagerank_weighted_run, src/pagerank.rs:210-289.
+ * w[e] is edge_weight(u, col[e]) as the adapter returns it; it is clamped with
+ * Rust's max(.., 0.0) here, at the two places the reference clamps.
+ */
+int orc_pagerank_weighted_run(int64_t n, const int64_t *row_ptr,
+                              const int32_t *col, const double *w,
+                              orc_config cfg, double *scores, orc_run *run) {
+    if (n == 0) { empty_run(run); return 0; }
+    const double n_f64 = (double)n;
+    double *x = scores;
+    double *nx = (double *)malloc(sizeof(double) * (size_t)n);
+    double *ws = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!nx || !ws) { free(nx); free(ws); return -1; }
+    for (int64_t i = 0; i < n; ++i) x[i] = 1.0 / n_f64;          /* :222 */
+    for (int64_t u = 0; u < n; ++u) {                            /* :227-234 */
+        double s = 0.0;
+        for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e)
+            s += rust_max(w[e], 0.0);
+        ws[u] = s;
+    }
+    uint64_t iters = 0;
+    double last_diff = INFINITY;
+    int converged = 0;
+    for (uint64_t it = 0; it < cfg.max_iterations; ++it) {
+        iters += 1;
+        double dangling_sum = 0.0;                               /* :241-246 */
+        for (int64_t i = 0; i < n; ++i)
+            if (ws[i] == 0.0) dangling_sum += x[i];
+        const double dangling_contrib = cfg.damping * dangling_sum / n_f64;
+        const double teleport = (1.0 - cfg.damping) / n_f64;
+        const double fill = teleport + dangling_contrib;
+        for (int64_t i = 0; i < n; ++i) nx[i] = fill;
+        for (int64_t u = 0; u < n; ++u) {                        /* :252-263 */
+            const double wsu = ws[u];
+            if (wsu > 0.0) {
+                for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e) {
+                    const double we = rust_max(w[e], 0.0);
+                    if (we > 0.0) nx[col[e]] += cfg.damping * x[u] * (we / wsu);
+                }
+            }
+        }
+        const double diff = l1_seq(x, nx, n);
+        last_diff = diff;
+        double *t = x; x = nx; nx = t;
+        if (diff < cfg.tolerance) { converged = 1; break; }
+    }
+    if (x != scores) { memcpy(scores, x, sizeof(double) * (size_t)n); free(x); }
+    else free(nx);
+    free(ws);
+    run->iterations = iters;
+    run->diff_l1 = last_diff;
+    run->converged = converged;
+    return 0;
+}
+
+/*
+ * personalized_pagerank_run, src/ppr.rs:90-156.  Unweighted; the dangling
+ * mass goes back to p (src/ppr.rs:125-128), not uniformly.
+ * p: n raw personalization entries (normalised here, src/ppr.rs:104-109).
+ */
+int orc_ppr_run(int64_t n, const int64_t *row_ptr, const int32_t *col,
+                const double *p, orc_config cfg, double *scores, orc_run *run) {
+    if (n == 0) { empty_run(run); return 0; }
+    double *pv = (double *)malloc(sizeof(double) * (size_t)n);
+    double *nx = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!pv || !nx) { free(pv); free(nx); return -1; }
+    double p_sum = 0.0;
+    for (int64_t i = 0; i < n; ++i) p_sum += p[i];
+    if (p_sum > 0.0) {
+        for (int64_t i = 0; i < n; ++i) pv[i] = p[i] / p_sum;
+    } else {
+        for (int64_t i = 0; i < n; ++i) pv[i] = 1.0 / (double)n;
+    }
+    double *x = scores;
+    memcpy(x, pv, sizeof(double) * (size_t)n);                   /* :110 */
+    uint64_t iters = 0;
+    double last_diff = INFINITY;
+    int converged = 0;
+    for (uint64_t it = 0; it < cfg.max_iterations; ++it) {
+        iters += 1;
+        double dangling_sum = 0.0;                               /* :119-124 */
+        for (int64_t i = 0; i < n; ++i)
+            if (row_ptr[i + 1] == row_ptr[i]) dangling_sum += x[i];
+        for (int64_t i = 0; i < n; ++i)                          /* :125-128 */
+            nx[i] = (1.0 - cfg.damping) * pv[i] +
+                    cfg.damping * dangling_sum * pv[i];
+        for (int64_t u = 0; u < n; ++u) {                        /* :129-137 */
+            const int64_t deg = row_ptr[u + 1] - row_ptr[u];
+            if (deg > 0) {
+                const double share = cfg.damping * x[u] / (double)deg;
+                for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e)
+                    nx[col[e]] += share;
+            }
+        }
+        const double diff = l1_seq(x, nx, n);                    /* :138-142 */
+        last_diff = diff;
+        double *t = x; x = nx; nx = t;
+        if (diff < cfg.tolerance) { converged = 1; break; }      /* :145 */
+    }
+    if (x != scores) { memcpy(scores, x, sizeof(double) * (size_t)n); free(x); }
+    else free(nx);
+    free(pv);
+    run->iterations = iters;
+    run->diff_l1 = last_diff;
+    run->converged = converged;
+    return 0;
+}
+
+/*
+ * AdjacencyMatrix::neighbors, src/graph.rs:128-135: {j : M[u][j] > 0.0} in
+ * ascending j; the weighted view returns the raw cell (src/graph.rs:139-141).
+ * M is row-major n*n.  Writes row_ptr (n+1); col / w (capacity cap, w may be
+ * NULL).  Returns the number of edges, or -1 when cap is too small.
+ */
+int64_t orc_dense_to_csr(int64_t n, const double *M, int64_t *row_ptr,
+                         int32_t *col, double *w, int64_t cap) {
+    int64_t m = 0;
+    row_ptr[0] = 0;
+    for (int64_t u = 0; u < n; ++u) {
+        const double *row = M + u * n;
+        for (int64_t j = 0; j < n; ++j) {
+            if (row[j] > 0.0) {
+                if (m >= cap) return -1;
+                col[m] = (int32_t)j;
+                if (w) w[m] = row[j];
+                ++m;
+            }
+        }
+        row_ptr[u + 1] = m;
+    }
+    return m;
+}
+
+/*
+ * The reference's pagerank_run called with an AdjacencyMatrix: the O(n^2)
+ * neighbor precompute (src/pagerank.rs:136, src/graph.rs:128-135) followed by
+ * the power iteration.  This is what a caller of the reference pays at the
+ * dense 2,000-node configuration, and what the CPU baseline times there.
+ */
+int orc_pagerank_run_dense(int64_t n, const double *M, orc_config cfg,
+                           double *scores, orc_run *run) {
+    if (n == 0) { empty_run(run); return 0; }
+    int64_t cap = 0;
+    for (int64_t i = 0; i < n * n; ++i) cap += (M[i] > 0.0);
+    int64_t *rp = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n + 1));
+    int32_t *cl = (int32_t *)malloc(sizeof(int32_t) * (size_t)(cap ? cap : 1));
+    if (!rp || !cl) { free(rp); free(cl); return -1; }
+    orc_dense_to_csr(n, M, rp, cl, NULL, cap);
+    int rc = orc_pagerank_run(n, rp, cl, cfg, scores, run);
+    free(rp);
+    free(cl);
+    return rc;
+}
+
+/* ---- many independent PPR solves over host threads (CPU baseline) ---- */
+
+typedef struct {
+    int64_t n;
+    const int64_t *row_ptr;
+    const int32_t *col;
+    orc_config cfg;
+    const int64_t *seed_ptr;
+    const int32_t *seed_idx;
+    int64_t first, stride, count;
+    double *out;        /* count * n, or NULL */
+    uint64_t *iters;    /* count, or NULL */
+    int rc;
+} ppr_job;
+
+static void *ppr_worker(void *arg) {
+    ppr_job *j = (ppr_job *)arg;
+    double *p = (double *)calloc((size_t)j->n, sizeof(double));
+    double *s = (double *)malloc(sizeof(double) * (size_t)j->n);
+    if (!p || !s) { j->rc = -1; free(p); free(s); return NULL; }
+    for (int64_t c = j->first; c < j->count; c += j->stride) {
+        for (int64_t k = j->seed_ptr[c]; k < j->seed_ptr[c + 1]; ++k)
+            p[j->seed_idx[k]] += 1.0;
+        orc_run r;
+        if (orc_ppr_run(j->n, j->row_ptr, j->col, p, j->cfg, s, &r)) { j->rc = -1; break; }
+        if (j->out) memcpy(j->out + c * j->n, s, sizeof(double) * (size_t)j->n);
+        if (j->iters) j->iters[c] = r.iterations;
+        for (int64_t k = j->seed_ptr[c]; k < j->seed_ptr[c + 1]; ++k)
+            p[j->seed_idx[k]] = 0.0;
+    }
+    free(p);
+    free(s);
+    return NULL;
+}
+
+/*
+ * Runs orc_ppr_run once per seed set (personalization = 1 on each seed node),
+ * spread round-robin over `threads` host threads.  Each call is the
+ * single-threaded reference algorithm; the threads only run independent
+ * calls side by side.
+ */
+int orc_ppr_many(int64_t n, const int64_t *row_ptr, const int32_t *col,
+                 orc_config cfg, int64_t nsets, const int64_t *seed_ptr,
+                 const int32_t *seed_idx, int threads, double *out,
+                 uint64_t *iters) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    ppr_job jobs[256];
+    pthread_t tid[256];
+    for (int t = 0; t < threads; ++t) {
+        jobs[t] = (ppr_job){n, row_ptr, col, cfg, seed_ptr, seed_idx,
+                            t, threads, nsets, out, iters, 0};
+        if (threads == 1) ppr_worker(&jobs[t]);
+        else pthread_create(&tid[t], NULL, ppr_worker, &jobs[t]);
+    }
+    int rc = 0;
+    for (int t = 0; t < threads; ++t) {
+        if (threads > 1) pthread_join(tid[t], NULL);
+        rc |= jobs[t].rc;
+    }
+    return rc;
+}

@@ -1,0 +1,208 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.
+
+Bars (stated here, checked below):
+  * L1(gpu, reference restatement) <= 1e-6 and identical top-100 order
+    (ties within 1e-15 relative count as equal, as top_k sorts unstably);
+  * iteration counts equal to the reference's within +-1 (exact expected on
+    the small fixtures);
+  * L1 vs the FP64 oracle <= 1e-7 (the precision target);
+  * bit-identical results on repeated runs (determinism, src/lib.rs:10).
+"""
+import numpy as np
+import pytest
+
+import graphops_gb300 as go
+from graphops_gb300 import gen
+from conftest import case_csr, load_golden
+from oracle import fp64, port
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = load_golden()
+L1_PARITY = 1e-6
+L1_TARGET = 1e-7
+
+
+def cfg(c):
+    return go.PageRankConfig(damping=c["damping"], max_iterations=c["max_iterations"],
+                             tolerance=c["tolerance"])
+
+
+def top_order_matches(a, b, k=100):
+    ia = np.argsort(-a, kind="stable")[:k]
+    ib = np.argsort(-b, kind="stable")[:k]
+    for x, y in zip(ia, ib):
+        if x != y and abs(b[x] - b[y]) > 1e-15 * max(abs(b[x]), 1e-300):
+            return False
+    return True
+
+
+@pytest.mark.parametrize("c", GOLDEN, ids=[c["name"] for c in GOLDEN])
+def test_golden_cases(c):
+    rp, col, w = case_csr(c)
+    g = go.CsrAdjacency(rp, col, w)
+    if c["kind"] == "ppr":
+        r = go.personalized_pagerank_run(g, cfg(c), c["personalization"])
+    elif c["kind"] == "weighted":
+        r = go.pagerank_weighted_run(g, cfg(c))
+    else:
+        r = go.pagerank_run(g, cfg(c))
+    want = np.array([float.fromhex(x) for x in c["scores_hex"]])
+    assert r.scores.shape == want.shape
+    assert np.abs(r.scores - want).sum() <= 1e-9
+    assert r.iterations == c["iterations"]
+    assert r.converged == c["converged"]
+    d = float.fromhex(c["diff_l1_hex"])
+    assert abs(r.diff_l1 - d) <= 1e-6 * d + 1e-15
+
+
+def test_reference_doctests_and_examples():
+    cyc = [[0.0, 1.0, 0.0], [0.0, 0.0, 1.0], [1.0, 0.0, 0.0]]
+    s = go.pagerank(go.AdjacencyMatrix(cyc), go.PageRankConfig())   # src/pagerank.rs:100-113
+    assert len(s) == 3 and abs(s.sum() - 1.0) < 1e-6
+    p = go.personalized_pagerank(go.AdjacencyMatrix(cyc), go.PageRankConfig(), [1.0, 0.0, 0.0])
+    assert p[0] > p[1]                                              # src/ppr.rs:50-65
+    ex = [[0.0, 1.0, 1.0, 0.0], [0.0, 0.0, 1.0, 0.0], [1.0, 0.0, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0]]
+    s = go.pagerank(go.AdjacencyMatrix(ex), go.PageRankConfig(0.85, 100, 1e-8))
+    assert int(np.argmax(s)) == 2 and abs(s.sum() - 1) < 1e-6       # examples/pagerank.rs
+    w = [[0.0, 2.0, 1.0], [0.0, 0.0, 1.0], [0.0, 0.0, 0.0]]
+    s = go.pagerank_weighted(go.AdjacencyMatrix(w), go.PageRankConfig())
+    assert abs(s.sum() - 1.0) < 1e-6                                # src/pagerank.rs:344-359
+    h = [[0.0, 2.0, 1.0], [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]]
+    s = go.pagerank_weighted(go.AdjacencyMatrix(h), go.PageRankConfig())
+    assert s[1] >= s[2]                                             # src/pagerank.rs:361-377
+
+
+def test_petgraph_invariants():
+    """tests/invariants.rs:20-50 with the petgraph-like adapter."""
+    g = go.DiGraph(3)
+    g.add_edge(0, 1, 1.0)
+    g.add_edge(1, 2, 1.0)
+    for s in (go.pagerank(g, go.PageRankConfig()),
+              go.personalized_pagerank(g, go.PageRankConfig(), [1.0, 0.0, 0.0])):
+        assert len(s) == 3 and np.isfinite(s).all() and (s >= 0).all() and abs(s.sum() - 1) <= 1e-6
+
+
+def test_proptest_random_small_matrices():
+    """src/pagerank.rs:379-395 through the dense adapter on the device."""
+    rng = np.random.default_rng(0)
+    for _ in range(60):
+        n = int(rng.integers(1, 10))
+        M = np.zeros((n, n))
+        for _ in range(int(rng.integers(0, 40))):
+            u, v = rng.integers(0, 10, size=2)
+            if u < n and v < n and u != v:
+                M[u, v] = 1.0
+        s = go.pagerank_checked(go.AdjacencyMatrix(M), go.PageRankConfig())
+        assert len(s) == n and abs(s.sum() - 1.0) < 1e-6 and (s >= -1e-12).all()
+        want = port.pagerank_run_dense(M)[0]
+        assert np.abs(s - want).sum() < 1e-9
+
+
+def test_empty_graph():
+    r = go.pagerank_run(go.CsrAdjacency(np.zeros(1, np.int64), np.zeros(0, np.int32)))
+    assert r.scores.shape == (0,) and r.iterations == 0 and r.diff_l1 == 0.0 and r.converged
+    r = go.personalized_pagerank_run(go.AdjacencyMatrix(np.zeros((0, 0))), go.PageRankConfig(), [])
+    assert r.iterations == 0 and r.converged
+
+
+def test_er2000_dense_configuration():
+    """Directed ER n=2000, p=0.005, 1% forced dangling, dense AdjacencyMatrix,
+    d=0.85, tol 1e-6, max_iter 100, seed 0."""
+    g = gen.erdos_renyi(2000, 0.005, 0.01, seed=0)
+    M = gen.dense_adjacency(g)
+    r = go.pagerank_run(go.AdjacencyMatrix(M), go.PageRankConfig(0.85, 100, 1e-6))
+    ref = port.pagerank_run_dense(M, 0.85, 100, 1e-6)
+    assert np.abs(r.scores - ref[0]).sum() <= L1_PARITY
+    assert abs(r.iterations - ref[1]) <= 1 and r.iterations == ref[1]
+    assert r.converged == ref[3]
+    assert top_order_matches(r.scores, ref[0])
+    # the CSR adapter gives the same result as the dense one
+    r2 = go.pagerank_run(go.CsrAdjacency(g.row_ptr, g.col), go.PageRankConfig(0.85, 100, 1e-6))
+    assert np.array_equal(r.scores, r2.scores)
+
+
+@pytest.mark.parametrize("scale,weighted", [(12, False), (14, True), (16, False), (16, True)])
+def test_rmat_plain_and_weighted(scale, weighted):
+    g = gen.rmat(scale, 16, weighted=weighted, seed=scale)
+    conf = go.PageRankConfig(0.85, 1000, 1e-8)
+    if weighted:
+        r = go.pagerank_weighted_run(go.CsrAdjacency(g.row_ptr, g.col, g.weight), conf)
+        ref = port.pagerank_weighted_run(g.row_ptr, g.col, g.weight.astype(np.float64), 0.85, 1000, 1e-8)
+        x = fp64.fixed_point(g.n, g.row_ptr, g.col, 0.85, weights=g.weight)
+    else:
+        r = go.pagerank_run(go.CsrAdjacency(g.row_ptr, g.col), conf)
+        ref = port.pagerank_run(g.row_ptr, g.col, 0.85, 1000, 1e-8)
+        x = fp64.fixed_point(g.n, g.row_ptr, g.col, 0.85)
+    l1 = np.abs(r.scores - ref[0]).sum()
+    assert l1 <= L1_TARGET, l1
+    assert abs(r.iterations - ref[1]) <= 1
+    assert top_order_matches(r.scores, ref[0])
+    assert np.abs(r.scores - x).sum() <= np.abs(ref[0] - x).sum() + L1_TARGET
+
+
+def test_ppr_rmat():
+    g = gen.rmat(14, 16, seed=3)
+    sp, si = gen.seed_sets(g, 6, 1, 64, seed=1)
+    for i in range(6):
+        p = np.zeros(g.n)
+        p[si[sp[i]:sp[i + 1]]] = 1.0
+        r = go.personalized_pagerank_run(go.CsrAdjacency(g.row_ptr, g.col), go.PageRankConfig(0.85, 1000, 1e-7), p)
+        ref = port.ppr_run(g.row_ptr, g.col, p, 0.85, 1000, 1e-7)
+        assert np.abs(r.scores - ref[0]).sum() <= L1_TARGET
+        assert abs(r.iterations - ref[1]) <= 1
+        assert top_order_matches(r.scores, ref[0])
+
+
+def test_hub_rows_split_into_chunks():
+    """One node with 50,000 in-edges (many 2W-edge chunks) and a few medium
+    rows, plain and weighted."""
+    n = 60000
+    rng = np.random.default_rng(1)
+    rows = [[0] if u % 7 else [0, int(rng.integers(1, n))] for u in range(n)]
+    rows[0] = [1, 2, 3]
+    rp = np.zeros(n + 1, np.int64)
+    for u, r in enumerate(rows):
+        rp[u + 1] = rp[u] + len(r)
+    col = np.array([v for r in rows for v in r], np.int32)
+    w = rng.uniform(0.1, 1.0, size=col.shape[0])
+    conf = go.PageRankConfig(0.85, 500, 1e-10)
+    r = go.pagerank_run(go.CsrAdjacency(rp, col), conf)
+    ref = port.pagerank_run(rp, col, 0.85, 500, 1e-10)
+    assert np.abs(r.scores - ref[0]).sum() <= L1_TARGET and abs(r.iterations - ref[1]) <= 1
+    r = go.pagerank_weighted_run(go.CsrAdjacency(rp, col, w), conf)
+    ref = port.pagerank_weighted_run(rp, col, w, 0.85, 500, 1e-10)
+    assert np.abs(r.scores - ref[0]).sum() <= L1_TARGET and abs(r.iterations - ref[1]) <= 1
+
+
+def test_deterministic_bitwise():
+    g = gen.rmat(15, 16, weighted=True, seed=8)
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col, g.weight)
+    a = dg.pagerank_weighted_run(go.PageRankConfig(0.85, 1000, 1e-9))
+    b = dg.pagerank_weighted_run(go.PageRankConfig(0.85, 1000, 1e-9))
+    dg2 = go.DeviceGraph.from_csr(g.row_ptr, g.col, g.weight)
+    c = dg2.pagerank_weighted_run(go.PageRankConfig(0.85, 1000, 1e-9))
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[0], c[0])
+    assert a[1:] == b[1:] == c[1:]
+
+
+def test_nonconvergence_is_reported():
+    g = gen.rmat(12, 8, seed=1)
+    r = go.pagerank_run(go.CsrAdjacency(g.row_ptr, g.col), go.PageRankConfig(0.85, 3, 1e-12))
+    ref = port.pagerank_run(g.row_ptr, g.col, 0.85, 3, 1e-12)
+    assert r.iterations == 3 and not r.converged and ref[1] == 3
+    assert abs(r.diff_l1 - ref[2]) <= 1e-9 * ref[2]
+    assert np.abs(r.scores - ref[0]).sum() <= 1e-9
+
+
+def test_large_rmat20_weighted_tol_1e8():
+    """A size where the FP32 noise floor matters: the step norm must still get
+    below 1e-8 and match the reference's iteration count."""
+    g = gen.rmat(20, 16, weighted=True, seed=20)
+    conf = go.PageRankConfig(0.85, 1000, 1e-8)
+    r = go.pagerank_weighted_run(go.CsrAdjacency(g.row_ptr, g.col, g.weight), conf)
+    ref = port.pagerank_weighted_run(g.row_ptr, g.col, g.weight.astype(np.float64), 0.85, 1000, 1e-8)
+    assert r.converged and abs(r.iterations - ref[1]) <= 1
+    assert np.abs(r.scores - ref[0]).sum() <= L1_TARGET
+    assert top_order_matches(r.scores, ref[0])
+    assert abs(r.scores.sum() - 1.0) < 1e-6

@@ -1,0 +1,340 @@
+"""Benchmark: weighted PageRank on an R-MAT graph, GTEPS on GB300.
+
+Workload (default): R-MAT scale 22 (4,194,304 nodes), edge factor 16,
+a/b/c/d = 0.57/0.19/0.19/0.05, self loops and duplicates removed, weights
+uniform(0.1, 1.0) in FP32; damping 0.85, tolerance 1e-8 (L1 of the step),
+max_iterations 1000.  One step = one full solve to tolerance.
+GTEPS = m * iterations / time.
+
+  value     device-resident: the graph is on the device when the timed
+            region starts; CUDA events on the library's stream bracket K solves.
+  e2e       through the public API from pinned host buffers: every step
+            uploads the out-CSR and weights, builds the in-edge CSR on the
+            device, solves and copies the scores back.
+  roofline  the FP32-phase pull kernel (the dominant one): algorithmic bytes
+            per launch 8(N+1) + 8m + 8N over its mean CUDA-event duration,
+            against the measured HBM copy bandwidth.
+  cpu_baseline  the oracle's C restatement of pagerank_weighted_run (the
+            reference is single-threaded) on a bounded number of iterations.
+
+--impl reference times that CPU restatement alone, in the same JSON shape.
+Multi-GPU: one replica per rank (the solve does not shard without an
+exchange); value = all ranks' edges traversed / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "PPR seeds/s to L1 1e-7, learned+batched vs plain, 1 GB300; PageRank GTEPS"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--max-iter", type=int, default=1000)
+    ap.add_argument("--seed", type=int, default=22)
+    ap.add_argument("--cpu-iters", type=int, default=0,
+                    help="iterations of the CPU sample (0: sized to ~10 s)")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(a, m):
+    return {
+        "workload": f"weighted PageRank, R-MAT scale {a.scale} edge factor {a.edge_factor} "
+                    f"(0.57/0.19/0.19/0.05, dedup, no self loops), w~U(0.1,1) FP32",
+        "nodes": 1 << a.scale, "edges": int(m), "damping": 0.85, "tolerance": a.tol,
+        "max_iterations": a.max_iter, "graph_seed": a.seed,
+        "l2": "inputs larger than L2 (CSR + weights > 129 MB); no flush",
+    }
+
+
+def dist_init(a):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if a.impl == "gb300" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend)
+    return rank, ws
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.rows, self._stop = device, [], threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 3 + i and r[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_graph(a):
+    from graphops_gb300 import gen
+    return gen.rmat(a.scale, a.edge_factor, 0.57, 0.19, 0.19, weighted=True, wlo=0.1, whi=1.0,
+                    seed=a.seed)
+
+
+def cpu_sample(g, a, iters):
+    """The oracle's pagerank_weighted_run on `iters` iterations, 1 thread."""
+    from oracle import port
+    w64 = g.weight.astype(np.float64)
+    t0 = time.perf_counter()
+    _, it, _, _ = port.pagerank_weighted_run(g.row_ptr, g.col, w64, 0.85, iters, a.tol)
+    dt = time.perf_counter() - t0
+    return g.m * it / dt / 1e9, it, dt
+
+
+def cpu_iters_for(g, a):
+    if a.cpu_iters:
+        return a.cpu_iters
+    # roughly 10 s of single-thread work at ~100 M edge updates/s
+    return int(max(1, min(20, 1.0e9 / max(g.m, 1))))
+
+
+def run_reference(a):
+    rank, ws = dist_init(a)
+    if rank != 0:
+        return
+    g = make_graph(a)
+    iters = cpu_iters_for(g, a)
+    for _ in range(max(0, a.warmup)):
+        cpu_sample(g, a, 1)
+    vals, its, secs = [], 0, 0.0
+    for _ in range(max(1, a.steps)):
+        v, it, dt = cpu_sample(g, a, iters)
+        vals.append(v)
+        its += it
+        secs += dt
+    value = g.m * its / secs / 1e9
+    line = {
+        "metric": METRIC, "impl": "reference", "value": round(value, 6), "unit": "GTEPS",
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": round(secs / max(1, a.steps) * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(a, g.m),
+        "cpu_baseline": {"value": round(value, 6), "unit": "GTEPS", "cores": 1, "kind": "port",
+                         "sample": f"{iters} iterations of pagerank_weighted_run per step "
+                                   f"(C restatement, FP64, single thread: the reference path is "
+                                   f"single-threaded)"},
+        "e2e": {"value": round(value, 6), "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(a):
+    rank, ws = dist_init(a)
+    import ctypes
+    import torch
+    import graphops_gb300 as go
+    from graphops_gb300 import _native
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    ctx = _native.Context(dev)
+    g = make_graph(a)
+    n, m = g.n, g.m
+    conf = go.PageRankConfig(0.85, a.max_iter, a.tol)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", dev))
+
+    # ---- device-resident solves ----
+    dg = _native.DeviceGraph.from_csr(g.row_ptr, g.col, g.weight.astype(np.float64), ctx=ctx)
+    for _ in range(max(3, a.warmup)):
+        dg.pagerank_weighted_run(conf, out=False)
+    ctx.set_timing(True)
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    iters, launches, f32_ms, f32_n, df_ms, df_n = 0, 0, 0.0, 0, 0.0, 0
+    with ClockSampler(dev) as clk:
+        ev0.record(stream)
+        for _ in range(a.steps):
+            _, it, diff, conv = dg.pagerank_weighted_run(conf, out=False)
+            st = ctx.stats()
+            iters += it
+            launches += st.kernel_launches
+            f32_ms += st.f32_ms
+            f32_n += st.f32_launches
+            df_ms += st.df_ms
+            df_n += st.df_launches
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ctx.set_timing(False)
+    t_ms = max_over_ranks(ev0.elapsed_time(ev1), ws)
+    value = ws * m * iters / (t_ms * 1e-3) / 1e9
+    ms_per_step = t_ms / a.steps
+
+    # ---- roofline of the FP32-phase pull kernel ----
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    bytes_per_launch = 8 * (n + 1) + 8 * m + 8 * n
+    mean_f32 = f32_ms / max(1, f32_n)
+    achieved = bytes_per_launch / (mean_f32 * 1e-3) / 1e9 if f32_n else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(f"rmat{a.scale}_weighted_f32")
+        except Exception:
+            traffic = None
+
+    # ---- end to end through the public API from pinned host buffers ----
+    rp_h = torch.from_numpy(g.row_ptr).pin_memory()
+    col_h = torch.from_numpy(g.col).pin_memory()
+    w_h = torch.from_numpy(g.weight.astype(np.float64)).pin_memory()
+    out_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    lib = ctx._l
+    cfg_c = _native.Config(conf.damping, conf.max_iterations, conf.tolerance)
+
+    def e2e_step():
+        h = ctypes.c_void_p()
+        ctx.check(lib.gops_graph_upload(ctx.handle, n, ctypes.c_void_p(rp_h.data_ptr()),
+                                        ctypes.c_void_p(col_h.data_ptr()),
+                                        ctypes.c_void_p(w_h.data_ptr()), ctypes.byref(h)))
+        up = ctx.stats()
+        r = _native.Run()
+        ctx.check(lib.gops_pagerank_weighted_run(ctx.handle, h, ctypes.byref(cfg_c),
+                                                 ctypes.c_void_p(out_h.data_ptr()), ctypes.byref(r)))
+        st = ctx.stats()
+        lib.gops_graph_destroy(h)
+        return int(r.iterations), up.h2d_bytes + st.h2d_bytes, st.d2h_bytes, up.kernel_launches + st.kernel_launches
+
+    e2e_steps = max(1, min(a.steps, 3))
+    for _ in range(2):
+        e2e_step()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_iters, h2d, d2h = 0, 0, 0
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        it, hb, db, _ = e2e_step()
+        e_iters += it
+        h2d += hb
+        d2h += db
+    e1.record(stream)
+    e1.synchronize()
+    wall = time.perf_counter() - t0
+    e_ms = max_over_ranks(max(e0.elapsed_time(e1), wall * 1e3), ws)
+    e2e_value = ws * m * e_iters / (e_ms * 1e-3) / 1e9
+
+    # ---- CPU baseline (rank 0, bounded sample) ----
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        ci = cpu_iters_for(g, a)
+        v, it, dt = cpu_sample(g, a, ci)
+        cpu = {"value": round(v, 6), "unit": "GTEPS", "cores": 1, "kind": "port",
+               "sample": f"{it} iterations of pagerank_weighted_run ({dt:.1f} s), C restatement, "
+                         f"FP64, single thread (the reference path is single-threaded)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": ws,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms_per_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (double-float first phase, exact 64-bit fixed-point sums)",
+            "data": "synthetic", "config": workload_config(a, m),
+            "iterations_per_solve": iters / a.steps,
+            "e2e": {"value": round(e2e_value, 4), "unit": "GTEPS",
+                    "h2d_bytes_per_step": int(h2d / e2e_steps), "d2h_bytes_per_step": int(d2h / e2e_steps)},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
+                         "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4) if achieved else None,
+                         "traffic": traffic, "kernel": "iterate_kernel<PrecF32, weighted>",
+                         "bytes_per_launch": bytes_per_launch,
+                         "mean_launch_ms": round(mean_f32, 5), "launches": f32_n,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
+                         "df_phase_mean_ms": round(df_ms / max(1, df_n), 5), "df_launches": df_n},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)

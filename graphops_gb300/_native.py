@@ -39,7 +39,8 @@ class Run(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("solve_ms", _dbl), ("iterate_ms", _dbl), ("kernel_launches", _u64),
-                ("iterations", _u64), ("h2d_bytes", _u64), ("d2h_bytes", _u64)]
+                ("iterations", _u64), ("h2d_bytes", _u64), ("d2h_bytes", _u64),
+                ("df_ms", _dbl), ("df_launches", _u64), ("f32_ms", _dbl), ("f32_launches", _u64)]
 
 
 # (name, restype, argtypes) for every symbol include/gops.h declares
@@ -50,6 +51,7 @@ SIGNATURES = [
     ("gops_last_error", ctypes.c_char_p, [_p]),
     ("gops_ctx_stats", ctypes.c_int, [_p, ctypes.POINTER(Stats)]),
     ("gops_ctx_stream", _p, [_p]),
+    ("gops_ctx_set_timing", ctypes.c_int, [_p, ctypes.c_int]),
     ("gops_config_validate", ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_char_p, ctypes.c_size_t]),
     ("gops_weights_validate", ctypes.c_int, [_i64, _p, ctypes.c_char_p, ctypes.c_size_t]),
     ("gops_personalization_validate", ctypes.c_int, [_i64, _i64, _p, ctypes.c_char_p, ctypes.c_size_t]),
@@ -118,6 +120,9 @@ class Context:
         s = Stats()
         self.check(self._l.gops_ctx_stats(self.handle, ctypes.byref(s)))
         return s
+
+    def set_timing(self, enable: bool) -> None:
+        self.check(self._l.gops_ctx_set_timing(self.handle, int(bool(enable))))
 
     def stream(self) -> int:
         return self._l.gops_ctx_stream(self.handle) or 0

@@ -122,6 +122,7 @@ void gops_ctx_destroy(gops_ctx *ctx) {
   for (int i = 0; i < 4; ++i)
     if (x.ev[i]) cudaEventDestroy(x.ev[i]);
   if (x.host_state) cudaFreeHost(x.host_state);
+  for (cudaEvent_t e : x.tev) cudaEventDestroy(e);
   if (x.stream) cudaStreamDestroy(x.stream);
   delete ctx;
 }
@@ -137,6 +138,12 @@ int gops_ctx_stats(const gops_ctx *ctx, gops_stats *out) {
 }
 
 void *gops_ctx_stream(gops_ctx *ctx) { return ctx ? (void *)ctx->impl.stream : nullptr; }
+
+int gops_ctx_set_timing(gops_ctx *ctx, int enable) {
+  if (!ctx) return GOPS_ERR_INVALID;
+  ctx->impl.timing = enable != 0;
+  return GOPS_OK;
+}
 
 int gops_config_validate(const gops_config *cfg, char *msg, size_t cap) {
   if (!cfg) return write_msg(msg, cap, "config is NULL");

@@ -2,6 +2,7 @@
 #pragma once
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "gops_internal.cuh"
 
@@ -34,6 +35,7 @@ struct Workspace {
 
 struct SolveState {
   unsigned long long iterations;
+  unsigned long long f32_from;  // first step run in the FP32 phase (0: none)
   double diff_l1;
   int done;
   int converged;
@@ -65,6 +67,9 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   SolveState *host_state = nullptr;  // pinned
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // optional per-launch timing of the iteration kernels (gops_ctx_set_timing)
+  bool timing = false;
+  std::vector<cudaEvent_t> tev;
   std::string last_error;
   gops_stats stats{};
   const double *last_scores = nullptr;  // device scores of the last solve

@@ -192,6 +192,7 @@ __device__ bool prologue(const IterParams &p, df *dsum) {
   if (f32 == WANT_DF) return false;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     p.st->f32_phase = f32 ? 1 : 0;
+    if (f32 && p.st->f32_from == 0) p.st->f32_from = k;
     const int nxt = (int)((k + 1) % 3);
     for (int i = 0; i < 4; ++i) p.sums[nxt * 4 + i] = 0;
   }
@@ -429,6 +430,19 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   bool f32_known = false;
   unsigned long long k = 1;
   const int chunk = 4;
+  // per-launch timing: (step, is_df) of every timed launch, events 2i / 2i+1
+  std::vector<std::pair<unsigned long long, bool>> timed;
+  auto timed_launch = [&](bool is_df) -> Status {
+    if (!ctx->timing) return Status::ok();
+    const size_t need = 2 * (timed.size() + 1);
+    while (ctx->tev.size() < need) {
+      cudaEvent_t e;
+      GOPS_CUDA_TRY(cudaEventCreate(&e));
+      ctx->tev.push_back(e);
+    }
+    timed.push_back({k, is_df});
+    return Status::ok();
+  };
   for (;;) {
     for (int j = 0; j < chunk && k - 1 <= cfg->max_iterations; ++j, ++k) {
       p.k = k;
@@ -437,11 +451,17 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
       p.gdf_out = ws.gdf[k & 1];
       p.gf_out = ws.gf[k & 1];
       if (!f32_known) {
+        GOPS_TRY(timed_launch(true));
+        if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 2], s));
         iterate_kernel<PrecDF, MODE><<<grid_df, kThreads, smem_df, s>>>(p);
+        if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 1], s));
         ++launches;
       }
       if (k >= 2) {
+        GOPS_TRY(timed_launch(false));
+        if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 2], s));
         iterate_kernel<PrecF32, MODE><<<grid_f, kThreads, smem_f, s>>>(p);
+        if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 1], s));
         ++launches;
       }
     }
@@ -470,6 +490,22 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   cudaEventElapsedTime(&t_it, ctx->ev[1], ctx->ev[2]);
   ctx->stats.solve_ms = t_all;
   ctx->stats.iterate_ms = t_it;
+  if (ctx->timing) {
+    // launches that did the work of a step (not the ones that found the run
+    // finished or the other precision active)
+    const unsigned long long its = ctx->host_state->iterations;
+    const unsigned long long f32_from = ctx->host_state->f32_from;
+    for (size_t i = 0; i < timed.size(); ++i) {
+      const unsigned long long kk = timed[i].first;
+      const bool is_df = timed[i].second;
+      const bool active = kk <= its && (is_df ? (f32_from == 0 || kk < f32_from) : (f32_from && kk >= f32_from));
+      if (!active) continue;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ctx->tev[2 * i], ctx->tev[2 * i + 1]);
+      if (is_df) { ctx->stats.df_ms += ms; ctx->stats.df_launches++; }
+      else { ctx->stats.f32_ms += ms; ctx->stats.f32_launches++; }
+    }
+  }
   ctx->stats.kernel_launches += launches;
   ctx->stats.iterations = run->iterations;
   return Status::ok();

@@ -70,6 +70,12 @@ typedef struct gops_stats {
   uint64_t iterations;      /* iterations of the solve (sum over columns for batches) */
   uint64_t h2d_bytes;       /* host-to-device bytes copied by the call                */
   uint64_t d2h_bytes;       /* device-to-host bytes copied by the call                */
+  /* with gops_ctx_set_timing(ctx, 1): summed CUDA-event durations of the
+   * iteration-kernel launches that performed a step, per precision phase */
+  double df_ms;
+  uint64_t df_launches;
+  double f32_ms;
+  uint64_t f32_launches;
 } gops_stats;
 
 /* ---- library / context (no reference counterpart: the reference is a pure
@@ -82,6 +88,9 @@ int gops_ctx_stats(const gops_ctx *ctx, gops_stats *out);
 /* The context's CUDA stream (a cudaStream_t), for callers that order their
  * own work against the library's. */
 void *gops_ctx_stream(gops_ctx *ctx);
+/* Enables (1) or disables (0) per-launch CUDA-event timing of the iteration
+ * kernels; the results appear in gops_stats.  Off by default. */
+int gops_ctx_set_timing(gops_ctx *ctx, int enable);
 
 /* PageRankConfig::validate (src/pagerank.rs:63-85).  Writes the reference's
  * exact message ("damping must be finite", ...) into msg on failure and

@@ -29,14 +29,6 @@ int write_msg(char *msg, size_t cap, const char *text) {
   return GOPS_ERR_INVALID;
 }
 
-void free_graph_device(Graph &g) {
-  cudaFree(g.in_rp); cudaFree(g.in_col); cudaFree(g.in_val); cudaFree(g.deg);
-  cudaFree(g.dmask_w); cudaFree(g.items);
-  workspace_free(g.ws);
-  g.in_rp = nullptr; g.in_col = nullptr; g.in_val = nullptr; g.deg = nullptr;
-  g.dmask_w = nullptr; g.items = nullptr;
-}
-
 Status check_csr_host(int64_t n, const int64_t *row_ptr, const int32_t *col) {
   if (n < 0 || n >= INT32_MAX) return Status{GOPS_ERR_INVALID, "node count out of range"};
   if (!row_ptr) return Status{GOPS_ERR_INVALID, "row_ptr is NULL"};
@@ -194,7 +186,7 @@ int gops_graph_upload(gops_ctx *ctx, int64_t n, const int64_t *row_ptr, const in
   g->impl.ctx = &c;
   Status st = upload_impl(&c, n, row_ptr, col, weights, &g->impl);
   if (st.code != GOPS_OK) {
-    free_graph_device(g->impl);
+    graph_free_device(g->impl);
     delete g;
     return c.set(st);
   }
@@ -240,7 +232,7 @@ int gops_graph_from_dense(gops_ctx *ctx, int64_t n, const double *matrix, gops_g
   free_async(d_w, s);
   cudaStreamSynchronize(s);
   if (st.code != GOPS_OK) {
-    free_graph_device(g->impl);
+    graph_free_device(g->impl);
     delete g;
     return c.set(st);
   }
@@ -254,7 +246,7 @@ void gops_graph_destroy(gops_graph *g) {
     cudaSetDevice(g->impl.ctx->device);
     cudaStreamSynchronize(g->impl.ctx->stream);
   }
-  free_graph_device(g->impl);
+  graph_free_device(g->impl);
   delete g;
 }
 

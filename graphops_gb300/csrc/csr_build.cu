@@ -6,11 +6,13 @@
 //      src/pagerank.rs:136-137,226-234 and src/ppr.rs:112); then a stable radix
 //      sort of edge ids by destination, so every in-row lists its sources in
 //      ascending source order, the order the reference scatters in
-//      (src/pagerank.rs:154-162).
-//  K2  the pull kernels' work partition: runs of rows whose in-edges start in
-//      the same W-edge window (so fewer than 2W in-edges, staged in shared
-//      memory), at most kRowCap rows each; rows with more than W in-edges
-//      ("hubs") are split into 2W-edge chunks.
+//      (src/pagerank.rs:154-162).  In-row offsets come from the sorted keys
+//      (no atomics on hub destinations).
+//  K2  relabelling and the pull kernels' plan: a stable radix sort of nodes by
+//      in-degree (descending) gives perm; the in-edge CSR is rewritten in that
+//      order with relabelled sources; rows then fall into contiguous degree
+//      classes (segments), each processed with one sub-warp width, and rows
+//      above kHubThreshold in-edges are split into kHubChunk-edge warp tasks.
 //  Dense  AdjacencyMatrix (src/graph.rs:128-141) -> out-CSR by a warp-ballot
 //      compaction of each matrix row (entries > 0.0, ascending column).
 #include <algorithm>
@@ -20,23 +22,17 @@
 
 namespace gops {
 
-constexpr int kRowCap = 256;  // rows per normal item (one epilogue thread each)
-
 namespace {
 
-__global__ void out_row_pass(int64_t n, const int64_t *__restrict__ rp, const int32_t *__restrict__ col,
-                             const double *__restrict__ w, uint32_t *__restrict__ src,
-                             float *__restrict__ val_out, float *__restrict__ deg_f,
-                             uint32_t *__restrict__ dmask, unsigned long long *__restrict__ indeg) {
+__global__ void out_row_pass(int64_t n, const int64_t *__restrict__ rp, const double *__restrict__ w,
+                             uint32_t *__restrict__ src, float *__restrict__ val_out,
+                             float *__restrict__ deg_f, uint32_t *__restrict__ dmask) {
   const int lane = threadIdx.x & 31;
   const int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (u >= n) return;
   const int64_t b = rp[u], e = rp[u + 1];
   if (lane == 0) deg_f[u] = (float)(e - b);
-  for (int64_t i = b + lane; i < e; i += 32) {
-    src[i] = (uint32_t)u;
-    atomicAdd(&indeg[col[i]], 1ull);
-  }
+  for (int64_t i = b + lane; i < e; i += 32) src[i] = (uint32_t)u;
   if (w) {
     double s = 0.0;
     for (int64_t i = b + lane; i < e; i += 32) s += fmax(w[i], 0.0);
@@ -63,68 +59,106 @@ __global__ void copy_keys(const int32_t *col, uint32_t *keys, int64_t m) {
     keys[i] = (uint32_t)col[i];
 }
 
-__global__ void gather_in_edges(const uint32_t *order, const uint32_t *src, const float *val_out,
-                                int32_t *in_col, float *in_val, int64_t m) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+// rp[v] = first position i of the sorted destination keys K with K[i] >= v.
+__global__ void rp_from_sorted(const uint32_t *K, int64_t m, int64_t n, int64_t *rp) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= m;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t e = order[i];
-    in_col[i] = (int32_t)src[e];
-    if (in_val) in_val[i] = val_out[e];
+    const int64_t prev = i == 0 ? -1 : (int64_t)K[i - 1];
+    const int64_t cur = i == m ? n : (int64_t)K[i];
+    for (int64_t v = prev + 1; v <= cur; ++v) rp[v] = i;
   }
 }
 
-__device__ __forceinline__ bool is_long_row(const int64_t *rp, int64_t v, int W) {
-  return rp[v + 1] - rp[v] > W;
-}
-
-__device__ __forceinline__ bool is_start(const int64_t *rp, int64_t v, int64_t n, int W) {
-  if (v >= n) return true;
-  if (v == 0 || (v % kRowCap) == 0) return true;
-  if (is_long_row(rp, v, W) || is_long_row(rp, v - 1, W)) return true;
-  return (rp[v] / W) != (rp[v - 1] / W);
-}
-
-__global__ void item_units(const int64_t *rp, int64_t n, int W, int64_t *units) {
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v <= n;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    int64_t u = 0;
-    if (v < n && is_start(rp, v, n, W)) {
-      const int64_t d = rp[v + 1] - rp[v];
-      u = d > W ? ceil_div<int64_t>(d, 2 * (int64_t)W) : 1;
-    }
-    units[v] = u;
-  }
-}
-
-__global__ void item_fill(const int64_t *rp, int64_t n, int W, const int64_t *ibase, Item *items) {
+__global__ void max_indeg(const int64_t *rp, int64_t n, unsigned *out) {
+  unsigned best = 0;
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    const bool lng = is_long_row(rp, v, W);
-    if (is_start(rp, v, n, W)) {
-      const int64_t b = ibase[v];
-      if (lng) {
-        const int64_t nch = ibase[v + 1] - b;
-        for (int64_t c = 0; c < nch; ++c)
-          items[b + c] = Item{(int32_t)v, (int32_t)(v + 1), (int32_t)b, (int32_t)nch};
-      } else {
-        items[b].r0 = (int32_t)v;
-        items[b].first = -1;
-        items[b].nchunks = 0;
-      }
-    }
-    // the last row of a normal run closes it: its item is the one just
-    // before the next start's items
-    if (!lng && is_start(rp, v + 1, n, W)) items[ibase[v + 1] - 1].r1 = (int32_t)(v + 1);
-  }
-}
-
-__global__ void max_chunks_kernel(const Item *items, int64_t n_items, int *out) {
-  int best = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_items;
-       i += (int64_t)gridDim.x * blockDim.x)
-    best = max(best, items[i].nchunks);
+       v += (int64_t)gridDim.x * blockDim.x)
+    best = max(best, (unsigned)(rp[v + 1] - rp[v]));
   best = __reduce_max_sync(0xffffffffu, best);
   if ((threadIdx.x & 31) == 0) atomicMax(out, best);
+}
+
+__global__ void node_sort_keys(const int64_t *rp, int64_t n, const unsigned *maxdeg,
+                               uint32_t *keys, uint32_t *vals) {
+  const unsigned md = *maxdeg;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    keys[v] = md - (unsigned)(rp[v + 1] - rp[v]);
+    vals[v] = (uint32_t)v;
+  }
+}
+
+// Row i of the relabelled graph is node perm[i] = sorted_vals[i].
+__global__ void permute_nodes(const uint32_t *sorted_keys, const uint32_t *sorted_vals, int64_t n,
+                              const unsigned *maxdeg, int32_t *perm, int32_t *inv_perm,
+                              int64_t *new_deg, const float *deg_old, float *deg_new) {
+  const unsigned md = *maxdeg;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t old = sorted_vals[i];
+    perm[i] = (int32_t)old;
+    inv_perm[old] = (int32_t)i;
+    new_deg[i] = (int64_t)(md - sorted_keys[i]);
+    deg_new[i] = deg_old[old];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) new_deg[n] = 0;
+}
+
+__global__ void permute_dmask(const int32_t *perm, int64_t n, const uint32_t *old_mask,
+                              uint32_t *new_mask) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  unsigned bit = 0;
+  if (valid) {
+    const int32_t o = perm[i];
+    bit = (old_mask[o >> 5] >> (o & 31)) & 1u;
+  }
+  const unsigned word = __ballot_sync(0xffffffffu, bit);
+  if ((threadIdx.x & 31) == 0 && i < n) new_mask[i >> 5] = word;
+}
+
+// Sorted position i holds edge O[i] into node K[i]; it lands in relabelled
+// row inv_perm[K[i]] at the same offset within the row.
+__global__ void scatter_edges(const uint32_t *K, const uint32_t *O, int64_t m, const int64_t *rp_old,
+                              const int32_t *inv_perm, const int64_t *rp_new, const uint32_t *src,
+                              const float *val_out, int32_t *in_col, float *in_val) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = K[i];
+    const int64_t pos = rp_new[inv_perm[v]] + (i - rp_old[v]);
+    const uint32_t e = O[i];
+    in_col[pos] = inv_perm[src[e]];
+    if (in_val) in_val[pos] = val_out[e];
+  }
+}
+
+// out[j] = number of relabelled rows with in-degree >= thr[j] (degrees are
+// non-increasing along the rows: maxdeg - sorted_keys[i]).
+__global__ void count_ge(const uint32_t *sorted_keys, int64_t n, const unsigned *maxdeg,
+                         const int64_t *thr, int nthr, int64_t *out) {
+  const int j = threadIdx.x;
+  if (j >= nthr) return;
+  const unsigned md = *maxdeg;
+  int64_t lo = 0, hi = n;  // first row with degree < thr
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) / 2;
+    if ((int64_t)(md - sorted_keys[mid]) >= thr[j]) lo = mid + 1;
+    else hi = mid;
+  }
+  out[j] = lo;
+}
+
+__global__ void hub_chunks(const int64_t *rp, int32_t n_hub, int64_t *nch) {
+  for (int32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= n_hub; h += gridDim.x * blockDim.x)
+    nch[h] = h < n_hub ? ceil_div<int64_t>(rp[h + 1] - rp[h], kHubChunk) : 0;
+}
+
+__global__ void hub_fill(const int64_t *first64, int32_t n_hub, int32_t *first, int32_t *task_row) {
+  for (int32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= n_hub; h += gridDim.x * blockDim.x) {
+    first[h] = (int32_t)first64[h];
+    if (h < n_hub)
+      for (int64_t t = first64[h]; t < first64[h + 1]; ++t) task_row[t] = h;
+  }
 }
 
 // Dense matrix rows: count entries > 0 (pass 0) or write them in ascending
@@ -165,23 +199,32 @@ int bits_for(int64_t n) {
 
 }  // namespace
 
+void graph_free_device(Graph &g) {
+  cudaFree(g.in_rp); cudaFree(g.in_col); cudaFree(g.in_val); cudaFree(g.deg);
+  cudaFree(g.dmask_w); cudaFree(g.perm); cudaFree(g.hub_first); cudaFree(g.hub_task_row);
+  workspace_free(g.ws);
+  g.in_rp = nullptr; g.in_col = nullptr; g.in_val = nullptr; g.deg = nullptr;
+  g.dmask_w = nullptr; g.perm = nullptr; g.hub_first = nullptr; g.hub_task_row = nullptr;
+}
+
 Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_rp,
                                        const int32_t *d_out_col, const double *d_w) {
   cudaStream_t s = ctx->stream;
   const int64_t n = g->n, m = g->m;
-  const int W = g->window > 0 ? g->window : 1024;
-  g->window = W;
   g->weighted = d_w != nullptr;
   Status st;
   uint32_t *src = nullptr, *keys = nullptr, *vals = nullptr, *keys2 = nullptr, *vals2 = nullptr;
-  float *val_out = nullptr;
-  unsigned long long *indeg = nullptr;
-  int64_t *units = nullptr;
-  int *maxc = nullptr;
+  uint32_t *nk = nullptr, *nv = nullptr, *nk2 = nullptr, *nv2 = nullptr, *dmask_old = nullptr;
+  float *val_out = nullptr, *deg_old = nullptr;
+  int64_t *rp_old = nullptr, *new_deg = nullptr, *small = nullptr;
+  int32_t *inv_perm = nullptr;
+  unsigned *maxdeg = nullptr;
   auto cleanup = [&]() {
-    free_async(src, s); free_async(keys, s); free_async(vals, s);
-    free_async(keys2, s); free_async(vals2, s); free_async(val_out, s);
-    free_async(indeg, s); free_async(units, s); free_async(maxc, s);
+    free_async(src, s); free_async(keys, s); free_async(vals, s); free_async(keys2, s);
+    free_async(vals2, s); free_async(nk, s); free_async(nv, s); free_async(nk2, s);
+    free_async(nv2, s); free_async(dmask_old, s); free_async(val_out, s); free_async(deg_old, s);
+    free_async(rp_old, s); free_async(new_deg, s); free_async(small, s); free_async(inv_perm, s);
+    free_async(maxdeg, s);
   };
 #define BUILD_TRY(expr)                                                                     \
   do {                                                                                      \
@@ -192,71 +235,147 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
                     std::string("graph build: ") + #expr + ": " + cudaGetErrorString(_e)}; \
     }                                                                                       \
   } while (0)
-  const size_t mm = (size_t)std::max<int64_t>(m, 1);
+#define BUILD_ST(expr)                       \
+  do {                                       \
+    st = (expr);                             \
+    if (st.code != GOPS_OK) { cleanup(); return st; } \
+  } while (0)
+  const size_t mm = (size_t)std::max<int64_t>(m, 1) + 64;  // padded edge arrays
+  const size_t nn = (size_t)std::max<int64_t>(n, 1);
+  const size_t nwords = (size_t)(n / 32 + 1);
   BUILD_TRY(cudaMalloc(&g->in_rp, sizeof(int64_t) * (n + 1)));
   BUILD_TRY(cudaMalloc(&g->in_col, sizeof(int32_t) * mm));
-  BUILD_TRY(cudaMalloc(&g->deg, sizeof(float) * std::max<int64_t>(n, 1)));
+  BUILD_TRY(cudaMemsetAsync(g->in_col, 0, sizeof(int32_t) * mm, s));
+  BUILD_TRY(cudaMalloc(&g->deg, sizeof(float) * nn));
+  BUILD_TRY(cudaMalloc(&g->perm, sizeof(int32_t) * nn));
+  BUILD_TRY(cudaMallocAsync((void **)&deg_old, sizeof(float) * nn, s));
   if (g->weighted) {
     BUILD_TRY(cudaMalloc(&g->in_val, sizeof(float) * mm));
-    BUILD_TRY(cudaMalloc(&g->dmask_w, sizeof(uint32_t) * (size_t)(n / 32 + 1)));
-    BUILD_TRY(cudaMemsetAsync(g->dmask_w, 0, sizeof(uint32_t) * (size_t)(n / 32 + 1), s));
+    BUILD_TRY(cudaMemsetAsync(g->in_val, 0, sizeof(float) * mm, s));
+    BUILD_TRY(cudaMalloc(&g->dmask_w, sizeof(uint32_t) * nwords));
+    BUILD_TRY(cudaMemsetAsync(g->dmask_w, 0, sizeof(uint32_t) * nwords, s));
+    BUILD_TRY(cudaMallocAsync((void **)&dmask_old, sizeof(uint32_t) * nwords, s));
+    BUILD_TRY(cudaMemsetAsync(dmask_old, 0, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(cudaMallocAsync((void **)&val_out, sizeof(float) * mm, s));
   }
   BUILD_TRY(cudaMallocAsync((void **)&src, sizeof(uint32_t) * mm, s));
-  BUILD_TRY(cudaMallocAsync((void **)&indeg, sizeof(unsigned long long) * (n + 1), s));
-  BUILD_TRY(cudaMemsetAsync(indeg, 0, sizeof(unsigned long long) * (n + 1), s));
   if (n > 0) {
-    out_row_pass<<<(unsigned)ceil_div<int64_t>(n, 8), 256, 0, s>>>(
-        n, d_out_rp, d_out_col, d_w, src, val_out, g->deg, g->dmask_w, indeg);
+    out_row_pass<<<(unsigned)ceil_div<int64_t>(n, 8), 256, 0, s>>>(n, d_out_rp, d_w, src, val_out,
+                                                                   deg_old, dmask_old);
     BUILD_TRY(cudaGetLastError());
   }
-  // in_rp = exclusive scan of in-degrees (entry n is 0, so in_rp[n] == m)
-  st = exclusive_scan_i64((const int64_t *)indeg, g->in_rp, n + 1, s);
-  if (st.code != GOPS_OK) { cleanup(); return st; }
+  // K1: stable sort of edge ids by destination
+  BUILD_TRY(cudaMallocAsync((void **)&keys, sizeof(uint32_t) * mm, s));
+  BUILD_TRY(cudaMallocAsync((void **)&vals, sizeof(uint32_t) * mm, s));
+  BUILD_TRY(cudaMallocAsync((void **)&keys2, sizeof(uint32_t) * mm, s));
+  BUILD_TRY(cudaMallocAsync((void **)&vals2, sizeof(uint32_t) * mm, s));
+  uint32_t *K = keys, *O = vals;
   if (m > 0) {
-    BUILD_TRY(cudaMallocAsync((void **)&keys, sizeof(uint32_t) * mm, s));
-    BUILD_TRY(cudaMallocAsync((void **)&vals, sizeof(uint32_t) * mm, s));
-    BUILD_TRY(cudaMallocAsync((void **)&keys2, sizeof(uint32_t) * mm, s));
-    BUILD_TRY(cudaMallocAsync((void **)&vals2, sizeof(uint32_t) * mm, s));
     copy_keys<<<grid_for(m, 256), 256, 0, s>>>(d_out_col, keys, m);
     iota_u32<<<grid_for(m, 256), 256, 0, s>>>(vals, m);
     BUILD_TRY(cudaGetLastError());
     bool alt = false;
-    st = radix_sort_pairs_u32(keys, vals, keys2, vals2, m, bits_for(n), &alt, s);
-    if (st.code != GOPS_OK) { cleanup(); return st; }
-    gather_in_edges<<<grid_for(m, 256), 256, 0, s>>>(alt ? vals2 : vals, src, val_out, g->in_col,
-                                                     g->in_val, m);
-    BUILD_TRY(cudaGetLastError());
+    BUILD_ST(radix_sort_pairs_u32(keys, vals, keys2, vals2, m, bits_for(n), &alt, s));
+    if (alt) { K = keys2; O = vals2; }
   }
-  // K2: work items
-  BUILD_TRY(cudaMallocAsync((void **)&units, sizeof(int64_t) * (n + 1), s));
-  item_units<<<grid_for(n + 1, 256), 256, 0, s>>>(g->in_rp, n, W, units);
+  BUILD_TRY(cudaMallocAsync((void **)&rp_old, sizeof(int64_t) * (n + 1), s));
+  rp_from_sorted<<<grid_for(m + 1, 256), 256, 0, s>>>(K, m, n, rp_old);
   BUILD_TRY(cudaGetLastError());
-  st = exclusive_scan_i64(units, units, n + 1, s);
-  if (st.code != GOPS_OK) { cleanup(); return st; }
-  int64_t n_items = 0;
-  BUILD_TRY(cudaMemcpyAsync(&n_items, units + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-  BUILD_TRY(cudaStreamSynchronize(s));
-  if (n_items >= INT32_MAX) { cleanup(); return Status{GOPS_ERR_INVALID, "graph too large"}; }
-  g->n_items = (int32_t)n_items;
-  BUILD_TRY(cudaMalloc(&g->items, sizeof(Item) * std::max<int64_t>(n_items, 1)));
+  // K2: relabel by in-degree, descending (stable: ties keep id order)
+  BUILD_TRY(cudaMallocAsync((void **)&maxdeg, sizeof(unsigned), s));
+  BUILD_TRY(cudaMemsetAsync(maxdeg, 0, sizeof(unsigned), s));
+  BUILD_TRY(cudaMallocAsync((void **)&nk, sizeof(uint32_t) * nn, s));
+  BUILD_TRY(cudaMallocAsync((void **)&nv, sizeof(uint32_t) * nn, s));
+  BUILD_TRY(cudaMallocAsync((void **)&nk2, sizeof(uint32_t) * nn, s));
+  BUILD_TRY(cudaMallocAsync((void **)&nv2, sizeof(uint32_t) * nn, s));
+  BUILD_TRY(cudaMallocAsync((void **)&inv_perm, sizeof(int32_t) * nn, s));
+  BUILD_TRY(cudaMallocAsync((void **)&new_deg, sizeof(int64_t) * (n + 1), s));
+  unsigned md = 0;
+  uint32_t *SK = nk, *SV = nv;
   if (n > 0) {
-    item_fill<<<grid_for(n, 256), 256, 0, s>>>(g->in_rp, n, W, units, g->items);
+    max_indeg<<<grid_for(n, 256), 256, 0, s>>>(rp_old, n, maxdeg);
+    node_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(rp_old, n, maxdeg, nk, nv);
+    BUILD_TRY(cudaGetLastError());
+    BUILD_TRY(cudaMemcpyAsync(&md, maxdeg, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    BUILD_TRY(cudaStreamSynchronize(s));
+    bool alt = false;
+    BUILD_ST(radix_sort_pairs_u32(nk, nv, nk2, nv2, n, bits_for((int64_t)md + 1), &alt, s));
+    if (alt) { SK = nk2; SV = nv2; }
+    permute_nodes<<<grid_for(n, 256), 256, 0, s>>>(SK, SV, n, maxdeg, g->perm, inv_perm, new_deg,
+                                                   deg_old, g->deg);
+    BUILD_TRY(cudaGetLastError());
+    if (g->weighted) {
+      permute_dmask<<<(unsigned)ceil_div<int64_t>(n, 256), 256, 0, s>>>(g->perm, n, dmask_old, g->dmask_w);
+      BUILD_TRY(cudaGetLastError());
+    }
+  } else {
+    BUILD_TRY(cudaMemsetAsync(new_deg, 0, sizeof(int64_t), s));
+  }
+  BUILD_ST(exclusive_scan_i64(new_deg, g->in_rp, n + 1, s));
+  if (m > 0) {
+    scatter_edges<<<grid_for(m, 256), 256, 0, s>>>(K, O, m, rp_old, inv_perm, g->in_rp, src, val_out,
+                                                   g->in_col, g->in_val);
     BUILD_TRY(cudaGetLastError());
   }
-  BUILD_TRY(cudaMallocAsync((void **)&maxc, sizeof(int), s));
-  BUILD_TRY(cudaMemsetAsync(maxc, 0, sizeof(int), s));
-  if (n_items > 0) {
-    max_chunks_kernel<<<grid_for(n_items, 256), 256, 0, s>>>(g->items, n_items, maxc);
+  // plan: degree classes over the (non-increasing) relabelled degrees
+  const int L = 4;  // target edges per lane
+  const int64_t thr_h[7] = {kHubThreshold + 1, 32 * L, 16 * L, 8 * L, 4 * L, 2 * L, 0};
+  int64_t cnt_h[7] = {0, 0, 0, 0, 0, 0, 0};
+  BUILD_TRY(cudaMallocAsync((void **)&small, sizeof(int64_t) * 16, s));
+  if (n > 0) {
+    BUILD_TRY(cudaMemcpyAsync(small, thr_h, sizeof(thr_h), cudaMemcpyHostToDevice, s));
+    count_ge<<<1, 32, 0, s>>>(SK, n, maxdeg, small, 7, small + 8);
     BUILD_TRY(cudaGetLastError());
+    BUILD_TRY(cudaMemcpyAsync(cnt_h, small + 8, sizeof(cnt_h), cudaMemcpyDeviceToHost, s));
+    BUILD_TRY(cudaStreamSynchronize(s));
   }
-  int mc = 0;
-  BUILD_TRY(cudaMemcpyAsync(&mc, maxc, sizeof(int), cudaMemcpyDeviceToHost, s));
+  Plan &pl = g->plan;
+  pl = Plan{};
+  pl.n_hub = (int32_t)cnt_h[0];
+  const int sws[6] = {32, 16, 8, 4, 2, 1};
+  int64_t row = pl.n_hub, task = 0;
+  for (int c = 0; c < 6; ++c) {
+    const int64_t end = c == 5 ? n : std::max<int64_t>(row, cnt_h[c + 1]);
+    if (end > row) {
+      Segment &sg = pl.segs[pl.n_segs++];
+      sg.row_begin = (int32_t)row;
+      sg.row_end = (int32_t)end;
+      sg.sw = sws[c];
+      sg.task_begin = (int32_t)task;  // relative to the first segment task
+      task += ceil_div<int64_t>((end - row) * sws[c], 32);
+      row = end;
+    }
+  }
+  // hub tasks
+  if (pl.n_hub > 0) {
+    int64_t *nch = nullptr;
+    BUILD_TRY(cudaMallocAsync((void **)&nch, sizeof(int64_t) * (pl.n_hub + 1), s));
+    hub_chunks<<<grid_for(pl.n_hub + 1, 256), 256, 0, s>>>(g->in_rp, pl.n_hub, nch);
+    Status s2 = exclusive_scan_i64(nch, nch, pl.n_hub + 1, s);
+    int64_t nht = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && s2.code == GOPS_OK)
+      e = cudaMemcpyAsync(&nht, nch + pl.n_hub, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMalloc(&g->hub_first, sizeof(int32_t) * (pl.n_hub + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&g->hub_task_row, sizeof(int32_t) * std::max<int64_t>(nht, 1));
+    if (e == cudaSuccess) {
+      hub_fill<<<grid_for(pl.n_hub + 1, 256), 256, 0, s>>>(nch, pl.n_hub, g->hub_first, g->hub_task_row);
+      e = cudaGetLastError();
+    }
+    free_async(nch, s);
+    if (s2.code != GOPS_OK) { cleanup(); return s2; }
+    BUILD_TRY(e);
+    pl.n_hub_tasks = (int32_t)nht;
+  }
+  for (int i = 0; i < pl.n_segs; ++i) pl.segs[i].task_begin += pl.n_hub_tasks;
+  if (task + pl.n_hub_tasks >= INT32_MAX) { cleanup(); return Status{GOPS_ERR_INVALID, "graph too large"}; }
+  pl.n_tasks = (int32_t)(task + pl.n_hub_tasks);
   BUILD_TRY(cudaStreamSynchronize(s));
-  g->max_chunks = mc;
   cleanup();
   return Status::ok();
 #undef BUILD_TRY
+#undef BUILD_ST
 }
 
 // Dense AdjacencyMatrix -> device out-CSR -> the build above.

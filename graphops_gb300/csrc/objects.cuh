@@ -8,15 +8,31 @@
 
 namespace gops {
 
-// One unit of work of the pull kernels.  Normal items are a run of whole rows
-// [r0, r1) whose in-edges fit the shared-memory stage; a row with more than
-// `long_row` in-edges is split into `nchunks` items (first = index of its
-// chunk 0) whose partial sums are combined by the chunk that finishes last.
-struct Item {
-  int32_t r0, r1;
-  int32_t first;    // -1 for a normal item
-  int32_t nchunks;  // chunks of the long row (0 for a normal item)
+// Device layout of a graph.  Nodes are relabelled once at build time by a
+// stable sort on in-degree (descending): row i of the in-edge CSR is node
+// perm[i].  Rows of equal degree class are then contiguous, so each class is
+// one "segment" processed with one sub-warp width, and the most-gathered
+// nodes sit together at the front of every per-node vector.
+constexpr int kMaxSegments = 8;
+
+struct Segment {
+  int32_t row_begin, row_end;  // rows [row_begin, row_end) of this class
+  int32_t sw;                  // lanes per row (1..32); 32/sw rows per warp task
+  int32_t task_begin;          // first task index of the segment
 };
+
+struct Plan {
+  // hub rows (in-degree > kHubThreshold) are rows [0, n_hub); row h is split
+  // into tasks hub_first[h] .. hub_first[h+1]-1 of kHubChunk edges each
+  int32_t n_hub = 0;
+  int32_t n_hub_tasks = 0;
+  int32_t n_segs = 0;
+  int32_t n_tasks = 0;  // n_hub_tasks + tasks of all segments
+  Segment segs[kMaxSegments];
+};
+
+constexpr int kHubChunk = 1024;      // edges per hub task (one warp)
+constexpr int kHubThreshold = 4096;  // rows above this in-degree are hubs
 
 // Solver workspace held by a graph (allocated on first solve, reused).
 struct Workspace {
@@ -26,10 +42,10 @@ struct Workspace {
   float2 *acc = nullptr;                // x while in the double-float phase
   float *tail = nullptr;                // sum of the FP32-phase steps
   float2 *pdf = nullptr;                // personalization (normalised) as double-float
-  double *scores = nullptr;             // final x = acc + tail
+  double *scores = nullptr;             // final x = acc + tail, in node order
   long long *sums = nullptr;            // 3 slots x {dangling, l1, nonfinite, spare}
-  float2 *lpart = nullptr;              // long-row chunk partials, per item
-  unsigned *lcnt = nullptr;             // long-row arrival counters, per item
+  float2 *lpart = nullptr;              // hub chunk partials, per hub task
+  unsigned *lcnt = nullptr;             // hub arrival counters, per hub row
   struct SolveState *state = nullptr;   // device-side run record
 };
 
@@ -47,17 +63,17 @@ struct Graph {
   struct Ctx *ctx = nullptr;
   int64_t n = 0, m = 0;
   bool weighted = false;
-  // in-edge CSR (row v lists the sources u of edges u->v, in source order)
+  // in-edge CSR over relabelled ids: row i lists the (relabelled) sources of
+  // the edges into node perm[i], in ascending original source order
   int64_t *in_rp = nullptr;
   int32_t *in_col = nullptr;
-  float *in_val = nullptr;    // max(w,0)/weight-sum of the source (weighted graphs)
-  float *deg = nullptr;       // out-degree as float; 0 marks an unweighted-dangling node
-  uint32_t *dmask_w = nullptr;  // weighted-dangling bitmask (weight sum == 0)
-  // work partition of the pull kernels
-  Item *items = nullptr;
-  int32_t n_items = 0;
-  int32_t window = 0;  // edge window W (normal items hold < 2W in-edges)
-  int32_t max_chunks = 0;
+  float *in_val = nullptr;      // max(w,0)/weight-sum of the source (weighted graphs)
+  float *deg = nullptr;         // out-degree (relabelled order); 0 = unweighted-dangling
+  uint32_t *dmask_w = nullptr;  // weighted-dangling bitmask (relabelled order)
+  int32_t *perm = nullptr;      // relabelled row i -> original node id
+  int32_t *hub_first = nullptr;     // n_hub + 1 task offsets
+  int32_t *hub_task_row = nullptr;  // hub task -> hub row
+  Plan plan;
   Workspace ws;
 };
 
@@ -83,5 +99,6 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
                                        const int32_t *d_out_col, const double *d_w);
 Status workspace_ensure(Ctx *ctx, Graph *g);
 void workspace_free(Workspace &ws);
+void graph_free_device(Graph &g);
 
 }  // namespace gops

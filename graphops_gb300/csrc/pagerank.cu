@@ -21,6 +21,15 @@
 // (dangling mass, L1 norm) are exact 64-bit fixed-point integer sums, so they
 // are independent of summation order and bit-reproducible.
 //
+// Work layout.  Rows are relabelled by in-degree (descending) at build time,
+// so each degree class is a contiguous segment.  A warp task covers 32/sw
+// consecutive rows of one segment with sw lanes per row (sw chosen so a lane
+// has about four edges); every lane keeps four independent column loads and
+// four gathers in flight, and a row's sum is an xor-shuffle reduction over its
+// sw lanes.  Rows above kHubThreshold in-edges are split into kHubChunk-edge
+// warp tasks whose partials are combined, in chunk order, by the task that
+// finishes last.  No block-wide barrier sits on the edge path.
+//
 // Convergence is decided on the device: the kernel for step k first reads
 // diff_{k-1}; if it is below tol (or k-1 == max_iterations) it records the
 // run and every block returns, so the host may launch steps ahead.
@@ -36,7 +45,6 @@ enum Mode : int { kPlain = 0, kWeighted = 1, kPpr = 2 };
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / kWarp;
-constexpr int kRowCapIter = 256;  // must match kRowCap of the item builder
 constexpr double kTheta = 1e-2;   // double-float phase while ||r||_1 >= kTheta
 
 struct IterParams {
@@ -46,9 +54,9 @@ struct IterParams {
   const float *val;
   const float *deg;
   const uint32_t *dmask;
-  const Item *items;
-  int n_items;
-  int cap;  // stage capacity in edges (2W)
+  const int32_t *hub_first;
+  const int32_t *hub_task_row;
+  Plan plan;
   const float2 *gdf_in;
   float2 *gdf_out;
   const float *gf_in;
@@ -201,77 +209,113 @@ __device__ bool prologue(const IterParams &p, df *dsum) {
   return true;
 }
 
+// Sum of a row's terms over edges [eb, ee): lane li of the sub-warp takes
+// edges eb+li, eb+li+SW, ... (four per round, loads issued together).
+template <class P, int MODE, int SW>
+__device__ __forceinline__ typename P::T row_sum(const IterParams &p, int64_t eb, int64_t ee, int li) {
+  using T = typename P::T;
+  T s = P::zero();
+  for (int64_t e = eb + li; e < ee; e += 4 * SW) {
+    const bool o1 = e + SW < ee, o2 = e + 2 * SW < ee, o3 = e + 3 * SW < ee;
+    const int32_t c0 = __ldg(&p.col[e]);
+    const int32_t c1 = o1 ? __ldg(&p.col[e + SW]) : 0;
+    const int32_t c2 = o2 ? __ldg(&p.col[e + 2 * SW]) : 0;
+    const int32_t c3 = o3 ? __ldg(&p.col[e + 3 * SW]) : 0;
+    float w0 = 1.f, w1 = 1.f, w2 = 1.f, w3 = 1.f;
+    if (MODE == kWeighted) {
+      w0 = __ldg(&p.val[e]);
+      w1 = o1 ? __ldg(&p.val[e + SW]) : 0.f;
+      w2 = o2 ? __ldg(&p.val[e + 2 * SW]) : 0.f;
+      w3 = o3 ? __ldg(&p.val[e + 3 * SW]) : 0.f;
+    }
+    const T g0 = P::load_g(p, c0);
+    const T g1 = o1 ? P::load_g(p, c1) : P::zero();
+    const T g2 = o2 ? P::load_g(p, c2) : P::zero();
+    const T g3 = o3 ? P::load_g(p, c3) : P::zero();
+    if (MODE == kWeighted) {
+      s = P::add(s, P::scale(g0, w0));
+      if (o1) s = P::add(s, P::scale(g1, w1));
+      if (o2) s = P::add(s, P::scale(g2, w2));
+      if (o3) s = P::add(s, P::scale(g3, w3));
+    } else {
+      s = P::add(s, g0);
+      if (o1) s = P::add(s, g1);
+      if (o2) s = P::add(s, g2);
+      if (o3) s = P::add(s, g3);
+    }
+  }
+  return s;
+}
+
+template <class P, int MODE, int SW>
+__device__ __forceinline__ void row_task(const IterParams &p, const Segment &sg, int local, int lane,
+                                         df dsum, Acc &a) {
+  using T = typename P::T;
+  const int64_t row = (int64_t)sg.row_begin + (int64_t)local * (32 / SW) + lane / SW;
+  const int li = lane & (SW - 1);
+  const bool valid = row < sg.row_end;
+  int64_t eb = 0, ee = 0;
+  if (valid) {
+    eb = __ldg(&p.rp[row]);
+    ee = __ldg(&p.rp[row + 1]);
+  }
+  T s = row_sum<P, MODE, SW>(p, eb, ee, li);
+#pragma unroll
+  for (int o = SW >> 1; o > 0; o >>= 1) s = P::add(s, P::shfl(s, o));
+  if (valid && li == 0) epilogue<P, MODE>(p, row, s, dsum, a);
+}
+
+template <class P, int MODE>
+__device__ __forceinline__ void hub_task(const IterParams &p, int t, int lane, df dsum, Acc &a) {
+  using T = typename P::T;
+  const int32_t h = __ldg(&p.hub_task_row[t]);
+  const int32_t first = __ldg(&p.hub_first[h]);
+  const int32_t nch = __ldg(&p.hub_first[h + 1]) - first;
+  const int64_t rb = __ldg(&p.rp[h]), re = __ldg(&p.rp[h + 1]);
+  const int64_t cs = rb + (int64_t)(t - first) * kHubChunk;
+  const int64_t ce = min(re, cs + (int64_t)kHubChunk);
+  T s = row_sum<P, MODE, 32>(p, cs, ce, lane);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s = P::add(s, P::shfl(s, o));
+  if (lane == 0) {
+    p.lpart[t] = P::pack(s);
+    __threadfence();
+    const unsigned tk = atomicAdd(&p.lcnt[h], 1u);
+    if (tk == (unsigned)(nch - 1)) {
+      __threadfence();
+      T sum = P::zero();
+      for (int j = 0; j < nch; ++j) sum = P::add(sum, P::unpack(__ldcg(&p.lpart[first + j])));
+      p.lcnt[h] = 0;
+      epilogue<P, MODE>(p, h, sum, dsum, a);
+    }
+  }
+}
+
 template <class P, int MODE>
 __global__ void __launch_bounds__(kThreads) iterate_kernel(IterParams p) {
-  using T = typename P::T;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *stage = reinterpret_cast<T *>(smem_raw);
-  __shared__ int roff[kRowCapIter + 1];
-  __shared__ T rowsum[kRowCapIter];
-  __shared__ T wred[kWarps];
-  __shared__ int last_flag;
   __shared__ long long bred[2][kWarps];
   __shared__ int bbad[kWarps];
-
   df dsum;
   if (!prologue<P::kDF>(p, &dsum)) return;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarps = gridDim.x * kWarps;
   Acc a;
-
-  for (int item = blockIdx.x; item < p.n_items; item += gridDim.x) {
-    const Item it = p.items[item];
-    if (it.first < 0) {
-      // ---- a run of whole rows: stage products, reduce per row, epilogue
-      const int r0 = it.r0, nr = it.r1 - it.r0;
-      const int64_t e0 = p.rp[r0];
-      for (int i = tid; i <= nr; i += kThreads) roff[i] = (int)(p.rp[r0 + i] - e0);
-      __syncthreads();
-      const int ne = roff[nr];
-      for (int j = tid; j < ne; j += kThreads) stage[j] = edge_term<P, MODE>(p, e0 + j);
-      __syncthreads();
-      int sw = 1;
-      const int avg = nr > 0 ? (ne + nr - 1) / nr : 1;
-      while (sw < avg && sw < 32) sw <<= 1;
-      const int per_pass = kThreads / sw;
-      for (int base = 0; base < nr; base += per_pass) {
-        const int rr = base + tid / sw, li = tid & (sw - 1);
-        T s = P::zero();
-        if (rr < nr)
-          for (int j = roff[rr] + li; j < roff[rr + 1]; j += sw) s = P::add(s, stage[j]);
-        for (int o = sw >> 1; o > 0; o >>= 1) s = P::add(s, P::shfl(s, o));
-        if (rr < nr && li == 0) rowsum[rr] = s;
-      }
-      __syncthreads();
-      for (int i = tid; i < nr; i += kThreads) epilogue<P, MODE>(p, r0 + i, rowsum[i], dsum, a);
-      __syncthreads();
-    } else {
-      // ---- one chunk of a hub row; the chunk that arrives last combines
-      const int64_t v = it.r0;
-      const int c = item - it.first;
-      const int64_t cs = p.rp[v] + (int64_t)c * p.cap;
-      const int64_t ce = min(p.rp[v + 1], cs + (int64_t)p.cap);
-      T s = P::zero();
-      for (int64_t e = cs + tid; e < ce; e += kThreads) s = P::add(s, edge_term<P, MODE>(p, e));
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s = P::add(s, P::shfl(s, o));
-      if (lane == 0) wred[wid] = s;
-      __syncthreads();
-      if (tid == 0) {
-        T tot = wred[0];
-        for (int w = 1; w < kWarps; ++w) tot = P::add(tot, wred[w]);
-        p.lpart[item] = P::pack(tot);
-        __threadfence();
-        const unsigned t = atomicAdd(&p.lcnt[it.first], 1u);
-        last_flag = (t == (unsigned)(it.nchunks - 1));
-        if (last_flag) {
-          __threadfence();
-          T sum = P::zero();
-          for (int j = 0; j < it.nchunks; ++j) sum = P::add(sum, P::unpack(__ldcg(&p.lpart[it.first + j])));
-          p.lcnt[it.first] = 0;
-          epilogue<P, MODE>(p, v, sum, dsum, a);
-        }
-      }
-      __syncthreads();
+  for (int t = blockIdx.x * kWarps + wid; t < p.plan.n_tasks; t += nwarps) {
+    if (t < p.plan.n_hub_tasks) {
+      hub_task<P, MODE>(p, t, lane, dsum, a);
+      continue;
+    }
+    int si = 0;
+    while (si + 1 < p.plan.n_segs && t >= p.plan.segs[si + 1].task_begin) ++si;
+    const Segment sg = p.plan.segs[si];
+    const int local = t - sg.task_begin;
+    switch (sg.sw) {
+      case 32: row_task<P, MODE, 32>(p, sg, local, lane, dsum, a); break;
+      case 16: row_task<P, MODE, 16>(p, sg, local, lane, dsum, a); break;
+      case 8: row_task<P, MODE, 8>(p, sg, local, lane, dsum, a); break;
+      case 4: row_task<P, MODE, 4>(p, sg, local, lane, dsum, a); break;
+      case 2: row_task<P, MODE, 2>(p, sg, local, lane, dsum, a); break;
+      default: row_task<P, MODE, 1>(p, sg, local, lane, dsum, a); break;
     }
   }
 
@@ -280,7 +324,7 @@ __global__ void __launch_bounds__(kThreads) iterate_kernel(IterParams p) {
   int bad = warp_or(a.bad);
   if (lane == 0) { bred[0][wid] = l1; bred[1][wid] = dg; bbad[wid] = bad; }
   __syncthreads();
-  if (tid == 0) {
+  if (threadIdx.x == 0) {
     long long t1 = 0, t2 = 0;
     int tb = 0;
     for (int w = 0; w < kWarps; ++w) { t1 += bred[0][w]; t2 += bred[1][w]; tb |= bbad[w]; }
@@ -324,10 +368,19 @@ __global__ void __launch_bounds__(kThreads) init_kernel(IterParams p) {
   }
 }
 
-__global__ void finalize_kernel(int64_t n, const float2 *acc, const float *tail, double *x) {
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (int64_t)gridDim.x * blockDim.x)
-    x[v] = (double)acc[v].x + (double)acc[v].y + (double)tail[v];
+// x in original node order: x[perm[i]] = acc[i] + tail[i].
+__global__ void finalize_kernel(int64_t n, const float2 *acc, const float *tail, const int32_t *perm,
+                                double *x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[perm[i]] = (double)acc[i].x + (double)acc[i].y + (double)tail[i];
+}
+
+// Personalization into relabelled order: dst[i] = src[perm[i]].
+__global__ void permute_pdf(int64_t n, const float2 *src, const int32_t *perm, float2 *dst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[perm[i]];
 }
 
 // --------------------------------------------------------------------------
@@ -345,7 +398,8 @@ Status workspace_ensure(Ctx *ctx, Graph *g) {
   Workspace &ws = g->ws;
   if (ws.sums) return Status::ok();
   const size_t n = (size_t)std::max<int64_t>(g->n, 1);
-  const size_t ni = (size_t)std::max<int32_t>(g->n_items, 1);
+  const size_t nht = (size_t)std::max<int32_t>(g->plan.n_hub_tasks, 1);
+  const size_t nh = (size_t)std::max<int32_t>(g->plan.n_hub, 1);
   GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[0], sizeof(float2) * n));
   GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[1], sizeof(float2) * n));
   GOPS_CUDA_TRY(cudaMalloc(&ws.gf[0], sizeof(float) * n));
@@ -354,8 +408,8 @@ Status workspace_ensure(Ctx *ctx, Graph *g) {
   GOPS_CUDA_TRY(cudaMalloc(&ws.tail, sizeof(float) * n));
   GOPS_CUDA_TRY(cudaMalloc(&ws.pdf, sizeof(float2) * n));
   GOPS_CUDA_TRY(cudaMalloc(&ws.scores, sizeof(double) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.lpart, sizeof(float2) * ni));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.lcnt, sizeof(unsigned) * ni));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.lpart, sizeof(float2) * nht));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.lcnt, sizeof(unsigned) * nh));
   GOPS_CUDA_TRY(cudaMalloc(&ws.state, sizeof(SolveState)));
   GOPS_CUDA_TRY(cudaMalloc(&ws.sums, sizeof(long long) * 12));
   ws.n = g->n;
@@ -365,13 +419,12 @@ Status workspace_ensure(Ctx *ctx, Graph *g) {
 namespace {
 
 template <class P, int MODE>
-int grid_for_iter(const Ctx *ctx, const Graph *g, size_t smem) {
+int grid_for_iter(const Ctx *ctx, const Graph *g) {
   int occ = 0;
-  cudaFuncSetAttribute(iterate_kernel<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, iterate_kernel<P, MODE>, kThreads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, iterate_kernel<P, MODE>, kThreads, 0);
   occ = std::max(1, occ);
-  return (int)std::max<int64_t>(1, std::min<int64_t>(g->n_items, (int64_t)ctx->num_sms * occ));
+  const int64_t blocks_needed = ceil_div<int64_t>(std::max<int32_t>(g->plan.n_tasks, 1), kWarps);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(blocks_needed, (int64_t)ctx->num_sms * occ));
 }
 
 template <int MODE>
@@ -385,9 +438,9 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   p.val = g->in_val;
   p.deg = g->deg;
   p.dmask = g->dmask_w;
-  p.items = g->items;
-  p.n_items = g->n_items;
-  p.cap = 2 * g->window;
+  p.hub_first = g->hub_first;
+  p.hub_task_row = g->hub_task_row;
+  p.plan = g->plan;
   p.acc = ws.acc;
   p.tail = ws.tail;
   p.pdf = ws.pdf;
@@ -409,7 +462,7 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
 
   GOPS_CUDA_TRY(cudaMemsetAsync(ws.sums, 0, sizeof(long long) * 12, s));
   GOPS_CUDA_TRY(cudaMemsetAsync(ws.state, 0, sizeof(SolveState), s));
-  GOPS_CUDA_TRY(cudaMemsetAsync(ws.lcnt, 0, sizeof(unsigned) * std::max<int32_t>(g->n_items, 1), s));
+  GOPS_CUDA_TRY(cudaMemsetAsync(ws.lcnt, 0, sizeof(unsigned) * std::max<int32_t>(g->plan.n_hub, 1), s));
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   uint64_t launches = 0;
   // step 0
@@ -423,10 +476,8 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   ++launches;
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
 
-  const size_t smem_df = sizeof(float2) * (size_t)p.cap;
-  const size_t smem_f = sizeof(float) * (size_t)p.cap;
-  const int grid_df = grid_for_iter<PrecDF, MODE>(ctx, g, smem_df);
-  const int grid_f = grid_for_iter<PrecF32, MODE>(ctx, g, smem_f);
+  const int grid_df = grid_for_iter<PrecDF, MODE>(ctx, g);
+  const int grid_f = grid_for_iter<PrecF32, MODE>(ctx, g);
   bool f32_known = false;
   unsigned long long k = 1;
   const int chunk = 4;
@@ -453,14 +504,14 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
       if (!f32_known) {
         GOPS_TRY(timed_launch(true));
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 2], s));
-        iterate_kernel<PrecDF, MODE><<<grid_df, kThreads, smem_df, s>>>(p);
+        iterate_kernel<PrecDF, MODE><<<grid_df, kThreads, 0, s>>>(p);
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 1], s));
         ++launches;
       }
       if (k >= 2) {
         GOPS_TRY(timed_launch(false));
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 2], s));
-        iterate_kernel<PrecF32, MODE><<<grid_f, kThreads, smem_f, s>>>(p);
+        iterate_kernel<PrecF32, MODE><<<grid_f, kThreads, 0, s>>>(p);
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 1], s));
         ++launches;
       }
@@ -476,7 +527,7 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   }
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   finalize_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(g->n, 256), 4096)),
-                    256, 0, s>>>(g->n, ws.acc, ws.tail, ws.scores);
+                    256, 0, s>>>(g->n, ws.acc, ws.tail, g->perm, ws.scores);
   GOPS_CUDA_TRY(cudaGetLastError());
   ++launches;
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
@@ -541,9 +592,14 @@ Status solve(Ctx *ctx, Graph *g, const gops_config *cfg, int mode, const double 
       const df d = df_from_double(v);
       pdf[(size_t)i] = make_float2(d.hi, d.lo);
     }
-    GOPS_CUDA_TRY(cudaMemcpyAsync(g->ws.pdf, pdf.data(), sizeof(float2) * (size_t)n,
+    // staged in gdf[1] (free before the solve starts), then relabelled
+    GOPS_CUDA_TRY(cudaMemcpyAsync(g->ws.gdf[1], pdf.data(), sizeof(float2) * (size_t)n,
                                   cudaMemcpyHostToDevice, ctx->stream));
+    permute_pdf<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), 4096)), 256, 0,
+                  ctx->stream>>>(n, g->ws.gdf[1], g->perm, g->ws.pdf);
+    GOPS_CUDA_TRY(cudaGetLastError());
     ctx->stats.h2d_bytes += sizeof(float2) * (size_t)n;
+    ctx->stats.kernel_launches += 1;
     GOPS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     if (!std::isfinite(pv_l1)) pv_l1 = 1.0;
   }

@@ -12,7 +12,9 @@ import threading
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libgops.so")
+# GOPS_LIBRARY may name another build of the same ABI (e.g. one compiled with
+# different tuning macros); by default the in-tree build is loaded.
+LIB_PATH = os.environ.get("GOPS_LIBRARY") or os.path.join(_HERE, "libgops.so")
 
 GOPS_OK = 0
 GOPS_ERR_INVALID = 1

@@ -318,7 +318,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(cudaGetLastError());
   }
   // plan: degree classes over the (non-increasing) relabelled degrees
-  const int L = 4;  // target edges per lane
+  const int L = kLaneEdges;
   const int64_t thr_h[7] = {kHubThreshold + 1, 32 * L, 16 * L, 8 * L, 4 * L, 2 * L, 0};
   int64_t cnt_h[7] = {0, 0, 0, 0, 0, 0, 0};
   BUILD_TRY(cudaMallocAsync((void **)&small, sizeof(int64_t) * 16, s));
@@ -342,7 +342,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
       sg.row_end = (int32_t)end;
       sg.sw = sws[c];
       sg.task_begin = (int32_t)task;  // relative to the first segment task
-      task += ceil_div<int64_t>((end - row) * sws[c], 32);
+      task += ceil_div<int64_t>((end - row) * sws[c], 32 * kRowsPerLane);
       row = end;
     }
   }

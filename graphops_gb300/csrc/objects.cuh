@@ -33,6 +33,16 @@ struct Plan {
 
 constexpr int kHubChunk = 1024;      // edges per hub task (one warp)
 constexpr int kHubThreshold = 4096;  // rows above this in-degree are hubs
+#ifndef GOPS_ROWS_PER_LANE
+#define GOPS_ROWS_PER_LANE 2
+#endif
+#ifndef GOPS_LANE_EDGES
+#define GOPS_LANE_EDGES 4
+#endif
+// rows interleaved per sub-warp in one warp task
+constexpr int kRowsPerLane = GOPS_ROWS_PER_LANE;
+// target edges per lane when choosing a degree class's sub-warp width
+constexpr int kLaneEdges = GOPS_LANE_EDGES;
 
 // Solver workspace held by a graph (allocated on first solve, reused).
 struct Workspace {

@@ -45,6 +45,14 @@ enum Mode : int { kPlain = 0, kWeighted = 1, kPpr = 2 };
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / kWarp;
+#ifndef GOPS_UNROLL
+#define GOPS_UNROLL 4
+#endif
+#ifndef GOPS_MINB
+#define GOPS_MINB 4
+#endif
+constexpr int kUnroll = GOPS_UNROLL;   // edges per lane per round and row
+constexpr int kMinBlocks = GOPS_MINB;  // occupancy hint for the iteration kernels
 constexpr double kTheta = 1e-2;   // double-float phase while ||r||_1 >= kTheta
 
 struct IterParams {
@@ -105,72 +113,75 @@ struct PrecF32 {
   __device__ static T unpack(float2 v) { return v.x; }
 };
 
-__device__ __forceinline__ bool dangling(const IterParams &p, int mode, int64_t v) {
-  if (mode == kWeighted) return (__ldg(&p.dmask[v >> 5]) >> (v & 31)) & 1u;
-  return __ldg(&p.deg[v]) == 0.0f;
-}
-
 struct Acc {
   long long l1 = 0, dang = 0;
   int bad = 0;
 };
 
+// Per-row inputs of the epilogue, loaded before the row's edges so their
+// latency overlaps the edge loads: the running x part (acc in the
+// double-float phase, tail in the FP32 phase), the out-degree, the dangling
+// flag and the personalization entry.
+struct RowIn {
+  float2 x;
+  float2 red;
+  float deg;
+  int dang;
+};
+
+template <class P, int MODE>
+__device__ __forceinline__ RowIn row_in(const IterParams &p, int64_t v) {
+  RowIn in;
+  if constexpr (P::kDF) in.x = p.acc[v];
+  else in.x = make_float2(p.tail[v], 0.0f);
+  in.red = (MODE == kPpr) ? p.pdf[v] : make_float2(p.inv_n.hi, p.inv_n.lo);
+  if (MODE == kWeighted) {
+    in.deg = 1.0f;
+    in.dang = (__ldg(&p.dmask[v >> 5]) >> (v & 31)) & 1u;
+  } else {
+    in.deg = __ldg(&p.deg[v]);
+    in.dang = in.deg == 0.0f;
+  }
+  return in;
+}
+
 // Row v's new step value from its gathered sum s.
 template <int MODE>
-__device__ __forceinline__ void epilogue_df(const IterParams &p, int64_t v, df s, df dsum, Acc &a) {
-  const df red = (MODE == kPpr) ? PrecDF::unpack(p.pdf[v]) : p.inv_n;
+__device__ __forceinline__ void epilogue_df(const IterParams &p, int64_t v, df s, df dsum,
+                                            const RowIn &in, Acc &a) {
+  const df red = {in.red.x, in.red.y};
   df r = df_mul(p.d, df_add(s, df_mul(dsum, red)));
   if (p.k == 1) r = df_add(df_add(df_mul(p.omd, red), r), df_neg(red));  // F(x_0) - x_0
-  const float2 ao = p.acc[v];
-  const df an = df_add({ao.x, ao.y}, r);
+  const df an = df_add({in.x.x, in.x.y}, r);
   p.acc[v] = make_float2(an.hi, an.lo);
   const df ar = r.hi < 0.0f ? df_neg(r) : r;
   a.l1 += fx_of(ar.hi, p.fx_scale) + fx_of(ar.lo, p.fx_scale);
   a.bad |= !isfinite(r.hi);
+  if (in.dang) a.dang += fx_of(r.hi, p.fx_scale) + fx_of(r.lo, p.fx_scale);
   df g = r;
-  if (MODE != kWeighted) {
-    const float dg = __ldg(&p.deg[v]);
-    g = dg > 0.0f ? df_div_f(r, dg) : df{0.0f, 0.0f};
-    if (dg == 0.0f) a.dang += fx_of(r.hi, p.fx_scale) + fx_of(r.lo, p.fx_scale);
-  } else if (dangling(p, MODE, v)) {
-    a.dang += fx_of(r.hi, p.fx_scale) + fx_of(r.lo, p.fx_scale);
-  }
+  if (MODE != kWeighted) g = in.deg > 0.0f ? df_div_f(r, in.deg) : df{0.0f, 0.0f};
   p.gdf_out[v] = make_float2(g.hi, g.lo);
   p.gf_out[v] = g.hi;
 }
 
 template <int MODE>
 __device__ __forceinline__ void epilogue_f32(const IterParams &p, int64_t v, float s, float dsum,
-                                             Acc &a) {
-  const float red = (MODE == kPpr) ? p.pdf[v].x : p.inv_n.hi;
-  const float r = p.d.hi * (s + dsum * red);
-  p.tail[v] += r;
+                                             const RowIn &in, Acc &a) {
+  const float r = p.d.hi * (s + dsum * in.red.x);
+  p.tail[v] = in.x.x + r;
   a.l1 += fx_of(fabsf(r), p.fx_scale);
   a.bad |= !isfinite(r);
+  if (in.dang) a.dang += fx_of(r, p.fx_scale);
   float g = r;
-  if (MODE != kWeighted) {
-    const float dg = __ldg(&p.deg[v]);
-    g = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
-    if (dg == 0.0f) a.dang += fx_of(r, p.fx_scale);
-  } else if (dangling(p, MODE, v)) {
-    a.dang += fx_of(r, p.fx_scale);
-  }
+  if (MODE != kWeighted) g = in.deg > 0.0f ? __fdiv_rn(r, in.deg) : 0.0f;
   p.gf_out[v] = g;
 }
 
 template <class P, int MODE>
-__device__ __forceinline__ void epilogue(const IterParams &p, int64_t v, typename P::T s,
-                                         df dsum, Acc &a) {
-  if constexpr (P::kDF) epilogue_df<MODE>(p, v, s, dsum, a);
-  else epilogue_f32<MODE>(p, v, s, dsum.hi, a);
-}
-
-template <class P, int MODE>
-__device__ __forceinline__ typename P::T edge_term(const IterParams &p, int64_t e) {
-  const int32_t u = __ldg(&p.col[e]);
-  typename P::T g = P::load_g(p, u);
-  if (MODE == kWeighted) g = P::scale(g, __ldg(&p.val[e]));
-  return g;
+__device__ __forceinline__ void epilogue(const IterParams &p, int64_t v, typename P::T s, df dsum,
+                                         const RowIn &in, Acc &a) {
+  if constexpr (P::kDF) epilogue_df<MODE>(p, v, s, dsum, in, a);
+  else epilogue_f32<MODE>(p, v, s, dsum.hi, in, a);
 }
 
 // Reads diff_{k-1}; decides whether the run is over and whether this kernel's
@@ -209,60 +220,76 @@ __device__ bool prologue(const IterParams &p, df *dsum) {
   return true;
 }
 
-// Sum of a row's terms over edges [eb, ee): lane li of the sub-warp takes
-// edges eb+li, eb+li+SW, ... (four per round, loads issued together).
-template <class P, int MODE, int SW>
-__device__ __forceinline__ typename P::T row_sum(const IterParams &p, int64_t eb, int64_t ee, int li) {
-  using T = typename P::T;
-  T s = P::zero();
-  for (int64_t e = eb + li; e < ee; e += 4 * SW) {
-    const bool o1 = e + SW < ee, o2 = e + 2 * SW < ee, o3 = e + 3 * SW < ee;
-    const int32_t c0 = __ldg(&p.col[e]);
-    const int32_t c1 = o1 ? __ldg(&p.col[e + SW]) : 0;
-    const int32_t c2 = o2 ? __ldg(&p.col[e + 2 * SW]) : 0;
-    const int32_t c3 = o3 ? __ldg(&p.col[e + 3 * SW]) : 0;
-    float w0 = 1.f, w1 = 1.f, w2 = 1.f, w3 = 1.f;
-    if (MODE == kWeighted) {
-      w0 = __ldg(&p.val[e]);
-      w1 = o1 ? __ldg(&p.val[e + SW]) : 0.f;
-      w2 = o2 ? __ldg(&p.val[e + 2 * SW]) : 0.f;
-      w3 = o3 ? __ldg(&p.val[e + 3 * SW]) : 0.f;
-    }
-    const T g0 = P::load_g(p, c0);
-    const T g1 = o1 ? P::load_g(p, c1) : P::zero();
-    const T g2 = o2 ? P::load_g(p, c2) : P::zero();
-    const T g3 = o3 ? P::load_g(p, c3) : P::zero();
-    if (MODE == kWeighted) {
-      s = P::add(s, P::scale(g0, w0));
-      if (o1) s = P::add(s, P::scale(g1, w1));
-      if (o2) s = P::add(s, P::scale(g2, w2));
-      if (o3) s = P::add(s, P::scale(g3, w3));
-    } else {
-      s = P::add(s, g0);
-      if (o1) s = P::add(s, g1);
-      if (o2) s = P::add(s, g2);
-      if (o3) s = P::add(s, g3);
-    }
+// R rows per sub-warp, their edges interleaved so that every lane keeps
+// R * kUnroll column loads, then R * kUnroll gathers, in flight.  Lane li of
+// a row's sub-warp takes edges eb+li, eb+li+SW, ... and adds them in that
+// order, so a row's sum does not depend on R or kUnroll.
+template <class P, int MODE, int R>
+__device__ __forceinline__ void rows_sum(const IterParams &p, const int32_t (&eb)[R],
+                                         const int32_t (&ee)[R], int li, int SW,
+                                         typename P::T (&s)[R]) {
+  int32_t len = 0;
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    s[q] = P::zero();
+    len = max(len, ee[q] - eb[q]);
   }
-  return s;
+  for (int32_t off = li; off < len; off += kUnroll * SW) {
+    int32_t c[R][kUnroll];
+    float w[R][kUnroll];
+    bool ok[R][kUnroll];
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+#pragma unroll
+      for (int j = 0; j < kUnroll; ++j) {
+        const int32_t e = eb[q] + off + j * SW;
+        ok[q][j] = e < ee[q];
+        c[q][j] = ok[q][j] ? __ldg(&p.col[e]) : 0;
+        w[q][j] = (MODE == kWeighted && ok[q][j]) ? __ldg(&p.val[e]) : 1.0f;
+      }
+    typename P::T g[R][kUnroll];
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+#pragma unroll
+      for (int j = 0; j < kUnroll; ++j) g[q][j] = ok[q][j] ? P::load_g(p, c[q][j]) : P::zero();
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+#pragma unroll
+      for (int j = 0; j < kUnroll; ++j)
+        if (ok[q][j]) s[q] = P::add(s[q], MODE == kWeighted ? P::scale(g[q][j], w[q][j]) : g[q][j]);
+  }
 }
 
-template <class P, int MODE, int SW>
+template <class P, int MODE>
 __device__ __forceinline__ void row_task(const IterParams &p, const Segment &sg, int local, int lane,
                                          df dsum, Acc &a) {
   using T = typename P::T;
-  const int64_t row = (int64_t)sg.row_begin + (int64_t)local * (32 / SW) + lane / SW;
+  constexpr int R = kRowsPerLane;
+  const int SW = sg.sw;
+  const int lg = 31 - __clz(SW);   // sw is a power of two
+  const int RPW = 32 >> lg;        // rows per warp per interleave slot
   const int li = lane & (SW - 1);
-  const bool valid = row < sg.row_end;
-  int64_t eb = 0, ee = 0;
-  if (valid) {
-    eb = __ldg(&p.rp[row]);
-    ee = __ldg(&p.rp[row + 1]);
-  }
-  T s = row_sum<P, MODE, SW>(p, eb, ee, li);
+  int64_t row[R];
+  int32_t eb[R], ee[R];
+  bool valid[R];
+  RowIn in[R];
 #pragma unroll
-  for (int o = SW >> 1; o > 0; o >>= 1) s = P::add(s, P::shfl(s, o));
-  if (valid && li == 0) epilogue<P, MODE>(p, row, s, dsum, a);
+  for (int q = 0; q < R; ++q) {
+    row[q] = (int64_t)sg.row_begin + ((int64_t)local * R + q) * RPW + (lane >> lg);
+    valid[q] = row[q] < sg.row_end;
+    eb[q] = valid[q] ? (int32_t)__ldg(&p.rp[row[q]]) : 0;
+    ee[q] = valid[q] ? (int32_t)__ldg(&p.rp[row[q] + 1]) : 0;
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q)
+    if (valid[q] && li == 0) in[q] = row_in<P, MODE>(p, row[q]);
+  T s[R];
+  rows_sum<P, MODE, R>(p, eb, ee, li, SW, s);
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    for (int o = SW >> 1; o > 0; o >>= 1) s[q] = P::add(s[q], P::shfl(s[q], o));
+    if (valid[q] && li == 0) epilogue<P, MODE>(p, row[q], s[q], dsum, in[q], a);
+  }
 }
 
 template <class P, int MODE>
@@ -271,14 +298,15 @@ __device__ __forceinline__ void hub_task(const IterParams &p, int t, int lane, d
   const int32_t h = __ldg(&p.hub_task_row[t]);
   const int32_t first = __ldg(&p.hub_first[h]);
   const int32_t nch = __ldg(&p.hub_first[h + 1]) - first;
-  const int64_t rb = __ldg(&p.rp[h]), re = __ldg(&p.rp[h + 1]);
-  const int64_t cs = rb + (int64_t)(t - first) * kHubChunk;
-  const int64_t ce = min(re, cs + (int64_t)kHubChunk);
-  T s = row_sum<P, MODE, 32>(p, cs, ce, lane);
+  const int32_t rb = (int32_t)__ldg(&p.rp[h]), re = (int32_t)__ldg(&p.rp[h + 1]);
+  const int32_t cs = rb + (t - first) * kHubChunk;
+  const int32_t eb[1] = {cs}, ee[1] = {min(re, cs + kHubChunk)};
+  T s[1];
+  rows_sum<P, MODE, 1>(p, eb, ee, lane, 32, s);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s = P::add(s, P::shfl(s, o));
+  for (int o = 16; o > 0; o >>= 1) s[0] = P::add(s[0], P::shfl(s[0], o));
   if (lane == 0) {
-    p.lpart[t] = P::pack(s);
+    p.lpart[t] = P::pack(s[0]);
     __threadfence();
     const unsigned tk = atomicAdd(&p.lcnt[h], 1u);
     if (tk == (unsigned)(nch - 1)) {
@@ -286,13 +314,14 @@ __device__ __forceinline__ void hub_task(const IterParams &p, int t, int lane, d
       T sum = P::zero();
       for (int j = 0; j < nch; ++j) sum = P::add(sum, P::unpack(__ldcg(&p.lpart[first + j])));
       p.lcnt[h] = 0;
-      epilogue<P, MODE>(p, h, sum, dsum, a);
+      const RowIn in = row_in<P, MODE>(p, h);
+      epilogue<P, MODE>(p, h, sum, dsum, in, a);
     }
   }
 }
 
 template <class P, int MODE>
-__global__ void __launch_bounds__(kThreads) iterate_kernel(IterParams p) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) iterate_kernel(IterParams p) {
   __shared__ long long bred[2][kWarps];
   __shared__ int bbad[kWarps];
   df dsum;
@@ -308,15 +337,7 @@ __global__ void __launch_bounds__(kThreads) iterate_kernel(IterParams p) {
     int si = 0;
     while (si + 1 < p.plan.n_segs && t >= p.plan.segs[si + 1].task_begin) ++si;
     const Segment sg = p.plan.segs[si];
-    const int local = t - sg.task_begin;
-    switch (sg.sw) {
-      case 32: row_task<P, MODE, 32>(p, sg, local, lane, dsum, a); break;
-      case 16: row_task<P, MODE, 16>(p, sg, local, lane, dsum, a); break;
-      case 8: row_task<P, MODE, 8>(p, sg, local, lane, dsum, a); break;
-      case 4: row_task<P, MODE, 4>(p, sg, local, lane, dsum, a); break;
-      case 2: row_task<P, MODE, 2>(p, sg, local, lane, dsum, a); break;
-      default: row_task<P, MODE, 1>(p, sg, local, lane, dsum, a); break;
-    }
+    row_task<P, MODE>(p, sg, t - sg.task_begin, lane, dsum, a);
   }
 
   // ---- block totals of the exact fixed-point sums -> one atomic each

@@ -23,7 +23,8 @@ L1_PARITY = 1e-6
 L1_TARGET = 1e-7
 L1_FIXTURE = 1e-8   # small unweighted fixtures: the double-float first phase keeps errors ~1e-9
 L1_FIXTURE_W = 1e-7  # weighted fixtures: FP32 transition weights max(w,0)/sum shift the chain by ~1e-8
-DIFF_REL = 1e-4      # diff_l1 of a step taken in the FP32 phase carries FP32 rounding
+DIFF_REL = 1e-2      # diff_l1 of a step taken in the FP32 phase carries accumulated FP32
+                     # rounding (observed up to ~1e-3 relative at step norms ~1e-10)
 
 
 def cfg(c):

@@ -43,8 +43,24 @@ namespace gops {
 
 enum Mode : int { kPlain = 0, kWeighted = 1, kPpr = 2 };
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;  // init / small kernels
 constexpr int kWarps = kThreads / kWarp;
+#ifndef GOPS_BLOCK
+#define GOPS_BLOCK 256
+#endif
+#ifndef GOPS_GCACHE
+#define GOPS_GCACHE 0
+#endif
+#ifndef GOPS_L1HINT
+#define GOPS_L1HINT 0
+#endif
+// iteration kernels: threads per block, and how many of the first (hottest,
+// after the in-degree relabelling) entries of the gathered vector each block
+// stages in shared memory (FP32 entries; half as many double-float ones)
+constexpr int kIterThreads = GOPS_BLOCK;
+constexpr int kIterWarps = kIterThreads / kWarp;
+constexpr int kGCache = GOPS_GCACHE;
+constexpr bool kL1Hint = GOPS_L1HINT != 0;
 #ifndef GOPS_UNROLL
 #define GOPS_UNROLL 4
 #endif
@@ -83,6 +99,27 @@ struct IterParams {
   unsigned long long k, max_iter;
 };
 
+// Streamed loads (column indices, transition weights): with kL1Hint they do
+// not allocate in L1, which then keeps the hot lines of the gathered vector.
+__device__ __forceinline__ int32_t ld_stream_i32(const int32_t *a) {
+  if constexpr (kL1Hint) {
+    int32_t v;
+    asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(a));
+    return v;
+  } else {
+    return __ldg(a);
+  }
+}
+__device__ __forceinline__ float ld_stream_f32(const float *a) {
+  if constexpr (kL1Hint) {
+    float v;
+    asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(a));
+    return v;
+  } else {
+    return __ldg(a);
+  }
+}
+
 // --------------------------------------------------------------------------
 // precision policies
 // --------------------------------------------------------------------------
@@ -92,9 +129,17 @@ struct PrecDF {
   __device__ static T zero() { return {0.0f, 0.0f}; }
   __device__ static T add(T a, T b) { return df_add(a, b); }
   __device__ static T shfl(T v, int m) { return shfl_xor_df(v, m, 32); }
-  __device__ static T load_g(const IterParams &p, int32_t u) {
-    float2 g = __ldg(&p.gdf_in[u]);
+  static constexpr int kCached = kGCache / 2;  // float2 entries staged in shared memory
+  __device__ static T load_g(const IterParams &p, const void *cache, int32_t u) {
+    float2 g;
+    if (kCached > 0 && u < kCached) g = reinterpret_cast<const float2 *>(cache)[u];
+    else g = __ldg(&p.gdf_in[u]);
     return {g.x, g.y};
+  }
+  __device__ static void stage(const IterParams &p, void *cache, int64_t n) {
+    float2 *c = reinterpret_cast<float2 *>(cache);
+    const int lim = (int)(n < (int64_t)kCached ? n : (int64_t)kCached);
+    for (int i = threadIdx.x; i < lim; i += blockDim.x) c[i] = __ldg(&p.gdf_in[i]);
   }
   __device__ static T scale(T g, float w) { return df_mul_f(g, w); }
   __device__ static float2 pack(T v) { return make_float2(v.hi, v.lo); }
@@ -107,7 +152,16 @@ struct PrecF32 {
   __device__ static T zero() { return 0.0f; }
   __device__ static T add(T a, T b) { return a + b; }
   __device__ static T shfl(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
-  __device__ static T load_g(const IterParams &p, int32_t u) { return __ldg(&p.gf_in[u]); }
+  static constexpr int kCached = kGCache;
+  __device__ static T load_g(const IterParams &p, const void *cache, int32_t u) {
+    if (kCached > 0 && u < kCached) return reinterpret_cast<const float *>(cache)[u];
+    return __ldg(&p.gf_in[u]);
+  }
+  __device__ static void stage(const IterParams &p, void *cache, int64_t n) {
+    float *c = reinterpret_cast<float *>(cache);
+    const int lim = (int)(n < (int64_t)kCached ? n : (int64_t)kCached);
+    for (int i = threadIdx.x; i < lim; i += blockDim.x) c[i] = __ldg(&p.gf_in[i]);
+  }
   __device__ static T scale(T g, float w) { return g * w; }
   __device__ static float2 pack(T v) { return make_float2(v, 0.0f); }
   __device__ static T unpack(float2 v) { return v.x; }
@@ -225,9 +279,9 @@ __device__ bool prologue(const IterParams &p, df *dsum) {
 // a row's sub-warp takes edges eb+li, eb+li+SW, ... and adds them in that
 // order, so a row's sum does not depend on R or kUnroll.
 template <class P, int MODE, int R>
-__device__ __forceinline__ void rows_sum(const IterParams &p, const int32_t (&eb)[R],
-                                         const int32_t (&ee)[R], int li, int SW,
-                                         typename P::T (&s)[R]) {
+__device__ __forceinline__ void rows_sum(const IterParams &p, const void *cache,
+                                         const int32_t (&eb)[R], const int32_t (&ee)[R], int li,
+                                         int SW, typename P::T (&s)[R]) {
   int32_t len = 0;
 #pragma unroll
   for (int q = 0; q < R; ++q) {
@@ -244,14 +298,14 @@ __device__ __forceinline__ void rows_sum(const IterParams &p, const int32_t (&eb
       for (int j = 0; j < kUnroll; ++j) {
         const int32_t e = eb[q] + off + j * SW;
         ok[q][j] = e < ee[q];
-        c[q][j] = ok[q][j] ? __ldg(&p.col[e]) : 0;
-        w[q][j] = (MODE == kWeighted && ok[q][j]) ? __ldg(&p.val[e]) : 1.0f;
+        c[q][j] = ok[q][j] ? ld_stream_i32(&p.col[e]) : 0;
+        w[q][j] = (MODE == kWeighted && ok[q][j]) ? ld_stream_f32(&p.val[e]) : 1.0f;
       }
     typename P::T g[R][kUnroll];
 #pragma unroll
     for (int q = 0; q < R; ++q)
 #pragma unroll
-      for (int j = 0; j < kUnroll; ++j) g[q][j] = ok[q][j] ? P::load_g(p, c[q][j]) : P::zero();
+      for (int j = 0; j < kUnroll; ++j) g[q][j] = ok[q][j] ? P::load_g(p, cache, c[q][j]) : P::zero();
 #pragma unroll
     for (int q = 0; q < R; ++q)
 #pragma unroll
@@ -261,8 +315,8 @@ __device__ __forceinline__ void rows_sum(const IterParams &p, const int32_t (&eb
 }
 
 template <class P, int MODE>
-__device__ __forceinline__ void row_task(const IterParams &p, const Segment &sg, int local, int lane,
-                                         df dsum, Acc &a) {
+__device__ __forceinline__ void row_task(const IterParams &p, const void *cache, const Segment &sg,
+                                         int local, int lane, df dsum, Acc &a) {
   using T = typename P::T;
   constexpr int R = kRowsPerLane;
   const int SW = sg.sw;
@@ -284,7 +338,7 @@ __device__ __forceinline__ void row_task(const IterParams &p, const Segment &sg,
   for (int q = 0; q < R; ++q)
     if (valid[q] && li == 0) in[q] = row_in<P, MODE>(p, row[q]);
   T s[R];
-  rows_sum<P, MODE, R>(p, eb, ee, li, SW, s);
+  rows_sum<P, MODE, R>(p, cache, eb, ee, li, SW, s);
 #pragma unroll
   for (int q = 0; q < R; ++q) {
     for (int o = SW >> 1; o > 0; o >>= 1) s[q] = P::add(s[q], P::shfl(s[q], o));
@@ -293,7 +347,8 @@ __device__ __forceinline__ void row_task(const IterParams &p, const Segment &sg,
 }
 
 template <class P, int MODE>
-__device__ __forceinline__ void hub_task(const IterParams &p, int t, int lane, df dsum, Acc &a) {
+__device__ __forceinline__ void hub_task(const IterParams &p, const void *cache, int t, int lane,
+                                         df dsum, Acc &a) {
   using T = typename P::T;
   const int32_t h = __ldg(&p.hub_task_row[t]);
   const int32_t first = __ldg(&p.hub_first[h]);
@@ -302,7 +357,7 @@ __device__ __forceinline__ void hub_task(const IterParams &p, int t, int lane, d
   const int32_t cs = rb + (t - first) * kHubChunk;
   const int32_t eb[1] = {cs}, ee[1] = {min(re, cs + kHubChunk)};
   T s[1];
-  rows_sum<P, MODE, 1>(p, eb, ee, lane, 32, s);
+  rows_sum<P, MODE, 1>(p, cache, eb, ee, lane, 32, s);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s[0] = P::add(s[0], P::shfl(s[0], o));
   if (lane == 0) {
@@ -321,23 +376,28 @@ __device__ __forceinline__ void hub_task(const IterParams &p, int t, int lane, d
 }
 
 template <class P, int MODE>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) iterate_kernel(IterParams p) {
-  __shared__ long long bred[2][kWarps];
-  __shared__ int bbad[kWarps];
+__global__ void __launch_bounds__(kIterThreads, kMinBlocks) iterate_kernel(IterParams p) {
+  __shared__ long long bred[2][kIterWarps];
+  __shared__ int bbad[kIterWarps];
+  extern __shared__ __align__(16) unsigned char gcache[];
   df dsum;
   if (!prologue<P::kDF>(p, &dsum)) return;
+  if constexpr (P::kCached > 0) {
+    P::stage(p, gcache, p.n);
+    __syncthreads();
+  }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nwarps = gridDim.x * kWarps;
+  const int nwarps = gridDim.x * kIterWarps;
   Acc a;
-  for (int t = blockIdx.x * kWarps + wid; t < p.plan.n_tasks; t += nwarps) {
+  for (int t = blockIdx.x * kIterWarps + wid; t < p.plan.n_tasks; t += nwarps) {
     if (t < p.plan.n_hub_tasks) {
-      hub_task<P, MODE>(p, t, lane, dsum, a);
+      hub_task<P, MODE>(p, gcache, t, lane, dsum, a);
       continue;
     }
     int si = 0;
     while (si + 1 < p.plan.n_segs && t >= p.plan.segs[si + 1].task_begin) ++si;
     const Segment sg = p.plan.segs[si];
-    row_task<P, MODE>(p, sg, t - sg.task_begin, lane, dsum, a);
+    row_task<P, MODE>(p, gcache, sg, t - sg.task_begin, lane, dsum, a);
   }
 
   // ---- block totals of the exact fixed-point sums -> one atomic each
@@ -348,7 +408,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) iterate_kernel(IterParam
   if (threadIdx.x == 0) {
     long long t1 = 0, t2 = 0;
     int tb = 0;
-    for (int w = 0; w < kWarps; ++w) { t1 += bred[0][w]; t2 += bred[1][w]; tb |= bbad[w]; }
+    for (int w = 0; w < kIterWarps; ++w) { t1 += bred[0][w]; t2 += bred[1][w]; tb |= bbad[w]; }
     const int cur = (int)(p.k % 3);
     atomicAdd((unsigned long long *)&p.sums[cur * 4 + 1], (unsigned long long)t1);
     atomicAdd((unsigned long long *)&p.sums[cur * 4 + 0], (unsigned long long)t2);
@@ -439,12 +499,20 @@ Status workspace_ensure(Ctx *ctx, Graph *g) {
 
 namespace {
 
+template <class P>
+size_t iter_smem(const Graph *g) {
+  return P::kCached > 0 ? sizeof(typename P::T) * (size_t)std::min<int64_t>(g->n, P::kCached) : 0;
+}
+
 template <class P, int MODE>
 int grid_for_iter(const Ctx *ctx, const Graph *g) {
+  const size_t smem = iter_smem<P>(g);
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, iterate_kernel<P, MODE>, kThreads, 0);
+  if (smem > 0)
+    cudaFuncSetAttribute(iterate_kernel<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, iterate_kernel<P, MODE>, kIterThreads, smem);
   occ = std::max(1, occ);
-  const int64_t blocks_needed = ceil_div<int64_t>(std::max<int32_t>(g->plan.n_tasks, 1), kWarps);
+  const int64_t blocks_needed = ceil_div<int64_t>(std::max<int32_t>(g->plan.n_tasks, 1), kIterWarps);
   return (int)std::max<int64_t>(1, std::min<int64_t>(blocks_needed, (int64_t)ctx->num_sms * occ));
 }
 
@@ -499,6 +567,7 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
 
   const int grid_df = grid_for_iter<PrecDF, MODE>(ctx, g);
   const int grid_f = grid_for_iter<PrecF32, MODE>(ctx, g);
+  const size_t smem_df = iter_smem<PrecDF>(g), smem_f = iter_smem<PrecF32>(g);
   bool f32_known = false;
   unsigned long long k = 1;
   const int chunk = 4;
@@ -525,14 +594,14 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
       if (!f32_known) {
         GOPS_TRY(timed_launch(true));
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 2], s));
-        iterate_kernel<PrecDF, MODE><<<grid_df, kThreads, 0, s>>>(p);
+        iterate_kernel<PrecDF, MODE><<<grid_df, kIterThreads, smem_df, s>>>(p);
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 1], s));
         ++launches;
       }
       if (k >= 2) {
         GOPS_TRY(timed_launch(false));
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 2], s));
-        iterate_kernel<PrecF32, MODE><<<grid_f, kThreads, 0, s>>>(p);
+        iterate_kernel<PrecF32, MODE><<<grid_f, kIterThreads, smem_f, s>>>(p);
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 1], s));
         ++launches;
       }

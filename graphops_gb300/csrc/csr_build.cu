@@ -8,11 +8,11 @@
 //      ascending source order, the order the reference scatters in
 //      (src/pagerank.rs:154-162).  In-row offsets come from the sorted keys
 //      (no atomics on hub destinations).
-//  K2  relabelling and the pull kernel's plan: a stable radix sort of nodes by
+//  K2  relabelling and the pull kernels' plan: a stable radix sort of nodes by
 //      in-degree (descending) gives perm; the in-edge CSR is rewritten in that
 //      order with relabelled sources; rows then fall into contiguous degree
-//      classes (segments) cut into fixed-size batches, and rows above kBigRow
-//      in-edges are split into kBatchEdges-edge chunk batches.
+//      classes (segments), each processed with one sub-warp width, and rows
+//      above kHubThreshold in-edges are split into kHubChunk-edge warp tasks.
 //  Dense  AdjacencyMatrix (src/graph.rs:128-141) -> out-CSR by a warp-ballot
 //      compaction of each matrix row (entries > 0.0, ascending column).
 #include <algorithm>
@@ -132,6 +132,18 @@ __global__ void scatter_edges(const uint32_t *K, const uint32_t *O, int64_t m, c
   }
 }
 
+__global__ void pad_degrees(int64_t *deg, int64_t n, int align) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    deg[i] = (deg[i] + align - 1) / align * align;
+}
+
+__global__ void fill_i32(int32_t *a, int64_t count, int32_t v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+
 // out[j] = number of relabelled rows with in-degree >= thr[j] (degrees are
 // non-increasing along the rows: maxdeg - sorted_keys[i]).
 __global__ void count_ge(const uint32_t *sorted_keys, int64_t n, const unsigned *maxdeg,
@@ -150,7 +162,7 @@ __global__ void count_ge(const uint32_t *sorted_keys, int64_t n, const unsigned 
 
 __global__ void hub_chunks(const int64_t *rp, int32_t n_hub, int64_t *nch) {
   for (int32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= n_hub; h += gridDim.x * blockDim.x)
-    nch[h] = h < n_hub ? ceil_div<int64_t>(rp[h + 1] - rp[h], kBatchEdges) : 0;
+    nch[h] = h < n_hub ? ceil_div<int64_t>(rp[h + 1] - rp[h], kHubChunk) : 0;
 }
 
 __global__ void hub_fill(const int64_t *first64, int32_t n_hub, int32_t *first, int32_t *task_row) {
@@ -201,10 +213,10 @@ int bits_for(int64_t n) {
 
 void graph_free_device(Graph &g) {
   cudaFree(g.in_rp); cudaFree(g.in_col); cudaFree(g.in_val); cudaFree(g.deg);
-  cudaFree(g.dmask_w); cudaFree(g.perm); cudaFree(g.big_first); cudaFree(g.big_batch_row);
+  cudaFree(g.dmask_w); cudaFree(g.perm); cudaFree(g.hub_first); cudaFree(g.hub_task_row);
   workspace_free(g.ws);
   g.in_rp = nullptr; g.in_col = nullptr; g.in_val = nullptr; g.deg = nullptr;
-  g.dmask_w = nullptr; g.perm = nullptr; g.big_first = nullptr; g.big_batch_row = nullptr;
+  g.dmask_w = nullptr; g.perm = nullptr; g.hub_first = nullptr; g.hub_task_row = nullptr;
 }
 
 Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_rp,
@@ -243,16 +255,11 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   const size_t mm = (size_t)std::max<int64_t>(m, 1) + 64;  // padded edge arrays
   const size_t nn = (size_t)std::max<int64_t>(n, 1);
   const size_t nwords = (size_t)(n / 32 + 1);
-  BUILD_TRY(cudaMalloc(&g->in_rp, sizeof(int64_t) * (n + 4)));  // +3: aligned bulk copies
-  BUILD_TRY(cudaMemsetAsync(g->in_rp, 0, sizeof(int64_t) * (n + 4), s));
-  BUILD_TRY(cudaMalloc(&g->in_col, sizeof(int32_t) * mm));
-  BUILD_TRY(cudaMemsetAsync(g->in_col, 0, sizeof(int32_t) * mm, s));
+  BUILD_TRY(cudaMalloc(&g->in_rp, sizeof(int64_t) * (n + 1)));
   BUILD_TRY(cudaMalloc(&g->deg, sizeof(float) * nn));
   BUILD_TRY(cudaMalloc(&g->perm, sizeof(int32_t) * nn));
   BUILD_TRY(cudaMallocAsync((void **)&deg_old, sizeof(float) * nn, s));
   if (g->weighted) {
-    BUILD_TRY(cudaMalloc(&g->in_val, sizeof(float) * mm));
-    BUILD_TRY(cudaMemsetAsync(g->in_val, 0, sizeof(float) * mm, s));
     BUILD_TRY(cudaMalloc(&g->dmask_w, sizeof(uint32_t) * nwords));
     BUILD_TRY(cudaMemsetAsync(g->dmask_w, 0, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(cudaMallocAsync((void **)&dmask_old, sizeof(uint32_t) * nwords, s));
@@ -312,7 +319,27 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   } else {
     BUILD_TRY(cudaMemsetAsync(new_deg, 0, sizeof(int64_t), s));
   }
+  if (kRowAlign > 1 && n > 0) {
+    pad_degrees<<<grid_for(n, 256), 256, 0, s>>>(new_deg, n, kRowAlign);
+    BUILD_TRY(cudaGetLastError());
+  }
   BUILD_ST(exclusive_scan_i64(new_deg, g->in_rp, n + 1, s));
+  int64_t m_stored = 0;
+  BUILD_TRY(cudaMemcpyAsync(&m_stored, g->in_rp + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  BUILD_TRY(cudaStreamSynchronize(s));
+  g->m_stored = m_stored;
+  const size_t ms = (size_t)std::max<int64_t>(m_stored, 1) + 64;  // +64: vector loads past the end
+  BUILD_TRY(cudaMalloc(&g->in_col, sizeof(int32_t) * ms));
+  if (kRowAlign > 1) {
+    fill_i32<<<grid_for((int64_t)ms, 256), 256, 0, s>>>(g->in_col, (int64_t)ms, (int32_t)n);
+    BUILD_TRY(cudaGetLastError());
+  } else {
+    BUILD_TRY(cudaMemsetAsync(g->in_col, 0, sizeof(int32_t) * ms, s));
+  }
+  if (g->weighted) {
+    BUILD_TRY(cudaMalloc(&g->in_val, sizeof(float) * ms));
+    BUILD_TRY(cudaMemsetAsync(g->in_val, 0, sizeof(float) * ms, s));
+  }
   if (m > 0) {
     scatter_edges<<<grid_for(m, 256), 256, 0, s>>>(K, O, m, rp_old, inv_perm, g->in_rp, src, val_out,
                                                    g->in_col, g->in_val);
@@ -320,8 +347,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   }
   // plan: degree classes over the (non-increasing) relabelled degrees
   const int L = kLaneEdges;
-  // rows with degree >= thr: big rows, then the sub-warp classes 32..2
-  const int64_t thr_h[7] = {kBigRow + 1, 32 * L, 16 * L, 8 * L, 4 * L, 2 * L, 0};
+  const int64_t thr_h[7] = {kHubThreshold + 1, 32 * L, 16 * L, 8 * L, 4 * L, 2 * L, 0};
   int64_t cnt_h[7] = {0, 0, 0, 0, 0, 0, 0};
   BUILD_TRY(cudaMallocAsync((void **)&small, sizeof(int64_t) * 16, s));
   if (n > 0) {
@@ -333,12 +359,9 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   }
   Plan &pl = g->plan;
   pl = Plan{};
-  pl.n_big = (int32_t)cnt_h[0];
+  pl.n_hub = (int32_t)cnt_h[0];
   const int sws[6] = {32, 16, 8, 4, 2, 1};
-  // largest degree a class can hold: the big-row threshold for sw = 32,
-  // else one below the next class's lower bound
-  const int64_t hi_deg[6] = {kBigRow, 32 * L - 1, 16 * L - 1, 8 * L - 1, 4 * L - 1, 2 * L - 1};
-  int64_t row = pl.n_big, batch = 0;
+  int64_t row = pl.n_hub, task = 0;
   for (int c = 0; c < 6; ++c) {
     const int64_t end = c == 5 ? n : std::max<int64_t>(row, cnt_h[c + 1]);
     if (end > row) {
@@ -346,38 +369,36 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
       sg.row_begin = (int32_t)row;
       sg.row_end = (int32_t)end;
       sg.sw = sws[c];
-      sg.rows_per_batch = (int32_t)std::max<int64_t>(
-          1, std::min<int64_t>(kPullThreads / sws[c], kBatchEdges / std::max<int64_t>(hi_deg[c], 1)));
-      sg.batch_begin = (int32_t)batch;  // relative to the first segment batch
-      batch += ceil_div<int64_t>(end - row, sg.rows_per_batch);
+      sg.task_begin = (int32_t)task;  // relative to the first segment task
+      task += ceil_div<int64_t>((end - row) * sws[c], 32 * kRowsPerLane);
       row = end;
     }
   }
-  // chunk batches of the big rows
-  if (pl.n_big > 0) {
+  // hub tasks
+  if (pl.n_hub > 0) {
     int64_t *nch = nullptr;
-    BUILD_TRY(cudaMallocAsync((void **)&nch, sizeof(int64_t) * (pl.n_big + 1), s));
-    hub_chunks<<<grid_for(pl.n_big + 1, 256), 256, 0, s>>>(g->in_rp, pl.n_big, nch);
-    Status s2 = exclusive_scan_i64(nch, nch, pl.n_big + 1, s);
-    int64_t nbb = 0;
+    BUILD_TRY(cudaMallocAsync((void **)&nch, sizeof(int64_t) * (pl.n_hub + 1), s));
+    hub_chunks<<<grid_for(pl.n_hub + 1, 256), 256, 0, s>>>(g->in_rp, pl.n_hub, nch);
+    Status s2 = exclusive_scan_i64(nch, nch, pl.n_hub + 1, s);
+    int64_t nht = 0;
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && s2.code == GOPS_OK)
-      e = cudaMemcpyAsync(&nbb, nch + pl.n_big, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+      e = cudaMemcpyAsync(&nht, nch + pl.n_hub, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e == cudaSuccess) e = cudaMalloc(&g->big_first, sizeof(int32_t) * (pl.n_big + 1));
-    if (e == cudaSuccess) e = cudaMalloc(&g->big_batch_row, sizeof(int32_t) * std::max<int64_t>(nbb, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&g->hub_first, sizeof(int32_t) * (pl.n_hub + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&g->hub_task_row, sizeof(int32_t) * std::max<int64_t>(nht, 1));
     if (e == cudaSuccess) {
-      hub_fill<<<grid_for(pl.n_big + 1, 256), 256, 0, s>>>(nch, pl.n_big, g->big_first, g->big_batch_row);
+      hub_fill<<<grid_for(pl.n_hub + 1, 256), 256, 0, s>>>(nch, pl.n_hub, g->hub_first, g->hub_task_row);
       e = cudaGetLastError();
     }
     free_async(nch, s);
     if (s2.code != GOPS_OK) { cleanup(); return s2; }
     BUILD_TRY(e);
-    pl.n_big_batches = (int32_t)nbb;
+    pl.n_hub_tasks = (int32_t)nht;
   }
-  for (int i = 0; i < pl.n_segs; ++i) pl.segs[i].batch_begin += pl.n_big_batches;
-  if (batch + pl.n_big_batches >= INT32_MAX) { cleanup(); return Status{GOPS_ERR_INVALID, "graph too large"}; }
-  pl.n_batches = (int32_t)(batch + pl.n_big_batches);
+  for (int i = 0; i < pl.n_segs; ++i) pl.segs[i].task_begin += pl.n_hub_tasks;
+  if (task + pl.n_hub_tasks >= INT32_MAX) { cleanup(); return Status{GOPS_ERR_INVALID, "graph too large"}; }
+  pl.n_tasks = (int32_t)(task + pl.n_hub_tasks);
   BUILD_TRY(cudaStreamSynchronize(s));
   cleanup();
   return Status::ok();

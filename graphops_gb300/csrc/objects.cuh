@@ -10,41 +10,46 @@ namespace gops {
 
 // Device layout of a graph.  Nodes are relabelled once at build time by a
 // stable sort on in-degree (descending): row i of the in-edge CSR is node
-// perm[i].  Rows of one degree class are then contiguous, and the most
-// gathered nodes sit together at the front of every per-node vector.
-//
-// The pull kernel works in batches.  Rows [0, n_big) have more than kBigRow
-// in-edges; each is split into kBatchEdges-edge chunks, one batch per chunk.
-// The remaining rows form segments of one degree class each; a segment batch
-// is rows_per_batch consecutive rows with sw lanes per row, at most
-// kBatchEdges edges in all.  A batch's column indices, weights and row
-// offsets are contiguous in memory and arrive in shared memory by one bulk
-// copy each.
+// perm[i].  Rows of equal degree class are then contiguous, so each class is
+// one "segment" processed with one sub-warp width, and the most-gathered
+// nodes sit together at the front of every per-node vector.
 constexpr int kMaxSegments = 8;
-constexpr int kPullThreads = 512;   // threads of a pull block
-constexpr int kBatchEdges = 4096;   // edges per batch (shared-memory stage)
-constexpr int kBigRow = 256;        // rows above this in-degree are chunked
-#ifndef GOPS_LANE_EDGES
-#define GOPS_LANE_EDGES 4
-#endif
-// target edges per lane when choosing a degree class's sub-warp width
-constexpr int kLaneEdges = GOPS_LANE_EDGES;
 
 struct Segment {
   int32_t row_begin, row_end;  // rows [row_begin, row_end) of this class
-  int32_t sw;                  // lanes per row (1..32)
-  int32_t rows_per_batch;
-  int32_t batch_begin;         // first batch index of the segment
-  int32_t pad;
+  int32_t sw;                  // lanes per row (1..32); 32/sw rows per warp task
+  int32_t task_begin;          // first task index of the segment
 };
 
 struct Plan {
-  int32_t n_big = 0;          // chunked rows [0, n_big)
-  int32_t n_big_batches = 0;  // their chunks: batches [0, n_big_batches)
+  // hub rows (in-degree > kHubThreshold) are rows [0, n_hub); row h is split
+  // into tasks hub_first[h] .. hub_first[h+1]-1 of kHubChunk edges each
+  int32_t n_hub = 0;
+  int32_t n_hub_tasks = 0;
   int32_t n_segs = 0;
-  int32_t n_batches = 0;      // all batches
+  int32_t n_tasks = 0;  // n_hub_tasks + tasks of all segments
   Segment segs[kMaxSegments];
 };
+
+constexpr int kHubChunk = 1024;      // edges per hub task (one warp)
+constexpr int kHubThreshold = 4096;  // rows above this in-degree are hubs
+#ifndef GOPS_PAD4
+#define GOPS_PAD4 0
+#endif
+// With kRowAlign == 4 every in-row is padded to a multiple of four edges
+// (padding: column n, weight 0; entry n of the gathered vectors is 0), so a
+// lane loads four edges with one aligned 16-byte load.
+constexpr int kRowAlign = GOPS_PAD4 ? 4 : 1;
+#ifndef GOPS_ROWS_PER_LANE
+#define GOPS_ROWS_PER_LANE 2
+#endif
+#ifndef GOPS_LANE_EDGES
+#define GOPS_LANE_EDGES 4
+#endif
+// rows interleaved per sub-warp in one warp task
+constexpr int kRowsPerLane = GOPS_ROWS_PER_LANE;
+// target edges per lane when choosing a degree class's sub-warp width
+constexpr int kLaneEdges = GOPS_LANE_EDGES;
 
 // Solver workspace held by a graph (allocated on first solve, reused).
 struct Workspace {
@@ -56,9 +61,8 @@ struct Workspace {
   float2 *pdf = nullptr;                // personalization (normalised) as double-float
   double *scores = nullptr;             // final x = acc + tail, in node order
   long long *sums = nullptr;            // 3 slots x {dangling, l1, nonfinite, spare}
-  float2 *lpart = nullptr;              // chunk partials, per big-row batch
-  unsigned *lcnt = nullptr;             // arrival counters, per big row
-  int *err = nullptr;                   // device error word (bounded waits that ran out)
+  float2 *lpart = nullptr;              // hub chunk partials, per hub task
+  unsigned *lcnt = nullptr;             // hub arrival counters, per hub row
   struct SolveState *state = nullptr;   // device-side run record
 };
 
@@ -75,6 +79,7 @@ struct SolveState {
 struct Graph {
   struct Ctx *ctx = nullptr;
   int64_t n = 0, m = 0;
+  int64_t m_stored = 0;  // edges stored in the in-edge CSR (m plus row padding)
   bool weighted = false;
   // in-edge CSR over relabelled ids: row i lists the (relabelled) sources of
   // the edges into node perm[i], in ascending original source order
@@ -84,8 +89,8 @@ struct Graph {
   float *deg = nullptr;         // out-degree (relabelled order); 0 = unweighted-dangling
   uint32_t *dmask_w = nullptr;  // weighted-dangling bitmask (relabelled order)
   int32_t *perm = nullptr;      // relabelled row i -> original node id
-  int32_t *big_first = nullptr;      // n_big + 1 chunk-batch offsets
-  int32_t *big_batch_row = nullptr;  // chunk batch -> big row
+  int32_t *hub_first = nullptr;     // n_hub + 1 task offsets
+  int32_t *hub_task_row = nullptr;  // hub task -> hub row
   Plan plan;
   Workspace ws;
 };

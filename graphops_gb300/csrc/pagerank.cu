@@ -21,16 +21,14 @@
 // (dangling mass, L1 norm) are exact 64-bit fixed-point integer sums, so they
 // are independent of summation order and bit-reproducible.
 //
-// Data movement.  One block per SM walks its batches (see objects.cuh) in a
-// ring of kStages shared-memory stages: one thread issues bulk asynchronous
-// copies (TMA) of a batch's column indices, weights and row offsets several
-// batches ahead, completing on an mbarrier, so the edge streams never wait on
-// the threads.  The threads gather the previous step's vector at the staged
-// column indices; its first kHot entries -- the most gathered nodes after the
-// in-degree relabelling -- are staged in shared memory at kernel start.
-// Segment batches give each row sw lanes (an xor-shuffle reduction); chunks of
-// big rows are reduced by the whole block and combined, in chunk order, by the
-// chunk that finishes last.
+// Work layout.  Rows are relabelled by in-degree (descending) at build time,
+// so each degree class is a contiguous segment.  A warp task covers 32/sw
+// consecutive rows of one segment with sw lanes per row (sw chosen so a lane
+// has about four edges); every lane keeps four independent column loads and
+// four gathers in flight, and a row's sum is an xor-shuffle reduction over its
+// sw lanes.  Rows above kHubThreshold in-edges are split into kHubChunk-edge
+// warp tasks whose partials are combined, in chunk order, by the task that
+// finishes last.  No block-wide barrier sits on the edge path.
 //
 // Convergence is decided on the device: the kernel for step k first reads
 // diff_{k-1}; if it is below tol (or k-1 == max_iterations) it records the
@@ -47,30 +45,42 @@ enum Mode : int { kPlain = 0, kWeighted = 1, kPpr = 2 };
 
 constexpr int kThreads = 256;  // init / small kernels
 constexpr int kWarps = kThreads / kWarp;
-constexpr int kPullWarps = kPullThreads / kWarp;
-constexpr int kStages = 3;
-#ifndef GOPS_HOT
-#define GOPS_HOT 26624
+#ifndef GOPS_BLOCK
+#define GOPS_BLOCK 256
 #endif
-constexpr int kHot = GOPS_HOT;   // FP32 entries of the gathered vector staged per block
-constexpr double kTheta = 1e-2;  // double-float phase while ||r||_1 >= kTheta
-
-// shared-memory stage of one batch
-struct Stage {
-  int32_t col[kBatchEdges + 8];
-  float val[kBatchEdges + 8];
-  long long rp[kPullThreads + 4];
-};
-
-struct BatchDesc {
-  int kind;         // 0: segment rows, 1: chunk of a big row
-  int row0, nrows;  // segment rows / the big row (row0)
-  int sw;           // lanes per row (segment batches)
-  int e0a;          // first staged edge (16-byte aligned)
-  int rpa;          // first staged row offset (16-byte aligned)
-  int cs, ce;       // chunk edge range (big rows)
-  int first, nch;   // chunk batches of the big row
-};
+#ifndef GOPS_GCACHE
+#define GOPS_GCACHE 0
+#endif
+#ifndef GOPS_L1HINT
+#define GOPS_L1HINT 0
+#endif
+// iteration kernels: threads per block, and how many of the first (hottest,
+// after the in-degree relabelling) entries of the gathered vector each block
+// stages in shared memory (FP32 entries; half as many double-float ones)
+constexpr int kIterThreads = GOPS_BLOCK;
+constexpr int kIterWarps = kIterThreads / kWarp;
+constexpr int kGCache = GOPS_GCACHE;
+constexpr bool kL1Hint = GOPS_L1HINT != 0;
+#ifndef GOPS_L1POL
+#define GOPS_L1POL 0
+#endif
+#ifndef GOPS_L1HOT
+#define GOPS_L1HOT 49152
+#endif
+// With kL1Policy the streams (columns, weights) and gathers of cold nodes do
+// not allocate in L1, and gathers of the first kL1Hot (hottest) nodes are
+// marked evict-last, so L1 holds the hot prefix of the gathered vector.
+constexpr bool kL1Policy = GOPS_L1POL != 0;
+constexpr int kL1Hot = GOPS_L1HOT;
+#ifndef GOPS_UNROLL
+#define GOPS_UNROLL 4
+#endif
+#ifndef GOPS_MINB
+#define GOPS_MINB 4
+#endif
+constexpr int kUnroll = GOPS_UNROLL;   // edges per lane per round and row
+constexpr int kMinBlocks = GOPS_MINB;  // occupancy hint for the iteration kernels
+constexpr double kTheta = 1e-2;   // double-float phase while ||r||_1 >= kTheta
 
 struct IterParams {
   int64_t n;
@@ -79,8 +89,8 @@ struct IterParams {
   const float *val;
   const float *deg;
   const uint32_t *dmask;
-  const int32_t *big_first;
-  const int32_t *big_batch_row;
+  const int32_t *hub_first;
+  const int32_t *hub_task_row;
   Plan plan;
   const float2 *gdf_in;
   float2 *gdf_out;
@@ -93,7 +103,6 @@ struct IterParams {
   SolveState *st;
   float2 *lpart;
   unsigned *lcnt;
-  int *err;
   df d, omd, inv_n;
   float fx_scale;
   double fx_inv;
@@ -101,25 +110,89 @@ struct IterParams {
   unsigned long long k, max_iter;
 };
 
+// Streamed loads (column indices, transition weights): with kL1Hint they do
+// not allocate in L1, which then keeps the hot lines of the gathered vector.
+__device__ __forceinline__ int4 ld_stream_v4i(const int32_t *a) {
+  int4 v;
+  if constexpr (kL1Hint || kL1Policy) {
+    asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(a));
+  } else {
+    v = __ldg(reinterpret_cast<const int4 *>(a));
+  }
+  return v;
+}
+__device__ __forceinline__ float4 ld_stream_v4f(const float *a) {
+  float4 v;
+  if constexpr (kL1Hint || kL1Policy) {
+    asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(a));
+  } else {
+    v = __ldg(reinterpret_cast<const float4 *>(a));
+  }
+  return v;
+}
+// gathers under the L1 policy
+__device__ __forceinline__ float ld_gather_f32(const float *base, int32_t u) {
+  if constexpr (kL1Policy) {
+    float v;
+    if (u < kL1Hot) asm volatile("ld.global.nc.L1::evict_last.f32 %0, [%1];" : "=f"(v) : "l"(base + u));
+    else asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(base + u));
+    return v;
+  } else {
+    return __ldg(base + u);
+  }
+}
+__device__ __forceinline__ float2 ld_gather_f2(const float2 *base, int32_t u) {
+  if constexpr (kL1Policy) {
+    float2 v;
+    if (u < kL1Hot / 2)
+      asm volatile("ld.global.nc.L1::evict_last.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(base + u));
+    else
+      asm volatile("ld.global.nc.L1::no_allocate.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(base + u));
+    return v;
+  } else {
+    return __ldg(base + u);
+  }
+}
+__device__ __forceinline__ int32_t ld_stream_i32(const int32_t *a) {
+  if constexpr (kL1Hint || kL1Policy) {
+    int32_t v;
+    asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(a));
+    return v;
+  } else {
+    return __ldg(a);
+  }
+}
+__device__ __forceinline__ float ld_stream_f32(const float *a) {
+  if constexpr (kL1Hint || kL1Policy) {
+    float v;
+    asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(a));
+    return v;
+  } else {
+    return __ldg(a);
+  }
+}
+
 // --------------------------------------------------------------------------
 // precision policies
 // --------------------------------------------------------------------------
 struct PrecDF {
   using T = df;
   static constexpr bool kDF = true;
-  static constexpr int kCached = kHot / 2;  // double-float entries staged in shared memory
   __device__ static T zero() { return {0.0f, 0.0f}; }
   __device__ static T add(T a, T b) { return df_add(a, b); }
   __device__ static T shfl(T v, int m) { return shfl_xor_df(v, m, 32); }
+  static constexpr int kCached = kGCache / 2;  // float2 entries staged in shared memory
   __device__ static T load_g(const IterParams &p, const void *cache, int32_t u) {
     float2 g;
-    if (u < kCached) g = reinterpret_cast<const float2 *>(cache)[u];
-    else g = __ldg(&p.gdf_in[u]);
+    if (kCached > 0 && u < kCached) g = reinterpret_cast<const float2 *>(cache)[u];
+    else g = ld_gather_f2(p.gdf_in, u);
     return {g.x, g.y};
   }
-  __device__ static void stage(const IterParams &p, void *cache) {
+  __device__ static void stage(const IterParams &p, void *cache, int64_t n) {
     float2 *c = reinterpret_cast<float2 *>(cache);
-    const int lim = (int)(p.n < (int64_t)kCached ? p.n : (int64_t)kCached);
+    const int lim = (int)(n < (int64_t)kCached ? n : (int64_t)kCached);
     for (int i = threadIdx.x; i < lim; i += blockDim.x) c[i] = __ldg(&p.gdf_in[i]);
   }
   __device__ static T scale(T g, float w) { return df_mul_f(g, w); }
@@ -130,17 +203,17 @@ struct PrecDF {
 struct PrecF32 {
   using T = float;
   static constexpr bool kDF = false;
-  static constexpr int kCached = kHot;
   __device__ static T zero() { return 0.0f; }
   __device__ static T add(T a, T b) { return a + b; }
   __device__ static T shfl(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+  static constexpr int kCached = kGCache;
   __device__ static T load_g(const IterParams &p, const void *cache, int32_t u) {
-    if (u < kCached) return reinterpret_cast<const float *>(cache)[u];
-    return __ldg(&p.gf_in[u]);
+    if (kCached > 0 && u < kCached) return reinterpret_cast<const float *>(cache)[u];
+    return ld_gather_f32(p.gf_in, u);
   }
-  __device__ static void stage(const IterParams &p, void *cache) {
+  __device__ static void stage(const IterParams &p, void *cache, int64_t n) {
     float *c = reinterpret_cast<float *>(cache);
-    const int lim = (int)(p.n < (int64_t)kCached ? p.n : (int64_t)kCached);
+    const int lim = (int)(n < (int64_t)kCached ? n : (int64_t)kCached);
     for (int i = threadIdx.x; i < lim; i += blockDim.x) c[i] = __ldg(&p.gf_in[i]);
   }
   __device__ static T scale(T g, float w) { return g * w; }
@@ -154,9 +227,9 @@ struct Acc {
 };
 
 // Per-row inputs of the epilogue, loaded before the row's edges so their
-// latency overlaps the gathers: the running x part (acc in the double-float
-// phase, tail in the FP32 phase), the out-degree, the dangling flag and the
-// personalization entry.
+// latency overlaps the edge loads: the running x part (acc in the
+// double-float phase, tail in the FP32 phase), the out-degree, the dangling
+// flag and the personalization entry.
 struct RowIn {
   float2 x;
   float2 red;
@@ -255,202 +328,178 @@ __device__ bool prologue(const IterParams &p, df *dsum) {
   return true;
 }
 
-// Producer side: describes batch b and starts its bulk copies into stage st,
-// completing on bar.  Called by one thread.  Copies start and end on 16-byte
-// boundaries (the edge and row-offset arrays carry padding past their ends).
-template <int MODE>
-__device__ void issue_batch(const IterParams &p, int b, Stage &st, BatchDesc &dsc, uint64_t *bar) {
-  uint32_t rp_bytes = 0;
-  int e0a, e1a;
-  if (b < p.plan.n_big_batches) {
-    const int h = __ldg(&p.big_batch_row[b]);
-    const int first = __ldg(&p.big_first[h]);
-    const int rb = (int)__ldg(&p.rp[h]), re = (int)__ldg(&p.rp[h + 1]);
-    const int cs = rb + (b - first) * kBatchEdges;
-    const int ce = min(re, cs + kBatchEdges);
-    e0a = cs & ~3;
-    e1a = (ce + 3) & ~3;
-    dsc.kind = 1;
-    dsc.row0 = h;
-    dsc.nrows = 1;
-    dsc.sw = 32;
-    dsc.rpa = 0;
-    dsc.cs = cs;
-    dsc.ce = ce;
-    dsc.first = first;
-    dsc.nch = __ldg(&p.big_first[h + 1]) - first;
-  } else {
-    int si = 0;
-    while (si + 1 < p.plan.n_segs && b >= p.plan.segs[si + 1].batch_begin) ++si;
-    const Segment &sg = p.plan.segs[si];
-    const int r0 = sg.row_begin + (b - sg.batch_begin) * sg.rows_per_batch;
-    const int nr = min(sg.rows_per_batch, sg.row_end - r0);
-    const int e0 = (int)__ldg(&p.rp[r0]), e1 = (int)__ldg(&p.rp[r0 + nr]);
-    e0a = e0 & ~3;
-    e1a = (e1 + 3) & ~3;
-    const int rpa = r0 & ~1, rpe = (r0 + nr + 2) & ~1;  // covers rp[r0 .. r0+nr]
-    dsc.kind = 0;
-    dsc.row0 = r0;
-    dsc.nrows = nr;
-    dsc.sw = sg.sw;
-    dsc.rpa = rpa;
-    rp_bytes = (uint32_t)(rpe - rpa) * 8u;
+// R rows per sub-warp, their edges interleaved so that every lane keeps
+// R * kUnroll column loads, then R * kUnroll gathers, in flight.  Lane li of
+// a row's sub-warp takes edges eb+li, eb+li+SW, ... and adds them in that
+// order, so a row's sum does not depend on R or kUnroll.
+template <class P, int MODE, int R>
+__device__ __forceinline__ void rows_sum(const IterParams &p, const void *cache,
+                                         const int32_t (&eb)[R], const int32_t (&ee)[R], int li,
+                                         int SW, typename P::T (&s)[R]) {
+  int32_t len = 0;
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    s[q] = P::zero();
+    len = max(len, ee[q] - eb[q]);
   }
-  dsc.e0a = e0a;
-  const uint32_t eb = (uint32_t)(e1a - e0a) * 4u;
-  mbar_arrive_expect_tx(bar, rp_bytes + eb * (MODE == kWeighted ? 2u : 1u));
-  if (rp_bytes) bulk_g2s(st.rp, p.rp + dsc.rpa, rp_bytes, bar);
-  if (eb) {
-    bulk_g2s(st.col, p.col + e0a, eb, bar);
-    if (MODE == kWeighted) bulk_g2s(st.val, p.val + e0a, eb, bar);
+  if constexpr (kRowAlign == 4) {
+    // rows start and end on 4-edge boundaries: lane li takes the quads
+    // li, li+SW, ... of each row, kUnroll / 4 quads (at least one) per round
+    constexpr int QU = kUnroll >= 8 ? kUnroll / 4 : 1;
+    for (int32_t off = 4 * li; off < len; off += 4 * QU * SW) {
+      int4 c[R][QU];
+      float4 w[R][QU];
+      bool ok[R][QU];
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+#pragma unroll
+        for (int j = 0; j < QU; ++j) {
+          const int32_t e = eb[q] + off + 4 * j * SW;
+          ok[q][j] = e < ee[q];
+          c[q][j] = ok[q][j] ? ld_stream_v4i(&p.col[e]) : make_int4(0, 0, 0, 0);
+          w[q][j] = (MODE == kWeighted && ok[q][j]) ? ld_stream_v4f(&p.val[e])
+                                                     : make_float4(1.f, 1.f, 1.f, 1.f);
+        }
+      typename P::T g[R][QU][4];
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+#pragma unroll
+        for (int j = 0; j < QU; ++j) {
+          g[q][j][0] = ok[q][j] ? P::load_g(p, cache, c[q][j].x) : P::zero();
+          g[q][j][1] = ok[q][j] ? P::load_g(p, cache, c[q][j].y) : P::zero();
+          g[q][j][2] = ok[q][j] ? P::load_g(p, cache, c[q][j].z) : P::zero();
+          g[q][j][3] = ok[q][j] ? P::load_g(p, cache, c[q][j].w) : P::zero();
+        }
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+#pragma unroll
+        for (int j = 0; j < QU; ++j)
+          if (ok[q][j]) {
+            if (MODE == kWeighted) {
+              s[q] = P::add(s[q], P::scale(g[q][j][0], w[q][j].x));
+              s[q] = P::add(s[q], P::scale(g[q][j][1], w[q][j].y));
+              s[q] = P::add(s[q], P::scale(g[q][j][2], w[q][j].z));
+              s[q] = P::add(s[q], P::scale(g[q][j][3], w[q][j].w));
+            } else {
+              s[q] = P::add(s[q], g[q][j][0]);
+              s[q] = P::add(s[q], g[q][j][1]);
+              s[q] = P::add(s[q], g[q][j][2]);
+              s[q] = P::add(s[q], g[q][j][3]);
+            }
+          }
+    }
+    return;
+  }
+  for (int32_t off = li; off < len; off += kUnroll * SW) {
+    int32_t c[R][kUnroll];
+    float w[R][kUnroll];
+    bool ok[R][kUnroll];
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+#pragma unroll
+      for (int j = 0; j < kUnroll; ++j) {
+        const int32_t e = eb[q] + off + j * SW;
+        ok[q][j] = e < ee[q];
+        c[q][j] = ok[q][j] ? ld_stream_i32(&p.col[e]) : 0;
+        w[q][j] = (MODE == kWeighted && ok[q][j]) ? ld_stream_f32(&p.val[e]) : 1.0f;
+      }
+    typename P::T g[R][kUnroll];
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+#pragma unroll
+      for (int j = 0; j < kUnroll; ++j) g[q][j] = ok[q][j] ? P::load_g(p, cache, c[q][j]) : P::zero();
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+#pragma unroll
+      for (int j = 0; j < kUnroll; ++j)
+        if (ok[q][j]) s[q] = P::add(s[q], MODE == kWeighted ? P::scale(g[q][j], w[q][j]) : g[q][j]);
   }
 }
 
-// The pull kernel of step k in precision P (see the file comment).
 template <class P, int MODE>
-__global__ void __launch_bounds__(kPullThreads, 1) pull_kernel(IterParams p) {
+__device__ __forceinline__ void row_task(const IterParams &p, const void *cache, const Segment &sg,
+                                         int local, int lane, df dsum, Acc &a) {
   using T = typename P::T;
-  extern __shared__ __align__(128) unsigned char smem[];
-  Stage *stages = reinterpret_cast<Stage *>(smem);
-  void *cache = smem + sizeof(Stage) * kStages;
-  __shared__ uint64_t full[kStages];
-  __shared__ BatchDesc desc[kStages];
-  __shared__ T wred[kPullWarps];
-  __shared__ long long bred[2][kPullWarps];
-  __shared__ int bbad[kPullWarps];
+  constexpr int R = kRowsPerLane;
+  const int SW = sg.sw;
+  const int lg = 31 - __clz(SW);   // sw is a power of two
+  const int RPW = 32 >> lg;        // rows per warp per interleave slot
+  const int li = lane & (SW - 1);
+  int64_t row[R];
+  int32_t eb[R], ee[R];
+  bool valid[R];
+  RowIn in[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    row[q] = (int64_t)sg.row_begin + ((int64_t)local * R + q) * RPW + (lane >> lg);
+    valid[q] = row[q] < sg.row_end;
+    eb[q] = valid[q] ? (int32_t)__ldg(&p.rp[row[q]]) : 0;
+    ee[q] = valid[q] ? (int32_t)__ldg(&p.rp[row[q] + 1]) : 0;
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q)
+    if (valid[q] && li == 0) in[q] = row_in<P, MODE>(p, row[q]);
+  T s[R];
+  rows_sum<P, MODE, R>(p, cache, eb, ee, li, SW, s);
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    for (int o = SW >> 1; o > 0; o >>= 1) s[q] = P::add(s[q], P::shfl(s[q], o));
+    if (valid[q] && li == 0) epilogue<P, MODE>(p, row[q], s[q], dsum, in[q], a);
+  }
+}
 
+template <class P, int MODE>
+__device__ __forceinline__ void hub_task(const IterParams &p, const void *cache, int t, int lane,
+                                         df dsum, Acc &a) {
+  using T = typename P::T;
+  const int32_t h = __ldg(&p.hub_task_row[t]);
+  const int32_t first = __ldg(&p.hub_first[h]);
+  const int32_t nch = __ldg(&p.hub_first[h + 1]) - first;
+  const int32_t rb = (int32_t)__ldg(&p.rp[h]), re = (int32_t)__ldg(&p.rp[h + 1]);
+  const int32_t cs = rb + (t - first) * kHubChunk;
+  const int32_t eb[1] = {cs}, ee[1] = {min(re, cs + kHubChunk)};
+  T s[1];
+  rows_sum<P, MODE, 1>(p, cache, eb, ee, lane, 32, s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s[0] = P::add(s[0], P::shfl(s[0], o));
+  if (lane == 0) {
+    p.lpart[t] = P::pack(s[0]);
+    __threadfence();
+    const unsigned tk = atomicAdd(&p.lcnt[h], 1u);
+    if (tk == (unsigned)(nch - 1)) {
+      __threadfence();
+      T sum = P::zero();
+      for (int j = 0; j < nch; ++j) sum = P::add(sum, P::unpack(__ldcg(&p.lpart[first + j])));
+      p.lcnt[h] = 0;
+      const RowIn in = row_in<P, MODE>(p, h);
+      epilogue<P, MODE>(p, h, sum, dsum, in, a);
+    }
+  }
+}
+
+template <class P, int MODE>
+__global__ void __launch_bounds__(kIterThreads, kMinBlocks) iterate_kernel(IterParams p) {
+  __shared__ long long bred[2][kIterWarps];
+  __shared__ int bbad[kIterWarps];
+  extern __shared__ __align__(16) unsigned char gcache[];
   df dsum;
   if (!prologue<P::kDF>(p, &dsum)) return;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int nb = p.plan.n_batches;
-  // the batches of this block are blockIdx.x + j * gridDim.x, j = 0, 1, ...
-  if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
-    fence_mbar_init();
+  if constexpr (P::kCached > 0) {
+    P::stage(p, gcache, p.n);
+    __syncthreads();
   }
-  __syncthreads();
-  if (tid == 0)
-    for (int j = 0; j < kStages; ++j) {
-      const int b = blockIdx.x + j * gridDim.x;
-      if (b < nb) issue_batch<MODE>(p, b, stages[j], desc[j], &full[j]);
-    }
-  P::stage(p, cache);  // hot prefix of the gathered vector, while the copies fly
-  __syncthreads();
-
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarps = gridDim.x * kIterWarps;
   Acc a;
-  for (int j = 0;; ++j) {
-    const int b = blockIdx.x + j * gridDim.x;
-    if (b >= nb) break;
-    const int s = j % kStages;
-    const bool ok = mbar_wait(&full[s], (uint32_t)((j / kStages) & 1));
-    if (!__syncthreads_and(ok)) {
-      // a bounded wait ran out: record it, let the copies already issued
-      // land (bounded again), and leave
-      if (tid == 0) {
-        atomicOr(p.err, 1);
-        for (int jj = j; jj < j + kStages; ++jj)
-          if ((int)blockIdx.x + jj * (int)gridDim.x < nb)
-            mbar_wait(&full[jj % kStages], (uint32_t)((jj / kStages) & 1));
-      }
-      break;
+  for (int t = blockIdx.x * kIterWarps + wid; t < p.plan.n_tasks; t += nwarps) {
+    if (t < p.plan.n_hub_tasks) {
+      hub_task<P, MODE>(p, gcache, t, lane, dsum, a);
+      continue;
     }
-    const Stage &stg = stages[s];
-    const BatchDesc dsc = desc[s];
-    if (dsc.kind == 0) {
-      const int sw = dsc.sw;
-      const int lg = 31 - __clz(sw);
-      const int rr = tid >> lg, li = tid & (sw - 1);
-      const bool valid = rr < dsc.nrows;
-      const int64_t row = (int64_t)dsc.row0 + rr;
-      RowIn in;
-      if (valid && li == 0) in = row_in<P, MODE>(p, row);
-      int eb = 0, ee = 0;
-      if (valid) {
-        eb = (int)(stg.rp[dsc.row0 - dsc.rpa + rr] - dsc.e0a);
-        ee = (int)(stg.rp[dsc.row0 - dsc.rpa + rr + 1] - dsc.e0a);
-      }
-      T sum = P::zero();
-      for (int e = eb + li; e < ee; e += 4 * sw) {
-        const bool o1 = e + sw < ee, o2 = e + 2 * sw < ee, o3 = e + 3 * sw < ee;
-        const int32_t c0 = stg.col[e];
-        const int32_t c1 = o1 ? stg.col[e + sw] : 0;
-        const int32_t c2 = o2 ? stg.col[e + 2 * sw] : 0;
-        const int32_t c3 = o3 ? stg.col[e + 3 * sw] : 0;
-        const T g0 = P::load_g(p, cache, c0);
-        const T g1 = o1 ? P::load_g(p, cache, c1) : P::zero();
-        const T g2 = o2 ? P::load_g(p, cache, c2) : P::zero();
-        const T g3 = o3 ? P::load_g(p, cache, c3) : P::zero();
-        if (MODE == kWeighted) {
-          sum = P::add(sum, P::scale(g0, stg.val[e]));
-          if (o1) sum = P::add(sum, P::scale(g1, stg.val[e + sw]));
-          if (o2) sum = P::add(sum, P::scale(g2, stg.val[e + 2 * sw]));
-          if (o3) sum = P::add(sum, P::scale(g3, stg.val[e + 3 * sw]));
-        } else {
-          sum = P::add(sum, g0);
-          if (o1) sum = P::add(sum, g1);
-          if (o2) sum = P::add(sum, g2);
-          if (o3) sum = P::add(sum, g3);
-        }
-      }
-      for (int o = sw >> 1; o > 0; o >>= 1) sum = P::add(sum, P::shfl(sum, o));
-      if (valid && li == 0) epilogue<P, MODE>(p, row, sum, dsum, in, a);
-    } else {
-      // chunk [cs, ce) of big row row0, reduced by the whole block
-      const int lo = dsc.cs - dsc.e0a, hi = dsc.ce - dsc.e0a;
-      T sum = P::zero();
-      for (int e = lo + tid; e < hi; e += 4 * kPullThreads) {
-        const int e1 = e + kPullThreads, e2 = e + 2 * kPullThreads, e3 = e + 3 * kPullThreads;
-        const bool o1 = e1 < hi, o2 = e2 < hi, o3 = e3 < hi;
-        const T g0 = P::load_g(p, cache, stg.col[e]);
-        const T g1 = o1 ? P::load_g(p, cache, stg.col[e1]) : P::zero();
-        const T g2 = o2 ? P::load_g(p, cache, stg.col[e2]) : P::zero();
-        const T g3 = o3 ? P::load_g(p, cache, stg.col[e3]) : P::zero();
-        if (MODE == kWeighted) {
-          sum = P::add(sum, P::scale(g0, stg.val[e]));
-          if (o1) sum = P::add(sum, P::scale(g1, stg.val[e1]));
-          if (o2) sum = P::add(sum, P::scale(g2, stg.val[e2]));
-          if (o3) sum = P::add(sum, P::scale(g3, stg.val[e3]));
-        } else {
-          sum = P::add(sum, g0);
-          if (o1) sum = P::add(sum, g1);
-          if (o2) sum = P::add(sum, g2);
-          if (o3) sum = P::add(sum, g3);
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) sum = P::add(sum, P::shfl(sum, o));
-      if (lane == 0) wred[wid] = sum;
-      __syncthreads();
-      if (tid == 0) {
-        T tot = wred[0];
-        for (int w = 1; w < kPullWarps; ++w) tot = P::add(tot, wred[w]);
-        const int h = dsc.row0;
-        if (dsc.nch == 1) {
-          const RowIn in = row_in<P, MODE>(p, h);
-          epilogue<P, MODE>(p, h, tot, dsum, in, a);
-        } else {
-          p.lpart[b] = P::pack(tot);
-          __threadfence();
-          const unsigned tk = atomicAdd(&p.lcnt[h], 1u);
-          if (tk == (unsigned)(dsc.nch - 1)) {
-            __threadfence();
-            T all = P::zero();
-            for (int q = 0; q < dsc.nch; ++q) all = P::add(all, P::unpack(__ldcg(&p.lpart[dsc.first + q])));
-            p.lcnt[h] = 0;
-            const RowIn in = row_in<P, MODE>(p, h);
-            epilogue<P, MODE>(p, h, all, dsum, in, a);
-          }
-        }
-      }
-    }
-    __syncthreads();  // stage s is free again
-    if (tid == 0) {
-      const int bn = blockIdx.x + (j + kStages) * gridDim.x;
-      if (bn < nb) {
-        fence_proxy_async_smem();
-        issue_batch<MODE>(p, bn, stages[s], desc[s], &full[s]);
-      }
-    }
+    int si = 0;
+    while (si + 1 < p.plan.n_segs && t >= p.plan.segs[si + 1].task_begin) ++si;
+    const Segment sg = p.plan.segs[si];
+    row_task<P, MODE>(p, gcache, sg, t - sg.task_begin, lane, dsum, a);
   }
 
   // ---- block totals of the exact fixed-point sums -> one atomic each
@@ -458,10 +507,10 @@ __global__ void __launch_bounds__(kPullThreads, 1) pull_kernel(IterParams p) {
   int bad = warp_or(a.bad);
   if (lane == 0) { bred[0][wid] = l1; bred[1][wid] = dg; bbad[wid] = bad; }
   __syncthreads();
-  if (tid == 0) {
+  if (threadIdx.x == 0) {
     long long t1 = 0, t2 = 0;
     int tb = 0;
-    for (int w = 0; w < kPullWarps; ++w) { t1 += bred[0][w]; t2 += bred[1][w]; tb |= bbad[w]; }
+    for (int w = 0; w < kIterWarps; ++w) { t1 += bred[0][w]; t2 += bred[1][w]; tb |= bbad[w]; }
     const int cur = (int)(p.k % 3);
     atomicAdd((unsigned long long *)&p.sums[cur * 4 + 1], (unsigned long long)t1);
     atomicAdd((unsigned long long *)&p.sums[cur * 4 + 0], (unsigned long long)t2);
@@ -523,7 +572,7 @@ __global__ void permute_pdf(int64_t n, const float2 *src, const int32_t *perm, f
 void workspace_free(Workspace &ws) {
   cudaFree(ws.gdf[0]); cudaFree(ws.gdf[1]); cudaFree(ws.gf[0]); cudaFree(ws.gf[1]);
   cudaFree(ws.acc); cudaFree(ws.tail); cudaFree(ws.pdf); cudaFree(ws.scores);
-  cudaFree(ws.sums); cudaFree(ws.lpart); cudaFree(ws.lcnt); cudaFree(ws.state); cudaFree(ws.err);
+  cudaFree(ws.sums); cudaFree(ws.lpart); cudaFree(ws.lcnt); cudaFree(ws.state);
   ws = Workspace{};
 }
 
@@ -532,40 +581,44 @@ Status workspace_ensure(Ctx *ctx, Graph *g) {
   Workspace &ws = g->ws;
   if (ws.sums) return Status::ok();
   const size_t n = (size_t)std::max<int64_t>(g->n, 1);
-  const size_t nbb = (size_t)std::max<int32_t>(g->plan.n_big_batches, 1);
-  const size_t nbig = (size_t)std::max<int32_t>(g->plan.n_big, 1);
-  GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[0], sizeof(float2) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[1], sizeof(float2) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.gf[0], sizeof(float) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.gf[1], sizeof(float) * n));
+  const size_t nht = (size_t)std::max<int32_t>(g->plan.n_hub_tasks, 1);
+  const size_t nh = (size_t)std::max<int32_t>(g->plan.n_hub, 1);
+  // one extra entry: index n is the column of row padding and always 0
+  GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[0], sizeof(float2) * (n + 1)));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[1], sizeof(float2) * (n + 1)));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.gf[0], sizeof(float) * (n + 1)));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.gf[1], sizeof(float) * (n + 1)));
   GOPS_CUDA_TRY(cudaMalloc(&ws.acc, sizeof(float2) * n));
   GOPS_CUDA_TRY(cudaMalloc(&ws.tail, sizeof(float) * n));
   GOPS_CUDA_TRY(cudaMalloc(&ws.pdf, sizeof(float2) * n));
   GOPS_CUDA_TRY(cudaMalloc(&ws.scores, sizeof(double) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.lpart, sizeof(float2) * nbb));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.lcnt, sizeof(unsigned) * nbig));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.lpart, sizeof(float2) * nht));
+  GOPS_CUDA_TRY(cudaMalloc(&ws.lcnt, sizeof(unsigned) * nh));
   GOPS_CUDA_TRY(cudaMalloc(&ws.state, sizeof(SolveState)));
   GOPS_CUDA_TRY(cudaMalloc(&ws.sums, sizeof(long long) * 12));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.err, sizeof(int)));
   ws.n = g->n;
   return Status::ok();
 }
 
 namespace {
 
-constexpr size_t kPullSmem = sizeof(Stage) * kStages + sizeof(float) * kHot;
+template <class P>
+size_t iter_smem(const Graph *g) {
+  return P::kCached > 0 ? sizeof(typename P::T) * (size_t)std::min<int64_t>(g->n, P::kCached) : 0;
+}
 
 template <class P, int MODE>
-Status pull_grid(const Ctx *ctx, const Graph *g, int *grid) {
-  GOPS_CUDA_TRY(cudaFuncSetAttribute(pull_kernel<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kPullSmem));
+int grid_for_iter(const Ctx *ctx, const Graph *g) {
+  const size_t smem = iter_smem<P>(g);
   int occ = 0;
-  GOPS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pull_kernel<P, MODE>, kPullThreads,
-                                                              kPullSmem));
+  if (smem > 0)
+    cudaFuncSetAttribute(iterate_kernel<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (kL1Policy && smem == 0)
+    cudaFuncSetAttribute(iterate_kernel<P, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, iterate_kernel<P, MODE>, kIterThreads, smem);
   occ = std::max(1, occ);
-  *grid = (int)std::max<int64_t>(
-      1, std::min<int64_t>(std::max<int32_t>(g->plan.n_batches, 1), (int64_t)ctx->num_sms * occ));
-  return Status::ok();
+  const int64_t blocks_needed = ceil_div<int64_t>(std::max<int32_t>(g->plan.n_tasks, 1), kIterWarps);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(blocks_needed, (int64_t)ctx->num_sms * occ));
 }
 
 template <int MODE>
@@ -579,8 +632,8 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   p.val = g->in_val;
   p.deg = g->deg;
   p.dmask = g->dmask_w;
-  p.big_first = g->big_first;
-  p.big_batch_row = g->big_batch_row;
+  p.hub_first = g->hub_first;
+  p.hub_task_row = g->hub_task_row;
   p.plan = g->plan;
   p.acc = ws.acc;
   p.tail = ws.tail;
@@ -589,7 +642,6 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   p.st = ws.state;
   p.lpart = ws.lpart;
   p.lcnt = ws.lcnt;
-  p.err = ws.err;
   p.d = df_from_double(cfg->damping);
   p.omd = df_from_double(1.0 - cfg->damping);
   p.inv_n = df_from_double(1.0 / (double)g->n);
@@ -603,9 +655,12 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   p.max_iter = cfg->max_iterations;
 
   GOPS_CUDA_TRY(cudaMemsetAsync(ws.sums, 0, sizeof(long long) * 12, s));
+  for (int b = 0; b < 2; ++b) {  // padding entry n of the gathered vectors
+    GOPS_CUDA_TRY(cudaMemsetAsync(ws.gdf[b] + g->n, 0, sizeof(float2), s));
+    GOPS_CUDA_TRY(cudaMemsetAsync(ws.gf[b] + g->n, 0, sizeof(float), s));
+  }
   GOPS_CUDA_TRY(cudaMemsetAsync(ws.state, 0, sizeof(SolveState), s));
-  GOPS_CUDA_TRY(cudaMemsetAsync(ws.err, 0, sizeof(int), s));
-  GOPS_CUDA_TRY(cudaMemsetAsync(ws.lcnt, 0, sizeof(unsigned) * std::max<int32_t>(g->plan.n_big, 1), s));
+  GOPS_CUDA_TRY(cudaMemsetAsync(ws.lcnt, 0, sizeof(unsigned) * std::max<int32_t>(g->plan.n_hub, 1), s));
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   uint64_t launches = 0;
   // step 0
@@ -619,9 +674,9 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   ++launches;
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
 
-  int grid_df = 1, grid_f = 1;
-  GOPS_TRY((pull_grid<PrecDF, MODE>(ctx, g, &grid_df)));
-  GOPS_TRY((pull_grid<PrecF32, MODE>(ctx, g, &grid_f)));
+  const int grid_df = grid_for_iter<PrecDF, MODE>(ctx, g);
+  const int grid_f = grid_for_iter<PrecF32, MODE>(ctx, g);
+  const size_t smem_df = iter_smem<PrecDF>(g), smem_f = iter_smem<PrecF32>(g);
   bool f32_known = false;
   unsigned long long k = 1;
   const int chunk = 4;
@@ -631,9 +686,9 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
     if (!ctx->timing) return Status::ok();
     const size_t need = 2 * (timed.size() + 1);
     while (ctx->tev.size() < need) {
-      cudaEvent_t ev;
-      GOPS_CUDA_TRY(cudaEventCreate(&ev));
-      ctx->tev.push_back(ev);
+      cudaEvent_t e;
+      GOPS_CUDA_TRY(cudaEventCreate(&e));
+      ctx->tev.push_back(e);
     }
     timed.push_back({k, is_df});
     return Status::ok();
@@ -648,14 +703,14 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
       if (!f32_known) {
         GOPS_TRY(timed_launch(true));
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 2], s));
-        pull_kernel<PrecDF, MODE><<<grid_df, kPullThreads, kPullSmem, s>>>(p);
+        iterate_kernel<PrecDF, MODE><<<grid_df, kIterThreads, smem_df, s>>>(p);
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 1], s));
         ++launches;
       }
       if (k >= 2) {
         GOPS_TRY(timed_launch(false));
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 2], s));
-        pull_kernel<PrecF32, MODE><<<grid_f, kPullThreads, kPullSmem, s>>>(p);
+        iterate_kernel<PrecF32, MODE><<<grid_f, kIterThreads, smem_f, s>>>(p);
         if (ctx->timing) GOPS_CUDA_TRY(cudaEventRecord(ctx->tev[2 * timed.size() - 1], s));
         ++launches;
       }
@@ -669,8 +724,6 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
     if (k - 1 > cfg->max_iterations)
       return Status{GOPS_ERR_INTERNAL, "solver did not record completion"};
   }
-  int err = 0;
-  GOPS_CUDA_TRY(cudaMemcpyAsync(&err, ws.err, sizeof(int), cudaMemcpyDeviceToHost, s));
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   finalize_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(g->n, 256), 4096)),
                     256, 0, s>>>(g->n, ws.acc, ws.tail, g->perm, ws.scores);
@@ -678,7 +731,6 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
   ++launches;
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
   GOPS_CUDA_TRY(cudaEventSynchronize(ctx->ev[3]));
-  if (err) return Status{GOPS_ERR_TIMEOUT, "a bounded device wait ran out in the pull kernel"};
   run->iterations = ctx->host_state->iterations;
   run->diff_l1 = ctx->host_state->diff_l1;
   run->converged = ctx->host_state->converged;
@@ -696,8 +748,7 @@ Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_r
     for (size_t i = 0; i < timed.size(); ++i) {
       const unsigned long long kk = timed[i].first;
       const bool is_df = timed[i].second;
-      const bool active =
-          kk <= its && (is_df ? (f32_from == 0 || kk < f32_from) : (f32_from && kk >= f32_from));
+      const bool active = kk <= its && (is_df ? (f32_from == 0 || kk < f32_from) : (f32_from && kk >= f32_from));
       if (!active) continue;
       float ms = 0.f;
       cudaEventElapsedTime(&ms, ctx->tev[2 * i], ctx->tev[2 * i + 1]);

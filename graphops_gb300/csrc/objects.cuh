@@ -34,7 +34,7 @@ struct Plan {
 constexpr int kHubChunk = 1024;      // edges per hub task (one warp)
 constexpr int kHubThreshold = 4096;  // rows above this in-degree are hubs
 #ifndef GOPS_PAD4
-#define GOPS_PAD4 0
+#define GOPS_PAD4 1
 #endif
 // With kRowAlign == 4 every in-row is padded to a multiple of four edges
 // (padding: column n, weight 0; entry n of the gathered vectors is 0), so a

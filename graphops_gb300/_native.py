@@ -65,6 +65,7 @@ SIGNATURES = [
     ("gops_pagerank_weighted_run", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, ctypes.POINTER(Run)]),
     ("gops_personalized_pagerank_run", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, _p, ctypes.POINTER(Run)]),
     ("gops_ctx_scores_device", _p, [_p]),
+    ("gops_pagerank_run_noalloc", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, ctypes.POINTER(Run)]),
 ]
 
 _lib = None

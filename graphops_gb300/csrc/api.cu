@@ -15,12 +15,6 @@ Status dense_to_out_csr_device(Ctx *ctx, int64_t n, const double *d_M, int64_t *
 
 using namespace gops;
 
-struct gops_ctx {
-  Ctx impl;
-};
-struct gops_graph {
-  Graph impl;
-};
 
 namespace {
 

@@ -113,6 +113,8 @@ struct Ctx {
   }
 };
 
+Status solve_plain_in_workspace(Ctx *ctx, Graph *g, const gops_config *cfg, Workspace &ws,
+                                double *scores_host, gops_run *run);
 Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_rp,
                                        const int32_t *d_out_col, const double *d_w);
 Status workspace_ensure(Ctx *ctx, Graph *g);
@@ -120,3 +122,11 @@ void workspace_free(Workspace &ws);
 void graph_free_device(Graph &g);
 
 }  // namespace gops
+
+// the opaque handles of include/gops.h
+struct gops_ctx {
+  gops::Ctx impl;
+};
+struct gops_graph {
+  gops::Graph impl;
+};

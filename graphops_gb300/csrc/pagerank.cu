@@ -622,9 +622,9 @@ int grid_for_iter(const Ctx *ctx, const Graph *g) {
 }
 
 template <int MODE>
-Status run_mode(Ctx *ctx, Graph *g, const gops_config *cfg, double pv_l1, gops_run *run) {
+Status run_mode(Ctx *ctx, Graph *g, Workspace &ws, const gops_config *cfg, double pv_l1,
+                gops_run *run) {
   cudaStream_t s = ctx->stream;
-  Workspace &ws = g->ws;
   IterParams p{};
   p.n = g->n;
   p.rp = g->in_rp;
@@ -803,13 +803,40 @@ Status solve(Ctx *ctx, Graph *g, const gops_config *cfg, int mode, const double 
     if (!std::isfinite(pv_l1)) pv_l1 = 1.0;
   }
   Status st;
-  if (mode == kPlain) st = run_mode<kPlain>(ctx, g, cfg, pv_l1, run);
-  else if (mode == kWeighted) st = run_mode<kWeighted>(ctx, g, cfg, pv_l1, run);
-  else st = run_mode<kPpr>(ctx, g, cfg, pv_l1, run);
+  if (mode == kPlain) st = run_mode<kPlain>(ctx, g, g->ws, cfg, pv_l1, run);
+  else if (mode == kWeighted) st = run_mode<kWeighted>(ctx, g, g->ws, cfg, pv_l1, run);
+  else st = run_mode<kPpr>(ctx, g, g->ws, cfg, pv_l1, run);
   GOPS_TRY(st);
   ctx->last_scores = g->ws.scores;
   if (scores_host) {
     GOPS_CUDA_TRY(cudaMemcpyAsync(scores_host, g->ws.scores, sizeof(double) * (size_t)g->n,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    GOPS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->stats.d2h_bytes += sizeof(double) * (size_t)g->n;
+  }
+  return Status::ok();
+}
+
+// Plain PageRank (as solve(.., kPlain, ..)) on a workspace the caller
+// provides; performs no device or pinned allocation of its own.
+Status solve_plain_in_workspace(Ctx *ctx, Graph *g, const gops_config *cfg, Workspace &ws,
+                                double *scores_host, gops_run *run) {
+  ctx->stats = gops_stats{};
+  if (g->n == 0) {
+    run->iterations = 0;
+    run->diff_l1 = 0.0;
+    run->converged = 1;
+    run->reserved = 0;
+    return Status::ok();
+  }
+  const bool timing = ctx->timing;
+  ctx->timing = false;  // per-launch timing would create events
+  Status st = run_mode<kPlain>(ctx, g, ws, cfg, 1.0, run);
+  ctx->timing = timing;
+  GOPS_TRY(st);
+  ctx->last_scores = ws.scores;
+  if (scores_host) {
+    GOPS_CUDA_TRY(cudaMemcpyAsync(scores_host, ws.scores, sizeof(double) * (size_t)g->n,
                                   cudaMemcpyDeviceToHost, ctx->stream));
     GOPS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     ctx->stats.d2h_bytes += sizeof(double) * (size_t)g->n;

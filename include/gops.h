@@ -151,6 +151,22 @@ int gops_personalized_pagerank_run(gops_ctx *ctx, const gops_graph *g, const gop
  * the next solve on this context. */
 const double *gops_ctx_scores_device(const gops_ctx *ctx);
 
+/* gops_pagerank_run without any allocation.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory when
+ * they solve -- a process whose device memory belongs to another allocator
+ * (a framework's caching pool), or a latency-critical path where
+ * cudaMalloc/cudaFree would synchronize the device.  Same kernels and results
+ * as gops_pagerank_run; the per-solve scratch lives in a fixed __device__
+ * array of the library (about 13 MB, held by every GPU that loads the
+ * library until exit) instead of the graph's workspace.  Limits: at most
+ * 262,144 nodes and 65,536 hub tasks, else GOPS_ERR_INVALID.  The graph must
+ * already be uploaded (that call allocates).  All calls share the array:
+ * calls that overlap on the GPU race and must be serialized by the caller.
+ * The first call on a device looks up the array's address, so make it
+ * before any stream capture. */
+int gops_pagerank_run_noalloc(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg,
+                              double *scores, gops_run *run);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,6 +29,7 @@ from .pagerank import (
     top_k,
 )
 from ._native import Context, DeviceGraph, GopsError, default_context
+from .batch import BatchRun, ppr_batch, seed_sets_to_csr
 
 __all__ = [
     "AdjacencyMatrix", "CsrAdjacency", "DiGraph", "GraphopsError", "InvalidParameter",
@@ -37,5 +38,5 @@ __all__ = [
     "pagerank_weighted_checked_run", "pagerank_weighted_run", "personalized_pagerank",
     "personalized_pagerank_checked", "personalized_pagerank_checked_run",
     "personalized_pagerank_run", "top_k", "Context", "DeviceGraph", "GopsError",
-    "default_context",
+    "default_context", "BatchRun", "ppr_batch", "seed_sets_to_csr",
 ]

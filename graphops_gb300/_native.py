@@ -66,6 +66,8 @@ SIGNATURES = [
     ("gops_personalized_pagerank_run", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, _p, ctypes.POINTER(Run)]),
     ("gops_ctx_scores_device", _p, [_p]),
     ("gops_pagerank_run_noalloc", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, ctypes.POINTER(Run)]),
+    ("gops_ppr_batch", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
+    ("gops_ppr_batch_device", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
 ]
 
 _lib = None
@@ -209,6 +211,26 @@ class DeviceGraph:
             rc = fn(self.ctx.handle, self.handle, ctypes.byref(c), ptr(pp), ptr(scores), ctypes.byref(r))
         self.ctx.check(rc)
         return scores, int(r.iterations), float(r.diff_l1), bool(r.converged)
+
+    def ppr_batch(self, cfg, seed_ptr, seed_idx, x0=None, out=True):
+        """Batched PPR over seed sets (CSR: seed_ptr[nsets+1], seed_idx).
+        Returns (scores float32 [nsets, n] or None, runs as a structured array)."""
+        sp = np.ascontiguousarray(seed_ptr, dtype=np.int64)
+        si = np.ascontiguousarray(seed_idx, dtype=np.int32)
+        ns = int(sp.shape[0]) - 1
+        c = Config(float(cfg.damping), int(cfg.max_iterations), float(cfg.tolerance))
+        scores = np.empty((ns, self.n), dtype=np.float32) if out else None
+        xx = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float32)
+        if xx is not None and xx.shape != (ns, self.n):
+            raise ValueError("x0 must have shape (nsets, n)")
+        runs = (Run * max(ns, 1))()
+        self.ctx.check(self.ctx._l.gops_ppr_batch(self.ctx.handle, self.handle, ctypes.byref(c), ns,
+                                                  ptr(sp), ptr(si), ptr(xx), ptr(scores),
+                                                  ctypes.cast(runs, ctypes.c_void_p)))
+        its = np.array([runs[i].iterations for i in range(ns)], dtype=np.int64)
+        diffs = np.array([runs[i].diff_l1 for i in range(ns)], dtype=np.float64)
+        conv = np.array([bool(runs[i].converged) for i in range(ns)])
+        return scores, its, diffs, conv
 
     def pagerank_run(self, cfg, out=True):
         return self._solve("gops_pagerank_run", cfg, out=out)

@@ -11,6 +11,9 @@ Status solve(Ctx *ctx, Graph *g, const gops_config *cfg, int mode, const double 
              double *scores_host, gops_run *run);
 Status dense_to_out_csr_device(Ctx *ctx, int64_t n, const double *d_M, int64_t **d_rp,
                                int32_t **d_col, double **d_w, int64_t *m_out);
+Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, const int64_t *seed_ptr,
+                 const int32_t *seed_idx, const float *x0, bool x0_on_device, float *scores,
+                 bool scores_on_device, gops_run *runs);
 }  // namespace gops
 
 using namespace gops;
@@ -276,6 +279,31 @@ int gops_pagerank_weighted_run(gops_ctx *ctx, const gops_graph *g, const gops_co
 int gops_personalized_pagerank_run(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg,
                                    const double *personalization, double *scores, gops_run *run) {
   return run_common(ctx, g, cfg, 2, personalization, scores, run);
+}
+
+static int batch_common(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,
+                        const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0,
+                        float *scores, gops_run *runs, bool on_device) {
+  if (!ctx) return GOPS_ERR_INVALID;
+  Ctx &c = ctx->impl;
+  if (!g || !cfg || nsets < 0 || (nsets > 0 && (!seed_ptr || (!seed_idx && seed_ptr[nsets] > seed_ptr[0]))))
+    return c.set(Status{GOPS_ERR_INVALID, "null argument"});
+  if (g->impl.ctx != &c) return c.set(Status{GOPS_ERR_INVALID, "graph belongs to another context"});
+  cudaSetDevice(c.device);
+  return c.set(ppr_batch(&c, const_cast<Graph *>(&g->impl), cfg, nsets, seed_ptr, seed_idx, x0, on_device,
+                         scores, on_device, runs));
+}
+
+int gops_ppr_batch(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,
+                   const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0, float *scores,
+                   gops_run *runs) {
+  return batch_common(ctx, g, cfg, nsets, seed_ptr, seed_idx, x0, scores, runs, false);
+}
+
+int gops_ppr_batch_device(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,
+                          const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0_device,
+                          float *scores_device, gops_run *runs) {
+  return batch_common(ctx, g, cfg, nsets, seed_ptr, seed_idx, x0_device, scores_device, runs, true);
 }
 
 const double *gops_ctx_scores_device(const gops_ctx *ctx) {

@@ -93,7 +93,10 @@ struct Graph {
   int32_t *hub_task_row = nullptr;  // hub task -> hub row
   Plan plan;
   Workspace ws;
+  struct BatchState *batch = nullptr;  // batched-PPR plan and workspace (built on first use)
 };
+
+void batch_free(Graph &g);
 
 struct Ctx {
   int device = 0;

@@ -1,0 +1,695 @@
+// Batched personalized PageRank (K5): many seed sets per pass over the graph.
+//
+// Each seed set is one independent personalized_pagerank_run of the
+// reference (src/ppr.rs:90-156) with personalization 1 on each seed node
+// (repeats count), normalised as src/ppr.rs:104-109 does -- an empty set gives
+// the uniform vector.  Sets run in waves of kCols columns.  Per wave the
+// library keeps row-major n x kCols blocks (relabelled node order) of the
+// gathered step vector, the double-float accumulator and the FP32 tail --
+// the residual form of the single solve (csrc/pagerank.cu), column by column:
+//   r_1 = F(x_0) - x_0,  r_{k+1} = A r_k,  x_k = x_0 + sum r,  diff_k = ||r_k||_1
+// with a double-float phase while some column's step norm is >= theta.
+//
+// Kernel layout: a warp owns a row and lane c owns column c, so every
+// gathered in-neighbour row is one coalesced 128-byte load (FP32 phase);
+// 32 column indices are loaded at once and broadcast by shuffles, eight
+// gathers in flight per lane.  Rows with more than kSpmmBig in-edges are split
+// into kSpmmChunk-edge warp tasks combined, in chunk order, by the task that
+// arrives last.  Per-column dangling and L1 sums are exact 64-bit fixed-point
+// integers held per lane, so every column's result is independent of the
+// others and of the schedule.  A column whose step norm fell below tol at step
+// k-1 retires at step k: its values freeze (the reference returns that x) and
+// it stops contributing; the wave ends when every column has retired or
+// max_iterations is reached.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <vector>
+
+#include "objects.cuh"
+#include "primitives.cuh"
+
+namespace gops {
+
+constexpr int kCols = 32;       // columns per wave (one per lane)
+constexpr int kSpmmBig = 256;   // rows above this in-degree are chunked
+constexpr int kSpmmChunk = 256; // edges per chunk task
+constexpr int kBThreads = 256;
+constexpr int kBWarps = kBThreads / kWarp;
+constexpr double kBTheta = 1e-2;
+
+struct ColState {
+  unsigned long long iterations;
+  double diff_l1;
+  int retired;
+  int converged;
+  int uniform;  // personalization is uniform (empty seed set)
+  int pad;
+};
+
+struct WaveState {
+  int done;
+  int f32_phase;
+  unsigned long long f32_from;
+  unsigned long long steps;  // last step that did work
+};
+
+struct BatchState {
+  int64_t n = 0;
+  // plan: rows [0, n_big) in chunk tasks, then one warp task per row
+  int32_t n_big = 0, n_big_tasks = 0;
+  int64_t n_tasks = 0;
+  int32_t *big_first = nullptr, *big_task_row = nullptr;
+  // wave workspace
+  float2 *gdf[2] = {nullptr, nullptr};
+  float *gf[2] = {nullptr, nullptr};
+  float2 *acc = nullptr;
+  float *tail = nullptr;
+  float2 *lpart = nullptr;
+  unsigned *lcnt = nullptr;
+  long long *sums = nullptr;  // 3 slots x kCols x {dangling, l1, nonfinite, spare}
+  ColState *cols = nullptr;
+  WaveState *wave = nullptr;
+  int32_t *prow = nullptr;    // n + 1
+  int32_t *pslot = nullptr;   // seed entries of the wave: column slot
+  float2 *pval = nullptr;     //   and normalised weight (double-float)
+  int32_t *prows_sorted = nullptr;
+  int64_t pcap = 0;
+  float *x0 = nullptr;        // warm-start vectors of the wave (set-major, original order)
+  float *out = nullptr;       // results of the wave (set-major, original order)
+  std::vector<int32_t> inv_perm;  // host: original id -> relabelled row
+};
+
+void batch_free(Graph &g) {
+  BatchState *b = g.batch;
+  if (!b) return;
+  cudaFree(b->big_first); cudaFree(b->big_task_row);
+  cudaFree(b->gdf[0]); cudaFree(b->gdf[1]); cudaFree(b->gf[0]); cudaFree(b->gf[1]);
+  cudaFree(b->acc); cudaFree(b->tail); cudaFree(b->lpart); cudaFree(b->lcnt);
+  cudaFree(b->sums); cudaFree(b->cols); cudaFree(b->wave); cudaFree(b->prow);
+  cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted); cudaFree(b->x0); cudaFree(b->out);
+  delete b;
+  g.batch = nullptr;
+}
+
+struct BatchParams {
+  int64_t n;
+  const int64_t *rp;
+  const int32_t *col;
+  const float *deg;
+  const int32_t *perm;
+  int32_t n_big, n_big_tasks;
+  int64_t n_tasks;
+  const int32_t *big_first, *big_task_row;
+  const int32_t *prow, *pslot;
+  const float2 *pval;
+  const float2 *gdf_in;
+  float2 *gdf_out;
+  const float *gf_in;
+  float *gf_out;
+  float2 *acc;
+  float *tail;
+  float2 *lpart;
+  unsigned *lcnt;
+  long long *sums;
+  ColState *cols;
+  WaveState *wave;
+  const float *x0;  // nullable
+  float *out;
+  int ncols;
+  df d, omd, inv_n;
+  float fx_scale;
+  double fx_inv;
+  double tol, theta;
+  unsigned long long k, max_iter;
+};
+
+namespace {
+
+struct BDF {
+  using T = df;
+  static constexpr bool kDF = true;
+  __device__ static T zero() { return {0.0f, 0.0f}; }
+  __device__ static T add(T a, T b) { return df_add(a, b); }
+  __device__ static T load(const BatchParams &p, int64_t i) {
+    const float2 v = __ldg(&p.gdf_in[i]);
+    return {v.x, v.y};
+  }
+  __device__ static float2 pack(T v) { return make_float2(v.hi, v.lo); }
+  __device__ static T unpack(float2 v) { return {v.x, v.y}; }
+};
+
+struct BF32 {
+  using T = float;
+  static constexpr bool kDF = false;
+  __device__ static T zero() { return 0.0f; }
+  __device__ static T add(T a, T b) { return a + b; }
+  __device__ static T load(const BatchParams &p, int64_t i) { return __ldg(&p.gf_in[i]); }
+  __device__ static float2 pack(T v) { return make_float2(v, 0.0f); }
+  __device__ static T unpack(float2 v) { return v.x; }
+};
+
+// personalization entry of (row v, column lane), double-float
+__device__ __forceinline__ df red_of(const BatchParams &p, int64_t v, int lane, bool uniform) {
+  if (uniform) return p.inv_n;
+  df red = {0.0f, 0.0f};
+  const int pb = __ldg(&p.prow[v]), pe = __ldg(&p.prow[v + 1]);
+  for (int e = pb; e < pe; ++e)
+    if (__ldg(&p.pslot[e]) == lane) {
+      const float2 w = __ldg(&p.pval[e]);
+      red = {w.x, w.y};
+    }
+  return red;
+}
+
+struct LaneAcc {
+  long long l1 = 0, dang = 0;
+  int bad = 0;
+};
+
+// Gathered sum of row edges [eb, ee) for this lane's column.
+template <class P>
+__device__ __forceinline__ typename P::T gather_sum(const BatchParams &p, int eb, int ee, int lane) {
+  using T = typename P::T;
+  T s = P::zero();
+  for (int base = eb; base < ee; base += 32) {
+    const int cnt = min(32, ee - base);
+    const int my = base + lane;
+    const int32_t cidx = my < ee ? __ldg(&p.col[my]) : (int32_t)p.n;
+    for (int j = 0; j < cnt; j += 8) {
+      T g[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int32_t c = __shfl_sync(0xffffffffu, cidx, (j + q) & 31);
+        g[q] = (j + q < cnt) ? P::load(p, (int64_t)c * kCols + lane) : P::zero();
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (j + q < cnt) s = P::add(s, g[q]);
+    }
+  }
+  return s;
+}
+
+template <class P>
+__device__ __forceinline__ void col_epilogue(const BatchParams &p, int64_t v, typename P::T s, df dsum,
+                                             bool uniform, LaneAcc &a, int lane) {
+  const df red = red_of(p, v, lane, uniform);
+  const float dg = __ldg(&p.deg[v]);
+  const int64_t i = v * kCols + lane;
+  if constexpr (P::kDF) {
+    const float2 ao = p.acc[i];
+    df r = df_mul(p.d, df_add(s, df_mul(dsum, red)));
+    if (p.k == 1) r = df_add(df_add(df_mul(p.omd, red), r), df_neg({ao.x, ao.y}));  // F(x_0) - x_0
+    const df an = df_add({ao.x, ao.y}, r);
+    p.acc[i] = make_float2(an.hi, an.lo);
+    const df ar = r.hi < 0.0f ? df_neg(r) : r;
+    a.l1 += fx_of(ar.hi, p.fx_scale) + fx_of(ar.lo, p.fx_scale);
+    a.bad |= !isfinite(r.hi);
+    if (dg == 0.0f) a.dang += fx_of(r.hi, p.fx_scale) + fx_of(r.lo, p.fx_scale);
+    const df g = dg > 0.0f ? df_div_f(r, dg) : df{0.0f, 0.0f};
+    p.gdf_out[i] = make_float2(g.hi, g.lo);
+    p.gf_out[i] = g.hi;
+  } else {
+    const float r = p.d.hi * (s + dsum.hi * red.hi);
+    p.tail[i] += r;
+    a.l1 += fx_of(fabsf(r), p.fx_scale);
+    a.bad |= !isfinite(r);
+    if (dg == 0.0f) a.dang += fx_of(r, p.fx_scale);
+    p.gf_out[i] = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
+  }
+}
+
+// Per-column view of step k: which columns are still active, their dangling
+// sums, and whether this kernel's precision is the active one.  Returns false
+// when the block should exit.  Every warp evaluates it identically.
+template <bool WANT_DF>
+__device__ bool batch_prologue(const BatchParams &p, int lane, bool *active, df *dsum, bool *uniform) {
+  const unsigned long long k = p.k;
+  if (*(volatile int *)&p.wave->done) return false;
+  const int prev = (int)((k - 1) % 3);
+  const bool col_ok = lane < p.ncols;
+  const int retired0 = col_ok ? *(volatile int *)&p.cols[lane].retired : 1;
+  double diff = INFINITY;
+  if (k > 1) {
+    const long long raw = *(volatile long long *)&p.sums[(prev * kCols + lane) * 4 + 1];
+    const long long badc = *(volatile long long *)&p.sums[(prev * kCols + lane) * 4 + 2];
+    diff = badc ? NAN : (double)raw * p.fx_inv;
+  }
+  const bool conv = !retired0 && k > 1 && diff < p.tol;
+  const bool cap = !retired0 && !conv && k - 1 >= p.max_iter;
+  const bool act = !retired0 && !conv && !cap;
+  if (blockIdx.x == 0 && threadIdx.x < 32 && (conv || cap)) {
+    p.cols[lane].retired = 1;
+    p.cols[lane].converged = conv ? 1 : 0;
+    p.cols[lane].iterations = k - 1;
+    p.cols[lane].diff_l1 = diff;
+  }
+  const unsigned any = __ballot_sync(0xffffffffu, act);
+  if (!any) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) p.wave->done = 1;
+    return false;
+  }
+  const bool big = act && !(diff < p.theta);
+  const bool f32 = k > 1 && (*(volatile int *)&p.wave->f32_phase || !__any_sync(0xffffffffu, big));
+  if (f32 == WANT_DF) return false;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    p.wave->f32_phase = f32 ? 1 : 0;
+    if (f32 && p.wave->f32_from == 0) p.wave->f32_from = k;
+    p.wave->steps = k;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    const int nxt = (int)((k + 1) % 3);
+    for (int i = 0; i < 4; ++i) p.sums[(nxt * kCols + lane) * 4 + i] = 0;
+  }
+  *active = act;
+  *uniform = col_ok && p.cols[lane].uniform;
+  const long long draw = *(volatile long long *)&p.sums[(prev * kCols + lane) * 4 + 0];
+  *dsum = df_from_double((double)draw * p.fx_inv);
+  return true;
+}
+
+template <class P>
+__global__ void __launch_bounds__(kBThreads) spmm_kernel(BatchParams p) {
+  using T = typename P::T;
+  __shared__ long long bl1[kBWarps][32], bdg[kBWarps][32];
+  __shared__ int bbad[kBWarps][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  bool active = false, uniform = false;
+  df dsum;
+  if (!batch_prologue<P::kDF>(p, lane, &active, &dsum, &uniform)) return;
+  LaneAcc a;
+  const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
+  for (int64_t t = (int64_t)blockIdx.x * kBWarps + wid; t < p.n_tasks; t += nwarps) {
+    if (t < p.n_big_tasks) {
+      const int h = __ldg(&p.big_task_row[t]);
+      const int first = __ldg(&p.big_first[h]);
+      const int nch = __ldg(&p.big_first[h + 1]) - first;
+      const int rb = (int)__ldg(&p.rp[h]), re = (int)__ldg(&p.rp[h + 1]);
+      const int cs = rb + ((int)t - first) * kSpmmChunk;
+      const int ce = min(re, cs + kSpmmChunk);
+      const T s = gather_sum<P>(p, cs, ce, lane);
+      p.lpart[t * kCols + lane] = P::pack(s);
+      __threadfence();
+      __syncwarp();
+      unsigned tk = 0;
+      if (lane == 0) tk = atomicAdd(&p.lcnt[h], 1u);
+      tk = __shfl_sync(0xffffffffu, tk, 0);
+      if (tk == (unsigned)(nch - 1)) {
+        __threadfence();
+        T all = P::zero();
+        for (int q = 0; q < nch; ++q) all = P::add(all, P::unpack(__ldcg(&p.lpart[(int64_t)(first + q) * kCols + lane])));
+        if (lane == 0) p.lcnt[h] = 0;
+        if (active) col_epilogue<P>(p, h, all, dsum, uniform, a, lane);
+      }
+    } else {
+      const int64_t v = p.n_big + (t - p.n_big_tasks);
+      const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
+      const T s = gather_sum<P>(p, eb, ee, lane);
+      if (active) col_epilogue<P>(p, v, s, dsum, uniform, a, lane);
+    }
+  }
+  bl1[wid][lane] = a.l1;
+  bdg[wid][lane] = a.dang;
+  bbad[wid][lane] = a.bad;
+  __syncthreads();
+  if (wid == 0) {
+    long long t1 = 0, t2 = 0;
+    int tb = 0;
+    for (int w = 0; w < kBWarps; ++w) { t1 += bl1[w][lane]; t2 += bdg[w][lane]; tb |= bbad[w][lane]; }
+    const int cur = (int)(p.k % 3);
+    long long *sl = &p.sums[(cur * kCols + lane) * 4];
+    if (t1) atomicAdd((unsigned long long *)&sl[1], (unsigned long long)t1);
+    if (t2) atomicAdd((unsigned long long *)&sl[0], (unsigned long long)t2);
+    if (tb) atomicAdd((unsigned long long *)&sl[2], 1ull);
+  }
+}
+
+// x_0 (p, or the warm start), acc = x_0, tail = 0, gathered vector for step 1,
+// per-column dangling sums of x_0; zero padding row n of the gathered blocks.
+__global__ void __launch_bounds__(kBThreads) batch_init(BatchParams p, int64_t set0) {
+  __shared__ long long bdg[kBWarps][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const bool col_ok = lane < p.ncols;
+  const bool uniform = col_ok && p.cols[lane].uniform;
+  long long dang = 0;
+  const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
+  for (int64_t v = (int64_t)blockIdx.x * kBWarps + wid; v <= p.n; v += nwarps) {
+    const int64_t i = v * kCols + lane;
+    if (v == p.n) {  // padding row: gathers of padded edges read zeros
+      p.gdf_out[i] = make_float2(0.f, 0.f);
+      p.gf_out[i] = 0.f;
+      const_cast<float2 *>(p.gdf_in)[i] = make_float2(0.f, 0.f);
+      const_cast<float *>(p.gf_in)[i] = 0.f;
+      continue;
+    }
+    df x0 = {0.f, 0.f};
+    if (col_ok) x0 = p.x0 ? df_make(p.x0[(set0 + lane) * p.n + p.perm[v]]) : red_of(p, v, lane, uniform);
+    const float dg = p.deg[v];
+    p.acc[i] = make_float2(x0.hi, x0.lo);
+    p.tail[i] = 0.f;
+    const df g = dg > 0.f ? df_div_f(x0, dg) : df{0.f, 0.f};
+    p.gdf_out[i] = make_float2(g.hi, g.lo);
+    p.gf_out[i] = g.hi;
+    if (dg == 0.f) dang += fx_of(x0.hi, p.fx_scale) + fx_of(x0.lo, p.fx_scale);
+  }
+  bdg[wid][lane] = dang;
+  __syncthreads();
+  if (wid == 0) {
+    long long t = 0;
+    for (int w = 0; w < kBWarps; ++w) t += bdg[w][lane];
+    if (t) atomicAdd((unsigned long long *)&p.sums[lane * 4 + 0], (unsigned long long)t);
+  }
+}
+
+// results of the wave: out[c * n + perm[v]] = acc + tail (FP32)
+__global__ void batch_finalize(BatchParams p) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t v = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid; v < p.n; v += nwarps) {
+    const int64_t i = v * kCols + lane;
+    if (lane < p.ncols) {
+      const float2 a = p.acc[i];
+      p.out[(int64_t)lane * p.n + p.perm[v]] = (float)((double)a.x + (double)a.y + (double)p.tail[i]);
+    }
+  }
+}
+
+__global__ void chunk_counts(const int64_t *rp, int32_t n_big, int64_t *nch) {
+  for (int32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= n_big; h += gridDim.x * blockDim.x)
+    nch[h] = h < n_big ? ceil_div<int64_t>(rp[h + 1] - rp[h], kSpmmChunk) : 0;
+}
+
+__global__ void chunk_fill(const int64_t *first64, int32_t n_big, int32_t *first, int32_t *task_row) {
+  for (int32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= n_big; h += gridDim.x * blockDim.x) {
+    first[h] = (int32_t)first64[h];
+    if (h < n_big)
+      for (int64_t t = first64[h]; t < first64[h + 1]; ++t) task_row[t] = h;
+  }
+}
+
+// first row with in-degree <= kSpmmBig (rows are in non-increasing degree)
+__global__ void count_big(const int64_t *rp, int64_t n, int64_t *out) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) / 2;
+    if (rp[mid + 1] - rp[mid] > kSpmmBig) lo = mid + 1;
+    else hi = mid;
+  }
+  *out = lo;
+}
+
+// prow[v] = first entry whose row >= v (entries sorted by row)
+__global__ void prow_from_sorted(const int32_t *rows, int64_t e, int64_t n, int32_t *prow) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= e;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t prev = i == 0 ? -1 : (int64_t)rows[i - 1];
+    const int64_t cur = i == e ? n : (int64_t)rows[i];
+    for (int64_t v = prev + 1; v <= cur; ++v) prow[v] = (int32_t)i;
+  }
+}
+
+int blocks_for(int64_t work, int threads, int cap) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(work, threads), cap));
+}
+
+Status batch_prepare(Ctx *ctx, Graph *g) {
+  if (g->batch) return Status::ok();
+  cudaStream_t s = ctx->stream;
+  BatchState *b = new BatchState();
+  g->batch = b;
+  const int64_t n = g->n;
+  b->n = n;
+  int64_t *tmp = nullptr;
+  GOPS_CUDA_TRY(cudaMallocAsync((void **)&tmp, sizeof(int64_t) * 2, s));
+  count_big<<<1, 1, 0, s>>>(g->in_rp, n, tmp);
+  int64_t nbig = 0;
+  GOPS_CUDA_TRY(cudaMemcpyAsync(&nbig, tmp, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+  free_async(tmp, s);
+  b->n_big = (int32_t)nbig;
+  if (nbig > 0) {
+    int64_t *nch = nullptr;
+    GOPS_CUDA_TRY(cudaMallocAsync((void **)&nch, sizeof(int64_t) * (nbig + 1), s));
+    chunk_counts<<<blocks_for(nbig + 1, 256, 4096), 256, 0, s>>>(g->in_rp, b->n_big, nch);
+    GOPS_TRY(exclusive_scan_i64(nch, nch, nbig + 1, s));
+    int64_t tasks = 0;
+    GOPS_CUDA_TRY(cudaMemcpyAsync(&tasks, nch + nbig, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+    GOPS_CUDA_TRY(cudaMalloc(&b->big_first, sizeof(int32_t) * (nbig + 1)));
+    GOPS_CUDA_TRY(cudaMalloc(&b->big_task_row, sizeof(int32_t) * std::max<int64_t>(tasks, 1)));
+    chunk_fill<<<blocks_for(nbig + 1, 256, 4096), 256, 0, s>>>(nch, b->n_big, b->big_first, b->big_task_row);
+    GOPS_CUDA_TRY(cudaGetLastError());
+    free_async(nch, s);
+    b->n_big_tasks = (int32_t)tasks;
+  }
+  b->n_tasks = b->n_big_tasks + (n - nbig);
+  const size_t blk = (size_t)(n + 1) * kCols;
+  GOPS_CUDA_TRY(cudaMalloc(&b->gdf[0], sizeof(float2) * blk));
+  GOPS_CUDA_TRY(cudaMalloc(&b->gdf[1], sizeof(float2) * blk));
+  GOPS_CUDA_TRY(cudaMalloc(&b->gf[0], sizeof(float) * blk));
+  GOPS_CUDA_TRY(cudaMalloc(&b->gf[1], sizeof(float) * blk));
+  GOPS_CUDA_TRY(cudaMalloc(&b->acc, sizeof(float2) * blk));
+  GOPS_CUDA_TRY(cudaMalloc(&b->tail, sizeof(float) * blk));
+  GOPS_CUDA_TRY(cudaMalloc(&b->lpart, sizeof(float2) * (size_t)std::max<int32_t>(b->n_big_tasks, 1) * kCols));
+  GOPS_CUDA_TRY(cudaMalloc(&b->lcnt, sizeof(unsigned) * (size_t)std::max<int32_t>(b->n_big, 1)));
+  GOPS_CUDA_TRY(cudaMalloc(&b->sums, sizeof(long long) * 3 * kCols * 4));
+  GOPS_CUDA_TRY(cudaMalloc(&b->cols, sizeof(ColState) * kCols));
+  GOPS_CUDA_TRY(cudaMalloc(&b->wave, sizeof(WaveState)));
+  GOPS_CUDA_TRY(cudaMalloc(&b->prow, sizeof(int32_t) * (n + 1)));
+  GOPS_CUDA_TRY(cudaMalloc(&b->out, sizeof(float) * (size_t)n * kCols));
+  // host copy of the relabelling, inverted
+  std::vector<int32_t> perm((size_t)n);
+  GOPS_CUDA_TRY(cudaMemcpyAsync(perm.data(), g->perm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+  b->inv_perm.assign((size_t)n, 0);
+  for (int64_t i = 0; i < n; ++i) b->inv_perm[(size_t)perm[(size_t)i]] = (int32_t)i;
+  return Status::ok();
+}
+
+Status ensure_entries(BatchState *b, int64_t e) {
+  if (e <= b->pcap) return Status::ok();
+  cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted);
+  b->pslot = nullptr; b->pval = nullptr; b->prows_sorted = nullptr;
+  const int64_t cap = std::max<int64_t>(e, 1024);
+  GOPS_CUDA_TRY(cudaMalloc(&b->pslot, sizeof(int32_t) * cap));
+  GOPS_CUDA_TRY(cudaMalloc(&b->pval, sizeof(float2) * cap));
+  GOPS_CUDA_TRY(cudaMalloc(&b->prows_sorted, sizeof(int32_t) * cap));
+  b->pcap = cap;
+  return Status::ok();
+}
+
+}  // namespace
+
+// nsets seed sets -> scores (host or device, set-major, original node order)
+Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, const int64_t *seed_ptr,
+                 const int32_t *seed_idx, const float *x0, bool x0_on_device, float *scores,
+                 bool scores_on_device, gops_run *runs) {
+  ctx->stats = gops_stats{};
+  const int64_t n = g->n;
+  if (nsets <= 0) return Status::ok();
+  if (n == 0) {  // src/ppr.rs:96-103
+    if (runs)
+      for (int64_t s = 0; s < nsets; ++s) runs[s] = gops_run{0, 0.0, 1, 0};
+    return Status::ok();
+  }
+  for (int64_t s = 0; s < nsets; ++s)
+    if (seed_ptr[s + 1] < seed_ptr[s]) return Status{GOPS_ERR_INVALID, "seed_ptr must be non-decreasing"};
+  for (int64_t k = seed_ptr[0]; k < seed_ptr[nsets]; ++k)
+    if (seed_idx[k] < 0 || seed_idx[k] >= n) return Status{GOPS_ERR_INVALID, "seed index out of range"};
+  GOPS_TRY(batch_prepare(ctx, g));
+  BatchState *b = g->batch;
+  cudaStream_t st = ctx->stream;
+  if (x0 && !x0_on_device && !b->x0) GOPS_CUDA_TRY(cudaMalloc(&b->x0, sizeof(float) * (size_t)n * kCols));
+
+  BatchParams p{};
+  p.n = n;
+  p.rp = g->in_rp;
+  p.col = g->in_col;
+  p.deg = g->deg;
+  p.perm = g->perm;
+  p.n_big = b->n_big;
+  p.n_big_tasks = b->n_big_tasks;
+  p.n_tasks = b->n_tasks;
+  p.big_first = b->big_first;
+  p.big_task_row = b->big_task_row;
+  p.prow = b->prow;
+  p.acc = b->acc;
+  p.tail = b->tail;
+  p.lpart = b->lpart;
+  p.lcnt = b->lcnt;
+  p.sums = b->sums;
+  p.cols = b->cols;
+  p.wave = b->wave;
+  p.d = df_from_double(cfg->damping);
+  p.omd = df_from_double(1.0 - cfg->damping);
+  p.inv_n = df_from_double(1.0 / (double)n);
+  p.tol = cfg->tolerance;
+  p.theta = kBTheta;
+  p.max_iter = cfg->max_iterations;
+
+  int occ_df = 0, occ_f = 0;
+  GOPS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_df, spmm_kernel<BDF>, kBThreads, 0));
+  GOPS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, spmm_kernel<BF32>, kBThreads, 0));
+  const int64_t need = ceil_div<int64_t>(std::max<int64_t>(b->n_tasks, 1), kBWarps);
+  const int grid_df = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * std::max(occ_df, 1)));
+  const int grid_f = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * std::max(occ_f, 1)));
+  const int grid_rows = blocks_for(n + 1, kBWarps, ctx->num_sms * 16);
+
+  uint64_t launches = 0, col_iters = 0;
+  float spmm_ms = 0.f;
+  uint64_t spmm_launches = 0;
+  std::vector<ColState> cols_h(kCols);
+  std::vector<int32_t> erow, eslot;
+  std::vector<float2> eval;
+  GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], st));
+  for (int64_t set0 = 0; set0 < nsets; set0 += kCols) {
+    const int ncols = (int)std::min<int64_t>(kCols, nsets - set0);
+    p.ncols = ncols;
+    // ---- personalization entries of the wave: (row, column, weight)
+    std::map<std::pair<int32_t, int32_t>, double> ent;
+    for (int c = 0; c < kCols; ++c) cols_h[c] = ColState{0, 0.0, c < ncols ? 0 : 1, 0, 0, 0};
+    double wmax = 1.0;
+    for (int c = 0; c < ncols; ++c) {
+      const int64_t a0 = seed_ptr[set0 + c], a1 = seed_ptr[set0 + c + 1];
+      if (a1 == a0) { cols_h[c].uniform = 1; continue; }  // sum <= 0: uniform (src/ppr.rs:108)
+      const double inv = 1.0 / (double)(a1 - a0);
+      for (int64_t k = a0; k < a1; ++k) ent[{b->inv_perm[(size_t)seed_idx[k]], c}] += inv;
+    }
+    erow.clear(); eslot.clear(); eval.clear();
+    for (const auto &kv : ent) {
+      erow.push_back(kv.first.first);
+      eslot.push_back(kv.first.second);
+      const df w = df_from_double(kv.second);
+      eval.push_back(make_float2(w.hi, w.lo));
+    }
+    const int64_t ne = (int64_t)erow.size();
+    GOPS_TRY(ensure_entries(b, ne));
+    if (ne) {
+      GOPS_CUDA_TRY(cudaMemcpyAsync(b->prows_sorted, erow.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, st));
+      GOPS_CUDA_TRY(cudaMemcpyAsync(b->pslot, eslot.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, st));
+      GOPS_CUDA_TRY(cudaMemcpyAsync(b->pval, eval.data(), sizeof(float2) * ne, cudaMemcpyHostToDevice, st));
+      ctx->stats.h2d_bytes += (sizeof(int32_t) * 2 + sizeof(float2)) * ne;
+    }
+    prow_from_sorted<<<blocks_for(ne + 1, 256, 4096), 256, 0, st>>>(b->prows_sorted, ne, n, b->prow);
+    ++launches;
+    p.pslot = b->pslot;
+    p.pval = b->pval;
+    // ---- warm start of the wave
+    p.x0 = nullptr;
+    if (x0) {
+      if (x0_on_device) {
+        p.x0 = x0 + set0 * n;
+      } else {
+        GOPS_CUDA_TRY(cudaMemcpyAsync(b->x0, x0 + set0 * n, sizeof(float) * (size_t)ncols * n,
+                                      cudaMemcpyHostToDevice, st));
+        ctx->stats.h2d_bytes += sizeof(float) * (size_t)ncols * n;
+        p.x0 = b->x0;
+      }
+      // fixed-point range: a warm start of L1 norm up to 8 keeps every partial
+      // sum far below 2^63; larger or non-finite starts are flagged by the
+      // nonfinite counter and the column does not converge
+      wmax = 8.0;
+      p.x0 = x0_on_device ? x0 : p.x0;
+    }
+    int e = 0;
+    while (e < 20 && std::ldexp(1.0, e) < wmax) ++e;
+    const int F = 58 - 2 * e;
+    p.fx_scale = std::ldexp(1.0f, F);
+    p.fx_inv = std::ldexp(1.0, -F);
+    GOPS_CUDA_TRY(cudaMemcpyAsync(b->cols, cols_h.data(), sizeof(ColState) * kCols, cudaMemcpyHostToDevice, st));
+    GOPS_CUDA_TRY(cudaMemsetAsync(b->wave, 0, sizeof(WaveState), st));
+    GOPS_CUDA_TRY(cudaMemsetAsync(b->sums, 0, sizeof(long long) * 3 * kCols * 4, st));
+    GOPS_CUDA_TRY(cudaMemsetAsync(b->lcnt, 0, sizeof(unsigned) * std::max<int32_t>(b->n_big, 1), st));
+    p.k = 0;
+    p.gdf_in = b->gdf[1];
+    p.gf_in = b->gf[1];
+    p.gdf_out = b->gdf[0];
+    p.gf_out = b->gf[0];
+    const int64_t set_base = x0 && x0_on_device ? set0 : 0;
+    batch_init<<<grid_rows, kBThreads, 0, st>>>(p, set_base);
+    GOPS_CUDA_TRY(cudaGetLastError());
+    ++launches;
+    // ---- steps
+    bool f32_known = false;
+    unsigned long long k = 1;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evs;
+    for (;;) {
+      for (int j = 0; j < 4 && k - 1 <= cfg->max_iterations; ++j, ++k) {
+        p.k = k;
+        p.gdf_in = b->gdf[(k - 1) & 1];
+        p.gf_in = b->gf[(k - 1) & 1];
+        p.gdf_out = b->gdf[k & 1];
+        p.gf_out = b->gf[k & 1];
+        if (!f32_known) {
+          spmm_kernel<BDF><<<grid_df, kBThreads, 0, st>>>(p);
+          ++launches;
+        }
+        if (k >= 2) {
+          cudaEvent_t e0 = nullptr, e1 = nullptr;
+          if (ctx->timing) {
+            GOPS_CUDA_TRY(cudaEventCreate(&e0));
+            GOPS_CUDA_TRY(cudaEventCreate(&e1));
+            GOPS_CUDA_TRY(cudaEventRecord(e0, st));
+          }
+          spmm_kernel<BF32><<<grid_f, kBThreads, 0, st>>>(p);
+          if (ctx->timing) {
+            GOPS_CUDA_TRY(cudaEventRecord(e1, st));
+            evs.push_back({e0, e1});
+          }
+          ++launches;
+        }
+      }
+      GOPS_CUDA_TRY(cudaGetLastError());
+      WaveState ws{};
+      GOPS_CUDA_TRY(cudaMemcpyAsync(&ws, b->wave, sizeof(WaveState), cudaMemcpyDeviceToHost, st));
+      GOPS_CUDA_TRY(cudaStreamSynchronize(st));
+      if (ws.done) {
+        // time the FP32-phase launches that did work (step >= f32_from and <= steps)
+        for (size_t i = 0; i < evs.size(); ++i) {
+          const unsigned long long kk = i + 2;  // F32 launches start at step 2
+          if (ws.f32_from && kk >= ws.f32_from && kk <= ws.steps) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, evs[i].first, evs[i].second);
+            spmm_ms += ms;
+            ++spmm_launches;
+          }
+        }
+        for (auto &pr : evs) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+        break;
+      }
+      if (ws.f32_phase) f32_known = true;
+      if (k - 1 > cfg->max_iterations) return Status{GOPS_ERR_INTERNAL, "wave did not finish"};
+    }
+    // ---- results of the wave
+    p.out = scores_on_device ? scores + set0 * n : b->out;
+    if (scores) {
+      batch_finalize<<<grid_rows, kBThreads, 0, st>>>(p);
+      GOPS_CUDA_TRY(cudaGetLastError());
+      ++launches;
+      if (!scores_on_device) {
+        GOPS_CUDA_TRY(cudaMemcpyAsync(scores + set0 * n, b->out, sizeof(float) * (size_t)ncols * n,
+                                      cudaMemcpyDeviceToHost, st));
+        ctx->stats.d2h_bytes += sizeof(float) * (size_t)ncols * n;
+      }
+    }
+    GOPS_CUDA_TRY(cudaMemcpyAsync(cols_h.data(), b->cols, sizeof(ColState) * kCols, cudaMemcpyDeviceToHost, st));
+    GOPS_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int c = 0; c < ncols; ++c) {
+      col_iters += cols_h[c].iterations;
+      if (runs) runs[set0 + c] = gops_run{cols_h[c].iterations, cols_h[c].diff_l1, cols_h[c].converged, 0};
+    }
+  }
+  GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[3], st));
+  GOPS_CUDA_TRY(cudaEventSynchronize(ctx->ev[3]));
+  float t_all = 0.f;
+  cudaEventElapsedTime(&t_all, ctx->ev[0], ctx->ev[3]);
+  ctx->stats.solve_ms = t_all;
+  ctx->stats.kernel_launches = launches;
+  ctx->stats.iterations = col_iters;
+  ctx->stats.f32_ms = spmm_ms;
+  ctx->stats.f32_launches = spmm_launches;
+  return Status::ok();
+}
+
+}  // namespace gops

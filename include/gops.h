@@ -147,6 +147,27 @@ int gops_pagerank_weighted_run(gops_ctx *ctx, const gops_graph *g, const gops_co
 int gops_personalized_pagerank_run(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg,
                                    const double *personalization, double *scores, gops_run *run);
 
+/* Batched personalized PageRank: nsets independent personalized_pagerank_run
+ * calls (src/ppr.rs:90-156) in one pass per wave of 32 sets.  Set s is
+ * seed_idx[seed_ptr[s] .. seed_ptr[s+1]) (node ids; a repeated node counts
+ * twice); its personalization vector is 1 on each seed, normalised as
+ * src/ppr.rs:104-109 does, and an empty set means the uniform vector.  Each
+ * set stops at its own first step whose L1 norm is below tolerance.
+ * x0 (optional, nsets*n floats, set-major, original node order) replaces the
+ * start vector p by a caller-supplied one (a warm start, such as the learned
+ * one); the iteration and its stopping rule are unchanged.
+ * scores (optional): nsets*n floats, set-major, original node order (FP32).
+ * runs (optional): nsets run records. */
+int gops_ppr_batch(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,
+                   const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0,
+                   float *scores, gops_run *runs);
+
+/* As gops_ppr_batch, with x0 and scores in device memory (CUDA pointers,
+ * e.g. from another framework): no host copies of the score blocks. */
+int gops_ppr_batch_device(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,
+                          const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0_device,
+                          float *scores_device, gops_run *runs);
+
 /* Device pointer (double, n entries) of the last solve's scores, valid until
  * the next solve on this context. */
 const double *gops_ctx_scores_device(const gops_ctx *ctx);

@@ -1,0 +1,112 @@
+"""Batched PPR (gops_ppr_batch) against the oracle, set by set.
+
+Every seed set must equal one reference personalized_pagerank_run with
+personalization 1 on its seeds (oracle.port.ppr_many): L1 <= 1e-7 per set,
+iteration count within +-1 (exact expected), same convergence flag.
+"""
+import numpy as np
+import pytest
+
+import graphops_gb300 as go
+from graphops_gb300 import gen
+from oracle import fp64, port
+
+pytestmark = pytest.mark.gpu
+L1_TARGET = 1e-7
+
+
+def check(g, sp, si, tol=1e-7, max_iter=1000, x0=None):
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    conf = go.PageRankConfig(0.85, max_iter, tol)
+    r = go.ppr_batch(dg, conf, sp, si, x0=x0)
+    ref, its = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, max_iter, tol, threads=8)
+    return r, ref, its
+
+
+def test_waves_match_reference_per_set():
+    g = gen.rmat(12, 16, seed=4)
+    sp, si = gen.seed_sets(g, 70, 1, 64, seed=2)          # 3 waves, the last partial
+    r, ref, its = check(g, sp, si)
+    l1 = np.abs(r.scores.astype(np.float64) - ref).sum(axis=1)
+    assert l1.max() <= L1_TARGET, l1.max()
+    assert np.array_equal(r.iterations, its.astype(np.int64))
+    assert r.converged.all()
+
+
+def test_edge_cases_empty_repeated_and_capped():
+    g = gen.rmat(11, 8, seed=6)
+    sets = [[], [5, 5, 7], [0], list(range(40)), [3]]
+    sp, si = go.seed_sets_to_csr(sets)
+    r, ref, its = check(g, sp, si)
+    assert np.abs(r.scores.astype(np.float64) - ref).sum(axis=1).max() <= L1_TARGET
+    assert np.array_equal(r.iterations, its.astype(np.int64))
+    # empty set = uniform personalization (src/ppr.rs:104-109)
+    u, _, _, _ = port.ppr_run(g.row_ptr, g.col, np.zeros(g.n), 0.85, 1000, 1e-7)
+    assert np.abs(r.scores[0] - u).sum() <= L1_TARGET
+    # max_iterations reached: every set stops at 3, not converged
+    r3, ref3, its3 = check(g, sp, si, tol=1e-12, max_iter=3)
+    assert (r3.iterations == 3).all() and not r3.converged.any()
+    assert np.abs(r3.scores.astype(np.float64) - ref3).sum(axis=1).max() <= L1_TARGET
+
+
+def test_big_rows_are_chunked():
+    n = 20000
+    rows = [[0] if u % 3 else [0, (u * 7919) % n] for u in range(n)]
+    rows[0] = [1, 2, 3]
+    rp = np.zeros(n + 1, np.int64)
+    for u, rr in enumerate(rows):
+        rp[u + 1] = rp[u] + len(rr)
+    col = np.array([v for rr in rows for v in rr], np.int32)
+    g = gen.CsrGraph(n, rp, col)
+    sets = [[0], [1, 2], [17, 555, 9000], [], [n - 1]]
+    sp, si = go.seed_sets_to_csr(sets)
+    r, ref, its = check(g, sp, si, tol=1e-9)
+    assert np.abs(r.scores.astype(np.float64) - ref).sum(axis=1).max() <= L1_TARGET
+    assert np.abs(r.iterations - its.astype(np.int64)).max() <= 1
+
+
+def test_deterministic():
+    g = gen.rmat(12, 16, seed=9)
+    sp, si = gen.seed_sets(g, 40, 1, 32, seed=5)
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    conf = go.PageRankConfig(0.85, 1000, 1e-7)
+    a = go.ppr_batch(dg, conf, sp, si)
+    b = go.ppr_batch(dg, conf, sp, si)
+    assert np.array_equal(a.scores, b.scores) and np.array_equal(a.iterations, b.iterations)
+
+
+def test_warm_start_from_the_fixed_point_stops_early():
+    g = gen.rmat(11, 16, seed=3)
+    sp, si = gen.seed_sets(g, 8, 1, 16, seed=8)
+    x0 = np.zeros((8, g.n), np.float32)
+    for i in range(8):
+        p = np.zeros(g.n)
+        p[si[sp[i]:sp[i + 1]]] = 1.0
+        x0[i] = fp64.fixed_point(g.n, g.row_ptr, g.col, 0.85, personalization=p)
+    cold, ref, its = check(g, sp, si)
+    warm = go.ppr_batch(go.DeviceGraph.from_csr(g.row_ptr, g.col), go.PageRankConfig(0.85, 1000, 1e-7),
+                        sp, si, x0=x0)
+    assert warm.converged.all()
+    assert (warm.iterations < cold.iterations).all()
+    # a warm start changes where the iteration stops, not what it converges to
+    assert np.abs(warm.scores.astype(np.float64) - x0).sum(axis=1).max() <= 1e-6
+
+
+def test_device_pointers_variant():
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from graphops_gb300 import _native
+    g = gen.rmat(11, 16, seed=2)
+    sp, si = gen.seed_sets(g, 33, 1, 8, seed=1)
+    ctx = _native.default_context()
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    host = go.ppr_batch(dg, go.PageRankConfig(0.85, 1000, 1e-7), sp, si)
+    out = torch.empty((33, g.n), dtype=torch.float32, device="cuda")
+    cfg = _native.Config(0.85, 1000, 1e-7)
+    runs = (_native.Run * 33)()
+    torch.cuda.synchronize()
+    ctx.check(ctx._l.gops_ppr_batch_device(ctx.handle, dg.handle, ctypes.byref(cfg), 33,
+                                            _native.ptr(np.ascontiguousarray(sp)),
+                                            _native.ptr(np.ascontiguousarray(si)), None,
+                                            ctypes.c_void_p(out.data_ptr()), ctypes.cast(runs, ctypes.c_void_p)))
+    assert np.array_equal(out.cpu().numpy(), host.scores)

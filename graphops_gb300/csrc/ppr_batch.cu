@@ -31,7 +31,18 @@
 
 namespace gops {
 
-constexpr int kCols = 32;       // columns per wave (one per lane)
+#ifndef GOPS_BCOLS
+#define GOPS_BCOLS 32
+#endif
+#ifndef GOPS_L2POL
+#define GOPS_L2POL 0
+#endif
+constexpr int kCols = GOPS_BCOLS;  // columns per wave (one lane each; 32/kCols rows per warp)
+constexpr int kRowsPerWarp = 32 / kCols;
+// With kL2Policy gathers of the step block are marked evict-last in L2 and
+// the streamed data (columns, accumulators, written blocks) evict-first, so
+// the gathered block stays L2-resident.
+constexpr bool kL2Policy = GOPS_L2POL != 0;
 constexpr int kSpmmBig = 256;   // rows above this in-degree are chunked
 constexpr int kSpmmChunk = 256; // edges per chunk task
 constexpr int kBThreads = 256;
@@ -126,13 +137,33 @@ struct BatchParams {
 
 namespace {
 
+__device__ __forceinline__ uint64_t l2_keep() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+__device__ __forceinline__ float ld_keep_f32(const float *a, uint64_t pol) {
+  float v;
+  asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+  return v;
+}
+
+__device__ __forceinline__ float2 ld_keep_f2(const float2 *a, uint64_t pol) {
+  float2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0,%1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(a), "l"(pol));
+  return v;
+}
+
 struct BDF {
   using T = df;
   static constexpr bool kDF = true;
   __device__ static T zero() { return {0.0f, 0.0f}; }
   __device__ static T add(T a, T b) { return df_add(a, b); }
-  __device__ static T load(const BatchParams &p, int64_t i) {
-    const float2 v = __ldg(&p.gdf_in[i]);
+  __device__ static T load(const BatchParams &p, int64_t i, uint64_t pol) {
+    float2 v;
+    if constexpr (kL2Policy) v = ld_keep_f2(&p.gdf_in[i], pol);
+    else v = __ldg(&p.gdf_in[i]);
     return {v.x, v.y};
   }
   __device__ static float2 pack(T v) { return make_float2(v.hi, v.lo); }
@@ -144,7 +175,10 @@ struct BF32 {
   static constexpr bool kDF = false;
   __device__ static T zero() { return 0.0f; }
   __device__ static T add(T a, T b) { return a + b; }
-  __device__ static T load(const BatchParams &p, int64_t i) { return __ldg(&p.gf_in[i]); }
+  __device__ static T load(const BatchParams &p, int64_t i, uint64_t pol) {
+    if constexpr (kL2Policy) return ld_keep_f32(&p.gf_in[i], pol);
+    else return __ldg(&p.gf_in[i]);
+  }
   __device__ static float2 pack(T v) { return make_float2(v, 0.0f); }
   __device__ static T unpack(float2 v) { return v.x; }
 };
@@ -167,21 +201,23 @@ struct LaneAcc {
   int bad = 0;
 };
 
-// Gathered sum of row edges [eb, ee) for this lane's column.
+// Gathered sum of row edges [eb, ee) for column c of this lane's sub-group
+// (kCols lanes, shuffle mask gmask).
 template <class P>
-__device__ __forceinline__ typename P::T gather_sum(const BatchParams &p, int eb, int ee, int lane) {
+__device__ __forceinline__ typename P::T gather_sum(const BatchParams &p, int eb, int ee, int c,
+                                                    unsigned gmask, uint64_t pol) {
   using T = typename P::T;
   T s = P::zero();
-  for (int base = eb; base < ee; base += 32) {
-    const int cnt = min(32, ee - base);
-    const int my = base + lane;
+  for (int base = eb; base < ee; base += kCols) {
+    const int cnt = min(kCols, ee - base);
+    const int my = base + c;
     const int32_t cidx = my < ee ? __ldg(&p.col[my]) : (int32_t)p.n;
     for (int j = 0; j < cnt; j += 8) {
       T g[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        const int32_t c = __shfl_sync(0xffffffffu, cidx, (j + q) & 31);
-        g[q] = (j + q < cnt) ? P::load(p, (int64_t)c * kCols + lane) : P::zero();
+        const int32_t u = __shfl_sync(gmask, cidx, (j + q) & (kCols - 1), kCols);
+        g[q] = (j + q < cnt) ? P::load(p, (int64_t)u * kCols + c, pol) : P::zero();
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q)
@@ -193,10 +229,10 @@ __device__ __forceinline__ typename P::T gather_sum(const BatchParams &p, int eb
 
 template <class P>
 __device__ __forceinline__ void col_epilogue(const BatchParams &p, int64_t v, typename P::T s, df dsum,
-                                             bool uniform, LaneAcc &a, int lane) {
-  const df red = red_of(p, v, lane, uniform);
+                                             bool uniform, LaneAcc &a, int c) {
+  const df red = red_of(p, v, c, uniform);
   const float dg = __ldg(&p.deg[v]);
-  const int64_t i = v * kCols + lane;
+  const int64_t i = v * kCols + c;
   if constexpr (P::kDF) {
     const float2 ao = p.acc[i];
     df r = df_mul(p.d, df_add(s, df_mul(dsum, red)));
@@ -228,22 +264,23 @@ __device__ bool batch_prologue(const BatchParams &p, int lane, bool *active, df 
   const unsigned long long k = p.k;
   if (*(volatile int *)&p.wave->done) return false;
   const int prev = (int)((k - 1) % 3);
-  const bool col_ok = lane < p.ncols;
-  const int retired0 = col_ok ? *(volatile int *)&p.cols[lane].retired : 1;
+  const int c = lane & (kCols - 1);
+  const bool col_ok = c < p.ncols;
+  const int retired0 = col_ok ? *(volatile int *)&p.cols[c].retired : 1;
   double diff = INFINITY;
   if (k > 1) {
-    const long long raw = *(volatile long long *)&p.sums[(prev * kCols + lane) * 4 + 1];
-    const long long badc = *(volatile long long *)&p.sums[(prev * kCols + lane) * 4 + 2];
+    const long long raw = *(volatile long long *)&p.sums[(prev * kCols + c) * 4 + 1];
+    const long long badc = *(volatile long long *)&p.sums[(prev * kCols + c) * 4 + 2];
     diff = badc ? NAN : (double)raw * p.fx_inv;
   }
   const bool conv = !retired0 && k > 1 && diff < p.tol;
   const bool cap = !retired0 && !conv && k - 1 >= p.max_iter;
   const bool act = !retired0 && !conv && !cap;
-  if (blockIdx.x == 0 && threadIdx.x < 32 && (conv || cap)) {
-    p.cols[lane].retired = 1;
-    p.cols[lane].converged = conv ? 1 : 0;
-    p.cols[lane].iterations = k - 1;
-    p.cols[lane].diff_l1 = diff;
+  if (blockIdx.x == 0 && threadIdx.x < kCols && (conv || cap)) {
+    p.cols[c].retired = 1;
+    p.cols[c].converged = conv ? 1 : 0;
+    p.cols[c].iterations = k - 1;
+    p.cols[c].diff_l1 = diff;
   }
   const unsigned any = __ballot_sync(0xffffffffu, act);
   if (!any) {
@@ -258,13 +295,13 @@ __device__ bool batch_prologue(const BatchParams &p, int lane, bool *active, df 
     if (f32 && p.wave->f32_from == 0) p.wave->f32_from = k;
     p.wave->steps = k;
   }
-  if (blockIdx.x == 0 && threadIdx.x < 32) {
+  if (blockIdx.x == 0 && threadIdx.x < kCols) {
     const int nxt = (int)((k + 1) % 3);
-    for (int i = 0; i < 4; ++i) p.sums[(nxt * kCols + lane) * 4 + i] = 0;
+    for (int i = 0; i < 4; ++i) p.sums[(nxt * kCols + c) * 4 + i] = 0;
   }
   *active = act;
-  *uniform = col_ok && p.cols[lane].uniform;
-  const long long draw = *(volatile long long *)&p.sums[(prev * kCols + lane) * 4 + 0];
+  *uniform = col_ok && p.cols[c].uniform;
+  const long long draw = *(volatile long long *)&p.sums[(prev * kCols + c) * 4 + 0];
   *dsum = df_from_double((double)draw * p.fx_inv);
   return true;
 }
@@ -275,12 +312,21 @@ __global__ void __launch_bounds__(kBThreads) spmm_kernel(BatchParams p) {
   __shared__ long long bl1[kBWarps][32], bdg[kBWarps][32];
   __shared__ int bbad[kBWarps][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int sub = lane / kCols, c = lane & (kCols - 1);
+  const unsigned gmask = kCols == 32 ? 0xffffffffu : (((1u << kCols) - 1u) << (sub * kCols));
   bool active = false, uniform = false;
   df dsum;
   if (!batch_prologue<P::kDF>(p, lane, &active, &dsum, &uniform)) return;
+  uint64_t pol = 0;
+  if constexpr (kL2Policy) pol = l2_keep();
   LaneAcc a;
   const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
-  for (int64_t t = (int64_t)blockIdx.x * kBWarps + wid; t < p.n_tasks; t += nwarps) {
+  // unit u: chunk task (u < n_big_tasks) or row n_big + (u - n_big_tasks);
+  // a warp task covers kRowsPerWarp consecutive units, one per sub-group
+  const int64_t nwt = ceil_div<int64_t>(p.n_tasks, kRowsPerWarp);
+  for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
+    const int64_t t = w * kRowsPerWarp + sub;
+    if (t >= p.n_tasks) continue;
     if (t < p.n_big_tasks) {
       const int h = __ldg(&p.big_task_row[t]);
       const int first = __ldg(&p.big_first[h]);
@@ -288,35 +334,36 @@ __global__ void __launch_bounds__(kBThreads) spmm_kernel(BatchParams p) {
       const int rb = (int)__ldg(&p.rp[h]), re = (int)__ldg(&p.rp[h + 1]);
       const int cs = rb + ((int)t - first) * kSpmmChunk;
       const int ce = min(re, cs + kSpmmChunk);
-      const T s = gather_sum<P>(p, cs, ce, lane);
-      p.lpart[t * kCols + lane] = P::pack(s);
+      const T s = gather_sum<P>(p, cs, ce, c, gmask, pol);
+      p.lpart[t * kCols + c] = P::pack(s);
       __threadfence();
-      __syncwarp();
+      __syncwarp(gmask);
       unsigned tk = 0;
-      if (lane == 0) tk = atomicAdd(&p.lcnt[h], 1u);
-      tk = __shfl_sync(0xffffffffu, tk, 0);
+      if (c == 0) tk = atomicAdd(&p.lcnt[h], 1u);
+      tk = __shfl_sync(gmask, tk, 0, kCols);
       if (tk == (unsigned)(nch - 1)) {
         __threadfence();
         T all = P::zero();
-        for (int q = 0; q < nch; ++q) all = P::add(all, P::unpack(__ldcg(&p.lpart[(int64_t)(first + q) * kCols + lane])));
-        if (lane == 0) p.lcnt[h] = 0;
-        if (active) col_epilogue<P>(p, h, all, dsum, uniform, a, lane);
+        for (int q = 0; q < nch; ++q) all = P::add(all, P::unpack(__ldcg(&p.lpart[(int64_t)(first + q) * kCols + c])));
+        if (c == 0) p.lcnt[h] = 0;
+        if (active) col_epilogue<P>(p, h, all, dsum, uniform, a, c);
       }
     } else {
       const int64_t v = p.n_big + (t - p.n_big_tasks);
       const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
-      const T s = gather_sum<P>(p, eb, ee, lane);
-      if (active) col_epilogue<P>(p, v, s, dsum, uniform, a, lane);
+      const T s = gather_sum<P>(p, eb, ee, c, gmask, pol);
+      if (active) col_epilogue<P>(p, v, s, dsum, uniform, a, c);
     }
   }
   bl1[wid][lane] = a.l1;
   bdg[wid][lane] = a.dang;
   bbad[wid][lane] = a.bad;
   __syncthreads();
-  if (wid == 0) {
+  if (wid == 0 && lane < kCols) {
     long long t1 = 0, t2 = 0;
     int tb = 0;
-    for (int w = 0; w < kBWarps; ++w) { t1 += bl1[w][lane]; t2 += bdg[w][lane]; tb |= bbad[w][lane]; }
+    for (int w = 0; w < kBWarps; ++w)
+      for (int q = lane; q < 32; q += kCols) { t1 += bl1[w][q]; t2 += bdg[w][q]; tb |= bbad[w][q]; }
     const int cur = (int)(p.k % 3);
     long long *sl = &p.sums[(cur * kCols + lane) * 4];
     if (t1) atomicAdd((unsigned long long *)&sl[1], (unsigned long long)t1);
@@ -330,12 +377,13 @@ __global__ void __launch_bounds__(kBThreads) spmm_kernel(BatchParams p) {
 __global__ void __launch_bounds__(kBThreads) batch_init(BatchParams p, int64_t set0) {
   __shared__ long long bdg[kBWarps][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const bool col_ok = lane < p.ncols;
-  const bool uniform = col_ok && p.cols[lane].uniform;
+  const int sub = lane / kCols, c = lane & (kCols - 1);
+  const bool col_ok = c < p.ncols;
+  const bool uniform = col_ok && p.cols[c].uniform;
   long long dang = 0;
-  const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
-  for (int64_t v = (int64_t)blockIdx.x * kBWarps + wid; v <= p.n; v += nwarps) {
-    const int64_t i = v * kCols + lane;
+  const int64_t step = (int64_t)gridDim.x * kBWarps * kRowsPerWarp;
+  for (int64_t v = ((int64_t)blockIdx.x * kBWarps + wid) * kRowsPerWarp + sub; v <= p.n; v += step) {
+    const int64_t i = v * kCols + c;
     if (v == p.n) {  // padding row: gathers of padded edges read zeros
       p.gdf_out[i] = make_float2(0.f, 0.f);
       p.gf_out[i] = 0.f;
@@ -344,7 +392,7 @@ __global__ void __launch_bounds__(kBThreads) batch_init(BatchParams p, int64_t s
       continue;
     }
     df x0 = {0.f, 0.f};
-    if (col_ok) x0 = p.x0 ? df_make(p.x0[(set0 + lane) * p.n + p.perm[v]]) : red_of(p, v, lane, uniform);
+    if (col_ok) x0 = p.x0 ? df_make(p.x0[(set0 + c) * p.n + p.perm[v]]) : red_of(p, v, c, uniform);
     const float dg = p.deg[v];
     p.acc[i] = make_float2(x0.hi, x0.lo);
     p.tail[i] = 0.f;
@@ -355,9 +403,10 @@ __global__ void __launch_bounds__(kBThreads) batch_init(BatchParams p, int64_t s
   }
   bdg[wid][lane] = dang;
   __syncthreads();
-  if (wid == 0) {
+  if (wid == 0 && lane < kCols) {
     long long t = 0;
-    for (int w = 0; w < kBWarps; ++w) t += bdg[w][lane];
+    for (int w = 0; w < kBWarps; ++w)
+      for (int q = lane; q < 32; q += kCols) t += bdg[w][q];
     if (t) atomicAdd((unsigned long long *)&p.sums[lane * 4 + 0], (unsigned long long)t);
   }
 }
@@ -365,12 +414,13 @@ __global__ void __launch_bounds__(kBThreads) batch_init(BatchParams p, int64_t s
 // results of the wave: out[c * n + perm[v]] = acc + tail (FP32)
 __global__ void batch_finalize(BatchParams p) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t v = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid; v < p.n; v += nwarps) {
-    const int64_t i = v * kCols + lane;
-    if (lane < p.ncols) {
+  const int sub = lane / kCols, c = lane & (kCols - 1);
+  const int64_t step = (int64_t)gridDim.x * (blockDim.x >> 5) * kRowsPerWarp;
+  for (int64_t v = ((int64_t)blockIdx.x * (blockDim.x >> 5) + wid) * kRowsPerWarp + sub; v < p.n; v += step) {
+    const int64_t i = v * kCols + c;
+    if (c < p.ncols) {
       const float2 a = p.acc[i];
-      p.out[(int64_t)lane * p.n + p.perm[v]] = (float)((double)a.x + (double)a.y + (double)p.tail[i]);
+      p.out[(int64_t)c * p.n + p.perm[v]] = (float)((double)a.x + (double)a.y + (double)p.tail[i]);
     }
   }
 }
@@ -531,10 +581,10 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   int occ_df = 0, occ_f = 0;
   GOPS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_df, spmm_kernel<BDF>, kBThreads, 0));
   GOPS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, spmm_kernel<BF32>, kBThreads, 0));
-  const int64_t need = ceil_div<int64_t>(std::max<int64_t>(b->n_tasks, 1), kBWarps);
+  const int64_t need = ceil_div<int64_t>(ceil_div<int64_t>(std::max<int64_t>(b->n_tasks, 1), kRowsPerWarp), kBWarps);
   const int grid_df = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * std::max(occ_df, 1)));
   const int grid_f = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * std::max(occ_f, 1)));
-  const int grid_rows = blocks_for(n + 1, kBWarps, ctx->num_sms * 16);
+  const int grid_rows = blocks_for(n + 1, kBWarps * kRowsPerWarp, ctx->num_sms * 16);
 
   uint64_t launches = 0, col_iters = 0;
   float spmm_ms = 0.f;

@@ -43,6 +43,18 @@ constexpr int kRowsPerWarp = 32 / kCols;
 // the streamed data (columns, accumulators, written blocks) evict-first, so
 // the gathered block stays L2-resident.
 constexpr bool kL2Policy = GOPS_L2POL != 0;
+#ifndef GOPS_BROWS
+#define GOPS_BROWS 4
+#endif
+#ifndef GOPS_BROWS_DF
+#define GOPS_BROWS_DF 2
+#endif
+#ifndef GOPS_BMINB
+#define GOPS_BMINB 1
+#endif
+constexpr int kBRowsF32 = GOPS_BROWS;   // rows interleaved per warp, FP32 phase
+constexpr int kBRowsDF = GOPS_BROWS_DF; // rows interleaved per warp, double-float phase
+constexpr int kBMinBlocks = GOPS_BMINB;
 constexpr int kSpmmBig = 256;   // rows above this in-degree are chunked
 constexpr int kSpmmChunk = 256; // edges per chunk task
 constexpr int kBThreads = 256;
@@ -227,14 +239,32 @@ __device__ __forceinline__ typename P::T gather_sum(const BatchParams &p, int eb
   return s;
 }
 
+// Per-(row, column) epilogue inputs, loaded before the row's gathers.
+struct BIn {
+  df red;
+  float2 x;  // acc (double-float phase) or (tail, 0)
+  float deg;
+};
+
 template <class P>
-__device__ __forceinline__ void col_epilogue(const BatchParams &p, int64_t v, typename P::T s, df dsum,
-                                             bool uniform, LaneAcc &a, int c) {
-  const df red = red_of(p, v, c, uniform);
-  const float dg = __ldg(&p.deg[v]);
+__device__ __forceinline__ BIn b_in(const BatchParams &p, int64_t v, int c, bool uniform) {
+  BIn in;
+  in.red = red_of(p, v, c, uniform);
+  in.deg = __ldg(&p.deg[v]);
+  const int64_t i = v * kCols + c;
+  if constexpr (P::kDF) in.x = p.acc[i];
+  else in.x = make_float2(p.tail[i], 0.f);
+  return in;
+}
+
+template <class P>
+__device__ __forceinline__ void col_epilogue_in(const BatchParams &p, int64_t v, typename P::T s, df dsum,
+                                                const BIn &in, LaneAcc &a, int c) {
+  const df red = in.red;
+  const float dg = in.deg;
   const int64_t i = v * kCols + c;
   if constexpr (P::kDF) {
-    const float2 ao = p.acc[i];
+    const float2 ao = in.x;
     df r = df_mul(p.d, df_add(s, df_mul(dsum, red)));
     if (p.k == 1) r = df_add(df_add(df_mul(p.omd, red), r), df_neg({ao.x, ao.y}));  // F(x_0) - x_0
     const df an = df_add({ao.x, ao.y}, r);
@@ -248,12 +278,73 @@ __device__ __forceinline__ void col_epilogue(const BatchParams &p, int64_t v, ty
     p.gf_out[i] = g.hi;
   } else {
     const float r = p.d.hi * (s + dsum.hi * red.hi);
-    p.tail[i] += r;
+    p.tail[i] = in.x.x + r;
     a.l1 += fx_of(fabsf(r), p.fx_scale);
     a.bad |= !isfinite(r);
     if (dg == 0.0f) a.dang += fx_of(r, p.fx_scale);
     p.gf_out[i] = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
   }
+}
+
+template <class P>
+__device__ __forceinline__ void col_epilogue(const BatchParams &p, int64_t v, typename P::T s, df dsum,
+                                             bool uniform, LaneAcc &a, int c) {
+  const BIn in = b_in<P>(p, v, c, uniform);
+  col_epilogue_in<P>(p, v, s, dsum, in, a, c);
+}
+
+// Rows [v0, v0 + R) at once (kCols == 32: lane c is column c).  All R rows'
+// column indices, then all their gathers (8 per row per round) are issued
+// before any is consumed, and the epilogue inputs are loaded up front.
+template <class P, int R>
+__device__ __forceinline__ void rows_task(const BatchParams &p, int64_t v0, int64_t vend, int c,
+                                          bool active, bool uniform, df dsum, LaneAcc &a, uint64_t pol) {
+  using T = typename P::T;
+  int eb[R], ee[R];
+  BIn in[R];
+  const int64_t rl = (int64_t)c < (int64_t)R + 1 && v0 + c <= vend ? v0 + c : vend;
+  const int rpv = (int)__ldg(&p.rp[rl]);  // lane q holds rp[v0 + q]
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const bool ok = v0 + q < vend;
+    eb[q] = ok ? __shfl_sync(0xffffffffu, rpv, q) : 0;
+    ee[q] = ok ? __shfl_sync(0xffffffffu, rpv, q + 1) : 0;
+    if (ok && active) in[q] = b_in<P>(p, v0 + q, c, uniform);
+  }
+  int len = 0;
+#pragma unroll
+  for (int q = 0; q < R; ++q) len = max(len, ee[q] - eb[q]);
+  T s[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) s[q] = P::zero();
+  for (int base = 0; base < len; base += 32) {
+    int32_t cidx[R];
+    int cnt[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int e = eb[q] + base + c;
+      cidx[q] = e < ee[q] ? __ldg(&p.col[e]) : (int32_t)p.n;
+      cnt[q] = min(32, max(0, ee[q] - eb[q] - base));
+    }
+    for (int j = 0; j < 32; j += 8) {
+      T g[R][8];
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+#pragma unroll
+        for (int qq = 0; qq < 8; ++qq) {
+          const int32_t u = __shfl_sync(0xffffffffu, cidx[q], j + qq);
+          g[q][qq] = (j + qq < cnt[q]) ? P::load(p, (int64_t)u * kCols + c, pol) : P::zero();
+        }
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+#pragma unroll
+        for (int qq = 0; qq < 8; ++qq)
+          if (j + qq < cnt[q]) s[q] = P::add(s[q], g[q][qq]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q)
+    if (v0 + q < vend && active) col_epilogue_in<P>(p, v0 + q, s[q], dsum, in[q], a, c);
 }
 
 // Per-column view of step k: which columns are still active, their dangling
@@ -307,7 +398,7 @@ __device__ bool batch_prologue(const BatchParams &p, int lane, bool *active, df 
 }
 
 template <class P>
-__global__ void __launch_bounds__(kBThreads) spmm_kernel(BatchParams p) {
+__global__ void __launch_bounds__(kBThreads, kBMinBlocks) spmm_kernel(BatchParams p) {
   using T = typename P::T;
   __shared__ long long bl1[kBWarps][32], bdg[kBWarps][32];
   __shared__ int bbad[kBWarps][32];
@@ -321,6 +412,40 @@ __global__ void __launch_bounds__(kBThreads) spmm_kernel(BatchParams p) {
   if constexpr (kL2Policy) pol = l2_keep();
   LaneAcc a;
   const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
+  if constexpr (kCols == 32) {
+    // warp tasks: the chunk tasks, then groups of R consecutive rows
+    constexpr int R = P::kDF ? kBRowsDF : kBRowsF32;
+    const int64_t nrows = p.n - p.n_big;
+    const int64_t nwt = p.n_big_tasks + ceil_div<int64_t>(nrows, R);
+    for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
+      if (w < p.n_big_tasks) {
+        const int64_t t = w;
+        const int h = __ldg(&p.big_task_row[t]);
+        const int first = __ldg(&p.big_first[h]);
+        const int nch = __ldg(&p.big_first[h + 1]) - first;
+        const int rb = (int)__ldg(&p.rp[h]), re = (int)__ldg(&p.rp[h + 1]);
+        const int cs = rb + ((int)t - first) * kSpmmChunk;
+        const int ce = min(re, cs + kSpmmChunk);
+        const T s = gather_sum<P>(p, cs, ce, c, gmask, pol);
+        p.lpart[t * kCols + c] = P::pack(s);
+        __threadfence();
+        __syncwarp();
+        unsigned tk = 0;
+        if (c == 0) tk = atomicAdd(&p.lcnt[h], 1u);
+        tk = __shfl_sync(0xffffffffu, tk, 0);
+        if (tk == (unsigned)(nch - 1)) {
+          __threadfence();
+          T all = P::zero();
+          for (int q = 0; q < nch; ++q) all = P::add(all, P::unpack(__ldcg(&p.lpart[(int64_t)(first + q) * kCols + c])));
+          if (c == 0) p.lcnt[h] = 0;
+          if (active) col_epilogue<P>(p, h, all, dsum, uniform, a, c);
+        }
+      } else {
+        const int64_t v0 = p.n_big + (w - p.n_big_tasks) * R;
+        rows_task<P, R>(p, v0, p.n, c, active, uniform, dsum, a, pol);
+      }
+    }
+  } else {
   // unit u: chunk task (u < n_big_tasks) or row n_big + (u - n_big_tasks);
   // a warp task covers kRowsPerWarp consecutive units, one per sub-group
   const int64_t nwt = ceil_div<int64_t>(p.n_tasks, kRowsPerWarp);
@@ -354,6 +479,7 @@ __global__ void __launch_bounds__(kBThreads) spmm_kernel(BatchParams p) {
       const T s = gather_sum<P>(p, eb, ee, c, gmask, pol);
       if (active) col_epilogue<P>(p, v, s, dsum, uniform, a, c);
     }
+  }
   }
   bl1[wid][lane] = a.l1;
   bdg[wid][lane] = a.dang;

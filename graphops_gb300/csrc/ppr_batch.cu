@@ -44,10 +44,10 @@ constexpr int kRowsPerWarp = 32 / kCols;
 // the gathered block stays L2-resident.
 constexpr bool kL2Policy = GOPS_L2POL != 0;
 #ifndef GOPS_BROWS
-#define GOPS_BROWS 4
+#define GOPS_BROWS 1
 #endif
 #ifndef GOPS_BROWS_DF
-#define GOPS_BROWS_DF 2
+#define GOPS_BROWS_DF 1
 #endif
 #ifndef GOPS_BMINB
 #define GOPS_BMINB 1
@@ -286,6 +286,35 @@ __device__ __forceinline__ void col_epilogue_in(const BatchParams &p, int64_t v,
   }
 }
 
+// Gathered sum over edges [eb, ee) when in-rows are padded to multiples of 4
+// edges and start 16-byte aligned: every lane loads the same 4 column indices
+// (one broadcast 16-byte load per 4 edges), padding edges point at the zero
+// row n, so no per-edge predicate is needed; two groups are in flight.
+template <class P>
+__device__ __forceinline__ typename P::T gather_sum_q(const BatchParams &p, int eb, int ee, int c,
+                                                      uint64_t pol) {
+  using T = typename P::T;
+  T s = P::zero();
+  int e = eb;
+  for (; e + 8 <= ee; e += 8) {
+    const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
+    const int4 b = __ldg(reinterpret_cast<const int4 *>(p.col + e + 4));
+    const T g0 = P::load(p, (int64_t)a.x * kCols + c, pol), g1 = P::load(p, (int64_t)a.y * kCols + c, pol);
+    const T g2 = P::load(p, (int64_t)a.z * kCols + c, pol), g3 = P::load(p, (int64_t)a.w * kCols + c, pol);
+    const T g4 = P::load(p, (int64_t)b.x * kCols + c, pol), g5 = P::load(p, (int64_t)b.y * kCols + c, pol);
+    const T g6 = P::load(p, (int64_t)b.z * kCols + c, pol), g7 = P::load(p, (int64_t)b.w * kCols + c, pol);
+    s = P::add(s, g0); s = P::add(s, g1); s = P::add(s, g2); s = P::add(s, g3);
+    s = P::add(s, g4); s = P::add(s, g5); s = P::add(s, g6); s = P::add(s, g7);
+  }
+  if (e < ee) {  // one group of 4 left
+    const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
+    const T g0 = P::load(p, (int64_t)a.x * kCols + c, pol), g1 = P::load(p, (int64_t)a.y * kCols + c, pol);
+    const T g2 = P::load(p, (int64_t)a.z * kCols + c, pol), g3 = P::load(p, (int64_t)a.w * kCols + c, pol);
+    s = P::add(s, g0); s = P::add(s, g1); s = P::add(s, g2); s = P::add(s, g3);
+  }
+  return s;
+}
+
 template <class P>
 __device__ __forceinline__ void col_epilogue(const BatchParams &p, int64_t v, typename P::T s, df dsum,
                                              bool uniform, LaneAcc &a, int c) {
@@ -426,7 +455,7 @@ __global__ void __launch_bounds__(kBThreads, kBMinBlocks) spmm_kernel(BatchParam
         const int rb = (int)__ldg(&p.rp[h]), re = (int)__ldg(&p.rp[h + 1]);
         const int cs = rb + ((int)t - first) * kSpmmChunk;
         const int ce = min(re, cs + kSpmmChunk);
-        const T s = gather_sum<P>(p, cs, ce, c, gmask, pol);
+        const T s = kRowAlign == 4 ? gather_sum_q<P>(p, cs, ce, c, pol) : gather_sum<P>(p, cs, ce, c, gmask, pol);
         p.lpart[t * kCols + c] = P::pack(s);
         __threadfence();
         __syncwarp();
@@ -440,6 +469,13 @@ __global__ void __launch_bounds__(kBThreads, kBMinBlocks) spmm_kernel(BatchParam
           if (c == 0) p.lcnt[h] = 0;
           if (active) col_epilogue<P>(p, h, all, dsum, uniform, a, c);
         }
+      } else if (kRowAlign == 4 && R == 1) {
+        const int64_t v = p.n_big + (w - p.n_big_tasks);
+        BIn in;
+        if (active) in = b_in<P>(p, v, c, uniform);
+        const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
+        const T s = gather_sum_q<P>(p, eb, ee, c, pol);
+        if (active) col_epilogue_in<P>(p, v, s, dsum, in, a, c);
       } else {
         const int64_t v0 = p.n_big + (w - p.n_big_tasks) * R;
         rows_task<P, R>(p, v0, p.n, c, active, uniform, dsum, a, pol);

@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--cpu-iters", type=int, default=0,
                     help="iterations of the CPU sample (0: sized to ~10 s)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-PPR measurement")
+    ap.add_argument("--batch-scale", type=int, default=20)
+    ap.add_argument("--batch-sets", type=int, default=1024)
     return ap.parse_args()
 
 
@@ -159,6 +162,69 @@ def cpu_iters_for(g, a):
         return a.cpu_iters
     # roughly 10 s of single-thread work at ~100 M edge updates/s
     return int(max(1, min(20, 1.0e9 / max(g.m, 1))))
+
+
+def batch_workload(a):
+    return {"workload": f"batched personalized PageRank, R-MAT scale {a.batch_scale} edge factor 16 "
+                        f"(0.57/0.19/0.19/0.05, dedup, no self loops), unweighted; {a.batch_sets} seed sets "
+                        f"of sizes U[1,64], nodes drawn proportional to out-degree",
+            "nodes": 1 << a.batch_scale, "damping": 0.85, "tolerance_per_set": 1e-7,
+            "max_iterations": 1000, "graph_seed": 20, "seed_set_seed": 7}
+
+
+def batch_inputs(a):
+    from graphops_gb300 import gen
+    g = gen.rmat(a.batch_scale, 16, seed=20)
+    sp, si = gen.seed_sets(g, a.batch_sets, 1, 64, seed=7)
+    return g, sp, si
+
+
+def batch_cpu(g, sp, si, nsets, threads):
+    """The oracle's personalized_pagerank_run, one call per seed set, spread
+    over host threads (independent calls; each call is single-threaded)."""
+    from oracle import port
+    t0 = time.perf_counter()
+    _, its = port.ppr_many(g.row_ptr, g.col, sp[:nsets + 1], si[:sp[nsets]], 0.85, 1000, 1e-7,
+                           threads=threads, want_scores=False)
+    dt = time.perf_counter() - t0
+    return nsets / dt, dt
+
+
+def run_batch(a, ctx, rank, ws):
+    """Batched PPR seeds/s: device-resident graph; end to end with the score
+    blocks copied back; CPU reference on a sample of the same seed sets."""
+    import graphops_gb300 as go
+    from graphops_gb300 import _native
+    g, sp, si = batch_inputs(a)
+    conf = go.PageRankConfig(0.85, 1000, 1e-7)
+    dg = _native.DeviceGraph.from_csr(g.row_ptr, g.col, ctx=ctx)
+    dg.ppr_batch(conf, sp[:33], si[:sp[32]], out=False)  # plan + workspace
+    ctx.set_timing(True)
+    _, its, _, conv = dg.ppr_batch(conf, sp, si, out=False)
+    st = ctx.stats()
+    ctx.set_timing(False)
+    t = max_over_ranks(st.solve_ms, ws)
+    # end to end: scores of every set back in host memory
+    t0 = time.perf_counter()
+    dg2 = _native.DeviceGraph.from_csr(g.row_ptr, g.col, ctx=ctx)
+    s, _, _, _ = dg2.ppr_batch(conf, sp, si, out=True)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
+    out = {"config": batch_workload(a), "seeds_per_s": round(ws * a.batch_sets / (t * 1e-3), 2),
+           "ms": round(t, 3), "iterations_mean": float(its.mean()), "iterations_max": int(its.max()),
+           "all_converged": bool(conv.all()), "kernel_launches": int(st.kernel_launches),
+           "spmm_fp32_launch_ms": round(st.f32_ms / max(1, st.f32_launches), 4),
+           "e2e": {"seeds_per_s": round(ws * a.batch_sets / e2e_s, 2),
+                   "h2d_bytes_per_step": int(g.row_ptr.nbytes + g.col.nbytes + sp.nbytes + si.nbytes),
+                   "d2h_bytes_per_step": int(s.nbytes)}}
+    del s
+    if rank == 0 and not a.no_cpu:
+        threads = max(1, os.cpu_count() or 1)
+        ns = min(a.batch_sets, 2 * threads)
+        v, dt = batch_cpu(g, sp, si, ns, threads)
+        out["cpu_baseline"] = {"value": round(v, 3), "unit": "seeds/s", "cores": threads, "kind": "port",
+                               "sample": f"{ns} seed sets, one personalized_pagerank_run each "
+                                         f"(C restatement, FP64), {threads} threads, {dt:.1f} s"}
+    return out
 
 
 def run_reference(a):
@@ -304,6 +370,10 @@ def run_gpu(a):
                "sample": f"{it} iterations of pagerank_weighted_run ({dt:.1f} s), C restatement, "
                          f"FP64, single thread (the reference path is single-threaded)"}
 
+    batch = None
+    if not a.no_batch:
+        batch = run_batch(a, ctx, rank, ws)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": ws,
@@ -325,6 +395,7 @@ def run_gpu(a):
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
+            "ppr_batched": batch,
         }
         print(json.dumps(line))
     if ws > 1:

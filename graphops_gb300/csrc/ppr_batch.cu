@@ -59,7 +59,7 @@ constexpr int kSpmmBig = 256;   // rows above this in-degree are chunked
 constexpr int kSpmmChunk = 256; // edges per chunk task
 constexpr int kBThreads = 256;
 constexpr int kBWarps = kBThreads / kWarp;
-constexpr double kBTheta = 1e-2;
+constexpr double kBTheta = 1e-1;  // double-float phase while some column has ||r||_1 >= kBTheta
 
 struct ColState {
   unsigned long long iterations;

@@ -45,6 +45,17 @@ class Stats(ctypes.Structure):
                 ("df_ms", _dbl), ("df_launches", _u64), ("f32_ms", _dbl), ("f32_launches", _u64)]
 
 
+class WarmConfig(ctypes.Structure):
+    _fields_ = [("clusters", _i32), ("code_steps", _i32), ("kmeans_iters", _i32), ("minibatch", _i32),
+                ("chunk", _i32), ("epochs", _i32), ("lr", ctypes.c_float), ("ridge", ctypes.c_float),
+                ("seed", _u64), ("push_budget", _i64)]
+
+
+class WarmStats(ctypes.Structure):
+    _fields_ = [("loss_first", _dbl), ("loss_last", _dbl), ("steps", _i64), ("sets", _i64),
+                ("target_ms", _dbl), ("fit_ms", _dbl)]
+
+
 # (name, restype, argtypes) for every symbol include/gops.h declares
 SIGNATURES = [
     ("gops_abi_version", ctypes.c_int, []),
@@ -68,6 +79,21 @@ SIGNATURES = [
     ("gops_pagerank_run_noalloc", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, ctypes.POINTER(Run)]),
     ("gops_ppr_batch", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
     ("gops_ppr_batch_device", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
+    ("gops_warm_config_default", None, [ctypes.POINTER(WarmConfig)]),
+    ("gops_warm_create", ctypes.c_int, [_p, _p, _p, _p, ctypes.POINTER(WarmConfig), ctypes.POINTER(_p)]),
+    ("gops_warm_destroy", None, [_p]),
+    ("gops_warm_train", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, ctypes.POINTER(WarmStats)]),
+    ("gops_warm_predict", ctypes.c_int, [_p, _p, _dbl, _i64, _p, _p, _p, _p]),
+    ("gops_ppr_batch_learned", ctypes.c_int, [_p, _p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
+    ("gops_ppr_batch_learned_device", ctypes.c_int,
+     [_p, _p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
+    ("gops_ppr_batch_judged_device", ctypes.c_int,
+     [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p, _p, _p]),
+    ("gops_warm_count", _i64, [_p, ctypes.c_int]),
+    ("gops_warm_get", ctypes.c_int, [_p, _p, ctypes.c_int, _p, _i64]),
+    ("gops_warm_set", ctypes.c_int, [_p, _p, ctypes.c_int, _p, _i64]),
+    ("gops_warm_loss_grad", ctypes.c_int, [_p, _p, _dbl, _i64, _p, _p, _p, ctypes.POINTER(_dbl), _p]),
+    ("gops_warm_push", ctypes.c_int, [_p, _p, _dbl, _p, _i64, _p, _p, ctypes.POINTER(_dbl), ctypes.POINTER(_dbl)]),
 ]
 
 _lib = None

@@ -13,7 +13,7 @@ Status dense_to_out_csr_device(Ctx *ctx, int64_t n, const double *d_M, int64_t *
                                int32_t **d_col, double **d_w, int64_t *m_out);
 Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, const int64_t *seed_ptr,
                  const int32_t *seed_idx, const float *x0, bool x0_on_device, float *scores,
-                 bool scores_on_device, gops_run *runs);
+                 bool scores_on_device, gops_run *runs, const double *r1_max, int32_t *rejected);
 }  // namespace gops
 
 using namespace gops;
@@ -291,7 +291,7 @@ static int batch_common(gops_ctx *ctx, const gops_graph *g, const gops_config *c
   if (g->impl.ctx != &c) return c.set(Status{GOPS_ERR_INVALID, "graph belongs to another context"});
   cudaSetDevice(c.device);
   return c.set(ppr_batch(&c, const_cast<Graph *>(&g->impl), cfg, nsets, seed_ptr, seed_idx, x0, on_device,
-                         scores, on_device, runs));
+                         scores, on_device, runs, nullptr, nullptr));
 }
 
 int gops_ppr_batch(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,

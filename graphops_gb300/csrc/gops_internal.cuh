@@ -191,4 +191,10 @@ __host__ __device__ inline T ceil_div(T a, T b) {
   return (a + b - 1) / b;
 }
 
+// CTAs for `work` items of `threads` each, at least 1 and at most `cap`
+inline int blocks_for(int64_t work, int threads, int cap) {
+  const int64_t b = (work + threads - 1) / threads;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
 }  // namespace gops

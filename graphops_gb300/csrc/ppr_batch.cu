@@ -66,8 +66,9 @@ struct ColState {
   double diff_l1;
   int retired;
   int converged;
-  int uniform;  // personalization is uniform (empty seed set)
-  int pad;
+  int uniform;   // personalization is uniform (empty seed set)
+  int rejected;  // warm start rejected after step 1 (its residual exceeded r1_max)
+  double r1_max; // largest first-step residual accepted from a warm start
 };
 
 struct WaveState {
@@ -393,12 +394,17 @@ __device__ bool batch_prologue(const BatchParams &p, int lane, bool *active, df 
     const long long badc = *(volatile long long *)&p.sums[(prev * kCols + c) * 4 + 2];
     diff = badc ? NAN : (double)raw * p.fx_inv;
   }
-  const bool conv = !retired0 && k > 1 && diff < p.tol;
-  const bool cap = !retired0 && !conv && k - 1 >= p.max_iter;
-  const bool act = !retired0 && !conv && !cap;
-  if (blockIdx.x == 0 && threadIdx.x < kCols && (conv || cap)) {
+  // a warm start is judged by its first residual: one that does not drop
+  // below the cold start's (or is not finite) retires the column, and the
+  // caller solves that set again from the personalization vector
+  const bool rej = !retired0 && k == 2 && p.x0 && !(diff <= p.cols[c].r1_max);
+  const bool conv = !retired0 && !rej && k > 1 && diff < p.tol;
+  const bool cap = !retired0 && !rej && !conv && k - 1 >= p.max_iter;
+  const bool act = !retired0 && !rej && !conv && !cap;
+  if (blockIdx.x == 0 && threadIdx.x < kCols && (conv || cap || rej)) {
     p.cols[c].retired = 1;
     p.cols[c].converged = conv ? 1 : 0;
+    p.cols[c].rejected = rej ? 1 : 0;
     p.cols[c].iterations = k - 1;
     p.cols[c].diff_l1 = diff;
   }
@@ -621,10 +627,6 @@ __global__ void prow_from_sorted(const int32_t *rows, int64_t e, int64_t n, int3
   }
 }
 
-int blocks_for(int64_t work, int threads, int cap) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(work, threads), cap));
-}
-
 Status batch_prepare(Ctx *ctx, Graph *g) {
   if (g->batch) return Status::ok();
   cudaStream_t s = ctx->stream;
@@ -696,7 +698,7 @@ Status ensure_entries(BatchState *b, int64_t e) {
 // nsets seed sets -> scores (host or device, set-major, original node order)
 Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, const int64_t *seed_ptr,
                  const int32_t *seed_idx, const float *x0, bool x0_on_device, float *scores,
-                 bool scores_on_device, gops_run *runs) {
+                 bool scores_on_device, gops_run *runs, const double *r1_max, int32_t *rejected) {
   ctx->stats = gops_stats{};
   const int64_t n = g->n;
   if (nsets <= 0) return Status::ok();
@@ -760,7 +762,9 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     p.ncols = ncols;
     // ---- personalization entries of the wave: (row, column, weight)
     std::map<std::pair<int32_t, int32_t>, double> ent;
-    for (int c = 0; c < kCols; ++c) cols_h[c] = ColState{0, 0.0, c < ncols ? 0 : 1, 0, 0, 0};
+    for (int c = 0; c < kCols; ++c)
+      cols_h[c] = ColState{0, 0.0, c < ncols ? 0 : 1, 0, 0, 0,
+                           r1_max && c < ncols ? r1_max[set0 + c] : (double)INFINITY};
     double wmax = 1.0;
     for (int c = 0; c < ncols; ++c) {
       const int64_t a0 = seed_ptr[set0 + c], a1 = seed_ptr[set0 + c + 1];
@@ -890,6 +894,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     for (int c = 0; c < ncols; ++c) {
       col_iters += cols_h[c].iterations;
       if (runs) runs[set0 + c] = gops_run{cols_h[c].iterations, cols_h[c].diff_l1, cols_h[c].converged, 0};
+      if (rejected) rejected[set0 + c] = cols_h[c].rejected;
     }
   }
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[3], st));

@@ -188,6 +188,127 @@ const double *gops_ctx_scores_device(const gops_ctx *ctx);
 int gops_pagerank_run_noalloc(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg,
                               double *scores, gops_run *run);
 
+/* ---- learned warm start for batched personalized PageRank ----
+ * No counterpart in the reference (it is the extension that feeds
+ * gops_ppr_batch's x0).  A per-graph model predicts each set's PPR vector:
+ *
+ *   x0 = (1-d) (s + d P s + d^2 P^2 s + d^3 P^3 s)          exact, sparse push
+ *      + tail_i = tm * w_i * m[a_i] / (sum_c m[c] * cw[a_i])  learned
+ *
+ * where s is the set's normalised indicator, P the transition matrix,
+ * tm = 1 - sum of the exact part, a_i a k-means cluster of node i over a
+ * seeded random-projection code (diffusion of Gaussian vectors over the
+ * graph), w_i = exp(MPNN(features of i)) a per-node weight from a two-layer
+ * message-passing network (hidden 128, BF16 operands, FP32 accumulation) fed
+ * log(1+out-degree), log(1+in-degree) and the code, m = relu(c K) the
+ * predicted cluster masses from the cluster mix c of P^3 s and P^4 s, and
+ * cw[c] = sum of w over cluster c.  K is fitted by least squares and the MPNN
+ * by Adam on an L1 loss, both against PPR vectors that gops_ppr_batch
+ * computes on the device.  The power iteration still runs to the same
+ * tolerance; a warm start whose first residual is not below the cold start's
+ * is rejected and the set is solved again from s. */
+typedef struct gops_warm gops_warm;
+
+typedef struct gops_warm_config {
+  int32_t clusters;     /* k-means clusters, 1..256 (default 128) */
+  int32_t code_steps;   /* diffusion steps of the 16-wide code (default 10) */
+  int32_t kmeans_iters; /* Lloyd iterations after k-means++ seeding (default 20) */
+  int32_t minibatch;    /* sets per Adam step, 1..32 (default 32) */
+  int32_t chunk;        /* training targets solved per batched call (default 512) */
+  int32_t epochs;       /* passes over the training sets (default 1) */
+  float lr;             /* Adam step size (default 3e-3) */
+  float ridge;          /* least-squares ridge, relative to the Gram trace (default 1e-9) */
+  uint64_t seed;        /* seeds the code, k-means++ and the initial weights */
+  int64_t push_budget;  /* edge visits of one set's push before it starts cold (default 1<<24) */
+} gops_warm_config;
+
+typedef struct gops_warm_stats {
+  double loss_first;    /* mean L1 loss of the first and last Adam steps */
+  double loss_last;
+  int64_t steps;        /* Adam steps taken */
+  int64_t sets;         /* training targets solved */
+  double target_ms;     /* device time: solving the targets */
+  double fit_ms;        /* device time: push, least squares and Adam steps */
+} gops_warm_stats;
+
+void gops_warm_config_default(gops_warm_config *cfg);
+
+/* Builds the model's graph-side state (CSR copies in original order, code,
+ * features, clusters; untrained weights).  row_ptr/col: the out-adjacency
+ * given to gops_graph_upload for g. */
+int gops_warm_create(gops_ctx *ctx, const gops_graph *g, const int64_t *row_ptr, const int32_t *col,
+                     const gops_warm_config *wcfg, gops_warm **out);
+void gops_warm_destroy(gops_warm *w);
+
+/* Trains on the given seed sets (layout as gops_ppr_batch): solves their PPR
+ * vectors with cfg on the device, fits K and runs the Adam steps. */
+int gops_warm_train(gops_ctx *ctx, gops_warm *w, const gops_config *cfg, int64_t nsets,
+                    const int64_t *seed_ptr, const int32_t *seed_idx, gops_warm_stats *stats);
+
+/* Warm starts for nsets sets into x0_device (nsets*n floats, set-major,
+ * original order).  r1_cold (optional, host, nsets): the first-step residual
+ * L1 norm of the cold start of each set.  A set whose push would exceed the
+ * budget gets x0 = s and r1_cold = +inf. */
+int gops_warm_predict(gops_ctx *ctx, gops_warm *w, double damping, int64_t nsets, const int64_t *seed_ptr,
+                      const int32_t *seed_idx, float *x0_device, double *r1_cold);
+
+/* gops_ppr_batch with learned warm starts: predict, solve, and solve again
+ * from s every set whose warm start was rejected (rejected: optional host
+ * flags, nsets).  scores: host buffer as in gops_ppr_batch, or NULL. */
+int gops_ppr_batch_learned(gops_ctx *ctx, const gops_graph *g, gops_warm *w, const gops_config *cfg,
+                           int64_t nsets, const int64_t *seed_ptr, const int32_t *seed_idx, float *scores,
+                           gops_run *runs, int32_t *rejected);
+/* The same with scores in device memory (nsets*n floats). */
+int gops_ppr_batch_learned_device(gops_ctx *ctx, const gops_graph *g, gops_warm *w, const gops_config *cfg,
+                                  int64_t nsets, const int64_t *seed_ptr, const int32_t *seed_idx,
+                                  float *scores_device, gops_run *runs, int32_t *rejected);
+
+/* Batched PPR from caller-supplied warm starts, judged: x0_device (nsets*n
+ * floats, set-major) as in gops_ppr_batch_device; a set whose first-step
+ * residual L1 norm is not below r1_max[s] (host, optional: NULL accepts every
+ * start) is retired after that step and solved again from its
+ * personalization vector (rejected[s] = 1).  gops_ppr_batch_learned is
+ * gops_warm_predict followed by this call with r1_max = the cold residuals. */
+int gops_ppr_batch_judged_device(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,
+                                 const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0_device,
+                                 const double *r1_max, float *scores_device, gops_run *runs, int32_t *rejected);
+
+/* Model state in and out (host buffers), for checkpoints and for checking the
+ * kernels against a CPU restatement.  `what`:
+ *   GOPS_WARM_PARAMS   float, gops_warm_param_count() entries (W1 48x128 with
+ *                      the layer-1 bias as row 36, W2 256x128, b2 128, w3 128, b3 1)
+ *   GOPS_WARM_COUPLING float, (2*clusters+1) x clusters (K)
+ *   GOPS_WARM_CLUSTERS int32, n (cluster of each node)
+ *   GOPS_WARM_FEATURES float, n x 48 (layer-1 input [x, mean_in x, 1, 0...], as BF16 values)
+ *   GOPS_WARM_CODE     float, n x 16
+ *   GOPS_WARM_WEIGHT   float, n (w of the current parameters) */
+enum {
+  GOPS_WARM_PARAMS = 0,
+  GOPS_WARM_COUPLING = 1,
+  GOPS_WARM_CLUSTERS = 2,
+  GOPS_WARM_FEATURES = 3,
+  GOPS_WARM_CODE = 4,
+  GOPS_WARM_WEIGHT = 5
+};
+int64_t gops_warm_count(const gops_warm *w, int what);
+int gops_warm_get(gops_ctx *ctx, gops_warm *w, int what, void *host, int64_t count);
+/* GOPS_WARM_PARAMS and GOPS_WARM_COUPLING only (resets the Adam moments). */
+int gops_warm_set(gops_ctx *ctx, gops_warm *w, int what, const void *host, int64_t count);
+
+/* One loss/gradient evaluation without a parameter update: targets_x (host,
+ * nsets*n floats, set-major) are the sets' PPR vectors; loss = mean over sets
+ * of the L1 error of the predicted tail; grad (host, param count floats) its
+ * gradient with respect to GOPS_WARM_PARAMS.  nsets <= 32. */
+int gops_warm_loss_grad(gops_ctx *ctx, gops_warm *w, double damping, int64_t nsets, const int64_t *seed_ptr,
+                        const int32_t *seed_idx, const float *targets_x, double *loss, float *grad);
+
+/* The exact part of the warm start for one set (host outputs): local (n
+ * doubles, the four push terms), mix (2*clusters+1 doubles: cluster mix of
+ * P^3 s, of P^4 s, and 1), tail mass and cold first residual.  Returns
+ * GOPS_ERR_INVALID when the set exceeds the push budget. */
+int gops_warm_push(gops_ctx *ctx, gops_warm *w, double damping, const int32_t *seeds, int64_t nseeds,
+                   double *local, double *mix, double *tail_mass, double *r1_cold);
+
 #ifdef __cplusplus
 }
 #endif

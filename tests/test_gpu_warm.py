@@ -1,0 +1,255 @@
+"""The learned warm start on the GPU against its CPU oracle
+(oracle/warm_oracle.py) and against the plain batched path.
+
+* the push (exact local terms, cluster mixes, tail mass, cold residual);
+* the random-projection code, the layer-1 features and the clusters;
+* the network's forward pass (w) and its loss / parameter gradient, with the
+  oracle emulating the same BF16 roundings (FP32 vs FP64 accumulation is the
+  only difference left: tolerances below);
+* the least-squares coupling against the oracle's fit of the same data;
+* training: fewer iterations than the cold start on held-out sets, with
+  results equal to the FP64 fixed point;
+* the judge: a deliberately bad start is rejected and the set solved again.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import graphops_gb300 as go
+from graphops_gb300 import gen, warm
+from oracle import port
+from oracle import warm_oracle as wo
+
+pytestmark = pytest.mark.gpu
+
+# tolerances: push terms are FP32 products summed exactly (fixed point)
+PUSH_L1 = 1e-6
+# network: BF16 operands emulated by the oracle; FP32 accumulation on the GPU
+W_REL_MEDIAN, W_REL_MAX = 1e-3, 5e-2
+GRAD_COS, GRAD_REL = 0.999, 3e-2
+
+
+@pytest.fixture(scope="module")
+def small():
+    g = gen.sbm(4000, 16, 1.2, 16.0, 4.0, seed=1)
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    cfg = warm.default_config(clusters=32, kmeans_iters=10, chunk=256, seed=7)
+    ws = warm.WarmStart(dg, g.row_ptr, g.col, cfg)
+    return g, dg, ws
+
+
+def test_push_matches_oracle(small):
+    g, dg, ws = small
+    cl = ws.get(warm.CLUSTERS)
+    r = int(cl.max()) + 1
+    assert r <= 32
+    for seeds in ([5], [3, 3, 900], list(range(0, 4000, 125)), [17, 2500, 2501, 3999]):
+        local, mix, tm, r1 = ws.push(0.85, seeds)
+        l_o, m_o, tm_o, r1_o = wo.push(g.n, g.row_ptr, g.col, cl, 32, seeds, 0.85)
+        assert np.abs(local - l_o).sum() <= PUSH_L1
+        assert np.abs(mix - m_o).max() <= PUSH_L1
+        assert abs(tm - tm_o) <= PUSH_L1 and abs(r1 - r1_o) <= PUSH_L1 * 10
+
+
+def test_code_and_features_match_oracle(small):
+    g, dg, ws = small
+    z0 = wo.code_init(g.n, ws.config.seed)
+    z = wo.code(g.n, g.row_ptr, g.col, z0, ws.config.code_steps)
+    zg = ws.get(warm.CODE).reshape(g.n, 16).astype(np.float64)
+    assert np.abs(zg - z).max() <= 2e-3
+    # layer-1 input from the GPU's code: standardised degrees and code, their
+    # in-neighbour means, the bias column
+    dout = np.diff(g.row_ptr).astype(np.float64)
+    din = np.bincount(g.col, minlength=g.n).astype(np.float64)
+    x = np.c_[np.log1p(dout), np.log1p(din), zg]
+    x = (x - x.mean(0)) / x.std(0)
+    in_rp, in_col = wo.in_csr(g.n, g.row_ptr, g.col)
+    dst = np.repeat(np.arange(g.n), np.diff(in_rp))
+    ax = np.zeros_like(x)
+    np.add.at(ax, dst, x[in_col])
+    ax *= np.where(din > 0, 1 / np.maximum(din, 1), 0)[:, None]
+    want = np.zeros((g.n, 48))
+    want[:, :18], want[:, 18:36], want[:, 36] = x, ax, 1.0
+    got = ws.get(warm.FEATURES).reshape(g.n, 48)
+    assert np.all(np.abs(got - wo.bf16(want)) <= 2.0 ** -7 * np.abs(want) + 1e-5)
+
+
+def test_clusters_follow_blocks(small):
+    g, dg, ws = small
+    cl = ws.get(warm.CLUSTERS)
+    pure = 0
+    for c in np.unique(cl):
+        b = np.bincount(g.block[cl == c])
+        pure += b.max()
+    assert pure / g.n >= 0.95
+
+
+def random_params(seed):
+    rng = np.random.default_rng(seed)
+    p = np.zeros(wo.P_COUNT, dtype=np.float32)
+    p[wo.P_W1:wo.P_W1 + 36 * 128] = 0.25 * rng.standard_normal(36 * 128)
+    p[wo.P_W1 + 36 * 128:wo.P_W1 + 37 * 128] = 0.05 * rng.standard_normal(128)
+    p[wo.P_W2:wo.P_B2] = (1 / 16) * rng.standard_normal(256 * 128)
+    p[wo.P_B2:wo.P_W3] = 0.05 * rng.standard_normal(128)
+    p[wo.P_W3:wo.P_B3] = 0.2 * rng.standard_normal(128)
+    p[wo.P_B3] = 0.1
+    return p
+
+
+def test_forward_matches_oracle(small):
+    g, dg, ws = small
+    p = random_params(3)
+    ws.set(warm.PARAMS, p)
+    w = ws.get(warm.WEIGHT).astype(np.float64)
+    x1 = ws.get(warm.FEATURES).reshape(g.n, 48)
+    in_rp, in_col = wo.in_csr(g.n, g.row_ptr, g.col)
+    wref, _ = wo.forward(x1, p.astype(np.float64), in_rp, in_col, emulate_bf16=True)
+    rel = np.abs(w - wref) / wref
+    assert np.median(rel) <= W_REL_MEDIAN and rel.max() <= W_REL_MAX, (np.median(rel), rel.max())
+    assert w.std() > 0.05 * w.mean()  # the test exercises a non-trivial network
+
+
+def test_loss_and_gradient_match_oracle(small):
+    g, dg, ws = small
+    p = random_params(4)
+    ws.set(warm.PARAMS, p)
+    cl = ws.get(warm.CLUSTERS)
+    r = 32
+    rng = np.random.default_rng(5)
+    K = np.abs(rng.standard_normal((2 * r + 1, r))).astype(np.float32)
+    ws.set(warm.COUPLING, K)
+    sp, si = gen.seed_sets(g, 8, 1, 32, seed=9)
+    xs, _ = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-12, threads=8)
+    loss, grad = ws.loss_grad(0.85, sp, si, xs.astype(np.float32))
+    pushes = [wo.push(g.n, g.row_ptr, g.col, cl, r, si[sp[j]:sp[j + 1]], 0.85) for j in range(8)]
+    tails = np.stack([xs.astype(np.float32).astype(np.float64)[j] - pushes[j][0] for j in range(8)])
+    mix = np.stack([q[1] for q in pushes])
+    tm = np.array([q[2] for q in pushes])
+    x1 = ws.get(warm.FEATURES).reshape(g.n, 48)
+    in_rp, in_col = wo.in_csr(g.n, g.row_ptr, g.col)
+    lref, gref = wo.loss_grad(p.astype(np.float64), x1, in_rp, in_col, g.row_ptr, g.col, cl, r, mix,
+                              K.astype(np.float64), tm, tails, emulate_bf16=True)
+    assert abs(loss - lref) <= 1e-3 * lref, (loss, lref)
+    for a, b in ((wo.P_W1, wo.P_W2), (wo.P_W2, wo.P_B2), (wo.P_B2, wo.P_W3), (wo.P_W3, wo.P_B3)):
+        u, v = grad[a:b].astype(np.float64), gref[a:b]
+        cos = u @ v / (np.linalg.norm(u) * np.linalg.norm(v))
+        rel = np.linalg.norm(u - v) / np.linalg.norm(v)
+        assert cos >= GRAD_COS and rel <= GRAD_REL, (a, cos, rel)
+    assert abs(grad[wo.P_B3] - gref[wo.P_B3]) <= GRAD_REL * abs(gref[wo.P_B3]) + 1e-6
+
+
+@pytest.fixture(scope="module")
+def trained():
+    g = gen.sbm(20000, 32, 1.2, 16.0, 4.0, seed=2)
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    cfg = warm.default_config(clusters=64, chunk=512, seed=11)
+    ws = warm.WarmStart(dg, g.row_ptr, g.col, cfg)
+    sp, si = gen.seed_sets(g, 1536, 1, 32, seed=21)
+    conf = go.PageRankConfig(0.85, 1000, 1e-7)
+    stats = ws.train(conf, sp, si)
+    return g, dg, ws, conf, stats
+
+
+def test_training_gains_over_cold_start(trained):
+    g, dg, ws, conf, stats = trained
+    assert stats.sets == 1536 and stats.steps > 0
+    assert stats.loss_last < stats.loss_first
+    sp, si = gen.seed_sets(g, 96, 1, 32, seed=99)   # held out
+    cold = go.ppr_batch(dg, conf, sp, si)
+    lr = ws.ppr_batch(conf, sp, si)
+    exact, _ = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-12, threads=8)
+    assert lr.converged.all() and not lr.rejected.any()
+    l1 = np.abs(lr.scores.astype(np.float64) - exact).sum(1)
+    assert l1.max() <= 1e-6, l1.max()
+    l1c = np.abs(cold.scores.astype(np.float64) - exact).sum(1)
+    assert l1c.max() <= 1e-6
+    gain = cold.iterations.mean() / lr.iterations.mean()
+    print(f"cold {cold.iterations.mean():.2f} learned {lr.iterations.mean():.2f} gain {gain:.2f}")
+    assert gain >= 1.4, gain
+    # identical top-100 ordering of the scores (ties aside) on most sets
+    same = 0
+    for j in range(96):
+        same += np.array_equal(np.argsort(-exact[j], kind="stable")[:100],
+                               np.argsort(-lr.scores[j].astype(np.float64), kind="stable")[:100])
+    assert same >= 90
+
+
+def test_least_squares_matches_oracle(trained):
+    g, dg, ws, conf, stats = trained
+    # refit the coupling from a fresh model on the same data with the oracle
+    K = ws.get(warm.COUPLING).reshape(2 * 64 + 1, 64)
+    cl = ws.get(warm.CLUSTERS)
+    sp, si = gen.seed_sets(g, 1536, 1, 32, seed=21)
+    xs, _ = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-7, threads=8)
+    loc, X, _ = wo.push_many(g.n, g.row_ptr, g.col, cl, 64, sp, si, 0.85)
+    Y = np.stack([np.bincount(cl, weights=xs[j] - loc[j], minlength=64) for j in range(1536)])
+    Kref = wo.fit_coupling(X, Y, ws.config.ridge)
+    # compare predictions (the coupling itself is ill-conditioned)
+    P, Pref = X @ K, X @ Kref
+    assert np.abs(P - Pref).sum(1).max() <= 2e-3, np.abs(P - Pref).sum(1).max()
+
+
+def test_judge_rejects_a_bad_start_and_resolves(trained):
+    g, dg, ws, conf, stats = trained
+    sp, si = gen.seed_sets(g, 40, 1, 8, seed=5)
+    n = g.n
+    cl = ws.get(warm.CLUSTERS)
+    # a deliberately bad start for the even sets: all mass on one node that
+    # is no seed; the learned start for the odd ones
+    x0 = torch.empty((40, n), dtype=torch.float32, device="cuda")
+    r1 = ws.predict_device(0.85, sp, si, x0.data_ptr())
+    bad = []
+    for j in range(0, 40, 2):
+        z = next(v for v in range(n) if v not in set(si[sp[j]:sp[j + 1]].tolist()))
+        x0[j].zero_()
+        x0[j, z] = 1.0
+        bad.append(j)
+    out = torch.empty((40, n), dtype=torch.float32, device="cuda")
+    runs = (go._native.Run * 40)()
+    rej = np.zeros(40, dtype=np.int32)
+    c = go._native.Config(0.85, 1000, 1e-7)
+    l = dg.ctx._l
+    spp = np.ascontiguousarray(sp, np.int64)
+    sii = np.ascontiguousarray(si, np.int32)
+    r1c = np.ascontiguousarray(r1, np.float64)
+    dg.ctx.check(l.gops_ppr_batch_judged_device(dg.ctx.handle, dg.handle, ctypes.byref(c), 40,
+                                                go._native.ptr(spp), go._native.ptr(sii),
+                                                ctypes.c_void_p(x0.data_ptr()), go._native.ptr(r1c),
+                                                ctypes.c_void_p(out.data_ptr()),
+                                                ctypes.cast(runs, ctypes.c_void_p), go._native.ptr(rej)))
+    # the oracle's judgement of the same starts: ||F(x0) - x0||_1 vs the cold one
+    x0h = x0.cpu().numpy().astype(np.float64)
+    deg = np.diff(g.row_ptr)
+    src = np.repeat(np.arange(n), deg)
+    for j in range(40):
+        s = np.zeros(n)
+        np.add.at(s, si[sp[j]:sp[j + 1]], 1.0 / (sp[j + 1] - sp[j]))
+        x = x0h[j]
+        y = np.zeros(n)
+        np.add.at(y, g.col, (x / np.maximum(deg, 1))[src])
+        F = 0.15 * s + 0.85 * y + 0.85 * x[deg == 0].sum() * s
+        assert bool(rej[j]) == (np.abs(F - x).sum() > r1[j] * (1 + 1e-5)), j
+    assert rej[bad].all() and not rej[1::2].any()
+    exact, _ = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-12, threads=8)
+    l1 = np.abs(out.cpu().numpy().astype(np.float64) - exact).sum(1)
+    assert l1.max() <= 1e-6
+    cold = go.ppr_batch(dg, go.PageRankConfig(0.85, 1000, 1e-7), sp, si)
+    its = np.array([runs[i].iterations for i in range(40)])
+    assert np.array_equal(its[bad], cold.iterations[bad])
+
+
+def test_budget_exceeded_starts_cold(small):
+    g, dg, ws, = small[:3]
+    cfg = warm.default_config(clusters=32, kmeans_iters=5, chunk=64, seed=7, push_budget=0)
+    w0 = warm.WarmStart(dg, g.row_ptr, g.col, cfg)
+    sp, si = go.seed_sets_to_csr([[1, 2], [], [7]])
+    conf = go.PageRankConfig(0.85, 1000, 1e-7)
+    lr = w0.ppr_batch(conf, sp, si)
+    cold = go.ppr_batch(dg, conf, sp, si)
+    # x0 = s (the uniform vector for the empty set): the cold iteration, up
+    # to the FP32 rounding of the start and the fixed-point scale of its sums
+    assert np.array_equal(lr.iterations, cold.iterations)
+    assert np.abs(lr.scores.astype(np.float64) - cold.scores).sum(1).max() <= 1e-8
+    assert not lr.rejected.any()

@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-PPR measurement")
     ap.add_argument("--batch-scale", type=int, default=20)
     ap.add_argument("--batch-sets", type=int, default=1024)
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start measurement")
+    ap.add_argument("--learned-n", type=int, default=500000)
+    ap.add_argument("--learned-train", type=int, default=50000)
+    ap.add_argument("--learned-sets", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -227,6 +231,85 @@ def run_batch(a, ctx, rank, ws):
     return out
 
 
+def learned_workload(a):
+    return {"workload": f"learned warm-start batched personalized PageRank, stochastic block model "
+                        f"n={a.learned_n}, 64 blocks with Zipf(1.2) sizes, intra-block mean out-degree 16, "
+                        f"inter-block 4 (directed), unit weights; trained on {a.learned_train} PPR vectors "
+                        f"of seed sets of sizes U[1,32] solved by the batched GPU path; evaluated on "
+                        f"{a.learned_sets} held-out sets of sizes U[1,32]; nodes drawn proportional "
+                        f"to out-degree",
+            "nodes": a.learned_n, "damping": 0.85, "tolerance_per_set": 1e-7, "max_iterations": 1000,
+            "graph_seed": 3, "train_seed": 31, "eval_seed": 77,
+            "model": "2-layer MPNN (hidden 128, BF16 operands, FP32 accumulation) per-node weight, "
+                     "128 k-means clusters of a 16-wide random-projection code, least-squares "
+                     "cluster coupling, exact 3-hop push"}
+
+
+def run_learned(a, ctx, rank, ws):
+    """Learned warm start vs plain batched PPR on the same graph and seed
+    sets: seeds/s of each (device-resident graph, scores left on the device;
+    the learned figure includes the warm-start inference), iterations, and
+    an end-to-end figure with the score blocks copied to the host."""
+    import graphops_gb300 as go
+    from graphops_gb300 import _native, gen, warm
+    g = gen.sbm(a.learned_n, 64, 1.2, 16.0, 4.0, seed=3)
+    conf = go.PageRankConfig(0.85, 1000, 1e-7)
+    dg = _native.DeviceGraph.from_csr(g.row_ptr, g.col, ctx=ctx)
+    t0 = time.perf_counter()
+    model = warm.WarmStart(dg, g.row_ptr, g.col, warm.default_config())
+    create_s = time.perf_counter() - t0
+    sp_t, si_t = gen.seed_sets(g, a.learned_train, 1, 32, seed=31)
+    t0 = time.perf_counter()
+    tst = model.train(conf, sp_t, si_t)
+    train_s = time.perf_counter() - t0
+    sp, si = gen.seed_sets(g, a.learned_sets, 1, 32, seed=77)
+    # warm-up of both paths (plans, workspaces)
+    dg.ppr_batch(conf, sp[:65], si[:sp[64]], out=False)
+    model.ppr_batch(conf, sp[:65], si[:sp[64]], scores=False)
+    _, its_p, _, conv_p = dg.ppr_batch(conf, sp, si, out=False)
+    st_p = ctx.stats()
+    lr = model.ppr_batch(conf, sp, si, scores=False)
+    st_l = ctx.stats()
+    tp = max_over_ranks(st_p.solve_ms, ws)
+    tl = max_over_ranks(st_l.solve_ms, ws)
+    # end to end: both through the public API, every score block to the host
+    t0 = time.perf_counter()
+    s = model.ppr_batch(conf, sp, si, scores=True).scores
+    e2e_l = max_over_ranks(time.perf_counter() - t0, ws)
+    d2h = int(s.nbytes)
+    del s
+    t0 = time.perf_counter()
+    s, _, _, _ = dg.ppr_batch(conf, sp, si, out=True)
+    e2e_p = max_over_ranks(time.perf_counter() - t0, ws)
+    del s
+    n_sets = a.learned_sets
+    out = {"config": learned_workload(a),
+           "learned_seeds_per_s": round(ws * n_sets / (tl * 1e-3), 2),
+           "plain_seeds_per_s": round(ws * n_sets / (tp * 1e-3), 2),
+           "ratio": round(tp / tl, 4),
+           "learned_ms": round(tl, 3), "plain_ms": round(tp, 3),
+           "iterations_mean_learned": float(lr.iterations.mean()),
+           "iterations_mean_plain": float(its_p.mean()),
+           "rejected": int(lr.rejected.sum()),
+           "all_converged": bool(lr.converged.all() and conv_p.all()),
+           "kernel_launches_learned": int(st_l.kernel_launches),
+           "train": {"sets": int(tst.sets), "adam_steps": int(tst.steps),
+                     "loss_first": round(tst.loss_first, 6), "loss_last": round(tst.loss_last, 6),
+                     "targets_ms": round(tst.target_ms, 1), "fit_ms": round(tst.fit_ms, 1),
+                     "wall_s": round(train_s, 2), "model_build_s": round(create_s, 2)},
+           "e2e": {"learned_seeds_per_s": round(ws * n_sets / e2e_l, 2),
+                   "plain_seeds_per_s": round(ws * n_sets / e2e_p, 2),
+                   "h2d_bytes_per_step": int(sp.nbytes + si.nbytes), "d2h_bytes_per_step": d2h}}
+    if rank == 0 and not a.no_cpu:
+        threads = max(1, os.cpu_count() or 1)
+        ns = min(n_sets, threads)
+        v, dt = batch_cpu(g, sp, si, ns, threads)
+        out["cpu_baseline"] = {"value": round(v, 3), "unit": "seeds/s", "cores": threads, "kind": "port",
+                               "sample": f"{ns} seed sets, one personalized_pagerank_run each "
+                                         f"(C restatement, FP64), {threads} threads, {dt:.1f} s"}
+    return out
+
+
 def run_reference(a):
     rank, ws = dist_init(a)
     if rank != 0:
@@ -373,6 +456,9 @@ def run_gpu(a):
     batch = None
     if not a.no_batch:
         batch = run_batch(a, ctx, rank, ws)
+    learned = None
+    if not a.no_learned:
+        learned = run_learned(a, ctx, rank, ws)
 
     if rank == 0:
         line = {
@@ -396,6 +482,7 @@ def run_gpu(a):
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
             "ppr_batched": batch,
+            "ppr_learned": learned,
         }
         print(json.dumps(line))
     if ws > 1:

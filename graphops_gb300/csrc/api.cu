@@ -181,6 +181,7 @@ int gops_graph_upload(gops_ctx *ctx, int64_t n, const int64_t *row_ptr, const in
   gops_graph *g = new (std::nothrow) gops_graph();
   if (!g) return c.set(Status{GOPS_ERR_OOM, "host allocation failed"});
   g->impl.ctx = &c;
+  g->impl.device = c.device;
   Status st = upload_impl(&c, n, row_ptr, col, weights, &g->impl);
   if (st.code != GOPS_OK) {
     graph_free_device(g->impl);
@@ -202,6 +203,7 @@ int gops_graph_from_dense(gops_ctx *ctx, int64_t n, const double *matrix, gops_g
   gops_graph *g = new (std::nothrow) gops_graph();
   if (!g) return c.set(Status{GOPS_ERR_OOM, "host allocation failed"});
   g->impl.ctx = &c;
+  g->impl.device = c.device;
   cudaStream_t s = c.stream;
   double *d_M = nullptr, *d_w = nullptr;
   int64_t *d_rp = nullptr;
@@ -239,10 +241,9 @@ int gops_graph_from_dense(gops_ctx *ctx, int64_t n, const double *matrix, gops_g
 
 void gops_graph_destroy(gops_graph *g) {
   if (!g) return;
-  if (g->impl.ctx) {
-    cudaSetDevice(g->impl.ctx->device);
-    cudaStreamSynchronize(g->impl.ctx->stream);
-  }
+  // the context may already be gone: use the device recorded at upload
+  // (cudaFree waits for the device's pending work before it frees)
+  cudaSetDevice(g->impl.device);
   graph_free_device(g->impl);
   delete g;
 }

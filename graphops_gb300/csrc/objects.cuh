@@ -77,7 +77,8 @@ struct SolveState {
 };
 
 struct Graph {
-  struct Ctx *ctx = nullptr;
+  struct Ctx *ctx = nullptr;  // the creating context (not dereferenced on destroy)
+  int device = 0;
   int64_t n = 0, m = 0;
   int64_t m_stored = 0;  // edges stored in the in-edge CSR (m plus row padding)
   bool weighted = false;

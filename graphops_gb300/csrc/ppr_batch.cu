@@ -60,6 +60,9 @@ constexpr int kSpmmChunk = 256; // edges per chunk task
 constexpr int kBThreads = 256;
 constexpr int kBWarps = kBThreads / kWarp;
 constexpr double kBTheta = 1e-1;  // double-float phase while some column has ||r||_1 >= kBTheta
+// with caller warm starts: their first residual is already small (a learned
+// start is typically 0.1-0.3), so the FP32 phase may begin at step 2
+constexpr double kBThetaWarm = 5e-1;
 
 struct ColState {
   unsigned long long iterations;
@@ -140,6 +143,8 @@ struct BatchParams {
   WaveState *wave;
   const float *x0;  // nullable
   float *out;
+  // set of each column: its row in x0 and in out (set-major, n floats each)
+  int64_t xcol[kCols], ocol[kCols];
   int ncols;
   df d, omd, inv_n;
   float fx_scale;
@@ -542,7 +547,7 @@ __global__ void __launch_bounds__(kBThreads, kBMinBlocks) spmm_kernel(BatchParam
 
 // x_0 (p, or the warm start), acc = x_0, tail = 0, gathered vector for step 1,
 // per-column dangling sums of x_0; zero padding row n of the gathered blocks.
-__global__ void __launch_bounds__(kBThreads) batch_init(BatchParams p, int64_t set0) {
+__global__ void __launch_bounds__(kBThreads) batch_init(BatchParams p) {
   __shared__ long long bdg[kBWarps][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int sub = lane / kCols, c = lane & (kCols - 1);
@@ -560,7 +565,7 @@ __global__ void __launch_bounds__(kBThreads) batch_init(BatchParams p, int64_t s
       continue;
     }
     df x0 = {0.f, 0.f};
-    if (col_ok) x0 = p.x0 ? df_make(p.x0[(set0 + c) * p.n + p.perm[v]]) : red_of(p, v, c, uniform);
+    if (col_ok) x0 = p.x0 ? df_make(p.x0[p.xcol[c] * p.n + p.perm[v]]) : red_of(p, v, c, uniform);
     const float dg = p.deg[v];
     p.acc[i] = make_float2(x0.hi, x0.lo);
     p.tail[i] = 0.f;
@@ -588,7 +593,7 @@ __global__ void batch_finalize(BatchParams p) {
     const int64_t i = v * kCols + c;
     if (c < p.ncols) {
       const float2 a = p.acc[i];
-      p.out[(int64_t)c * p.n + p.perm[v]] = (float)((double)a.x + (double)a.y + (double)p.tail[i]);
+      p.out[p.ocol[c] * p.n + p.perm[v]] = (float)((double)a.x + (double)a.y + (double)p.tail[i]);
     }
   }
 }
@@ -739,7 +744,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   p.omd = df_from_double(1.0 - cfg->damping);
   p.inv_n = df_from_double(1.0 / (double)n);
   p.tol = cfg->tolerance;
-  p.theta = kBTheta;
+  p.theta = x0 ? kBThetaWarm : kBTheta;
   p.max_iter = cfg->max_iterations;
 
   int occ_df = 0, occ_f = 0;
@@ -756,18 +761,30 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   std::vector<ColState> cols_h(kCols);
   std::vector<int32_t> erow, eslot;
   std::vector<float2> eval;
+  // waves of sets of similar size: a set's step count falls with its size,
+  // and a wave runs until its slowest column retires
+  std::vector<int64_t> order(nsets);
+  for (int64_t q = 0; q < nsets; ++q) order[q] = q;
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+    return seed_ptr[a + 1] - seed_ptr[a] < seed_ptr[b + 1] - seed_ptr[b];
+  });
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], st));
   for (int64_t set0 = 0; set0 < nsets; set0 += kCols) {
     const int ncols = (int)std::min<int64_t>(kCols, nsets - set0);
     p.ncols = ncols;
+    for (int c = 0; c < kCols; ++c) {
+      const int64_t sid = c < ncols ? order[set0 + c] : 0;
+      p.xcol[c] = x0 && !x0_on_device ? c : sid;
+      p.ocol[c] = scores && !scores_on_device ? c : sid;
+    }
     // ---- personalization entries of the wave: (row, column, weight)
     std::map<std::pair<int32_t, int32_t>, double> ent;
     for (int c = 0; c < kCols; ++c)
       cols_h[c] = ColState{0, 0.0, c < ncols ? 0 : 1, 0, 0, 0,
-                           r1_max && c < ncols ? r1_max[set0 + c] : (double)INFINITY};
+                           r1_max && c < ncols ? r1_max[order[set0 + c]] : (double)INFINITY};
     double wmax = 1.0;
     for (int c = 0; c < ncols; ++c) {
-      const int64_t a0 = seed_ptr[set0 + c], a1 = seed_ptr[set0 + c + 1];
+      const int64_t a0 = seed_ptr[order[set0 + c]], a1 = seed_ptr[order[set0 + c] + 1];
       if (a1 == a0) { cols_h[c].uniform = 1; continue; }  // sum <= 0: uniform (src/ppr.rs:108)
       const double inv = 1.0 / (double)(a1 - a0);
       for (int64_t k = a0; k < a1; ++k) ent[{b->inv_perm[(size_t)seed_idx[k]], c}] += inv;
@@ -795,10 +812,11 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     p.x0 = nullptr;
     if (x0) {
       if (x0_on_device) {
-        p.x0 = x0 + set0 * n;
+        p.x0 = x0;
       } else {
-        GOPS_CUDA_TRY(cudaMemcpyAsync(b->x0, x0 + set0 * n, sizeof(float) * (size_t)ncols * n,
-                                      cudaMemcpyHostToDevice, st));
+        for (int c = 0; c < ncols; ++c)
+          GOPS_CUDA_TRY(cudaMemcpyAsync(b->x0 + (size_t)c * n, x0 + order[set0 + c] * n, sizeof(float) * (size_t)n,
+                                        cudaMemcpyHostToDevice, st));
         ctx->stats.h2d_bytes += sizeof(float) * (size_t)ncols * n;
         p.x0 = b->x0;
       }
@@ -806,7 +824,6 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       // sum far below 2^63; larger or non-finite starts are flagged by the
       // nonfinite counter and the column does not converge
       wmax = 8.0;
-      p.x0 = x0_on_device ? x0 : p.x0;
     }
     int e = 0;
     while (e < 20 && std::ldexp(1.0, e) < wmax) ++e;
@@ -822,8 +839,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     p.gf_in = b->gf[1];
     p.gdf_out = b->gdf[0];
     p.gf_out = b->gf[0];
-    const int64_t set_base = x0 && x0_on_device ? set0 : 0;
-    batch_init<<<grid_rows, kBThreads, 0, st>>>(p, set_base);
+    batch_init<<<grid_rows, kBThreads, 0, st>>>(p);
     GOPS_CUDA_TRY(cudaGetLastError());
     ++launches;
     // ---- steps
@@ -878,14 +894,15 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       if (k - 1 > cfg->max_iterations) return Status{GOPS_ERR_INTERNAL, "wave did not finish"};
     }
     // ---- results of the wave
-    p.out = scores_on_device ? scores + set0 * n : b->out;
+    p.out = scores_on_device ? scores : b->out;
     if (scores) {
       batch_finalize<<<grid_rows, kBThreads, 0, st>>>(p);
       GOPS_CUDA_TRY(cudaGetLastError());
       ++launches;
       if (!scores_on_device) {
-        GOPS_CUDA_TRY(cudaMemcpyAsync(scores + set0 * n, b->out, sizeof(float) * (size_t)ncols * n,
-                                      cudaMemcpyDeviceToHost, st));
+        for (int c = 0; c < ncols; ++c)
+          GOPS_CUDA_TRY(cudaMemcpyAsync(scores + order[set0 + c] * n, b->out + (size_t)c * n, sizeof(float) * (size_t)n,
+                                        cudaMemcpyDeviceToHost, st));
         ctx->stats.d2h_bytes += sizeof(float) * (size_t)ncols * n;
       }
     }
@@ -893,8 +910,8 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     GOPS_CUDA_TRY(cudaStreamSynchronize(st));
     for (int c = 0; c < ncols; ++c) {
       col_iters += cols_h[c].iterations;
-      if (runs) runs[set0 + c] = gops_run{cols_h[c].iterations, cols_h[c].diff_l1, cols_h[c].converged, 0};
-      if (rejected) rejected[set0 + c] = cols_h[c].rejected;
+      if (runs) runs[order[set0 + c]] = gops_run{cols_h[c].iterations, cols_h[c].diff_l1, cols_h[c].converged, 0};
+      if (rejected) rejected[order[set0 + c]] = cols_h[c].rejected;
     }
   }
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[3], st));

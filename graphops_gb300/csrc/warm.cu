@@ -30,9 +30,9 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-constexpr int kPushThreads = 256;
+constexpr int kPushThreads = 512;
 constexpr int kMaxSeeds = 1024;  // distinct seeds of a set handled by the push
-constexpr int kMaxL1 = 4096;     // out-edges of a set's seeds handled by the push
+constexpr int kMaxL1 = 2048;     // out-edges of a set's seeds handled by the push
 constexpr float kFixF = 1099511627776.0f;  // 2^40 (kWFix)
 constexpr double kCentFix = 1073741824.0;  // 2^30: fixed point of the k-means sums
 
@@ -69,18 +69,63 @@ __global__ void offsets_from_sorted(const uint32_t *keys, int64_t m, int64_t n, 
   }
 }
 
-__global__ void degree_terms(const int64_t *out_rp, const int32_t *out_col, const int64_t *in_rp, int64_t n,
-                             float *inv_out, float *inv_in, int64_t *s2) {
+__global__ void degree_terms(const int64_t *out_rp, const int64_t *in_rp, int64_t n, float *inv_out, float *inv_in) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t dout = out_rp[i + 1] - out_rp[i], din = in_rp[i + 1] - in_rp[i];
     inv_out[i] = dout > 0 ? 1.0f / (float)dout : 0.0f;
     inv_in[i] = din > 0 ? 1.0f / (float)din : 0.0f;
-    int64_t t = 0;
-    for (int64_t e = out_rp[i]; e < out_rp[i + 1]; ++e) {
-      const int64_t x = out_col[e];
-      t += out_rp[x + 1] - out_rp[x];
+  }
+}
+
+// Cluster distributions of out-neighbourhoods as sparse runs:
+//   LEVEL 1: h(w)[c]  = #{x in out(w): a_x = c} / deg(w)
+//   LEVEL 2: h2(w)[c] = sum over x in out(w) of h(x)[c] / deg(w)
+// A warp per node sums its bins in a warp-private fixed-point histogram
+// (order-independent); the count pass writes the number of nonzero bins,
+// the fill pass writes them in cluster order at rp[w].
+template <int LEVEL>
+__global__ void runs_kernel(const int64_t *out_rp, const int32_t *out_col, const float *inv_out,
+                            const int32_t *cluster, const int64_t *hrp, const int32_t *hcl, const float *hwt,
+                            int64_t n, int r, int64_t *rp, int32_t *ocl, float *owt, int fill) {
+  extern __shared__ __align__(16) long long hsm[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  long long *h = hsm + (int64_t)wid * r;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid; w < n; w += nw) {
+    for (int c = lane; c < r; c += 32) h[c] = 0;
+    __syncwarp();
+    const float iw = inv_out[w];
+    for (int64_t e = out_rp[w] + lane; e < out_rp[w + 1]; e += 32) {
+      const int32_t x = out_col[e];
+      if (LEVEL == 1) {
+        atomicAdd(reinterpret_cast<unsigned long long *>(&h[cluster[x]]), (unsigned long long)fx40(iw));
+      } else {
+        for (int64_t q = hrp[x]; q < hrp[x + 1]; ++q)
+          atomicAdd(reinterpret_cast<unsigned long long *>(&h[hcl[q]]), (unsigned long long)fx40(hwt[q] * iw));
+      }
     }
-    s2[i] = t;
+    __syncwarp();
+    if (!fill) {
+      int cnt = 0;
+      for (int c = lane; c < r; c += 32) cnt += h[c] != 0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+      if (lane == 0) rp[w] = cnt;
+    } else {
+      int64_t base = rp[w];
+      for (int c0 = 0; c0 < r; c0 += 32) {
+        const int c = c0 + lane;
+        const bool nz = c < r && h[c] != 0;
+        const unsigned mask = __ballot_sync(0xffffffffu, nz);
+        if (nz) {
+          const int64_t pos = base + __popc(mask & ((1u << lane) - 1u));
+          ocl[pos] = c;
+          owt[pos] = (float)((double)h[c] / kWFix);
+        }
+        base += __popc(mask);
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -185,6 +230,53 @@ __global__ void pack_y(const float *code, const float *acode, int64_t n, float *
   }
 }
 
+// t3[u][:] = sum over v in out(u) of h2(v)[:] / deg(u): a warp per node,
+// fixed-point sums in a warp-private histogram, written as a dense row
+__global__ void table_from_runs(const int64_t *out_rp, const int32_t *out_col, const float *inv_out,
+                                const int64_t *hrp, const int32_t *hcl, const float *hwt, int64_t n, int r,
+                                float *T) {
+  extern __shared__ __align__(16) long long tsm[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  long long *h = tsm + (int64_t)wid * r;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid; u < n; u += nw) {
+    for (int c = lane; c < r; c += 32) h[c] = 0;
+    __syncwarp();
+    const float iu = inv_out[u];
+    for (int64_t e = out_rp[u] + lane; e < out_rp[u + 1]; e += 32) {
+      const int32_t v = out_col[e];
+      for (int64_t q = hrp[v]; q < hrp[v + 1]; ++q)
+        atomicAdd(reinterpret_cast<unsigned long long *>(&h[hcl[q]]), (unsigned long long)fx40(hwt[q] * iu));
+    }
+    __syncwarp();
+    for (int c = lane; c < r; c += 32) T[u * r + c] = (float)((double)h[c] / kWFix);
+    __syncwarp();
+  }
+}
+
+// t4[u][:] = sum over v in out(u) of t3[v][:] / deg(u): a warp per node,
+// lanes over bins, out-edges in order
+__global__ void table_next(const int64_t *out_rp, const int32_t *out_col, const float *inv_out, const float *T3,
+                           int64_t n, int r, float *T4) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n; u += nw) {
+    float acc[kWMaxClusters / 32];
+#pragma unroll
+    for (int k = 0; k < kWMaxClusters / 32; ++k) acc[k] = 0.f;
+    for (int64_t e = out_rp[u]; e < out_rp[u + 1]; ++e) {
+      const int64_t v = out_col[e];
+#pragma unroll
+      for (int k = 0; k < kWMaxClusters / 32; ++k)
+        if (lane + 32 * k < r) acc[k] += T3[v * r + lane + 32 * k];
+    }
+    const float iu = inv_out[u];
+#pragma unroll
+    for (int k = 0; k < kWMaxClusters / 32; ++k)
+      if (lane + 32 * k < r) T4[u * r + lane + 32 * k] = acc[k] * iu;
+  }
+}
+
 // ---- k-means (k-means++ seeding, Arthur & Vassilvitskii 2007; Lloyd iterations)
 __global__ void kmpp_dist(const float *y, int64_t n, const float *c, int first, float *d2) {
   __shared__ float cs[kWY];
@@ -284,7 +376,7 @@ struct PushArgs {
   const int64_t *out_rp;
   const int32_t *out_col;
   const float *inv_out;
-  const int64_t *s2;
+  const float *t3, *t4;  // per-node cluster distributions of P^3 e_u and P^4 e_u
   const int32_t *cluster;
   const int64_t *sptr;  // set offsets into sidx (device)
   const int32_t *sidx;
@@ -355,15 +447,16 @@ struct PushSmem {
   long long f1s[kMaxSeeds];      // (P s) at each seed, fixed point
   int64_t pre0[kMaxSeeds];       // inclusive prefix of seed out-degrees
   int32_t l1node[kMaxL1];        // level-1 items (out-edges of the seeds)
-  float l1a[kMaxL1];             //   and their mass
+  float l1a[kMaxL1];             //   their mass
+  float l1iv[kMaxL1];            //   1 / out-degree of the item's node
+  int64_t l1rp[kMaxL1];          //   first out-edge of the item's node
   int64_t pre1[kMaxL1];          // inclusive prefix of level-1 out-degrees
-  long long hist[2 * kWMaxClusters];
   long long mass[4];
   int64_t tmp[kPushThreads + 1];
   int nseeds, over;
 };
 
-__global__ void __launch_bounds__(kPushThreads) push_kernel(PushArgs p) {
+__global__ void __launch_bounds__(kPushThreads, 2) push_kernel(PushArgs p) {
   extern __shared__ __align__(16) unsigned char smraw[];
   PushSmem &S = *reinterpret_cast<PushSmem *>(smraw);
   const int64_t set = blockIdx.x;
@@ -376,7 +469,6 @@ __global__ void __launch_bounds__(kPushThreads) push_kernel(PushArgs p) {
     S.over = L == 0 ? 2 : 0;  // 2: empty set (uniform personalization)
     S.nseeds = 0;
   }
-  for (int i = threadIdx.x; i < 2 * p.r; i += blockDim.x) S.hist[i] = 0;
   if (threadIdx.x < 4) S.mass[threadIdx.x] = 0;
   __syncthreads();
   // distinct sorted seeds with counts (a single thread: at most kMaxSeeds)
@@ -429,10 +521,13 @@ __global__ void __launch_bounds__(kPushThreads) push_kernel(PushArgs p) {
       const int i = upper_bound_i64(S.pre0, ns, t);
       const int32_t u = S.seeds[i];
       const int64_t first = i == 0 ? 0 : S.pre0[i - 1];
-      const int32_t v = p.out_col[p.out_rp[u] + (t - first)];
+      const int32_t v = __ldg(&p.out_col[__ldg(&p.out_rp[u]) + (t - first)]);
+      const int64_t rb = __ldg(&p.out_rp[v]), re = __ldg(&p.out_rp[v + 1]);
       S.l1node[t] = v;
-      S.l1a[t] = (ws * (float)S.scount[i]) * p.inv_out[u];
-      S.pre1[t] = p.out_rp[v + 1] - p.out_rp[v];
+      S.l1a[t] = (ws * (float)S.scount[i]) * __ldg(&p.inv_out[u]);
+      S.l1iv[t] = __ldg(&p.inv_out[v]);
+      S.l1rp[t] = rb;
+      S.pre1[t] = re - rb;
     }
   __syncthreads();
   int64_t L2 = 0;
@@ -444,10 +539,9 @@ __global__ void __launch_bounds__(kPushThreads) push_kernel(PushArgs p) {
     int64_t work = 0;
     for (int64_t t = threadIdx.x; t < L2; t += blockDim.x) {
       const int i = upper_bound_i64(S.pre1, (int)L1, t);
-      const int32_t v = S.l1node[i];
       const int64_t first = i == 0 ? 0 : S.pre1[i - 1];
-      const int32_t w = p.out_col[p.out_rp[v] + (t - first)];
-      work += (p.out_rp[w + 1] - p.out_rp[w]) + p.s2[w];
+      const int32_t w = __ldg(&p.out_col[S.l1rp[i] + (t - first)]);
+      work += __ldg(&p.out_rp[w + 1]) - __ldg(&p.out_rp[w]);
     }
     S.tmp[threadIdx.x] = work;
     __syncthreads();
@@ -489,34 +583,50 @@ __global__ void __launch_bounds__(kPushThreads) push_kernel(PushArgs p) {
     const int si = find_sorted(S.seeds, ns, v);
     if (si >= 0) atomicAdd(reinterpret_cast<unsigned long long *>(&S.f1s[si]), (unsigned long long)fx40(a));
   }
-  // hops 2 and 3, and the cluster mixes of P^3 s and P^4 s
-  long long *h3 = S.hist, *h4 = S.hist + p.r;
+  // hops 2 and 3; each item's loads are issued together (one dependent round
+  // trip for w, one for its range, then its out-edges four at a time)
+  long long m3 = 0;
   for (int64_t t = threadIdx.x; t < L2; t += blockDim.x) {
     const int i = upper_bound_i64(S.pre1, (int)L1, t);
-    const int32_t v = S.l1node[i];
     const int64_t first = i == 0 ? 0 : S.pre1[i - 1];
-    const int32_t w = p.out_col[p.out_rp[v] + (t - first)];
-    const float a2 = S.l1a[i] * p.inv_out[v];
+    const int32_t w = __ldg(&p.out_col[S.l1rp[i] + (t - first)]);
+    const float a2 = S.l1a[i] * S.l1iv[i];
+    const float iw = __ldg(&p.inv_out[w]);
+    const int64_t eb = __ldg(&p.out_rp[w]), ee = __ldg(&p.out_rp[w + 1]);
     atomicAdd(reinterpret_cast<unsigned long long *>(&loc[w]), (unsigned long long)fx40(c2 * a2));
-    const float iw = p.inv_out[w];
     if (iw == 0.f) continue;
-    atomicAdd(reinterpret_cast<unsigned long long *>(&S.mass[3]), (unsigned long long)fx40(a2));
-    const float a3 = a2 * iw;
-    const long long a3f = fx40(a3);
-    for (int64_t e = p.out_rp[w]; e < p.out_rp[w + 1]; ++e) {
-      const int32_t x = p.out_col[e];
-      atomicAdd(reinterpret_cast<unsigned long long *>(&loc[x]), (unsigned long long)fx40(c3 * a3));
-      atomicAdd(reinterpret_cast<unsigned long long *>(&h3[p.cluster[x]]), (unsigned long long)a3f);
-      const float ix = p.inv_out[x];
-      if (ix == 0.f) continue;
-      const long long a4f = fx40(a3 * ix);
-      for (int64_t e2 = p.out_rp[x]; e2 < p.out_rp[x + 1]; ++e2)
-        atomicAdd(reinterpret_cast<unsigned long long *>(&h4[p.cluster[p.out_col[e2]]]), (unsigned long long)a4f);
+    m3 += fx40(a2);
+    const unsigned long long a3c = (unsigned long long)fx40(c3 * (a2 * iw));
+    int64_t e = eb;
+    for (; e + 4 <= ee; e += 4) {
+      const int32_t x0 = __ldg(&p.out_col[e]), x1 = __ldg(&p.out_col[e + 1]);
+      const int32_t x2 = __ldg(&p.out_col[e + 2]), x3 = __ldg(&p.out_col[e + 3]);
+      atomicAdd(reinterpret_cast<unsigned long long *>(&loc[x0]), a3c);
+      atomicAdd(reinterpret_cast<unsigned long long *>(&loc[x1]), a3c);
+      atomicAdd(reinterpret_cast<unsigned long long *>(&loc[x2]), a3c);
+      atomicAdd(reinterpret_cast<unsigned long long *>(&loc[x3]), a3c);
     }
+    for (; e < ee; ++e) atomicAdd(reinterpret_cast<unsigned long long *>(&loc[__ldg(&p.out_col[e])]), a3c);
+  }
+  S.tmp[threadIdx.x] = m3;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long t3 = 0;
+    for (int q = 0; q < kPushThreads; ++q) t3 += S.tmp[q];
+    S.mass[3] = t3;
   }
   __syncthreads();
+  // cluster mixes of P^3 s and P^4 s: the seeds' rows of t3 and t4 weighted
+  // by their share of s (linear in s), summed in seed order
   const int F = 2 * p.r + 1;
-  for (int i = threadIdx.x; i < 2 * p.r; i += blockDim.x) p.mix[set * F + i] = (double)S.hist[i] / kWFix;
+  for (int i = threadIdx.x; i < 2 * p.r; i += blockDim.x) {
+    const float *T = i < p.r ? p.t3 : p.t4;
+    const int c = i < p.r ? i : i - p.r;
+    double acc = 0.0;
+    for (int k = 0; k < ns; ++k)
+      acc += (double)(ws * (float)S.scount[k]) * (double)__ldg(&T[(int64_t)S.seeds[k] * p.r + c]);
+    p.mix[set * F + i] = acc;
+  }
   if (threadIdx.x == 0) {
     p.mix[set * F + 2 * p.r] = 1.0;
     // mass[1..3]: non-dangling mass of hops 0..2 = total mass of hops 1..3
@@ -558,29 +668,36 @@ __global__ void coef_kernel(const double *mix, const float *K, const float *cw, 
   }
 }
 
-// x0[j][i] = local + w_i coef[j][a_i]; clears the push scratch
+// x0[j][i] = local + w_i coef[j][a_i].  A thread per node walks the sets, so
+// each access is coalesced across the warp and the node's weight and cluster
+// are read once.  (The caller clears the push scratch afterwards with one
+// memset: clearing it here, line by line after the read, was several times
+// slower than the whole pass.)
 __global__ void compose_kernel(long long *push, const float *w, const int32_t *cluster, const float *coef,
                                const int32_t *over, int64_t n, int r, int64_t nsets, float *x0) {
-  const int64_t total = n * nsets;
   const float inv_n = 1.0f / (float)n;
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = q / n, i = q - j * n;
-    const long long f = push[q];
-    push[q] = 0;
-    float v = (float)((double)f / kWFix);
-    if (over[j] == 2) v = inv_n;
-    else v += w[i] * coef[j * r + cluster[i]];
-    x0[q] = v;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float wi = w[i];
+    const int c = cluster[i];
+    for (int64_t j = 0; j < nsets; ++j) {
+      const int64_t q = j * n + i;
+      const long long f = __ldcs(&push[q]);
+      float v = (float)((double)f / kWFix);
+      const int o = over[j];
+      if (o == 2) v = inv_n;
+      else if (o == 0) v += wi * __ldg(&coef[j * r + c]);
+      __stcs(&x0[q], v);
+    }
   }
 }
 
-// t[j][i] = x*[j][i] - local (in place); clears the push scratch
-__global__ void tail_targets(long long *push, int64_t total, float *t) {
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
-    const long long f = push[q];
-    push[q] = 0;
-    t[q] -= (float)((double)f / kWFix);
-  }
+// t[j][i] = x*[j][i] - local (in place); the caller clears the push scratch
+__global__ void tail_targets(const long long *push, int64_t n, int64_t nsets, float *t) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t j = 0; j < nsets; ++j) {
+      const int64_t q = j * n + i;
+      t[q] -= (float)((double)__ldcs(&push[q]) / kWFix);
+    }
 }
 
 // ymass[j][c] = sum over the members of cluster c of t[j][i] (warp per (j, c), member order)
@@ -743,7 +860,7 @@ double wall_ms() {
 WarmModel::~WarmModel() {
   void *ptrs[] = {out_rp, out_col, in_rp, in_col, inv_out, inv_in, code, x1, cluster, members, cl_off,
                   params, adam_m, adam_v, w1t, w2t, w2, coupling, h1, a1, h2, g2, gx, w, du, cw, grad, part,
-                  push, mix, tmass, r1c, over, coef, d_sptr, d_sidx, s2, targets, gsign, csum, ymass, gram,
+                  push, mix, tmass, r1c, over, coef, d_sptr, d_sidx, t3, t4, targets, gsign, csum, ymass, gram,
                   rhs, chol, lpart, x0};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -912,6 +1029,60 @@ Status build_members(WarmModel &w) {
   return Status::ok();
 }
 
+// the tables t3 and t4: sparse runs of the 1- and 2-step cluster
+// distributions h and h2 (count, scan, fill per level), then t3 from h2 and
+// t4 from t3; the runs are freed afterwards
+Status build_tables(WarmModel &w) {
+  cudaStream_t s = w.ctx->stream;
+  const int64_t n = w.n;
+  const size_t smem = sizeof(long long) * 8 * w.r;
+  const int grid = blocks_for(n, 8, w.ctx->num_sms * 32);
+  int64_t *rp[2] = {nullptr, nullptr};
+  int32_t *cl[2] = {nullptr, nullptr};
+  float *wt[2] = {nullptr, nullptr};
+  struct Guard {
+    int64_t **rp;
+    int32_t **cl;
+    float **wt;
+    ~Guard() {
+      for (int l = 0; l < 2; ++l) {
+        cudaFree(rp[l]);
+        cudaFree(cl[l]);
+        cudaFree(wt[l]);
+      }
+    }
+  } guard{rp, cl, wt};
+  for (int level = 1; level <= 2; ++level) {
+    const int L = level - 1;
+    GOPS_CUDA_TRY(cudaMalloc(&rp[L], sizeof(int64_t) * (n + 1)));
+    GOPS_CUDA_TRY(cudaMemsetAsync(rp[L] + n, 0, sizeof(int64_t), s));
+    for (int fill = 0; fill < 2; ++fill) {
+      if (fill) {
+        GOPS_TRY(exclusive_scan_i64(rp[L], rp[L], n + 1, s));
+        int64_t total = 0;
+        GOPS_CUDA_TRY(cudaMemcpyAsync(&total, rp[L] + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+        GOPS_CUDA_TRY(cudaMalloc(&cl[L], sizeof(int32_t) * std::max<int64_t>(total, 1)));
+        GOPS_CUDA_TRY(cudaMalloc(&wt[L], sizeof(float) * std::max<int64_t>(total, 1)));
+      }
+      if (level == 1)
+        runs_kernel<1><<<grid, 256, smem, s>>>(w.out_rp, w.out_col, w.inv_out, w.cluster, nullptr, nullptr, nullptr,
+                                               n, w.r, rp[0], cl[0], wt[0], fill);
+      else
+        runs_kernel<2><<<grid, 256, smem, s>>>(w.out_rp, w.out_col, w.inv_out, w.cluster, rp[0], cl[0], wt[0], n,
+                                               w.r, rp[1], cl[1], wt[1], fill);
+      GOPS_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  GOPS_CUDA_TRY(cudaMalloc(&w.t3, sizeof(float) * n * w.r));
+  GOPS_CUDA_TRY(cudaMalloc(&w.t4, sizeof(float) * n * w.r));
+  table_from_runs<<<grid, 256, smem, s>>>(w.out_rp, w.out_col, w.inv_out, rp[1], cl[1], wt[1], n, w.r, w.t3);
+  table_next<<<grid, 256, 0, s>>>(w.out_rp, w.out_col, w.inv_out, w.t3, n, w.r, w.t4);
+  GOPS_CUDA_TRY(cudaGetLastError());
+  GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+  return Status::ok();
+}
+
 Status ensure_sets(WarmModel &w, int64_t sets) {
   if (sets <= w.set_cap) return Status::ok();
   cudaFree(w.mix); cudaFree(w.tmass); cudaFree(w.r1c); cudaFree(w.over); cudaFree(w.coef); cudaFree(w.ymass);
@@ -968,7 +1139,7 @@ Status upload_sets(WarmModel &w, const int64_t *sptr, const int32_t *sidx, int64
 }
 
 Status run_push(WarmModel &w, double damping, int64_t cnt) {
-  PushArgs a{w.out_rp, w.out_col, w.inv_out, w.s2, w.cluster, w.d_sptr, w.d_sidx, w.n, w.r, (float)damping,
+  PushArgs a{w.out_rp, w.out_col, w.inv_out, w.t3, w.t4, w.cluster, w.d_sptr, w.d_sidx, w.n, w.r, (float)damping,
              w.cfg.push_budget, w.push, w.mix, w.tmass, w.r1c, w.over};
   static bool attr = false;
   if (!attr) {
@@ -1047,6 +1218,7 @@ Status loss_grad(WarmModel &w, const float *tails, int64_t s0, int B, double *lo
 Status warm_create(Ctx *ctx, const Graph *g, const int64_t *row_ptr, const int32_t *col, const gops_warm_config *cfg,
                    WarmModel &w) {
   w.ctx = ctx;
+  w.device = ctx->device;
   w.graph = g;
   w.cfg = *cfg;
   w.n = g->n;
@@ -1070,7 +1242,6 @@ Status warm_create(Ctx *ctx, const Graph *g, const int64_t *row_ptr, const int32
   GOPS_CUDA_TRY(cudaMalloc(&w.in_col, sizeof(int32_t) * std::max<int64_t>(m, 1)));
   GOPS_CUDA_TRY(cudaMalloc(&w.inv_out, sizeof(float) * n));
   GOPS_CUDA_TRY(cudaMalloc(&w.inv_in, sizeof(float) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&w.s2, sizeof(int64_t) * n));
   GOPS_CUDA_TRY(cudaMalloc(&w.code, sizeof(float) * n * kWCode));
   GOPS_CUDA_TRY(cudaMalloc(&w.x1, sizeof(bf16) * n * kWIn));
   GOPS_CUDA_TRY(cudaMalloc(&w.cluster, sizeof(int32_t) * n));
@@ -1105,7 +1276,7 @@ Status warm_create(Ctx *ctx, const Graph *g, const int64_t *row_ptr, const int32
     GOPS_TRY(st);
     GOPS_CUDA_TRY(cudaGetLastError());
   }
-  degree_terms<<<blocks_for(n, 256, 8192), 256, 0, s>>>(w.out_rp, w.out_col, w.in_rp, n, w.inv_out, w.inv_in, w.s2);
+  degree_terms<<<blocks_for(n, 256, 8192), 256, 0, s>>>(w.out_rp, w.in_rp, n, w.inv_out, w.inv_in);
   GOPS_CUDA_TRY(cudaGetLastError());
   // random-projection code: Gaussian columns diffused over the graph
   float *tmp = nullptr;
@@ -1143,6 +1314,7 @@ Status warm_create(Ctx *ctx, const Graph *g, const int64_t *row_ptr, const int32
   }
   GOPS_TRY(kmeans(w, tmp));
   GOPS_TRY(build_members(w));
+  GOPS_TRY(build_tables(w));
   GOPS_TRY(nn_alloc(w));
   GOPS_TRY(nn_init_params(w));
   GOPS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1174,7 +1346,8 @@ Status warm_train(WarmModel &w, const gops_config *cfg, int64_t nsets, const int
       // exact part, tails, cluster masses, normal equations
       GOPS_TRY(upload_sets(w, seed_ptr, seed_idx, c0, cnt));
       GOPS_TRY(run_push(w, cfg->damping, cnt));
-      tail_targets<<<blocks_for(cnt * w.n, 256, 16384), 256, 0, s>>>(w.push, cnt * w.n, w.targets);
+      tail_targets<<<blocks_for(w.n, 256, w.ctx->num_sms * 8), 256, 0, s>>>(w.push, w.n, cnt, w.targets);
+      GOPS_CUDA_TRY(cudaMemsetAsync(w.push, 0, sizeof(long long) * cnt * w.n, s));
       if (ep == 0) {
         cluster_mass<<<blocks_for(cnt * w.r, 8, 8192), 256, 0, s>>>(w.targets, w.members, w.cl_off, w.r, w.n, cnt,
                                                                      w.ymass);
@@ -1231,9 +1404,10 @@ Status warm_predict(WarmModel &w, double damping, int64_t nsets, const int64_t *
     GOPS_TRY(upload_sets(w, seed_ptr, seed_idx, c0, cnt));
     GOPS_TRY(run_push(w, damping, cnt));
     GOPS_TRY(run_coef(w, 0, cnt));
-    compose_kernel<<<blocks_for(cnt * w.n, 256, 16384), 256, 0, s>>>(w.push, w.w, w.cluster, w.coef, w.over, w.n, w.r,
-                                                                     cnt, x0 + c0 * w.n);
+    compose_kernel<<<blocks_for(w.n, 256, w.ctx->num_sms * 8), 256, 0, s>>>(w.push, w.w, w.cluster, w.coef, w.over,
+                                                                             w.n, w.r, cnt, x0 + c0 * w.n);
     GOPS_CUDA_TRY(cudaGetLastError());
+    GOPS_CUDA_TRY(cudaMemsetAsync(w.push, 0, sizeof(long long) * cnt * w.n, s));
     if (r1_cold) {
       GOPS_CUDA_TRY(cudaMemcpyAsync(r1_cold + c0, w.r1c, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s));
       GOPS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1335,7 +1509,8 @@ Status warm_loss_grad(WarmModel &w, double damping, int64_t nsets, const int64_t
   GOPS_CUDA_TRY(cudaMemcpyAsync(w.targets, targets_x, sizeof(float) * nsets * w.n, cudaMemcpyHostToDevice, s));
   GOPS_TRY(upload_sets(w, seed_ptr, seed_idx, 0, nsets));
   GOPS_TRY(run_push(w, damping, nsets));
-  tail_targets<<<blocks_for(nsets * w.n, 256, 16384), 256, 0, s>>>(w.push, nsets * w.n, w.targets);
+  tail_targets<<<blocks_for(w.n, 256, w.ctx->num_sms * 8), 256, 0, s>>>(w.push, w.n, nsets, w.targets);
+  GOPS_CUDA_TRY(cudaMemsetAsync(w.push, 0, sizeof(long long) * nsets * w.n, s));
   GOPS_TRY(nn_forward(w));
   GOPS_TRY(run_coef(w, 0, nsets));
   GOPS_TRY(loss_grad(w, w.targets, 0, (int)nsets, loss));
@@ -1454,8 +1629,9 @@ int gops_warm_create(gops_ctx *ctx, const gops_graph *g, const int64_t *row_ptr,
 
 void gops_warm_destroy(gops_warm *w) {
   if (!w) return;
-  cudaSetDevice(w->impl.ctx->device);
-  cudaStreamSynchronize(w->impl.ctx->stream);
+  // the context may already be gone: use the device recorded at creation
+  // (cudaFree waits for the device's pending work before it frees)
+  cudaSetDevice(w->impl.device);
   delete w;
 }
 

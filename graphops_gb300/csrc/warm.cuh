@@ -28,7 +28,8 @@ constexpr int kPB3 = kPW3 + kWH;              // b3 [1]
 constexpr int kPCount = kPB3 + 1;
 
 struct WarmModel {
-  Ctx *ctx = nullptr;
+  Ctx *ctx = nullptr;  // the creating context (not dereferenced on destroy)
+  int device = 0;
   const Graph *graph = nullptr;
   gops_warm_config cfg{};
   int64_t n = 0, m = 0;
@@ -77,7 +78,9 @@ struct WarmModel {
   int64_t *d_sptr = nullptr;       // seed sets of the current call
   int32_t *d_sidx = nullptr;
   int64_t sidx_cap = 0, sptr_cap = 0;
-  int64_t *s2 = nullptr;           // n: sum of the out-degrees of each node's out-neighbours
+  // cluster distributions of the 3- and 4-step walks from each node:
+  // t3[u][c] = (H^T P^3 e_u)[c], t4[u][c] = (H^T P^4 e_u)[c]  (n x r each)
+  float *t3 = nullptr, *t4 = nullptr;
   // training
   float *targets = nullptr;        // targets_cap x n: PPR vectors, then their tails
   int64_t targets_cap = 0;

@@ -14,8 +14,10 @@
  *  - All host buffers are owned by the caller; the library copies inputs in
  *    and writes results into caller-allocated outputs.  No pointer passed in
  *    is retained after the call returns.
- *  - Device memory is owned by gops_ctx / gops_graph objects and released by
- *    their destroy functions.
+ *  - Device memory is owned by gops_ctx / gops_graph / gops_warm objects and
+ *    released by their destroy functions, which may run in any order (a
+ *    graph or model may outlive the context that created it, for destruction
+ *    only).
  *  - A context is used by one host thread at a time (one context per thread,
  *    or external locking).  Different contexts may run concurrently.
  *  - Results are deterministic: the same inputs and configuration give

@@ -248,8 +248,11 @@ def test_budget_exceeded_starts_cold(small):
     conf = go.PageRankConfig(0.85, 1000, 1e-7)
     lr = w0.ppr_batch(conf, sp, si)
     cold = go.ppr_batch(dg, conf, sp, si)
-    # x0 = s (the uniform vector for the empty set): the cold iteration, up
-    # to the FP32 rounding of the start and the fixed-point scale of its sums
+    # x0 = s (the uniform vector for the empty set): the cold iteration's
+    # steps and, within the batched path's bound, its FP64 iterates (a caller
+    # start enters the FP32 phase at a larger residual than a cold one)
     assert np.array_equal(lr.iterations, cold.iterations)
-    assert np.abs(lr.scores.astype(np.float64) - cold.scores).sum(1).max() <= 1e-8
+    ref, its = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-7, threads=8)
+    assert np.array_equal(lr.iterations, its.astype(np.int64))
+    assert np.abs(lr.scores.astype(np.float64) - ref).sum(1).max() <= 1e-7
     assert not lr.rejected.any()

@@ -64,7 +64,7 @@ def build_gops(force: bool = False, verbose: bool = False, extra: list | None = 
             if verbose and out.strip():
                 print(out)
     if force or jobs or not os.path.exists(LIBGOPS) or os.path.getmtime(LIBGOPS) < _newest(objs):
-        _run([nvcc, *ARCH, "-shared", "-o", LIBGOPS, *objs, "-lcuda"])
+        _run([nvcc, *ARCH, "-shared", "-o", LIBGOPS, *objs, "-lcuda", "-lpthread"])
     return LIBGOPS
 
 

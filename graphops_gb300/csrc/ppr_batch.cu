@@ -1,3 +1,5 @@
+#include <cstring>
+#include <thread>
 // Batched personalized PageRank (K5): many seed sets per pass over the graph.
 //
 // Each seed set is one independent personalized_pagerank_run of the
@@ -104,6 +106,7 @@ struct BatchState {
   int64_t pcap = 0;
   float *x0 = nullptr;        // warm-start vectors of the wave (set-major, original order)
   float *out = nullptr;       // results of the wave (set-major, original order)
+  float *hstage[2] = {nullptr, nullptr};  // pinned host copies of two waves' results
   std::vector<int32_t> inv_perm;  // host: original id -> relabelled row
 };
 
@@ -115,6 +118,8 @@ void batch_free(Graph &g) {
   cudaFree(b->acc); cudaFree(b->tail); cudaFree(b->lpart); cudaFree(b->lcnt);
   cudaFree(b->sums); cudaFree(b->cols); cudaFree(b->wave); cudaFree(b->prow);
   cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted); cudaFree(b->x0); cudaFree(b->out);
+  if (b->hstage[0]) cudaFreeHost(b->hstage[0]);
+  if (b->hstage[1]) cudaFreeHost(b->hstage[1]);
   delete b;
   g.batch = nullptr;
 }
@@ -761,6 +766,25 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   std::vector<ColState> cols_h(kCols);
   std::vector<int32_t> erow, eslot;
   std::vector<float2> eval;
+  // host results: each wave's block goes to a pinned buffer in one copy, and
+  // host threads scatter its columns to the sets' rows while the GPU runs
+  // the next wave (two buffers; a buffer's scatter is joined before reuse)
+  const size_t block_bytes = sizeof(float) * (size_t)kCols * (size_t)n;
+  const bool staged = scores && !scores_on_device && block_bytes <= (size_t(1) << 30);
+  if (staged && !b->hstage[0]) {
+    GOPS_CUDA_TRY(cudaMallocHost(&b->hstage[0], block_bytes));
+    GOPS_CUDA_TRY(cudaMallocHost(&b->hstage[1], block_bytes));
+  }
+  constexpr int kScatterThreads = 4;
+  struct Scatter {
+    std::vector<std::thread> t[2];
+    void join(int q) {
+      for (auto &x : t[q])
+        if (x.joinable()) x.join();
+      t[q].clear();
+    }
+    ~Scatter() { join(0); join(1); }
+  } scatter;
   // waves of sets of similar size: a set's step count falls with its size,
   // and a wave runs until its slowest column retires
   std::vector<int64_t> order(nsets);
@@ -899,7 +923,12 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       batch_finalize<<<grid_rows, kBThreads, 0, st>>>(p);
       GOPS_CUDA_TRY(cudaGetLastError());
       ++launches;
-      if (!scores_on_device) {
+      if (staged) {
+        scatter.join((int)((set0 / kCols) & 1));
+        GOPS_CUDA_TRY(cudaMemcpyAsync(b->hstage[(set0 / kCols) & 1], b->out, sizeof(float) * (size_t)ncols * n,
+                                      cudaMemcpyDeviceToHost, st));
+        ctx->stats.d2h_bytes += sizeof(float) * (size_t)ncols * n;
+      } else if (!scores_on_device) {
         for (int c = 0; c < ncols; ++c)
           GOPS_CUDA_TRY(cudaMemcpyAsync(scores + order[set0 + c] * n, b->out + (size_t)c * n, sizeof(float) * (size_t)n,
                                         cudaMemcpyDeviceToHost, st));
@@ -908,12 +937,24 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     }
     GOPS_CUDA_TRY(cudaMemcpyAsync(cols_h.data(), b->cols, sizeof(ColState) * kCols, cudaMemcpyDeviceToHost, st));
     GOPS_CUDA_TRY(cudaStreamSynchronize(st));
+    if (staged) {  // the block is in the pinned buffer: scatter it in the background
+      const int q = (int)((set0 / kCols) & 1);
+      const float *src = b->hstage[q];
+      const std::vector<int64_t> ids(order.begin() + set0, order.begin() + set0 + ncols);
+      for (int t = 0; t < kScatterThreads; ++t)
+        scatter.t[q].emplace_back([=]() {
+          for (int c = t; c < ncols; c += kScatterThreads)
+            std::memcpy(scores + ids[c] * n, src + (size_t)c * n, sizeof(float) * (size_t)n);
+        });
+    }
     for (int c = 0; c < ncols; ++c) {
       col_iters += cols_h[c].iterations;
       if (runs) runs[order[set0 + c]] = gops_run{cols_h[c].iterations, cols_h[c].diff_l1, cols_h[c].converged, 0};
       if (rejected) rejected[order[set0 + c]] = cols_h[c].rejected;
     }
   }
+  scatter.join(0);
+  scatter.join(1);
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[3], st));
   GOPS_CUDA_TRY(cudaEventSynchronize(ctx->ev[3]));
   float t_all = 0.f;

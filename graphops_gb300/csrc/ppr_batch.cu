@@ -107,6 +107,8 @@ struct BatchState {
   float *x0 = nullptr;        // warm-start vectors of the wave (set-major, original order)
   float *out = nullptr;       // results of the wave (set-major, original order)
   float *hstage[2] = {nullptr, nullptr};  // pinned host copies of two waves' results
+  WaveState *hwave = nullptr;             // pinned: two polled copies of the wave record
+  cudaEvent_t wev[2] = {nullptr, nullptr};
   std::vector<int32_t> inv_perm;  // host: original id -> relabelled row
 };
 
@@ -120,6 +122,9 @@ void batch_free(Graph &g) {
   cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted); cudaFree(b->x0); cudaFree(b->out);
   if (b->hstage[0]) cudaFreeHost(b->hstage[0]);
   if (b->hstage[1]) cudaFreeHost(b->hstage[1]);
+  if (b->hwave) cudaFreeHost(b->hwave);
+  for (cudaEvent_t e : b->wev)
+    if (e) cudaEventDestroy(e);
   delete b;
   g.batch = nullptr;
 }
@@ -644,6 +649,9 @@ Status batch_prepare(Ctx *ctx, Graph *g) {
   g->batch = b;
   const int64_t n = g->n;
   b->n = n;
+  GOPS_CUDA_TRY(cudaMallocHost(&b->hwave, 2 * sizeof(WaveState)));
+  GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->wev[0], cudaEventDisableTiming));
+  GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->wev[1], cudaEventDisableTiming));
   int64_t *tmp = nullptr;
   GOPS_CUDA_TRY(cudaMallocAsync((void **)&tmp, sizeof(int64_t) * 2, s));
   count_big<<<1, 1, 0, s>>>(g->in_rp, n, tmp);
@@ -866,11 +874,14 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     batch_init<<<grid_rows, kBThreads, 0, st>>>(p);
     GOPS_CUDA_TRY(cudaGetLastError());
     ++launches;
-    // ---- steps
+    // ---- steps: chunks of 4 launches; one chunk stays queued ahead of the
+    // host's poll of the wave record, so the GPU does not wait for the host
+    // between chunks (a step launched after the wave is done returns in its
+    // prologue)
     bool f32_known = false;
     unsigned long long k = 1;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evs;
-    for (;;) {
+    auto launch_chunk = [&]() -> Status {
       for (int j = 0; j < 4 && k - 1 <= cfg->max_iterations; ++j, ++k) {
         p.k = k;
         p.gdf_in = b->gdf[(k - 1) & 1];
@@ -897,10 +908,28 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
         }
       }
       GOPS_CUDA_TRY(cudaGetLastError());
-      WaveState ws{};
-      GOPS_CUDA_TRY(cudaMemcpyAsync(&ws, b->wave, sizeof(WaveState), cudaMemcpyDeviceToHost, st));
-      GOPS_CUDA_TRY(cudaStreamSynchronize(st));
+      return Status::ok();
+    };
+    auto poll_after = [&](int slot) -> Status {
+      GOPS_CUDA_TRY(cudaMemcpyAsync(&b->hwave[slot], b->wave, sizeof(WaveState), cudaMemcpyDeviceToHost, st));
+      GOPS_CUDA_TRY(cudaEventRecord(b->wev[slot], st));
+      return Status::ok();
+    };
+    int pending[2], npend = 0;
+    for (int q = 0; q < 2 && k - 1 <= cfg->max_iterations; ++q) {
+      GOPS_TRY(launch_chunk());
+      GOPS_TRY(poll_after(q));
+      pending[npend++] = q;
+    }
+    bool finished = false;
+    while (npend > 0) {
+      const int slot = pending[0];
+      pending[0] = pending[1];
+      --npend;
+      GOPS_CUDA_TRY(cudaEventSynchronize(b->wev[slot]));
+      const WaveState ws = b->hwave[slot];
       if (ws.done) {
+        GOPS_CUDA_TRY(cudaStreamSynchronize(st));
         // time the FP32-phase launches that did work (step >= f32_from and <= steps)
         for (size_t i = 0; i < evs.size(); ++i) {
           const unsigned long long kk = i + 2;  // F32 launches start at step 2
@@ -912,11 +941,17 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
           }
         }
         for (auto &pr : evs) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+        finished = true;
         break;
       }
       if (ws.f32_phase) f32_known = true;
-      if (k - 1 > cfg->max_iterations) return Status{GOPS_ERR_INTERNAL, "wave did not finish"};
+      if (k - 1 <= cfg->max_iterations) {
+        GOPS_TRY(launch_chunk());
+        GOPS_TRY(poll_after(slot));
+        pending[npend++] = slot;
+      }
     }
+    if (!finished) return Status{GOPS_ERR_INTERNAL, "wave did not finish"};
     // ---- results of the wave
     p.out = scores_on_device ? scores : b->out;
     if (scores) {

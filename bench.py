@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--batch-scale", type=int, default=20)
     ap.add_argument("--batch-sets", type=int, default=1024)
     ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start measurement")
+    ap.add_argument("--only", choices=["all", "pagerank", "batched", "learned"], default="all",
+                    help="run one section (profiling); the default runs all three")
     ap.add_argument("--learned-n", type=int, default=500000)
     ap.add_argument("--learned-train", type=int, default=50000)
     ap.add_argument("--learned-sets", type=int, default=4096)
@@ -341,7 +343,24 @@ def run_reference(a):
     print(json.dumps(line))
 
 
+def run_section(a):
+    """--only batched|learned: one section's object alone (for profiling)."""
+    rank, ws = dist_init(a)
+    import torch
+    from graphops_gb300 import _native
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    ctx = _native.Context(dev)
+    out = run_batch(a, ctx, rank, ws) if a.only == "batched" else run_learned(a, ctx, rank, ws)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "section": a.only, "n_gpus": ws, a.only: out}))
+
+
 def run_gpu(a):
+    if a.only in ("batched", "learned"):
+        return run_section(a)
+    if a.only == "pagerank":
+        a.no_batch = a.no_learned = True
     rank, ws = dist_init(a)
     import ctypes
     import torch

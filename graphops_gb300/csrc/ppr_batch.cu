@@ -476,7 +476,10 @@ __global__ void __launch_bounds__(kBThreads, kBMinBlocks) spmm_kernel(BatchParam
         const int rb = (int)__ldg(&p.rp[h]), re = (int)__ldg(&p.rp[h + 1]);
         const int cs = rb + ((int)t - first) * kSpmmChunk;
         const int ce = min(re, cs + kSpmmChunk);
-        const T s = kRowAlign == 4 ? gather_sum_q<P>(p, cs, ce, c, pol) : gather_sum<P>(p, cs, ce, c, gmask, pol);
+        // a retired column's lane gathers nothing (its sectors are not read)
+        T s = P::zero();
+        if (kRowAlign != 4) s = gather_sum<P>(p, cs, ce, c, gmask, pol);
+        else if (active) s = gather_sum_q<P>(p, cs, ce, c, pol);
         p.lpart[t * kCols + c] = P::pack(s);
         __threadfence();
         __syncwarp();
@@ -494,9 +497,11 @@ __global__ void __launch_bounds__(kBThreads, kBMinBlocks) spmm_kernel(BatchParam
         const int64_t v = p.n_big + (w - p.n_big_tasks);
         BIn in;
         if (active) in = b_in<P>(p, v, c, uniform);
-        const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
-        const T s = gather_sum_q<P>(p, eb, ee, c, pol);
-        if (active) col_epilogue_in<P>(p, v, s, dsum, in, a, c);
+        if (active) {  // a retired column's lane gathers nothing
+          const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
+          const T s = gather_sum_q<P>(p, eb, ee, c, pol);
+          col_epilogue_in<P>(p, v, s, dsum, in, a, c);
+        }
       } else {
         const int64_t v0 = p.n_big + (w - p.n_big_tasks) * R;
         rows_task<P, R>(p, v0, p.n, c, active, uniform, dsum, a, pol);

@@ -30,6 +30,9 @@ from .pagerank import (
 )
 from ._native import Context, DeviceGraph, GopsError, default_context
 from .batch import BatchRun, ppr_batch, seed_sets_to_csr
+from .centrality import (EigenvectorRun, KatzConfig, KatzRun, eigenvector_centrality,
+                         eigenvector_centrality_run, katz_centrality, katz_centrality_checked,
+                         katz_centrality_run)
 
 __all__ = [
     "AdjacencyMatrix", "CsrAdjacency", "DiGraph", "GraphopsError", "InvalidParameter",
@@ -38,5 +41,7 @@ __all__ = [
     "pagerank_weighted_checked_run", "pagerank_weighted_run", "personalized_pagerank",
     "personalized_pagerank_checked", "personalized_pagerank_checked_run",
     "personalized_pagerank_run", "top_k", "Context", "DeviceGraph", "GopsError",
-    "default_context", "BatchRun", "ppr_batch", "seed_sets_to_csr",
+    "default_context", "BatchRun", "ppr_batch", "seed_sets_to_csr", "KatzConfig", "KatzRun",
+    "EigenvectorRun", "katz_centrality", "katz_centrality_run", "katz_centrality_checked",
+    "eigenvector_centrality", "eigenvector_centrality_run",
 ]

@@ -45,6 +45,10 @@ class Stats(ctypes.Structure):
                 ("df_ms", _dbl), ("df_launches", _u64), ("f32_ms", _dbl), ("f32_launches", _u64)]
 
 
+class KatzConfig(ctypes.Structure):
+    _fields_ = [("alpha", _dbl), ("beta", _dbl), ("max_iterations", _u64), ("tolerance", _dbl)]
+
+
 class WarmConfig(ctypes.Structure):
     _fields_ = [("clusters", _i32), ("code_steps", _i32), ("kmeans_iters", _i32), ("minibatch", _i32),
                 ("chunk", _i32), ("epochs", _i32), ("lr", ctypes.c_float), ("ridge", ctypes.c_float),
@@ -79,6 +83,9 @@ SIGNATURES = [
     ("gops_pagerank_run_noalloc", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, ctypes.POINTER(Run)]),
     ("gops_ppr_batch", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
     ("gops_ppr_batch_device", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
+    ("gops_katz_config_validate", ctypes.c_int, [ctypes.POINTER(KatzConfig), ctypes.c_char_p, ctypes.c_size_t]),
+    ("gops_katz_run", ctypes.c_int, [_p, _p, ctypes.POINTER(KatzConfig), _p, ctypes.POINTER(Run)]),
+    ("gops_eigenvector_run", ctypes.c_int, [_p, _p, _u64, _dbl, _p, ctypes.POINTER(Run)]),
     ("gops_warm_config_default", None, [ctypes.POINTER(WarmConfig)]),
     ("gops_warm_create", ctypes.c_int, [_p, _p, _p, _p, ctypes.POINTER(WarmConfig), ctypes.POINTER(_p)]),
     ("gops_warm_destroy", None, [_p]),
@@ -257,6 +264,21 @@ class DeviceGraph:
         diffs = np.array([runs[i].diff_l1 for i in range(ns)], dtype=np.float64)
         conv = np.array([bool(runs[i].converged) for i in range(ns)])
         return scores, its, diffs, conv
+
+    def katz_run(self, alpha, beta, max_iterations, tolerance, out=True):
+        c = KatzConfig(float(alpha), float(beta), int(max_iterations), float(tolerance))
+        r = Run()
+        scores = np.empty(self.n, dtype=np.float64) if out else None
+        self.ctx.check(self.ctx._l.gops_katz_run(self.ctx.handle, self.handle, ctypes.byref(c), ptr(scores),
+                                                 ctypes.byref(r)))
+        return scores, int(r.iterations), float(r.diff_l1), bool(r.converged)
+
+    def eigenvector_run(self, max_iterations, tolerance, out=True):
+        r = Run()
+        scores = np.empty(self.n, dtype=np.float64) if out else None
+        self.ctx.check(self.ctx._l.gops_eigenvector_run(self.ctx.handle, self.handle, int(max_iterations),
+                                                        float(tolerance), ptr(scores), ctypes.byref(r)))
+        return scores, int(r.iterations), float(r.diff_l1), bool(r.converged)
 
     def pagerank_run(self, cfg, out=True):
         return self._solve("gops_pagerank_run", cfg, out=out)

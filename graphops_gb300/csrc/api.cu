@@ -66,8 +66,13 @@ Status upload_impl(Ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *c
     ctx->stats.h2d_bytes += sizeof(int64_t) * (n + 1) + sizeof(int32_t) * m + (w ? sizeof(double) * m : 0);
     st = graph_build_from_out_csr_device(ctx, g, d_rp, d_col, d_w);
   }
-  free_async(d_rp, s);
-  free_async(d_col, s);
+  if (st.code == GOPS_OK) {  // kept: the out-adjacency drives eigenvector centrality
+    g->out_rp = d_rp;
+    g->out_col = d_col;
+  } else {
+    free_async(d_rp, s);
+    free_async(d_col, s);
+  }
   free_async(d_w, s);
   cudaError_t e2 = cudaStreamSynchronize(s);
   if (st.code == GOPS_OK && e2 != cudaSuccess) st = fail(e2, "graph upload");
@@ -226,8 +231,13 @@ int gops_graph_from_dense(gops_ctx *ctx, int64_t n, const double *matrix, gops_g
     st = graph_build_from_out_csr_device(&c, &g->impl, d_rp, d_col, d_w);
   }
   free_async(d_M, s);
-  free_async(d_rp, s);
-  free_async(d_col, s);
+  if (st.code == GOPS_OK) {
+    g->impl.out_rp = d_rp;
+    g->impl.out_col = d_col;
+  } else {
+    free_async(d_rp, s);
+    free_async(d_col, s);
+  }
   free_async(d_w, s);
   cudaStreamSynchronize(s);
   if (st.code != GOPS_OK) {

@@ -214,10 +214,12 @@ int bits_for(int64_t n) {
 void graph_free_device(Graph &g) {
   cudaFree(g.in_rp); cudaFree(g.in_col); cudaFree(g.in_val); cudaFree(g.deg);
   cudaFree(g.dmask_w); cudaFree(g.perm); cudaFree(g.hub_first); cudaFree(g.hub_task_row);
+  cudaFree(g.out_rp); cudaFree(g.out_col);
   workspace_free(g.ws);
   batch_free(g);
   g.in_rp = nullptr; g.in_col = nullptr; g.in_val = nullptr; g.deg = nullptr;
   g.dmask_w = nullptr; g.perm = nullptr; g.hub_first = nullptr; g.hub_task_row = nullptr;
+  g.out_rp = nullptr; g.out_col = nullptr;
 }
 
 Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_rp,

@@ -90,6 +90,8 @@ struct Graph {
   float *deg = nullptr;         // out-degree (relabelled order); 0 = unweighted-dangling
   uint32_t *dmask_w = nullptr;  // weighted-dangling bitmask (relabelled order)
   int32_t *perm = nullptr;      // relabelled row i -> original node id
+  int64_t *out_rp = nullptr;    // the out-adjacency as uploaded (original ids, adapter order)
+  int32_t *out_col = nullptr;
   int32_t *hub_first = nullptr;     // n_hub + 1 task offsets
   int32_t *hub_task_row = nullptr;  // hub task -> hub row
   Plan plan;

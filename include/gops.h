@@ -190,6 +190,34 @@ const double *gops_ctx_scores_device(const gops_ctx *ctx);
 int gops_pagerank_run_noalloc(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg,
                               double *scores, gops_run *run);
 
+/* ---- Katz and eigenvector centrality: the same pull power iteration ---- */
+
+/* KatzConfig (src/katz.rs:19-57): attenuation alpha, baseline beta,
+ * max_iterations, tolerance on the L1 norm of the step. */
+typedef struct gops_katz_config {
+  double alpha;
+  double beta;
+  uint64_t max_iterations;
+  double tolerance;
+} gops_katz_config;
+
+/* KatzConfig::validate (src/katz.rs:60-86): the reference's messages. */
+int gops_katz_config_validate(const gops_katz_config *cfg, char *msg, size_t msg_cap);
+
+/* katz_centrality_run (src/katz.rs:136-201): x_0 = beta, x_{k+1}[v] = beta +
+ * alpha * sum over edges u->v of x_k[u] (multi-edges counted, weights
+ * ignored), stop at the first step whose L1 norm < tolerance.  FP64.
+ * scores: n doubles (or NULL). */
+int gops_katz_run(gops_ctx *ctx, const gops_graph *g, const gops_katz_config *cfg, double *scores,
+                  gops_run *run);
+
+/* eigenvector_centrality_run (src/eigenvector.rs:49-125): x_0 = 1/sqrt(n),
+ * y[v] = x[v] + sum over the out-neighbours u of v of x[u], then y divided by
+ * its L2 norm with the sign making its sum non-negative (unchanged when the
+ * norm is 0); stop at the first step whose L1 change < tolerance.  FP64. */
+int gops_eigenvector_run(gops_ctx *ctx, const gops_graph *g, uint64_t max_iterations, double tolerance,
+                         double *scores, gops_run *run);
+
 /* ---- learned warm start for batched personalized PageRank ----
  * No counterpart in the reference (it is the extension that feeds
  * gops_ppr_batch's x0).  A per-graph model predicts each set's PPR vector:

@@ -316,3 +316,102 @@ int orc_ppr_many(int64_t n, const int64_t *row_ptr, const int32_t *col,
     }
     return rc;
 }
+
+/*
+ * katz_centrality_run, src/katz.rs:136-201: x = beta; each step
+ * new = beta, then for u ascending, for v in neighbors(u): new[v] += alpha*x[u];
+ * diff = sequential sum |old - new|; swap; stop when diff < tol.
+ * Returns the last new vector; diff_l1 = INFINITY when no step ran.
+ */
+int orc_katz_run(int64_t n, const int64_t *row_ptr, const int32_t *col, double alpha,
+                 double beta, uint64_t max_iterations, double tolerance, double *scores,
+                 orc_run *run) {
+    if (n == 0) {
+        empty_run(run);
+        return 0;
+    }
+    double *x = scores, *y = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!y) return 1;
+    for (int64_t i = 0; i < n; ++i) x[i] = beta;
+    uint64_t iters = 0;
+    double last = INFINITY;
+    int conv = 0;
+    for (uint64_t k = 0; k < max_iterations; ++k) {
+        iters += 1;
+        for (int64_t i = 0; i < n; ++i) y[i] = beta;
+        for (int64_t u = 0; u < n; ++u) {
+            const double contrib = alpha * x[u];
+            for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e)
+                if (col[e] < n) y[col[e]] += contrib;
+        }
+        const double diff = l1_seq(x, y, n);
+        last = diff;
+        double *t = x; x = y; y = t;
+        if (diff < tolerance) {
+            conv = 1;
+            break;
+        }
+    }
+    if (x != scores) {
+        memcpy(scores, x, sizeof(double) * (size_t)n);
+        y = x;
+    }
+    free(y);
+    run->iterations = iters;
+    run->diff_l1 = last;
+    run->converged = conv;
+    return 0;
+}
+
+/*
+ * eigenvector_centrality_run, src/eigenvector.rs:49-125: x = 1/sqrt(n);
+ * new[v] = x[v] + sum over neighbors(v) of x[u]; L2-normalise with the sign
+ * that makes the sum non-negative (skipped when the norm is 0); diff =
+ * sequential sum |old - new|; swap; stop when diff < tol.
+ */
+int orc_eigenvector_run(int64_t n, const int64_t *row_ptr, const int32_t *col,
+                        uint64_t max_iterations, double tolerance, double *scores, orc_run *run) {
+    if (n == 0) {
+        empty_run(run);
+        return 0;
+    }
+    double *x = scores, *y = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!y) return 1;
+    const double init = 1.0 / sqrt((double)n);
+    for (int64_t i = 0; i < n; ++i) x[i] = init;
+    uint64_t iters = 0;
+    double diff = 0.0;
+    int conv = 0;
+    for (uint64_t k = 0; k < max_iterations; ++k) {
+        iters = k + 1;
+        for (int64_t v = 0; v < n; ++v) {
+            double s = x[v];
+            for (int64_t e = row_ptr[v]; e < row_ptr[v + 1]; ++e)
+                if (col[e] < n) s += x[col[e]];
+            y[v] = s;
+        }
+        double sq = 0.0, su = 0.0;
+        for (int64_t v = 0; v < n; ++v) sq += y[v] * y[v];
+        const double norm = sqrt(sq);
+        if (norm > 0.0) {
+            for (int64_t v = 0; v < n; ++v) su += y[v];
+            const double sign = su >= 0.0 ? 1.0 : -1.0;
+            for (int64_t v = 0; v < n; ++v) y[v] = y[v] * sign / norm;
+        }
+        diff = l1_seq(x, y, n);
+        double *t = x; x = y; y = t;
+        if (diff < tolerance) {
+            conv = 1;
+            break;
+        }
+    }
+    if (x != scores) {
+        memcpy(scores, x, sizeof(double) * (size_t)n);
+        y = x;
+    }
+    free(y);
+    run->iterations = iters;
+    run->diff_l1 = diff;
+    run->converged = conv;
+    return 0;
+}

@@ -41,6 +41,10 @@ def lib():
         l.orc_pagerank_run_dense.argtypes = [ctypes.c_int64, P, OrcConfig, P, ctypes.POINTER(OrcRun)]
         l.orc_ppr_many.argtypes = [ctypes.c_int64, P, P, OrcConfig, ctypes.c_int64, P, P,
                                    ctypes.c_int, P, P]
+        l.orc_katz_run.argtypes = [ctypes.c_int64, P, P, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                   ctypes.c_double, P, ctypes.POINTER(OrcRun)]
+        l.orc_eigenvector_run.argtypes = [ctypes.c_int64, P, P, ctypes.c_uint64, ctypes.c_double, P,
+                                          ctypes.POINTER(OrcRun)]
         _lib = l
     return _lib
 
@@ -125,3 +129,29 @@ def ppr_many(row_ptr, col, seed_ptr, seed_idx, damping=0.85, max_iterations=100,
                           _p(sp), _p(si), int(threads), _p(out), _p(its)):
         raise MemoryError
     return out, its
+
+
+def katz_run(row_ptr, col, alpha=0.1, beta=1.0, max_iterations=100, tolerance=1e-6):
+    """katz_centrality_run (src/katz.rs:136-201) in FP64."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    n = rp.shape[0] - 1
+    out = np.empty(max(n, 1))
+    r = OrcRun()
+    if lib().orc_katz_run(n, _p(rp), _p(cl), float(alpha), float(beta), int(max_iterations), float(tolerance),
+                          _p(out), ctypes.byref(r)):
+        raise MemoryError
+    return out[:n], int(r.iterations), float(r.diff_l1), bool(r.converged)
+
+
+def eigenvector_run(row_ptr, col, max_iterations=100, tolerance=1e-6):
+    """eigenvector_centrality_run (src/eigenvector.rs:49-125) in FP64."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    n = rp.shape[0] - 1
+    out = np.empty(max(n, 1))
+    r = OrcRun()
+    if lib().orc_eigenvector_run(n, _p(rp), _p(cl), int(max_iterations), float(tolerance), _p(out),
+                                 ctypes.byref(r)):
+        raise MemoryError
+    return out[:n], int(r.iterations), float(r.diff_l1), bool(r.converged)

@@ -1,0 +1,115 @@
+"""Katz and eigenvector centrality on the GPU (gops_katz_run,
+gops_eigenvector_run) against the C restatement of the reference loops:
+FP64 on both sides, summation order differs, so scores agree to ~1e-15
+relative and the iteration counts exactly (a step whose L1 lands within a
+few ulps of the tolerance could differ by one; none does here)."""
+import math
+
+import numpy as np
+import pytest
+
+import graphops_gb300 as go
+from graphops_gb300 import gen
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+REL = 1e-12
+
+
+def csr(adj):
+    rp = np.zeros(len(adj) + 1, dtype=np.int64)
+    for i, r in enumerate(adj):
+        rp[i + 1] = rp[i] + len(r)
+    col = np.array([v for r in adj for v in r], dtype=np.int32)
+    return rp, col
+
+
+def rel_l1(a, b):
+    return float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))
+
+
+SMALL = [
+    [[1], [0, 2], [1, 3], [2]],
+    [[1, 2], [0, 2], [0, 1]],
+    [[1, 2, 3, 4], [0], [0], [0], [0]],
+    [[1, 2, 3], [0, 2], [0, 1, 3], [0, 2]],
+    [[], [], []],
+    [[0, 1, 1], [2], []],            # self loop, duplicate edge, dangling node
+]
+
+
+@pytest.mark.parametrize("adj", SMALL)
+def test_small_graphs_match_oracle(adj):
+    rp, col = csr(adj)
+    dg = go.DeviceGraph.from_csr(rp, col)
+    for kw in ({}, {"alpha": 0.3, "beta": 2.0, "tolerance": 1e-10}):
+        cfg = go.KatzConfig(**kw)
+        r = go.katz_centrality_run(dg, cfg)
+        s, it, diff, conv = port.katz_run(rp, col, cfg.alpha, cfg.beta, cfg.max_iterations, cfg.tolerance)
+        assert r.iterations == it and r.converged == conv
+        assert rel_l1(r.scores, s) <= REL
+    r = go.eigenvector_centrality_run(dg, 100, 1e-8)
+    s, it, diff, conv = port.eigenvector_run(rp, col, 100, 1e-8)
+    assert r.iterations == it and r.converged == conv
+    assert rel_l1(r.scores, s) <= REL
+
+
+@pytest.mark.parametrize("scale", [10, 14])
+def test_rmat_katz_converging_and_diverging(scale):
+    g = gen.rmat(scale, 16, seed=scale)
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    indeg = np.bincount(g.col, minlength=g.n)
+    a = 0.5 / max(int(indeg.max()), 1)   # below 1/rho(A): converges
+    for alpha, tol, it_max in ((a, 1e-6, 1000), (0.1, 1e-6, 30)):   # 0.1: grows without bound
+        r = go.katz_centrality_run(dg, go.KatzConfig(alpha, 1.0, it_max, tol))
+        s, it, diff, conv = port.katz_run(g.row_ptr, g.col, alpha, 1.0, it_max, tol)
+        assert r.iterations == it and r.converged == conv
+        assert rel_l1(r.scores, s) <= REL
+        # the step norm sums differences of nearly equal values: its error
+        # scales with the vector's mass, not with the step
+        assert abs(r.diff_l1 - diff) <= 1e-13 * np.abs(s).sum()
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_eigenvector_directed_and_symmetric(seed):
+    g = gen.erdos_renyi(3000, 0.004, 0.02, seed=seed)
+    for rp, col in ((g.row_ptr, g.col), None):
+        if rp is None:   # symmetrised copy
+            src = np.repeat(np.arange(g.n), np.diff(g.row_ptr))
+            u = np.concatenate([src, g.col]); v = np.concatenate([g.col, src])
+            o = np.lexsort((v, u)); u, v = u[o], v[o]
+            rp = np.zeros(g.n + 1, np.int64); np.add.at(rp, u + 1, 1); rp = np.cumsum(rp)
+            col = v.astype(np.int32)
+        dg = go.DeviceGraph.from_csr(rp, col)
+        r = go.eigenvector_centrality_run(dg, 300, 1e-9)
+        s, it, diff, conv = port.eigenvector_run(rp, col, 300, 1e-9)
+        assert r.iterations == it and r.converged == conv
+        assert rel_l1(r.scores, s) <= REL
+        assert abs(np.sqrt((r.scores ** 2).sum()) - 1.0) < 1e-12
+
+
+def test_adapters_dense_and_weighted_ignore_weights():
+    rng = np.random.default_rng(3)
+    M = (rng.random((40, 40)) < 0.1) * rng.random((40, 40))
+    a = go.eigenvector_centrality(go.AdjacencyMatrix(M))
+    rp, col = port.dense_to_csr(M)[:2]
+    s, *_ = port.eigenvector_run(rp, col)
+    assert rel_l1(a, s) <= REL
+    g = gen.rmat(9, 8, weighted=True, seed=2)
+    dw = go.DeviceGraph.from_csr(g.row_ptr, g.col, g.weight.astype(np.float64))
+    du = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    k1 = go.katz_centrality(dw, go.KatzConfig(alpha=0.01))
+    k2 = go.katz_centrality(du, go.KatzConfig(alpha=0.01))
+    assert np.array_equal(k1, k2)
+
+
+def test_edge_runs():
+    rp, col = csr([[1], [0]])
+    dg = go.DeviceGraph.from_csr(rp, col)
+    r = go.katz_centrality_run(dg, go.KatzConfig(max_iterations=0))
+    assert r.iterations == 0 and math.isinf(r.diff_l1) and not r.converged and (r.scores == 1.0).all()
+    r = go.eigenvector_centrality_run(dg, 0, 1e-6)
+    assert r.iterations == 0 and r.diff_l1 == 0.0 and not r.converged
+    assert np.allclose(r.scores, 1 / math.sqrt(2))
+    e = go.eigenvector_centrality_run(go.CsrAdjacency(np.zeros(1, np.int64), np.zeros(0, np.int32)))
+    assert len(e.scores) == 0 and e.converged

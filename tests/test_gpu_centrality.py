@@ -73,8 +73,9 @@ def test_rmat_katz_converging_and_diverging(scale):
 @pytest.mark.parametrize("seed", [0, 1])
 def test_eigenvector_directed_and_symmetric(seed):
     g = gen.erdos_renyi(3000, 0.004, 0.02, seed=seed)
-    for rp, col in ((g.row_ptr, g.col), None):
-        if rp is None:   # symmetrised copy
+    for symmetric in (False, True):
+        rp, col = g.row_ptr, g.col
+        if symmetric:   # both directions of every edge
             src = np.repeat(np.arange(g.n), np.diff(g.row_ptr))
             u = np.concatenate([src, g.col]); v = np.concatenate([g.col, src])
             o = np.lexsort((v, u)); u, v = u[o], v[o]

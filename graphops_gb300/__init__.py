@@ -31,7 +31,7 @@ from .pagerank import (
 from ._native import Context, DeviceGraph, GopsError, default_context
 from .batch import BatchRun, ppr_batch, seed_sets_to_csr
 from .centrality import (EigenvectorRun, KatzConfig, KatzRun, eigenvector_centrality,
-                         eigenvector_centrality_run, katz_centrality, katz_centrality_checked,
+                         eigenvector_centrality_run, hits, katz_centrality, katz_centrality_checked,
                          katz_centrality_run)
 
 __all__ = [
@@ -43,5 +43,5 @@ __all__ = [
     "personalized_pagerank_run", "top_k", "Context", "DeviceGraph", "GopsError",
     "default_context", "BatchRun", "ppr_batch", "seed_sets_to_csr", "KatzConfig", "KatzRun",
     "EigenvectorRun", "katz_centrality", "katz_centrality_run", "katz_centrality_checked",
-    "eigenvector_centrality", "eigenvector_centrality_run",
+    "eigenvector_centrality", "eigenvector_centrality_run", "hits",
 ]

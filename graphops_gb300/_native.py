@@ -86,6 +86,10 @@ SIGNATURES = [
     ("gops_katz_config_validate", ctypes.c_int, [ctypes.POINTER(KatzConfig), ctypes.c_char_p, ctypes.c_size_t]),
     ("gops_katz_run", ctypes.c_int, [_p, _p, ctypes.POINTER(KatzConfig), _p, ctypes.POINTER(Run)]),
     ("gops_eigenvector_run", ctypes.c_int, [_p, _p, _u64, _dbl, _p, ctypes.POINTER(Run)]),
+    ("gops_hits_run", ctypes.c_int, [_p, _p, _u64, _dbl, _p, _p, ctypes.POINTER(Run)]),
+    ("gops_top_k_f64_device", ctypes.c_int, [_p, _p, _i64, _i64, _p, _p, ctypes.POINTER(_i64)]),
+    ("gops_top_k_f32_rows_device", ctypes.c_int, [_p, _p, _i64, _i64, _i64, _p, _p, _p]),
+    ("gops_normalize_f64_device", ctypes.c_int, [_p, _p, _i64]),
     ("gops_warm_config_default", None, [ctypes.POINTER(WarmConfig)]),
     ("gops_warm_create", ctypes.c_int, [_p, _p, _p, _p, ctypes.POINTER(WarmConfig), ctypes.POINTER(_p)]),
     ("gops_warm_destroy", None, [_p]),
@@ -279,6 +283,14 @@ class DeviceGraph:
         self.ctx.check(self.ctx._l.gops_eigenvector_run(self.ctx.handle, self.handle, int(max_iterations),
                                                         float(tolerance), ptr(scores), ctypes.byref(r)))
         return scores, int(r.iterations), float(r.diff_l1), bool(r.converged)
+
+    def hits_run(self, max_iterations, tolerance):
+        r = Run()
+        hub = np.empty(self.n, dtype=np.float64)
+        auth = np.empty(self.n, dtype=np.float64)
+        self.ctx.check(self.ctx._l.gops_hits_run(self.ctx.handle, self.handle, int(max_iterations),
+                                                 float(tolerance), ptr(hub), ptr(auth), ctypes.byref(r)))
+        return hub, auth, int(r.iterations), float(r.diff_l1), bool(r.converged)
 
     def pagerank_run(self, cfg, out=True):
         return self._solve("gops_pagerank_run", cfg, out=out)

@@ -1,4 +1,4 @@
-"""Katz and eigenvector centrality: the same pull power iteration as
+"""Katz, eigenvector and HITS centrality: the same pull power iteration as
 PageRank, on the GPU, with the reference crate's names, defaults, messages
 and diagnostics (graphops 0.4.1, src/katz.rs and src/eigenvector.rs).
 
@@ -86,3 +86,12 @@ def eigenvector_centrality_run(graph, max_iterations: int = 100, tolerance: floa
 def eigenvector_centrality(graph) -> np.ndarray:
     """eigenvector_centrality (src/eigenvector.rs:26-28): 100 iterations, tol 1e-6."""
     return eigenvector_centrality_run(graph, 100, 1e-6).scores
+
+
+def hits(graph, max_iter: int = 100, tol: float = 1e-6):
+    """hits (src/centrality.rs:114-166): (hub scores, authority scores)."""
+    if _n(graph) == 0:
+        return np.empty(0), np.empty(0)
+    dg = _device_graph(graph, weighted=False)
+    hub, auth, _, _, _ = dg.hits_run(max_iter, tol)
+    return hub, auth

@@ -129,6 +129,56 @@ __global__ void __launch_bounds__(kCThreads) eig_scale(int64_t n, const double *
   block_part(dl, sh, part, 1, 0);
 }
 
+// HITS: y[v] = sum over the row's edges of x[col] (no self term); part[b] =
+// this block's sum of y^2.  Rows of the relabelled in-CSR (x has n+1 entries,
+// x[n] = 0) or of the out-adjacency.
+__global__ void __launch_bounds__(kCThreads) pull_sum(const int64_t *__restrict__ rp, const int32_t *__restrict__ col,
+                                                      int64_t n, const double *__restrict__ x, double *__restrict__ y,
+                                                      double *__restrict__ part) {
+  __shared__ double sh[kCThreads];
+  const int lane = threadIdx.x & (kSub - 1);
+  const int64_t groups = (int64_t)gridDim.x * (kCThreads / kSub);
+  double sq = 0.0;
+  for (int64_t v = (int64_t)blockIdx.x * (kCThreads / kSub) + threadIdx.x / kSub; v < n; v += groups) {
+    double s = 0.0;
+    for (int64_t e = rp[v] + lane; e < rp[v + 1]; e += kSub) s += x[col[e]];
+    s = sub_sum(s);
+    if (lane == 0) {
+      y[v] = s;
+      sq += s * s;
+    }
+  }
+  block_part(sq, sh, part, 1, 0);
+}
+
+// HITS l2_normalize (src/centrality.rs:168-175) of y in place (skipped when
+// the norm is 0), then part[b] = this block's sum of (x - y)^2 for l2_diff
+// (src/centrality.rs:177-183); xo indexes x in y's order through `map`
+// (map == nullptr: same order)
+__global__ void __launch_bounds__(kCThreads) l2_scale(int64_t n, const double *__restrict__ sums,
+                                                      const double *__restrict__ x, const int32_t *__restrict__ map,
+                                                      double *__restrict__ y, double *__restrict__ part) {
+  __shared__ double sh[kCThreads];
+  const double norm = sqrt(sums[0]);
+  double dl = 0.0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    double yv = y[v];
+    if (norm > 0.0) {
+      yv = yv / norm;
+      y[v] = yv;
+    }
+    const double t = x[map ? map[v] : v] - yv;
+    dl += t * t;
+  }
+  block_part(dl, sh, part, 1, 0);
+}
+
+// out[i] = x[perm[i]] (original order -> relabelled order); out[n] = 0
+__global__ void permute_to_rows(const double *x, const int32_t *perm, int64_t n, double *out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = i < n ? x[perm[i]] : 0.0;
+}
+
 __global__ void fill_f64(double *a, int64_t n, double v) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
 }
@@ -256,6 +306,87 @@ Status eigenvector_run(Ctx *ctx, const Graph *g, uint64_t max_iterations, double
   return Status::ok();
 }
 
+// hits (src/centrality.rs:114-166): hub = auth = 1/sqrt(n); each step
+// auth' = l2n(A^T hub), hub' = l2n(A auth'); stop when both L2 changes < tol.
+// The reference returns (hub, auth) only; `run` adds the step count, the
+// larger of the two L2 changes, and whether both fell below tol.
+Status hits_run(Ctx *ctx, const Graph *g, uint64_t max_iterations, double tolerance, double *hub_out,
+                double *auth_out, gops_run *run) {
+  ctx->stats = gops_stats{};
+  const int64_t n = g->n;
+  *run = gops_run{0, 0.0, 0, 0};
+  if (n == 0) {
+    run->converged = 1;
+    return Status::ok();
+  }
+  if (!g->out_rp) return Status{GOPS_ERR_INTERNAL, "graph has no out-adjacency"};
+  cudaStream_t s = ctx->stream;
+  struct H {
+    double *hub = nullptr, *auth = nullptr, *nhub = nullptr, *nauth_r = nullptr, *nauth = nullptr,
+           *hub_r = nullptr, *part = nullptr, *sums = nullptr;
+    ~H() {
+      cudaFree(hub); cudaFree(auth); cudaFree(nhub); cudaFree(nauth_r); cudaFree(nauth); cudaFree(hub_r);
+      cudaFree(part); cudaFree(sums);
+    }
+  } h;
+  const int nb = grid_rows(n), nbs = blocks_for(n, 256, kCBlocks);
+  GOPS_CUDA_TRY(cudaMalloc(&h.hub, sizeof(double) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&h.auth, sizeof(double) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&h.nhub, sizeof(double) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&h.nauth_r, sizeof(double) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&h.nauth, sizeof(double) * n));
+  GOPS_CUDA_TRY(cudaMalloc(&h.hub_r, sizeof(double) * (n + 1)));
+  GOPS_CUDA_TRY(cudaMalloc(&h.part, sizeof(double) * std::max(nb, nbs)));
+  GOPS_CUDA_TRY(cudaMalloc(&h.sums, sizeof(double) * 4));
+  const double init = 1.0 / std::sqrt((double)n);  // src/centrality.rs:130
+  fill_f64<<<blocks_for(n, 256, 4096), 256, 0, s>>>(h.hub, n, init);
+  fill_f64<<<blocks_for(n, 256, 4096), 256, 0, s>>>(h.auth, n, init);
+  uint64_t it = 0, launches = 2;
+  double last = 0.0;
+  bool conv = false;
+  GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+  for (uint64_t k = 0; k < max_iterations; ++k) {
+    it = k + 1;
+    // authority: pull over the in-edge rows (relabelled), back to original order
+    permute_to_rows<<<blocks_for(n + 1, 256, 4096), 256, 0, s>>>(h.hub, g->perm, n, h.hub_r);
+    pull_sum<<<nb, kCThreads, 0, s>>>(g->in_rp, g->in_col, n, h.hub_r, h.nauth_r, h.part);
+    sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nb, 1, h.sums);
+    l2_scale<<<nbs, kCThreads, 0, s>>>(n, h.sums, h.auth, g->perm, h.nauth_r, h.part);
+    sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nbs, 1, h.sums + 2);
+    unpermute_f64<<<blocks_for(n, 256, 4096), 256, 0, s>>>(h.nauth_r, g->perm, n, h.nauth);
+    // hub: pull over the out-adjacency (original order)
+    pull_sum<<<nb, kCThreads, 0, s>>>(g->out_rp, g->out_col, n, h.nauth, h.nhub, h.part);
+    sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nb, 1, h.sums);
+    l2_scale<<<nbs, kCThreads, 0, s>>>(n, h.sums, h.hub, nullptr, h.nhub, h.part);
+    sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nbs, 1, h.sums + 3);
+    launches += 10;
+    double d[2] = {0.0, 0.0};
+    GOPS_CUDA_TRY(cudaMemcpyAsync(d, h.sums + 2, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+    const double ad = std::sqrt(d[0]), hd = std::sqrt(d[1]);
+    last = std::max(ad, hd);
+    std::swap(h.auth, h.nauth);
+    std::swap(h.hub, h.nhub);
+    if (ad < tolerance && hd < tolerance) {
+      conv = true;
+      break;
+    }
+  }
+  GOPS_CUDA_TRY(cudaGetLastError());
+  GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+  if (hub_out) GOPS_CUDA_TRY(cudaMemcpyAsync(hub_out, h.hub, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (auth_out) GOPS_CUDA_TRY(cudaMemcpyAsync(auth_out, h.auth, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+  ctx->stats.solve_ms = ms;
+  ctx->stats.kernel_launches = launches;
+  ctx->stats.iterations = it;
+  ctx->stats.d2h_bytes = sizeof(double) * n * ((hub_out ? 1 : 0) + (auth_out ? 1 : 0));
+  *run = gops_run{it, last, conv ? 1 : 0, 0};
+  return Status::ok();
+}
+
 }  // namespace gops
 
 using namespace gops;
@@ -296,6 +427,16 @@ int gops_eigenvector_run(gops_ctx *ctx, const gops_graph *g, uint64_t max_iterat
   if (g->impl.ctx != &c) return c.set(Status{GOPS_ERR_INVALID, "graph belongs to another context"});
   cudaSetDevice(c.device);
   return c.set(eigenvector_run(&c, &g->impl, max_iterations, tolerance, scores, run));
+}
+
+int gops_hits_run(gops_ctx *ctx, const gops_graph *g, uint64_t max_iterations, double tolerance, double *hub,
+                  double *auth, gops_run *run) {
+  if (!ctx) return GOPS_ERR_INVALID;
+  Ctx &c = ctx->impl;
+  if (!g || !run) return c.set(Status{GOPS_ERR_INVALID, "null argument"});
+  if (g->impl.ctx != &c) return c.set(Status{GOPS_ERR_INVALID, "graph belongs to another context"});
+  cudaSetDevice(c.device);
+  return c.set(hits_run(&c, &g->impl, max_iterations, tolerance, hub, auth, run));
 }
 
 }  // extern "C"

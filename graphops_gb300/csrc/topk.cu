@@ -1,0 +1,279 @@
+// top_k and normalize (src/topk.rs:17-61) on device-resident scores: the
+// k largest finite positive scores of each row, by score descending.  The
+// reference keeps, at the boundary, the entries met first (a later equal score
+// does not displace a kept one) and leaves the order of equal scores
+// unspecified; here equal scores are ordered by index, which selects the same
+// set and makes the output deterministic.
+//
+// One CTA per row: an MSB-first radix select on the value's bit pattern
+// (finite positive IEEE values order like their bits) finds the k-th largest
+// key in 4 (FP32) or 8 (FP64) passes of 8 bits over the row; a collection
+// pass takes every key above it and the lowest-index keys equal to it; a
+// bitonic sort in shared memory orders the at most k survivors.
+#include <cstdint>
+
+#include "objects.cuh"
+
+namespace gops {
+namespace {
+
+constexpr int kTThreads = 512;
+constexpr int kMaxK = 1024;
+
+template <class V>
+struct KeyOf;
+template <>
+struct KeyOf<float> {
+  using K = uint32_t;
+  static constexpr int kBits = 32;
+  __device__ static K key(float v) { return (isfinite(v) && v > 0.f) ? __float_as_uint(v) : 0u; }
+};
+template <>
+struct KeyOf<double> {
+  using K = unsigned long long;
+  static constexpr int kBits = 64;
+  __device__ static K key(double v) {
+    return (isfinite(v) && v > 0.0) ? (K)__double_as_longlong(v) : 0ull;
+  }
+};
+
+template <class V>
+__global__ void __launch_bounds__(kTThreads) topk_rows(const V *__restrict__ x, int64_t n, int k,
+                                                       int64_t *__restrict__ idx_out, V *__restrict__ val_out,
+                                                       int64_t *__restrict__ count_out) {
+  using KO = KeyOf<V>;
+  using K = typename KO::K;
+  __shared__ unsigned hist[256];
+  __shared__ K s_prefix;
+  __shared__ int s_need;     // how many keys >= the prefix still to take
+  __shared__ int s_valid;    // keys > 0 in the row (capped)
+  __shared__ K skey[kMaxK];
+  __shared__ int64_t sidx[kMaxK];
+  __shared__ int s_cnt;
+  __shared__ int s_eqbase;
+  const V *row = x + (int64_t)blockIdx.x * n;
+  // number of valid keys (capped at k): the answer holds min(k, valid) entries
+  if (threadIdx.x == 0) s_valid = 0;
+  __syncthreads();
+  {
+    int cnt = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) cnt += KO::key(row[i]) != 0;
+    if (cnt) atomicAdd(&s_valid, cnt);
+  }
+  __syncthreads();
+  const int take = s_valid < k ? s_valid : k;
+  if (take == 0) {
+    if (threadIdx.x == 0) count_out[blockIdx.x] = 0;
+    return;
+  }
+  // radix select of the take-th largest key
+  if (threadIdx.x == 0) {
+    s_prefix = 0;
+    s_need = take;
+  }
+  __syncthreads();
+  K mask = 0;
+  for (int shift = KO::kBits - 8; shift >= 0; shift -= 8) {
+    for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    const K prefix = s_prefix;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const K kk = KO::key(row[i]);
+      if (kk != 0 && (kk & mask) == prefix) atomicAdd(&hist[(unsigned)((kk >> shift) & 0xFF)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int need = s_need;
+      int b = 255;
+      for (; b > 0; --b) {
+        if ((int)hist[b] >= need) break;
+        need -= (int)hist[b];
+      }
+      s_prefix = prefix | ((K)b << shift);
+      s_need = need;  // keys equal to the final prefix still to take
+    }
+    __syncthreads();
+    mask |= (K)0xFF << shift;
+  }
+  const K thr = s_prefix;
+  const int need_eq = s_need;
+  // collection: every key above thr, and the need_eq lowest-index keys equal to it
+  if (threadIdx.x == 0) {
+    s_cnt = 0;
+    s_eqbase = 0;
+  }
+  __syncthreads();
+  __shared__ int wsum[kTThreads / 32];
+  for (int64_t base = 0; base < n; base += blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    const K kk = i < n ? KO::key(row[i]) : 0;
+    if (kk > thr) {
+      const int pos = atomicAdd(&s_cnt, 1);
+      skey[pos] = kk;
+      sidx[pos] = i;
+    }
+    // ties in index order: block-wide exclusive count of equal keys
+    const int eq = (i < n && kk == thr) ? 1 : 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, eq);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) wsum[wid] = __popc(bal);
+    __syncthreads();
+    int before = s_eqbase;
+    for (int w = 0; w < wid; ++w) before += wsum[w];
+    before += __popc(bal & ((1u << lane) - 1u));
+    if (eq && before < need_eq) {
+      const int pos = take - need_eq + before;  // tie slots follow the `take - need_eq` larger keys
+      skey[pos] = kk;
+      sidx[pos] = i;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+      s_eqbase += t;
+    }
+    __syncthreads();
+    if (s_eqbase >= need_eq && s_cnt >= take - need_eq) break;  // uniform: shared values after a barrier
+  }
+  __syncthreads();
+  // bitonic sort of take entries by (key desc, index asc), padded to a power of two
+  int p2 = 1;
+  while (p2 < take) p2 <<= 1;
+  for (int i = take + threadIdx.x; i < p2; i += blockDim.x) {
+    skey[i] = 0;
+    sidx[i] = INT64_MAX;
+  }
+  __syncthreads();
+  for (int size = 2; size <= p2; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < p2; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;  // this pair's half sorts "first before second"
+          // "a before b": larger key, or equal key and smaller index
+          const bool a_first = skey[i] > skey[j] || (skey[i] == skey[j] && sidx[i] < sidx[j]);
+          if (a_first != up) {
+            const K tk = skey[i];
+            skey[i] = skey[j];
+            skey[j] = tk;
+            const int64_t ti = sidx[i];
+            sidx[i] = sidx[j];
+            sidx[j] = ti;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < take; i += blockDim.x) {
+    idx_out[(int64_t)blockIdx.x * k + i] = sidx[i];
+    val_out[(int64_t)blockIdx.x * k + i] = row[sidx[i]];
+  }
+  if (threadIdx.x == 0) count_out[blockIdx.x] = take;
+}
+
+// normalize (src/topk.rs:53-61): divide by the sum when the sum > 0
+__global__ void sum_f64(const double *x, int64_t n, double *out) {
+  __shared__ double sh[1024];
+  double t = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) t += x[i];
+  sh[threadIdx.x] = t;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+__global__ void div_f64(double *x, int64_t n, const double *sum) {
+  const double s = *sum;
+  if (!(s > 0.0)) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] /= s;
+}
+
+template <class V>
+Status topk_impl(Ctx *ctx, const V *x, int64_t rows, int64_t n, int64_t k, int64_t *idx, V *val, int64_t *counts) {
+  if (rows < 0 || n < 0 || k < 0) return Status{GOPS_ERR_INVALID, "negative size"};
+  if (k > kMaxK) return Status{GOPS_ERR_INVALID, "k must be <= 1024"};
+  if (rows == 0) return Status::ok();
+  if (k == 0 || n == 0) {  // src/topk.rs:18-20
+    for (int64_t r = 0; r < rows; ++r) counts[r] = 0;
+    return Status::ok();
+  }
+  cudaStream_t s = ctx->stream;
+  int64_t *d_idx = nullptr, *d_cnt = nullptr;
+  V *d_val = nullptr;
+  Status st;
+  auto fail = [&](cudaError_t e) {
+    return Status{e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA, cudaGetErrorString(e)};
+  };
+  cudaError_t e = cudaMalloc(&d_idx, sizeof(int64_t) * rows * k);
+  if (e == cudaSuccess) e = cudaMalloc(&d_val, sizeof(V) * rows * k);
+  if (e == cudaSuccess) e = cudaMalloc(&d_cnt, sizeof(int64_t) * rows);
+  if (e == cudaSuccess) {
+    for (int64_t r0 = 0; r0 < rows && e == cudaSuccess; r0 += 65535) {
+      const int64_t nr = rows - r0 < 65535 ? rows - r0 : 65535;
+      topk_rows<V><<<(unsigned)nr, kTThreads, 0, s>>>(x + r0 * n, n, (int)k, d_idx + r0 * k, d_val + r0 * k,
+                                                       d_cnt + r0);
+      e = cudaGetLastError();
+    }
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(idx, d_idx, sizeof(int64_t) * rows * k, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(val, d_val, sizeof(V) * rows * k, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d_cnt, sizeof(int64_t) * rows, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) st = fail(e);
+  cudaFree(d_idx);
+  cudaFree(d_val);
+  cudaFree(d_cnt);
+  return st;
+}
+
+}  // namespace
+}  // namespace gops
+
+using namespace gops;
+
+extern "C" {
+
+int gops_top_k_f64_device(gops_ctx *ctx, const double *scores_device, int64_t n, int64_t k, int64_t *idx,
+                          double *val, int64_t *count) {
+  if (!ctx) return GOPS_ERR_INVALID;
+  Ctx &c = ctx->impl;
+  if ((n > 0 && !scores_device) || !idx || !val || !count) return c.set(Status{GOPS_ERR_INVALID, "null argument"});
+  cudaSetDevice(c.device);
+  return c.set(topk_impl<double>(&c, scores_device, 1, n, k, idx, val, count));
+}
+
+int gops_top_k_f32_rows_device(gops_ctx *ctx, const float *block_device, int64_t rows, int64_t n, int64_t k,
+                               int64_t *idx, float *val, int64_t *counts) {
+  if (!ctx) return GOPS_ERR_INVALID;
+  Ctx &c = ctx->impl;
+  if ((rows > 0 && n > 0 && !block_device) || !idx || !val || !counts)
+    return c.set(Status{GOPS_ERR_INVALID, "null argument"});
+  cudaSetDevice(c.device);
+  return c.set(topk_impl<float>(&c, block_device, rows, n, k, idx, val, counts));
+}
+
+int gops_normalize_f64_device(gops_ctx *ctx, double *scores_device, int64_t n) {
+  if (!ctx) return GOPS_ERR_INVALID;
+  Ctx &c = ctx->impl;
+  if (n < 0 || (n > 0 && !scores_device)) return c.set(Status{GOPS_ERR_INVALID, "null argument"});
+  if (n == 0) return GOPS_OK;
+  cudaSetDevice(c.device);
+  double *d_sum = nullptr;
+  cudaError_t e = cudaMalloc(&d_sum, sizeof(double));
+  if (e == cudaSuccess) {
+    sum_f64<<<1, 1024, 0, c.stream>>>(scores_device, n, d_sum);
+    div_f64<<<blocks_for(n, 256, 4096), 256, 0, c.stream>>>(scores_device, n, d_sum);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  cudaFree(d_sum);
+  if (e != cudaSuccess) return c.set(Status{GOPS_ERR_CUDA, cudaGetErrorString(e)});
+  return GOPS_OK;
+}
+
+}  // extern "C"

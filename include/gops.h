@@ -218,6 +218,32 @@ int gops_katz_run(gops_ctx *ctx, const gops_graph *g, const gops_katz_config *cf
 int gops_eigenvector_run(gops_ctx *ctx, const gops_graph *g, uint64_t max_iterations, double tolerance,
                          double *scores, gops_run *run);
 
+/* hits (src/centrality.rs:114-166): hub = auth = 1/sqrt(n); each step
+ * auth'[v] = sum over edges u->v of hub[u], L2-normalised; hub'[u] = sum over
+ * edges u->v of auth'[v], L2-normalised (a zero vector stays as is); stop
+ * when both L2 changes are below tolerance.  hub, auth: n doubles each (or
+ * NULL).  The reference returns only (hub, auth); run adds the step count,
+ * the larger L2 change of the last step and whether both fell below tol.
+ * FP64. */
+int gops_hits_run(gops_ctx *ctx, const gops_graph *g, uint64_t max_iterations, double tolerance, double *hub,
+                  double *auth, gops_run *run);
+
+/* ---- top_k and normalize (src/topk.rs:17-61) on device-resident scores ----
+ * The k largest finite, positive scores by score descending (the reference
+ * skips non-finite and non-positive entries); equal scores are ordered by
+ * index (the reference leaves their order unspecified and keeps, at the
+ * boundary, the entries met first: the same set).  k <= 1024.  idx / val:
+ * host buffers of k (per row: rows*k) entries; count(s): entries written. */
+int gops_top_k_f64_device(gops_ctx *ctx, const double *scores_device, int64_t n, int64_t k, int64_t *idx,
+                          double *val, int64_t *count);
+/* The same for each row of a row-major FP32 block (rows x n), e.g. the
+ * scores of gops_ppr_batch_device: top-k per seed set without copying the
+ * block to the host. */
+int gops_top_k_f32_rows_device(gops_ctx *ctx, const float *block_device, int64_t rows, int64_t n, int64_t k,
+                               int64_t *idx, float *val, int64_t *counts);
+/* normalize (src/topk.rs:53-61): divide by the sum when the sum is > 0. */
+int gops_normalize_f64_device(gops_ctx *ctx, double *scores_device, int64_t n);
+
 /* ---- learned warm start for batched personalized PageRank ----
  * No counterpart in the reference (it is the extension that feeds
  * gops_ppr_batch's x0).  A per-graph model predicts each set's PPR vector:

@@ -415,3 +415,81 @@ int orc_eigenvector_run(int64_t n, const int64_t *row_ptr, const int32_t *col,
     run->converged = conv;
     return 0;
 }
+
+/* l2_normalize and l2_diff, src/centrality.rs:168-183 (sequential sums). */
+static void l2n(double *v, int64_t n) {
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += v[i] * v[i];
+    const double norm = sqrt(s);
+    if (norm > 0.0)
+        for (int64_t i = 0; i < n; ++i) v[i] /= norm;
+}
+
+static double l2d(const double *a, const double *b, int64_t n) {
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += (a[i] - b[i]) * (a[i] - b[i]);
+    return sqrt(s);
+}
+
+/*
+ * hits, src/centrality.rs:114-166.  The in-neighbour lists are built by
+ * scanning u ascending (so each list is in source order, duplicates kept);
+ * auth' = l2n(sum over in-neighbours of hub), hub' = l2n(sum over
+ * neighbors(u) of auth'); stop when both L2 changes < tol.  run receives the
+ * step count, max(auth_diff, hub_diff) of the last step, and convergence.
+ */
+int orc_hits_run(int64_t n, const int64_t *row_ptr, const int32_t *col, uint64_t max_iterations,
+                 double tolerance, double *hub, double *auth, orc_run *run) {
+    if (n == 0) {
+        empty_run(run);
+        return 0;
+    }
+    const int64_t m = row_ptr[n];
+    int64_t *irp = (int64_t *)calloc((size_t)n + 1, sizeof(int64_t));
+    int32_t *icol = (int32_t *)malloc(sizeof(int32_t) * (size_t)(m > 0 ? m : 1));
+    int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+    double *na = (double *)malloc(sizeof(double) * (size_t)n);
+    double *nh = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!irp || !icol || !fill || !na || !nh) {
+        free(irp); free(icol); free(fill); free(na); free(nh);
+        return 1;
+    }
+    for (int64_t e = 0; e < m; ++e) irp[col[e] + 1] += 1;
+    for (int64_t v = 0; v < n; ++v) irp[v + 1] += irp[v];
+    for (int64_t v = 0; v < n; ++v) fill[v] = irp[v];
+    for (int64_t u = 0; u < n; ++u)
+        for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e) icol[fill[col[e]]++] = (int32_t)u;
+    const double init = 1.0 / sqrt((double)n);
+    for (int64_t i = 0; i < n; ++i) hub[i] = auth[i] = init;
+    uint64_t iters = 0;
+    double last = 0.0;
+    int conv = 0;
+    for (uint64_t k = 0; k < max_iterations; ++k) {
+        iters = k + 1;
+        for (int64_t v = 0; v < n; ++v) {
+            double s = 0.0;
+            for (int64_t e = irp[v]; e < irp[v + 1]; ++e) s += hub[icol[e]];
+            na[v] = s;
+        }
+        l2n(na, n);
+        for (int64_t u = 0; u < n; ++u) {
+            double s = 0.0;
+            for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e) s += na[col[e]];
+            nh[u] = s;
+        }
+        l2n(nh, n);
+        const double ad = l2d(auth, na, n), hd = l2d(hub, nh, n);
+        last = ad > hd ? ad : hd;
+        memcpy(auth, na, sizeof(double) * (size_t)n);
+        memcpy(hub, nh, sizeof(double) * (size_t)n);
+        if (ad < tolerance && hd < tolerance) {
+            conv = 1;
+            break;
+        }
+    }
+    free(irp); free(icol); free(fill); free(na); free(nh);
+    run->iterations = iters;
+    run->diff_l1 = last;
+    run->converged = conv;
+    return 0;
+}

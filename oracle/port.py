@@ -43,6 +43,8 @@ def lib():
                                    ctypes.c_int, P, P]
         l.orc_katz_run.argtypes = [ctypes.c_int64, P, P, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                    ctypes.c_double, P, ctypes.POINTER(OrcRun)]
+        l.orc_hits_run.argtypes = [ctypes.c_int64, P, P, ctypes.c_uint64, ctypes.c_double, P, P,
+                                   ctypes.POINTER(OrcRun)]
         l.orc_eigenvector_run.argtypes = [ctypes.c_int64, P, P, ctypes.c_uint64, ctypes.c_double, P,
                                           ctypes.POINTER(OrcRun)]
         _lib = l
@@ -155,3 +157,17 @@ def eigenvector_run(row_ptr, col, max_iterations=100, tolerance=1e-6):
                                  ctypes.byref(r)):
         raise MemoryError
     return out[:n], int(r.iterations), float(r.diff_l1), bool(r.converged)
+
+
+def hits_run(row_ptr, col, max_iterations=100, tolerance=1e-6):
+    """hits (src/centrality.rs:114-166) in FP64: (hub, auth, iterations, last L2 change, converged)."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    n = rp.shape[0] - 1
+    hub = np.empty(max(n, 1))
+    auth = np.empty(max(n, 1))
+    r = OrcRun()
+    if lib().orc_hits_run(n, _p(rp), _p(cl), int(max_iterations), float(tolerance), _p(hub), _p(auth),
+                          ctypes.byref(r)):
+        raise MemoryError
+    return hub[:n], auth[:n], int(r.iterations), float(r.diff_l1), bool(r.converged)

@@ -78,3 +78,12 @@ def test_eigenvector_isolated_and_empty():  # src/eigenvector.rs:168-202
     assert conv and it == 1
     s, it, diff, conv = port.eigenvector_run(np.zeros(1, np.int64), np.zeros(0, np.int32))
     assert len(s) == 0 and conv and it == 0
+
+
+def test_hits_star_and_empty():  # src/centrality.rs:245-275
+    hub, auth, it, d, conv = port.hits_run(*csr([[1, 2, 3, 4], [], [], [], []]), 100, 1e-10)
+    assert len(hub) == 5
+    assert all(hub[0] > hub[i] for i in range(1, 5))
+    assert all(auth[i] > auth[0] for i in range(1, 5))
+    hub, auth, it, d, conv = port.hits_run(np.zeros(1, np.int64), np.zeros(0, np.int32), 100, 1e-10)
+    assert len(hub) == 0 and len(auth) == 0

@@ -114,3 +114,24 @@ def test_edge_runs():
     assert np.allclose(r.scores, 1 / math.sqrt(2))
     e = go.eigenvector_centrality_run(go.CsrAdjacency(np.zeros(1, np.int64), np.zeros(0, np.int32)))
     assert len(e.scores) == 0 and e.converged
+
+
+@pytest.mark.parametrize("adj", SMALL + [[[1, 2, 3, 4], [], [], [], []]])
+def test_hits_small_match_oracle(adj):
+    rp, col = csr(adj)
+    dg = go.DeviceGraph.from_csr(rp, col)
+    hub, auth, it, d, conv = dg.hits_run(100, 1e-10)
+    rh, ra, rit, rd, rconv = port.hits_run(rp, col, 100, 1e-10)
+    assert it == rit and conv == rconv
+    assert rel_l1(hub, rh) <= REL and rel_l1(auth, ra) <= REL
+
+
+@pytest.mark.parametrize("scale", [10, 13])
+def test_hits_rmat_matches_oracle(scale):
+    g = gen.rmat(scale, 8, seed=scale + 5)
+    hub, auth = go.hits(go.CsrAdjacency(g.row_ptr, g.col), 200, 1e-9)
+    rh, ra, rit, rd, rconv = port.hits_run(g.row_ptr, g.col, 200, 1e-9)
+    assert rel_l1(hub, rh) <= 1e-10 and rel_l1(auth, ra) <= 1e-10
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    _, _, it, d, conv = dg.hits_run(200, 1e-9)
+    assert abs(it - rit) <= 1 and conv == rconv

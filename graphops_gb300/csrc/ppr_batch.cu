@@ -637,13 +637,18 @@ __global__ void count_big(const int64_t *rp, int64_t n, int64_t *out) {
   *out = lo;
 }
 
-// prow[v] = first entry whose row >= v (entries sorted by row)
+// prow[v] = first entry whose row >= v (entries sorted by row): a thread per
+// row and a binary search (a wave has a few hundred entries over n rows, so
+// a thread per entry filling its gap would leave one thread ~n writes)
 __global__ void prow_from_sorted(const int32_t *rows, int64_t e, int64_t n, int32_t *prow) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= e;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t prev = i == 0 ? -1 : (int64_t)rows[i - 1];
-    const int64_t cur = i == e ? n : (int64_t)rows[i];
-    for (int64_t v = prev + 1; v <= cur; ++v) prow[v] = (int32_t)i;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = e;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)rows[mid] < v) lo = mid + 1;
+      else hi = mid;
+    }
+    prow[v] = (int32_t)lo;
   }
 }
 
@@ -841,7 +846,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       GOPS_CUDA_TRY(cudaMemcpyAsync(b->pval, eval.data(), sizeof(float2) * ne, cudaMemcpyHostToDevice, st));
       ctx->stats.h2d_bytes += (sizeof(int32_t) * 2 + sizeof(float2)) * ne;
     }
-    prow_from_sorted<<<blocks_for(ne + 1, 256, 4096), 256, 0, st>>>(b->prows_sorted, ne, n, b->prow);
+    prow_from_sorted<<<blocks_for(n + 1, 256, ctx->num_sms * 8), 256, 0, st>>>(b->prows_sorted, ne, n, b->prow);
     ++launches;
     p.pslot = b->pslot;
     p.pval = b->pval;

@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--learned-n", type=int, default=500000)
     ap.add_argument("--learned-train", type=int, default=50000)
     ap.add_argument("--learned-sets", type=int, default=4096)
+    ap.add_argument("--learned-rmat", type=int, default=0,
+                    help="run the learned section on R-MAT of this scale (edge factor 16) instead of the SBM")
+    ap.add_argument("--learned-size-hi", type=int, default=32, help="largest seed set of the learned section")
     return ap.parse_args()
 
 
@@ -234,13 +237,17 @@ def run_batch(a, ctx, rank, ws):
 
 
 def learned_workload(a):
-    return {"workload": f"learned warm-start batched personalized PageRank, stochastic block model "
-                        f"n={a.learned_n}, 64 blocks with Zipf(1.2) sizes, intra-block mean out-degree 16, "
-                        f"inter-block 4 (directed), unit weights; trained on {a.learned_train} PPR vectors "
-                        f"of seed sets of sizes U[1,32] solved by the batched GPU path; evaluated on "
-                        f"{a.learned_sets} held-out sets of sizes U[1,32]; nodes drawn proportional "
-                        f"to out-degree",
-            "nodes": a.learned_n, "damping": 0.85, "tolerance_per_set": 1e-7, "max_iterations": 1000,
+    graph = (f"R-MAT scale {a.learned_rmat} edge factor 16 (0.57/0.19/0.19/0.05, dedup, no self loops)"
+             if a.learned_rmat else
+             f"stochastic block model n={a.learned_n}, 64 blocks with Zipf(1.2) sizes, intra-block mean "
+             f"out-degree 16, inter-block 4 (directed)")
+    hi = a.learned_size_hi
+    return {"workload": f"learned warm-start batched personalized PageRank, {graph}, unit weights; trained on "
+                        f"{a.learned_train} PPR vectors of seed sets of sizes U[1,{hi}] solved by the batched "
+                        f"GPU path; evaluated on {a.learned_sets} held-out sets of sizes U[1,{hi}]; nodes "
+                        f"drawn proportional to out-degree",
+            "nodes": (1 << a.learned_rmat) if a.learned_rmat else a.learned_n, "damping": 0.85,
+            "tolerance_per_set": 1e-7, "max_iterations": 1000,
             "graph_seed": 3, "train_seed": 31, "eval_seed": 77,
             "model": "2-layer MPNN (hidden 128, BF16 operands, FP32 accumulation) per-node weight, "
                      "128 k-means clusters of a 16-wide random-projection code, least-squares "
@@ -254,17 +261,19 @@ def run_learned(a, ctx, rank, ws):
     an end-to-end figure with the score blocks copied to the host."""
     import graphops_gb300 as go
     from graphops_gb300 import _native, gen, warm
-    g = gen.sbm(a.learned_n, 64, 1.2, 16.0, 4.0, seed=3)
+    g = gen.rmat(a.learned_rmat, 16, seed=25) if a.learned_rmat else gen.sbm(a.learned_n, 64, 1.2, 16.0, 4.0, seed=3)
     conf = go.PageRankConfig(0.85, 1000, 1e-7)
     dg = _native.DeviceGraph.from_csr(g.row_ptr, g.col, ctx=ctx)
     t0 = time.perf_counter()
-    model = warm.WarmStart(dg, g.row_ptr, g.col, warm.default_config())
+    # the push scratch and the targets hold chunk x n x 12 bytes: keep them to ~8 GB
+    chunk = int(max(32, min(512, 8e9 / (12.0 * g.n))))
+    model = warm.WarmStart(dg, g.row_ptr, g.col, warm.default_config(chunk=chunk))
     create_s = time.perf_counter() - t0
-    sp_t, si_t = gen.seed_sets(g, a.learned_train, 1, 32, seed=31)
+    sp_t, si_t = gen.seed_sets(g, a.learned_train, 1, a.learned_size_hi, seed=31)
     t0 = time.perf_counter()
     tst = model.train(conf, sp_t, si_t)
     train_s = time.perf_counter() - t0
-    sp, si = gen.seed_sets(g, a.learned_sets, 1, 32, seed=77)
+    sp, si = gen.seed_sets(g, a.learned_sets, 1, a.learned_size_hi, seed=77)
     # warm-up of both paths (plans, workspaces)
     dg.ppr_batch(conf, sp[:65], si[:sp[64]], out=False)
     model.ppr_batch(conf, sp[:65], si[:sp[64]], scores=False)

@@ -1,4 +1,5 @@
 // The extern "C" entry points declared in include/gops.h.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -26,18 +27,29 @@ int write_msg(char *msg, size_t cap, const char *text) {
   return GOPS_ERR_INVALID;
 }
 
+// Scalar checks on the host; the per-row and per-edge checks run on the
+// device after the upload (csr_checks), before anything reads the arrays.
 Status check_csr_host(int64_t n, const int64_t *row_ptr, const int32_t *col) {
   if (n < 0 || n >= INT32_MAX) return Status{GOPS_ERR_INVALID, "node count out of range"};
   if (!row_ptr) return Status{GOPS_ERR_INVALID, "row_ptr is NULL"};
   if (row_ptr[0] != 0) return Status{GOPS_ERR_INVALID, "row_ptr[0] must be 0"};
-  for (int64_t u = 0; u < n; ++u)
-    if (row_ptr[u + 1] < row_ptr[u]) return Status{GOPS_ERR_INVALID, "row_ptr must be non-decreasing"};
   const int64_t m = row_ptr[n];
+  if (m < 0) return Status{GOPS_ERR_INVALID, "row_ptr must be non-decreasing"};
   if (m >= INT32_MAX) return Status{GOPS_ERR_INVALID, "edge count out of range"};
   if (m > 0 && !col) return Status{GOPS_ERR_INVALID, "col is NULL"};
-  for (int64_t e = 0; e < m; ++e)
-    if (col[e] < 0 || col[e] >= n) return Status{GOPS_ERR_INVALID, "neighbor index out of range"};
   return Status::ok();
+}
+
+// flags[0]: some row_ptr[u+1] < row_ptr[u]; flags[1]: some col outside [0, n)
+__global__ void csr_checks(int64_t n, const int64_t *rp, int64_t m, const int32_t *col, int *flags) {
+  int bad_rp = 0, bad_col = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += stride)
+    bad_rp |= rp[u + 1] < rp[u];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += stride)
+    bad_col |= (col[e] < 0) | (col[e] >= n);
+  if (__any_sync(0xffffffffu, bad_rp) && (threadIdx.x & 31) == 0) atomicOr(&flags[0], 1);
+  if (__any_sync(0xffffffffu, bad_col) && (threadIdx.x & 31) == 0) atomicOr(&flags[1], 1);
 }
 
 Status upload_impl(Ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *col,
@@ -64,7 +76,22 @@ Status upload_impl(Ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *c
   if (e != cudaSuccess) st = fail(e, "graph upload");
   else {
     ctx->stats.h2d_bytes += sizeof(int64_t) * (n + 1) + sizeof(int32_t) * m + (w ? sizeof(double) * m : 0);
-    st = graph_build_from_out_csr_device(ctx, g, d_rp, d_col, d_w);
+    // the same checks (and messages, in the same order) the host would make
+    int *d_flags = nullptr;
+    int flags[2] = {0, 0};
+    e = cudaMallocAsync((void **)&d_flags, sizeof(int) * 2, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_flags, 0, sizeof(int) * 2, s);
+    if (e == cudaSuccess) {
+      csr_checks<<<blocks_for(std::max(n, m), 256, ctx->num_sms * 8), 256, 0, s>>>(n, d_rp, m, d_col, d_flags);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(flags, d_flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    free_async(d_flags, s);
+    if (e != cudaSuccess) st = fail(e, "graph upload");
+    else if (flags[0]) st = Status{GOPS_ERR_INVALID, "row_ptr must be non-decreasing"};
+    else if (flags[1]) st = Status{GOPS_ERR_INVALID, "neighbor index out of range"};
+    else st = graph_build_from_out_csr_device(ctx, g, d_rp, d_col, d_w);
   }
   if (st.code == GOPS_OK) {  // kept: the out-adjacency drives eigenvector centrality
     g->out_rp = d_rp;

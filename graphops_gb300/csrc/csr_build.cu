@@ -24,26 +24,75 @@ namespace gops {
 
 namespace {
 
+// Per out-row u: out-degree, source id of every entry, and (weighted) the
+// transition weight max(w,0) / sum_u max(w,0) in FP32 with the weighted-
+// dangling bit.  Rows of at most kRowBig entries (nearly all: R-MAT rows
+// average ~16): an 8-lane group per row in a persistent grid, the FP64 sum in
+// a fixed order per group (the shuffles name the group only: groups of a warp
+// run different numbers of rows).  Longer rows (hubs, up to ~1e5 entries): a
+// block per row in out_row_pass_big, a fixed-order block sum; the small pass
+// lists them in big[1..big[0]] (list order varies, per-row results do not).
+constexpr int kRowLanes = 8;
+constexpr int64_t kRowBig = 256;
 __global__ void out_row_pass(int64_t n, const int64_t *__restrict__ rp, const double *__restrict__ w,
                              uint32_t *__restrict__ src, float *__restrict__ val_out,
-                             float *__restrict__ deg_f, uint32_t *__restrict__ dmask) {
-  const int lane = threadIdx.x & 31;
-  const int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (u >= n) return;
-  const int64_t b = rp[u], e = rp[u + 1];
-  if (lane == 0) deg_f[u] = (float)(e - b);
-  for (int64_t i = b + lane; i < e; i += 32) src[i] = (uint32_t)u;
-  if (w) {
-    double s = 0.0;
-    for (int64_t i = b + lane; i < e; i += 32) s += fmax(w[i], 0.0);
+                             float *__restrict__ deg_f, uint32_t *__restrict__ dmask,
+                             uint32_t *__restrict__ big) {
+  const int lane = threadIdx.x & (kRowLanes - 1);
+  const unsigned gmask = ((1u << kRowLanes) - 1u) << ((threadIdx.x & 31) & ~(kRowLanes - 1));
+  const int64_t groups = (int64_t)gridDim.x * (blockDim.x / kRowLanes);
+  for (int64_t u = (int64_t)blockIdx.x * (blockDim.x / kRowLanes) + threadIdx.x / kRowLanes; u < n; u += groups) {
+    const int64_t b = rp[u], e = rp[u + 1];
+    if (e - b > kRowBig) {  // the whole group skips: same row
+      if (lane == 0) big[1 + atomicAdd(&big[0], 1u)] = (uint32_t)u;
+      continue;
+    }
+    if (lane == 0) deg_f[u] = (float)(e - b);
+    for (int64_t i = b + lane; i < e; i += kRowLanes) src[i] = (uint32_t)u;
+    if (w) {
+      double s = 0.0;
+      for (int64_t i = b + lane; i < e; i += kRowLanes) s += fmax(w[i], 0.0);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    const double inv = s > 0.0 ? 1.0 / s : 0.0;
-    for (int64_t i = b + lane; i < e; i += 32) {
+      for (int o = kRowLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, kRowLanes);
+      const double inv = s > 0.0 ? 1.0 / s : 0.0;
+      for (int64_t i = b + lane; i < e; i += kRowLanes) {
+        const double wc = fmax(w[i], 0.0);
+        val_out[i] = wc > 0.0 ? (float)(wc * inv) : 0.0f;
+      }
+      if (lane == 0 && s == 0.0) atomicOr(&dmask[u >> 5], 1u << (u & 31));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) out_row_pass_big(int64_t n, const int64_t *__restrict__ rp,
+                                                         const double *__restrict__ w, uint32_t *__restrict__ src,
+                                                         float *__restrict__ val_out, float *__restrict__ deg_f,
+                                                         uint32_t *__restrict__ dmask,
+                                                         const uint32_t *__restrict__ big) {
+  __shared__ double sh[256];
+  const uint32_t nbig = big[0];
+  for (uint32_t k = blockIdx.x; k < nbig; k += gridDim.x) {  // uniform per block
+    const int64_t u = big[1 + k];
+    const int64_t b = rp[u], e = rp[u + 1];
+    if (threadIdx.x == 0) deg_f[u] = (float)(e - b);
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) src[i] = (uint32_t)u;
+    if (!w) continue;
+    double s = 0.0;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) s += fmax(w[i], 0.0);
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+    }
+    const double tot = sh[0];
+    __syncthreads();
+    const double inv = tot > 0.0 ? 1.0 / tot : 0.0;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
       const double wc = fmax(w[i], 0.0);
       val_out[i] = wc > 0.0 ? (float)(wc * inv) : 0.0f;
     }
-    if (lane == 0 && s == 0.0) atomicOr(&dmask[u >> 5], 1u << (u & 31));
+    if (threadIdx.x == 0 && tot == 0.0) atomicOr(&dmask[u >> 5], 1u << (u & 31));
   }
 }
 
@@ -234,12 +283,13 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   int64_t *rp_old = nullptr, *new_deg = nullptr, *small = nullptr;
   int32_t *inv_perm = nullptr;
   unsigned *maxdeg = nullptr;
+  uint32_t *bigrows = nullptr;
   auto cleanup = [&]() {
     free_async(src, s); free_async(keys, s); free_async(vals, s); free_async(keys2, s);
     free_async(vals2, s); free_async(nk, s); free_async(nv, s); free_async(nk2, s);
     free_async(nv2, s); free_async(dmask_old, s); free_async(val_out, s); free_async(deg_old, s);
     free_async(rp_old, s); free_async(new_deg, s); free_async(small, s); free_async(inv_perm, s);
-    free_async(maxdeg, s);
+    free_async(maxdeg, s); free_async(bigrows, s);
   };
 #define BUILD_TRY(expr)                                                                     \
   do {                                                                                      \
@@ -271,8 +321,14 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   }
   BUILD_TRY(cudaMallocAsync((void **)&src, sizeof(uint32_t) * mm, s));
   if (n > 0) {
-    out_row_pass<<<(unsigned)ceil_div<int64_t>(n, 8), 256, 0, s>>>(n, d_out_rp, d_w, src, val_out,
-                                                                   deg_old, dmask_old);
+    // rows longer than kRowBig: at most m / (kRowBig + 1) of them
+    const int64_t nbig_cap = std::min<int64_t>(n, m / (kRowBig + 1)) + 1;
+    BUILD_TRY(cudaMallocAsync((void **)&bigrows, sizeof(uint32_t) * nbig_cap, s));
+    BUILD_TRY(cudaMemsetAsync(bigrows, 0, sizeof(uint32_t), s));
+    out_row_pass<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
+        n, d_out_rp, d_w, src, val_out, deg_old, dmask_old, bigrows);
+    out_row_pass_big<<<ctx->num_sms * 4, 256, 0, s>>>(n, d_out_rp, d_w, src, val_out, deg_old, dmask_old,
+                                                      bigrows);
     BUILD_TRY(cudaGetLastError());
   }
   // K1: stable sort of edge ids by destination

@@ -46,20 +46,28 @@ enum Mode : int { kPlain = 0, kWeighted = 1, kPpr = 2 };
 constexpr int kThreads = 256;  // init / small kernels
 constexpr int kWarps = kThreads / kWarp;
 #ifndef GOPS_BLOCK
-#define GOPS_BLOCK 256
+#define GOPS_BLOCK 1024
 #endif
 #ifndef GOPS_GCACHE
-#define GOPS_GCACHE 0
+#define GOPS_GCACHE 32768
+#endif
+#ifndef GOPS_GCACHE_U
+#define GOPS_GCACHE_U 0
 #endif
 #ifndef GOPS_L1HINT
 #define GOPS_L1HINT 0
 #endif
-// iteration kernels: threads per block, and how many of the first (hottest,
-// after the in-degree relabelling) entries of the gathered vector each block
-// stages in shared memory (FP32 entries; half as many double-float ones)
+// iteration kernels: threads per block (one block per SM), and how many of
+// the first (hottest, after the in-degree relabelling) entries of the FP32
+// gathered vector each block of the FP32 phase stages in shared memory:
+// kGCache when the step reads transition weights, kGCacheU when it does not
+// (measured at R-MAT 22: a 32 K-entry cache takes the weighted FP32 step from
+// 0.246 to 0.231 ms; it does not pay for the unweighted step, nor for the
+// double-float phase, whose 8-byte entries halve what fits).
 constexpr int kIterThreads = GOPS_BLOCK;
 constexpr int kIterWarps = kIterThreads / kWarp;
 constexpr int kGCache = GOPS_GCACHE;
+constexpr int kGCacheU = GOPS_GCACHE_U;
 constexpr bool kL1Hint = GOPS_L1HINT != 0;
 #ifndef GOPS_L1POL
 #define GOPS_L1POL 0
@@ -76,7 +84,7 @@ constexpr int kL1Hot = GOPS_L1HOT;
 #define GOPS_UNROLL 4
 #endif
 #ifndef GOPS_MINB
-#define GOPS_MINB 4
+#define GOPS_MINB 1
 #endif
 constexpr int kUnroll = GOPS_UNROLL;   // edges per lane per round and row
 constexpr int kMinBlocks = GOPS_MINB;  // occupancy hint for the iteration kernels
@@ -183,18 +191,14 @@ struct PrecDF {
   __device__ static T zero() { return {0.0f, 0.0f}; }
   __device__ static T add(T a, T b) { return df_add(a, b); }
   __device__ static T shfl(T v, int m) { return shfl_xor_df(v, m, 32); }
-  static constexpr int kCached = kGCache / 2;  // float2 entries staged in shared memory
-  __device__ static T load_g(const IterParams &p, const void *cache, int32_t u) {
-    float2 g;
-    if (kCached > 0 && u < kCached) g = reinterpret_cast<const float2 *>(cache)[u];
-    else g = ld_gather_f2(p.gdf_in, u);
+  static constexpr bool kCache = false;
+  template <int NC>
+  __device__ static T load_g(const IterParams &p, const void *, int32_t u) {
+    const float2 g = ld_gather_f2(p.gdf_in, u);
     return {g.x, g.y};
   }
-  __device__ static void stage(const IterParams &p, void *cache, int64_t n) {
-    float2 *c = reinterpret_cast<float2 *>(cache);
-    const int lim = (int)(n < (int64_t)kCached ? n : (int64_t)kCached);
-    for (int i = threadIdx.x; i < lim; i += blockDim.x) c[i] = __ldg(&p.gdf_in[i]);
-  }
+  template <int NC>
+  __device__ static void stage(const IterParams &, void *) {}
   __device__ static T scale(T g, float w) { return df_mul_f(g, w); }
   __device__ static float2 pack(T v) { return make_float2(v.hi, v.lo); }
   __device__ static T unpack(float2 v) { return {v.x, v.y}; }
@@ -206,20 +210,30 @@ struct PrecF32 {
   __device__ static T zero() { return 0.0f; }
   __device__ static T add(T a, T b) { return a + b; }
   __device__ static T shfl(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
-  static constexpr int kCached = kGCache;
+  static constexpr bool kCache = true;
+  // entries [0, NC) come from shared memory (u <= n: entries past n + 1 are
+  // staged by no block and read by no edge)
+  template <int NC>
   __device__ static T load_g(const IterParams &p, const void *cache, int32_t u) {
-    if (kCached > 0 && u < kCached) return reinterpret_cast<const float *>(cache)[u];
+    if (NC > 0 && u < NC) return reinterpret_cast<const float *>(cache)[u];
     return ld_gather_f32(p.gf_in, u);
   }
-  __device__ static void stage(const IterParams &p, void *cache, int64_t n) {
+  template <int NC>
+  __device__ static void stage(const IterParams &p, void *cache) {
     float *c = reinterpret_cast<float *>(cache);
-    const int lim = (int)(n < (int64_t)kCached ? n : (int64_t)kCached);
+    const int lim = (int)(p.n + 1 < (int64_t)NC ? p.n + 1 : (int64_t)NC);  // entry n: padding
     for (int i = threadIdx.x; i < lim; i += blockDim.x) c[i] = __ldg(&p.gf_in[i]);
   }
   __device__ static T scale(T g, float w) { return g * w; }
   __device__ static float2 pack(T v) { return make_float2(v, 0.0f); }
   __device__ static T unpack(float2 v) { return v.x; }
 };
+
+// FP32 entries of the gathered vector staged in shared memory per block
+template <class P, int MODE>
+__host__ __device__ constexpr int cache_entries() {
+  return P::kCache ? (MODE == kWeighted ? kGCache : kGCacheU) : 0;
+}
 
 struct Acc {
   long long l1 = 0, dang = 0;
@@ -336,6 +350,7 @@ template <class P, int MODE, int R>
 __device__ __forceinline__ void rows_sum(const IterParams &p, const void *cache,
                                          const int32_t (&eb)[R], const int32_t (&ee)[R], int li,
                                          int SW, typename P::T (&s)[R]) {
+  constexpr int NC = cache_entries<P, MODE>();
   int32_t len = 0;
 #pragma unroll
   for (int q = 0; q < R; ++q) {
@@ -365,10 +380,10 @@ __device__ __forceinline__ void rows_sum(const IterParams &p, const void *cache,
       for (int q = 0; q < R; ++q)
 #pragma unroll
         for (int j = 0; j < QU; ++j) {
-          g[q][j][0] = ok[q][j] ? P::load_g(p, cache, c[q][j].x) : P::zero();
-          g[q][j][1] = ok[q][j] ? P::load_g(p, cache, c[q][j].y) : P::zero();
-          g[q][j][2] = ok[q][j] ? P::load_g(p, cache, c[q][j].z) : P::zero();
-          g[q][j][3] = ok[q][j] ? P::load_g(p, cache, c[q][j].w) : P::zero();
+          g[q][j][0] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j].x) : P::zero();
+          g[q][j][1] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j].y) : P::zero();
+          g[q][j][2] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j].z) : P::zero();
+          g[q][j][3] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j].w) : P::zero();
         }
 #pragma unroll
       for (int q = 0; q < R; ++q)
@@ -407,7 +422,7 @@ __device__ __forceinline__ void rows_sum(const IterParams &p, const void *cache,
 #pragma unroll
     for (int q = 0; q < R; ++q)
 #pragma unroll
-      for (int j = 0; j < kUnroll; ++j) g[q][j] = ok[q][j] ? P::load_g(p, cache, c[q][j]) : P::zero();
+      for (int j = 0; j < kUnroll; ++j) g[q][j] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j]) : P::zero();
 #pragma unroll
     for (int q = 0; q < R; ++q)
 #pragma unroll
@@ -484,9 +499,11 @@ __global__ void __launch_bounds__(kIterThreads, kMinBlocks) iterate_kernel(IterP
   extern __shared__ __align__(16) unsigned char gcache[];
   df dsum;
   if (!prologue<P::kDF>(p, &dsum)) return;
-  if constexpr (P::kCached > 0) {
-    P::stage(p, gcache, p.n);
-    __syncthreads();
+  if constexpr (P::kCache) {
+    if (cache_entries<P, MODE>() > 0) {
+      P::template stage<cache_entries<P, MODE>()>(p, gcache);
+      __syncthreads();
+    }
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nwarps = gridDim.x * kIterWarps;
@@ -602,14 +619,14 @@ Status workspace_ensure(Ctx *ctx, Graph *g) {
 
 namespace {
 
-template <class P>
+template <class P, int MODE>
 size_t iter_smem(const Graph *g) {
-  return P::kCached > 0 ? sizeof(typename P::T) * (size_t)std::min<int64_t>(g->n, P::kCached) : 0;
+  return sizeof(float) * (size_t)std::min<int64_t>(g->n + 1, cache_entries<P, MODE>());
 }
 
 template <class P, int MODE>
 int grid_for_iter(const Ctx *ctx, const Graph *g) {
-  const size_t smem = iter_smem<P>(g);
+  const size_t smem = iter_smem<P, MODE>(g);
   int occ = 0;
   if (smem > 0)
     cudaFuncSetAttribute(iterate_kernel<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -676,7 +693,7 @@ Status run_mode(Ctx *ctx, Graph *g, Workspace &ws, const gops_config *cfg, doubl
 
   const int grid_df = grid_for_iter<PrecDF, MODE>(ctx, g);
   const int grid_f = grid_for_iter<PrecF32, MODE>(ctx, g);
-  const size_t smem_df = iter_smem<PrecDF>(g), smem_f = iter_smem<PrecF32>(g);
+  const size_t smem_df = iter_smem<PrecDF, MODE>(g), smem_f = iter_smem<PrecF32, MODE>(g);
   bool f32_known = false;
   unsigned long long k = 1;
   const int chunk = 4;

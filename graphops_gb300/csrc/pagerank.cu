@@ -80,6 +80,14 @@ constexpr bool kL1Hint = GOPS_L1HINT != 0;
 // marked evict-last, so L1 holds the hot prefix of the gathered vector.
 constexpr bool kL1Policy = GOPS_L1POL != 0;
 constexpr int kL1Hot = GOPS_L1HOT;
+#ifndef GOPS_L2STREAM
+#define GOPS_L2STREAM 0
+#endif
+#ifndef GOPS_L2GATHER
+#define GOPS_L2GATHER 0
+#endif
+constexpr bool kL2Stream = GOPS_L2STREAM != 0;
+constexpr bool kL2Gather = GOPS_L2GATHER != 0;
 #ifndef GOPS_UNROLL
 #define GOPS_UNROLL 4
 #endif
@@ -120,9 +128,25 @@ struct IterParams {
 
 // Streamed loads (column indices, transition weights): with kL1Hint they do
 // not allocate in L1, which then keeps the hot lines of the gathered vector.
+// L2 policies (kL2Stream / kL2Gather): the edge streams, read once per step,
+// are loaded evict-first and the gathered vector (re-read ~16 times per step)
+// evict-last, so the streams do not push the gathered vector out of L2.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ uint64_t l2_evict_last() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
 __device__ __forceinline__ int4 ld_stream_v4i(const int32_t *a) {
   int4 v;
-  if constexpr (kL1Hint || kL1Policy) {
+  if constexpr (kL2Stream) {
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.s32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(a), "l"(l2_evict_first()));
+  } else if constexpr (kL1Hint || kL1Policy) {
     asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0,%1,%2,%3}, [%4];"
                  : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(a));
   } else {
@@ -132,7 +156,10 @@ __device__ __forceinline__ int4 ld_stream_v4i(const int32_t *a) {
 }
 __device__ __forceinline__ float4 ld_stream_v4f(const float *a) {
   float4 v;
-  if constexpr (kL1Hint || kL1Policy) {
+  if constexpr (kL2Stream) {
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(a), "l"(l2_evict_first()));
+  } else if constexpr (kL1Hint || kL1Policy) {
     asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
                  : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(a));
   } else {
@@ -142,7 +169,11 @@ __device__ __forceinline__ float4 ld_stream_v4f(const float *a) {
 }
 // gathers under the L1 policy
 __device__ __forceinline__ float ld_gather_f32(const float *base, int32_t u) {
-  if constexpr (kL1Policy) {
+  if constexpr (kL2Gather) {
+    float v;
+    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(base + u), "l"(l2_evict_last()));
+    return v;
+  } else if constexpr (kL1Policy) {
     float v;
     if (u < kL1Hot) asm volatile("ld.global.nc.L1::evict_last.f32 %0, [%1];" : "=f"(v) : "l"(base + u));
     else asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(base + u));
@@ -152,7 +183,12 @@ __device__ __forceinline__ float ld_gather_f32(const float *base, int32_t u) {
   }
 }
 __device__ __forceinline__ float2 ld_gather_f2(const float2 *base, int32_t u) {
-  if constexpr (kL1Policy) {
+  if constexpr (kL2Gather) {
+    float2 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0,%1}, [%2], %3;"
+                 : "=f"(v.x), "=f"(v.y) : "l"(base + u), "l"(l2_evict_last()));
+    return v;
+  } else if constexpr (kL1Policy) {
     float2 v;
     if (u < kL1Hot / 2)
       asm volatile("ld.global.nc.L1::evict_last.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(base + u));
@@ -164,7 +200,11 @@ __device__ __forceinline__ float2 ld_gather_f2(const float2 *base, int32_t u) {
   }
 }
 __device__ __forceinline__ int32_t ld_stream_i32(const int32_t *a) {
-  if constexpr (kL1Hint || kL1Policy) {
+  if constexpr (kL2Stream) {
+    int32_t v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(l2_evict_first()));
+    return v;
+  } else if constexpr (kL1Hint || kL1Policy) {
     int32_t v;
     asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(a));
     return v;
@@ -173,7 +213,11 @@ __device__ __forceinline__ int32_t ld_stream_i32(const int32_t *a) {
   }
 }
 __device__ __forceinline__ float ld_stream_f32(const float *a) {
-  if constexpr (kL1Hint || kL1Policy) {
+  if constexpr (kL2Stream) {
+    float v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(l2_evict_first()));
+    return v;
+  } else if constexpr (kL1Hint || kL1Policy) {
     float v;
     asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(a));
     return v;

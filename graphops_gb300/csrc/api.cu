@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "objects.cuh"
@@ -15,6 +16,40 @@ Status dense_to_out_csr_device(Ctx *ctx, int64_t n, const double *d_M, int64_t *
 Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, const int64_t *seed_ptr,
                  const int32_t *seed_idx, const float *x0, bool x0_on_device, float *scores,
                  bool scores_on_device, gops_run *runs, const double *r1_max, int32_t *rejected);
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pool[kMaxDevices] = {};
+static bool g_pool_tried[kMaxDevices] = {};
+
+cudaMemPool_t library_pool(int device) {
+  if (device < 0 || device >= kMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (!g_pool_tried[device]) {
+    g_pool_tried[device] = true;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) == cudaSuccess)
+        g_pool[device] = pool;
+      else
+        cudaMemPoolDestroy(pool);
+    }
+    cudaGetLastError();  // a failed creation leaves the default pool in use
+  }
+  return g_pool[device];
+}
+
+void library_pool_trim(int device) {
+  if (device < 0 || device >= kMaxDevices) return;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (g_pool[device]) cudaMemPoolTrimTo(g_pool[device], 0);
+}
 }  // namespace gops
 
 using namespace gops;
@@ -67,19 +102,29 @@ Status upload_impl(Ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *c
     return Status{e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA,
                   std::string(what) + ": " + cudaGetErrorString(e)};
   };
-  cudaError_t e = cudaMallocAsync((void **)&d_rp, sizeof(int64_t) * (n + 1), s);
-  if (e == cudaSuccess) e = cudaMallocAsync((void **)&d_col, sizeof(int32_t) * (m > 0 ? m : 1), s);
-  if (e == cudaSuccess && w) e = cudaMallocAsync((void **)&d_w, sizeof(double) * (m > 0 ? m : 1), s);
+  cudaError_t e = dev_malloc_async((void **)&d_rp, sizeof(int64_t) * (n + 1), s);
+  if (e == cudaSuccess) e = dev_malloc_async((void **)&d_col, sizeof(int32_t) * (m > 0 ? m : 1), s);
+  if (e == cudaSuccess && w) e = dev_malloc_async((void **)&d_w, sizeof(double) * (m > 0 ? m : 1), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_rp, row_ptr, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(d_col, col, sizeof(int32_t) * m, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess && w && m > 0) e = cudaMemcpyAsync(d_w, w, sizeof(double) * m, cudaMemcpyHostToDevice, s);
+  // the weights (the largest array) follow on the copy stream while the
+  // checks and the edge sort, which do not read them, run on the main stream
+  bool w_async = false;
+  if (e == cudaSuccess && w && m > 0) {
+    e = cudaEventRecord(ctx->copy_ev[0], s);  // after d_w's allocation and the column copy
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[0], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_w, w, sizeof(double) * m, cudaMemcpyHostToDevice, ctx->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->copy_ev[1], ctx->copy_stream);
+    w_async = e == cudaSuccess;
+  }
   if (e != cudaSuccess) st = fail(e, "graph upload");
   else {
     ctx->stats.h2d_bytes += sizeof(int64_t) * (n + 1) + sizeof(int32_t) * m + (w ? sizeof(double) * m : 0);
     // the same checks (and messages, in the same order) the host would make
     int *d_flags = nullptr;
     int flags[2] = {0, 0};
-    e = cudaMallocAsync((void **)&d_flags, sizeof(int) * 2, s);
+    e = dev_malloc_async((void **)&d_flags, sizeof(int) * 2, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_flags, 0, sizeof(int) * 2, s);
     if (e == cudaSuccess) {
       csr_checks<<<blocks_for(std::max(n, m), 256, ctx->num_sms * 8), 256, 0, s>>>(n, d_rp, m, d_col, d_flags);
@@ -91,8 +136,10 @@ Status upload_impl(Ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *c
     if (e != cudaSuccess) st = fail(e, "graph upload");
     else if (flags[0]) st = Status{GOPS_ERR_INVALID, "row_ptr must be non-decreasing"};
     else if (flags[1]) st = Status{GOPS_ERR_INVALID, "neighbor index out of range"};
-    else st = graph_build_from_out_csr_device(ctx, g, d_rp, d_col, d_w);
+    else st = graph_build_from_out_csr_device(ctx, g, d_rp, d_col, d_w, w_async ? ctx->copy_ev[1] : nullptr);
   }
+  // every path: the main stream passes the weight copy before d_w is freed
+  if (w_async) cudaStreamWaitEvent(s, ctx->copy_ev[1], 0);
   if (st.code == GOPS_OK) {  // kept: the out-adjacency drives eigenvector centrality
     g->out_rp = d_rp;
     g->out_col = d_col;
@@ -127,6 +174,8 @@ int gops_ctx_create(int device, gops_ctx **out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost((void **)&x.host_state, sizeof(SolveState));
   for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&x.ev[i]);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x.copy_stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&x.copy_ev[i], cudaEventDisableTiming);
   if (e != cudaSuccess) {
     gops_ctx_destroy(c);
     return e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA;
@@ -142,9 +191,14 @@ void gops_ctx_destroy(gops_ctx *ctx) {
   if (x.stream) cudaStreamSynchronize(x.stream);
   for (int i = 0; i < 4; ++i)
     if (x.ev[i]) cudaEventDestroy(x.ev[i]);
+  if (x.copy_stream) cudaStreamSynchronize(x.copy_stream);
+  for (int i = 0; i < 2; ++i)
+    if (x.copy_ev[i]) cudaEventDestroy(x.copy_ev[i]);
+  if (x.copy_stream) cudaStreamDestroy(x.copy_stream);
   if (x.host_state) cudaFreeHost(x.host_state);
   for (cudaEvent_t e : x.tev) cudaEventDestroy(e);
   if (x.stream) cudaStreamDestroy(x.stream);
+  library_pool_trim(x.device);  // memory that no live graph or model holds
   delete ctx;
 }
 
@@ -243,7 +297,7 @@ int gops_graph_from_dense(gops_ctx *ctx, int64_t n, const double *matrix, gops_g
   int64_t m = 0;
   Status st;
   const size_t bytes = sizeof(double) * (size_t)std::max<int64_t>(n * n, 1);
-  cudaError_t e = cudaMallocAsync((void **)&d_M, bytes, s);
+  cudaError_t e = dev_malloc_async((void **)&d_M, bytes, s);
   if (e == cudaSuccess && n > 0) e = cudaMemcpyAsync(d_M, matrix, sizeof(double) * (size_t)(n * n), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) st = Status{e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA,
                                     std::string("dense upload: ") + cudaGetErrorString(e)};

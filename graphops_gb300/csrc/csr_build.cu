@@ -272,7 +272,8 @@ void graph_free_device(Graph &g) {
 }
 
 Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_rp,
-                                       const int32_t *d_out_col, const double *d_w) {
+                                       const int32_t *d_out_col, const double *d_w,
+                                       cudaEvent_t w_ready) {
   cudaStream_t s = ctx->stream;
   const int64_t n = g->n, m = g->m;
   g->weighted = d_w != nullptr;
@@ -308,34 +309,22 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   const size_t mm = (size_t)std::max<int64_t>(m, 1) + 64;  // padded edge arrays
   const size_t nn = (size_t)std::max<int64_t>(n, 1);
   const size_t nwords = (size_t)(n / 32 + 1);
-  BUILD_TRY(cudaMalloc(&g->in_rp, sizeof(int64_t) * (n + 1)));
-  BUILD_TRY(cudaMalloc(&g->deg, sizeof(float) * nn));
-  BUILD_TRY(cudaMalloc(&g->perm, sizeof(int32_t) * nn));
-  BUILD_TRY(cudaMallocAsync((void **)&deg_old, sizeof(float) * nn, s));
+  BUILD_TRY(dev_malloc_async(&g->in_rp, sizeof(int64_t) * (n + 1), s));
+  BUILD_TRY(dev_malloc_async(&g->deg, sizeof(float) * nn, s));
+  BUILD_TRY(dev_malloc_async(&g->perm, sizeof(int32_t) * nn, s));
+  BUILD_TRY(dev_malloc_async((void **)&deg_old, sizeof(float) * nn, s));
   if (g->weighted) {
-    BUILD_TRY(cudaMalloc(&g->dmask_w, sizeof(uint32_t) * nwords));
+    BUILD_TRY(dev_malloc_async(&g->dmask_w, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(cudaMemsetAsync(g->dmask_w, 0, sizeof(uint32_t) * nwords, s));
-    BUILD_TRY(cudaMallocAsync((void **)&dmask_old, sizeof(uint32_t) * nwords, s));
+    BUILD_TRY(dev_malloc_async((void **)&dmask_old, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(cudaMemsetAsync(dmask_old, 0, sizeof(uint32_t) * nwords, s));
-    BUILD_TRY(cudaMallocAsync((void **)&val_out, sizeof(float) * mm, s));
-  }
-  BUILD_TRY(cudaMallocAsync((void **)&src, sizeof(uint32_t) * mm, s));
-  if (n > 0) {
-    // rows longer than kRowBig: at most m / (kRowBig + 1) of them
-    const int64_t nbig_cap = std::min<int64_t>(n, m / (kRowBig + 1)) + 1;
-    BUILD_TRY(cudaMallocAsync((void **)&bigrows, sizeof(uint32_t) * nbig_cap, s));
-    BUILD_TRY(cudaMemsetAsync(bigrows, 0, sizeof(uint32_t), s));
-    out_row_pass<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
-        n, d_out_rp, d_w, src, val_out, deg_old, dmask_old, bigrows);
-    out_row_pass_big<<<ctx->num_sms * 4, 256, 0, s>>>(n, d_out_rp, d_w, src, val_out, deg_old, dmask_old,
-                                                      bigrows);
-    BUILD_TRY(cudaGetLastError());
+    BUILD_TRY(dev_malloc_async((void **)&val_out, sizeof(float) * mm, s));
   }
   // K1: stable sort of edge ids by destination
-  BUILD_TRY(cudaMallocAsync((void **)&keys, sizeof(uint32_t) * mm, s));
-  BUILD_TRY(cudaMallocAsync((void **)&vals, sizeof(uint32_t) * mm, s));
-  BUILD_TRY(cudaMallocAsync((void **)&keys2, sizeof(uint32_t) * mm, s));
-  BUILD_TRY(cudaMallocAsync((void **)&vals2, sizeof(uint32_t) * mm, s));
+  BUILD_TRY(dev_malloc_async((void **)&keys, sizeof(uint32_t) * mm, s));
+  BUILD_TRY(dev_malloc_async((void **)&vals, sizeof(uint32_t) * mm, s));
+  BUILD_TRY(dev_malloc_async((void **)&keys2, sizeof(uint32_t) * mm, s));
+  BUILD_TRY(dev_malloc_async((void **)&vals2, sizeof(uint32_t) * mm, s));
   uint32_t *K = keys, *O = vals;
   if (m > 0) {
     copy_keys<<<grid_for(m, 256), 256, 0, s>>>(d_out_col, keys, m);
@@ -345,18 +334,32 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_ST(radix_sort_pairs_u32(keys, vals, keys2, vals2, m, bits_for(n), &alt, s));
     if (alt) { K = keys2; O = vals2; }
   }
-  BUILD_TRY(cudaMallocAsync((void **)&rp_old, sizeof(int64_t) * (n + 1), s));
+  BUILD_TRY(dev_malloc_async((void **)&src, sizeof(uint32_t) * mm, s));
+  // the out-row pass is the first reader of the weights
+  if (w_ready) BUILD_TRY(cudaStreamWaitEvent(s, w_ready, 0));
+  if (n > 0) {
+    // rows longer than kRowBig: at most m / (kRowBig + 1) of them
+    const int64_t nbig_cap = std::min<int64_t>(n, m / (kRowBig + 1)) + 1;
+    BUILD_TRY(dev_malloc_async((void **)&bigrows, sizeof(uint32_t) * nbig_cap, s));
+    BUILD_TRY(cudaMemsetAsync(bigrows, 0, sizeof(uint32_t), s));
+    out_row_pass<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
+        n, d_out_rp, d_w, src, val_out, deg_old, dmask_old, bigrows);
+    out_row_pass_big<<<ctx->num_sms * 4, 256, 0, s>>>(n, d_out_rp, d_w, src, val_out, deg_old, dmask_old,
+                                                      bigrows);
+    BUILD_TRY(cudaGetLastError());
+  }
+  BUILD_TRY(dev_malloc_async((void **)&rp_old, sizeof(int64_t) * (n + 1), s));
   rp_from_sorted<<<grid_for(m + 1, 256), 256, 0, s>>>(K, m, n, rp_old);
   BUILD_TRY(cudaGetLastError());
   // K2: relabel by in-degree, descending (stable: ties keep id order)
-  BUILD_TRY(cudaMallocAsync((void **)&maxdeg, sizeof(unsigned), s));
+  BUILD_TRY(dev_malloc_async((void **)&maxdeg, sizeof(unsigned), s));
   BUILD_TRY(cudaMemsetAsync(maxdeg, 0, sizeof(unsigned), s));
-  BUILD_TRY(cudaMallocAsync((void **)&nk, sizeof(uint32_t) * nn, s));
-  BUILD_TRY(cudaMallocAsync((void **)&nv, sizeof(uint32_t) * nn, s));
-  BUILD_TRY(cudaMallocAsync((void **)&nk2, sizeof(uint32_t) * nn, s));
-  BUILD_TRY(cudaMallocAsync((void **)&nv2, sizeof(uint32_t) * nn, s));
-  BUILD_TRY(cudaMallocAsync((void **)&inv_perm, sizeof(int32_t) * nn, s));
-  BUILD_TRY(cudaMallocAsync((void **)&new_deg, sizeof(int64_t) * (n + 1), s));
+  BUILD_TRY(dev_malloc_async((void **)&nk, sizeof(uint32_t) * nn, s));
+  BUILD_TRY(dev_malloc_async((void **)&nv, sizeof(uint32_t) * nn, s));
+  BUILD_TRY(dev_malloc_async((void **)&nk2, sizeof(uint32_t) * nn, s));
+  BUILD_TRY(dev_malloc_async((void **)&nv2, sizeof(uint32_t) * nn, s));
+  BUILD_TRY(dev_malloc_async((void **)&inv_perm, sizeof(int32_t) * nn, s));
+  BUILD_TRY(dev_malloc_async((void **)&new_deg, sizeof(int64_t) * (n + 1), s));
   unsigned md = 0;
   uint32_t *SK = nk, *SV = nv;
   if (n > 0) {
@@ -388,7 +391,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   BUILD_TRY(cudaStreamSynchronize(s));
   g->m_stored = m_stored;
   const size_t ms = (size_t)std::max<int64_t>(m_stored, 1) + 64;  // +64: vector loads past the end
-  BUILD_TRY(cudaMalloc(&g->in_col, sizeof(int32_t) * ms));
+  BUILD_TRY(dev_malloc_async(&g->in_col, sizeof(int32_t) * ms, s));
   if (kRowAlign > 1) {
     fill_i32<<<grid_for((int64_t)ms, 256), 256, 0, s>>>(g->in_col, (int64_t)ms, (int32_t)n);
     BUILD_TRY(cudaGetLastError());
@@ -396,7 +399,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(cudaMemsetAsync(g->in_col, 0, sizeof(int32_t) * ms, s));
   }
   if (g->weighted) {
-    BUILD_TRY(cudaMalloc(&g->in_val, sizeof(float) * ms));
+    BUILD_TRY(dev_malloc_async(&g->in_val, sizeof(float) * ms, s));
     BUILD_TRY(cudaMemsetAsync(g->in_val, 0, sizeof(float) * ms, s));
   }
   if (m > 0) {
@@ -408,7 +411,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   const int L = kLaneEdges;
   const int64_t thr_h[7] = {kHubThreshold + 1, 32 * L, 16 * L, 8 * L, 4 * L, 2 * L, 0};
   int64_t cnt_h[7] = {0, 0, 0, 0, 0, 0, 0};
-  BUILD_TRY(cudaMallocAsync((void **)&small, sizeof(int64_t) * 16, s));
+  BUILD_TRY(dev_malloc_async((void **)&small, sizeof(int64_t) * 16, s));
   if (n > 0) {
     BUILD_TRY(cudaMemcpyAsync(small, thr_h, sizeof(thr_h), cudaMemcpyHostToDevice, s));
     count_ge<<<1, 32, 0, s>>>(SK, n, maxdeg, small, 7, small + 8);
@@ -436,7 +439,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   // hub tasks
   if (pl.n_hub > 0) {
     int64_t *nch = nullptr;
-    BUILD_TRY(cudaMallocAsync((void **)&nch, sizeof(int64_t) * (pl.n_hub + 1), s));
+    BUILD_TRY(dev_malloc_async((void **)&nch, sizeof(int64_t) * (pl.n_hub + 1), s));
     hub_chunks<<<grid_for(pl.n_hub + 1, 256), 256, 0, s>>>(g->in_rp, pl.n_hub, nch);
     Status s2 = exclusive_scan_i64(nch, nch, pl.n_hub + 1, s);
     int64_t nht = 0;
@@ -444,8 +447,8 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     if (e == cudaSuccess && s2.code == GOPS_OK)
       e = cudaMemcpyAsync(&nht, nch + pl.n_hub, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e == cudaSuccess) e = cudaMalloc(&g->hub_first, sizeof(int32_t) * (pl.n_hub + 1));
-    if (e == cudaSuccess) e = cudaMalloc(&g->hub_task_row, sizeof(int32_t) * std::max<int64_t>(nht, 1));
+    if (e == cudaSuccess) e = dev_malloc_async(&g->hub_first, sizeof(int32_t) * (pl.n_hub + 1), s);
+    if (e == cudaSuccess) e = dev_malloc_async(&g->hub_task_row, sizeof(int32_t) * std::max<int64_t>(nht, 1), s);
     if (e == cudaSuccess) {
       hub_fill<<<grid_for(pl.n_hub + 1, 256), 256, 0, s>>>(nch, pl.n_hub, g->hub_first, g->hub_task_row);
       e = cudaGetLastError();
@@ -470,7 +473,7 @@ Status dense_to_out_csr_device(Ctx *ctx, int64_t n, const double *d_M, int64_t *
                                int32_t **d_col, double **d_w, int64_t *m_out) {
   cudaStream_t s = ctx->stream;
   *d_rp = nullptr; *d_col = nullptr; *d_w = nullptr;
-  GOPS_CUDA_TRY(cudaMallocAsync((void **)d_rp, sizeof(int64_t) * (n + 1), s));
+  GOPS_CUDA_TRY(dev_malloc_async((void **)d_rp, sizeof(int64_t) * (n + 1), s));
   GOPS_CUDA_TRY(cudaMemsetAsync(*d_rp, 0, sizeof(int64_t) * (n + 1), s));
   if (n > 0) {
     dense_rows<<<(unsigned)ceil_div<int64_t>(n, 8), 256, 0, s>>>(n, d_M, *d_rp, nullptr, nullptr,
@@ -482,8 +485,8 @@ Status dense_to_out_csr_device(Ctx *ctx, int64_t n, const double *d_M, int64_t *
   GOPS_CUDA_TRY(cudaMemcpyAsync(&m, *d_rp + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   GOPS_CUDA_TRY(cudaStreamSynchronize(s));
   *m_out = m;
-  GOPS_CUDA_TRY(cudaMallocAsync((void **)d_col, sizeof(int32_t) * std::max<int64_t>(m, 1), s));
-  GOPS_CUDA_TRY(cudaMallocAsync((void **)d_w, sizeof(double) * std::max<int64_t>(m, 1), s));
+  GOPS_CUDA_TRY(dev_malloc_async((void **)d_col, sizeof(int32_t) * std::max<int64_t>(m, 1), s));
+  GOPS_CUDA_TRY(dev_malloc_async((void **)d_w, sizeof(double) * std::max<int64_t>(m, 1), s));
   if (n > 0 && m > 0) {
     dense_rows<<<(unsigned)ceil_div<int64_t>(n, 8), 256, 0, s>>>(n, d_M, nullptr, *d_rp, *d_col,
                                                                  *d_w);

@@ -107,6 +107,10 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   SolveState *host_state = nullptr;  // pinned
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // a second stream for the weight upload, which overlaps the input checks
+  // and the edge sort of gops_graph_upload; copy_ev orders it against stream
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev[2] = {nullptr, nullptr};
   // optional per-launch timing of the iteration kernels (gops_ctx_set_timing)
   bool timing = false;
   std::vector<cudaEvent_t> tev;
@@ -121,8 +125,11 @@ struct Ctx {
 
 Status solve_plain_in_workspace(Ctx *ctx, Graph *g, const gops_config *cfg, Workspace &ws,
                                 double *scores_host, gops_run *run);
+// w_ready (optional): an event after which d_w is complete; the build
+// orders its first read of d_w after it.
 Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_rp,
-                                       const int32_t *d_out_col, const double *d_w);
+                                       const int32_t *d_out_col, const double *d_w,
+                                       cudaEvent_t w_ready = nullptr);
 Status workspace_ensure(Ctx *ctx, Graph *g);
 void workspace_free(Workspace &ws);
 void graph_free_device(Graph &g);

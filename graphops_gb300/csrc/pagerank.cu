@@ -638,25 +638,24 @@ void workspace_free(Workspace &ws) {
 }
 
 Status workspace_ensure(Ctx *ctx, Graph *g) {
-  (void)ctx;
   Workspace &ws = g->ws;
   if (ws.sums) return Status::ok();
   const size_t n = (size_t)std::max<int64_t>(g->n, 1);
   const size_t nht = (size_t)std::max<int32_t>(g->plan.n_hub_tasks, 1);
   const size_t nh = (size_t)std::max<int32_t>(g->plan.n_hub, 1);
   // one extra entry: index n is the column of row padding and always 0
-  GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[0], sizeof(float2) * (n + 1)));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.gdf[1], sizeof(float2) * (n + 1)));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.gf[0], sizeof(float) * (n + 1)));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.gf[1], sizeof(float) * (n + 1)));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.acc, sizeof(float2) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.tail, sizeof(float) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.pdf, sizeof(float2) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.scores, sizeof(double) * n));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.lpart, sizeof(float2) * nht));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.lcnt, sizeof(unsigned) * nh));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.state, sizeof(SolveState)));
-  GOPS_CUDA_TRY(cudaMalloc(&ws.sums, sizeof(long long) * 12));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.gdf[0], sizeof(float2) * (n + 1), ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.gdf[1], sizeof(float2) * (n + 1), ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.gf[0], sizeof(float) * (n + 1), ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.gf[1], sizeof(float) * (n + 1), ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.acc, sizeof(float2) * n, ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.tail, sizeof(float) * n, ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.pdf, sizeof(float2) * n, ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.scores, sizeof(double) * n, ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.lpart, sizeof(float2) * nht, ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.lcnt, sizeof(unsigned) * nh, ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.state, sizeof(SolveState), ctx->stream));
+  GOPS_CUDA_TRY(dev_malloc_async(&ws.sums, sizeof(long long) * 12, ctx->stream));
   ws.n = g->n;
   return Status::ok();
 }

@@ -663,7 +663,7 @@ Status batch_prepare(Ctx *ctx, Graph *g) {
   GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->wev[0], cudaEventDisableTiming));
   GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->wev[1], cudaEventDisableTiming));
   int64_t *tmp = nullptr;
-  GOPS_CUDA_TRY(cudaMallocAsync((void **)&tmp, sizeof(int64_t) * 2, s));
+  GOPS_CUDA_TRY(dev_malloc_async((void **)&tmp, sizeof(int64_t) * 2, s));
   count_big<<<1, 1, 0, s>>>(g->in_rp, n, tmp);
   int64_t nbig = 0;
   GOPS_CUDA_TRY(cudaMemcpyAsync(&nbig, tmp, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -672,7 +672,7 @@ Status batch_prepare(Ctx *ctx, Graph *g) {
   b->n_big = (int32_t)nbig;
   if (nbig > 0) {
     int64_t *nch = nullptr;
-    GOPS_CUDA_TRY(cudaMallocAsync((void **)&nch, sizeof(int64_t) * (nbig + 1), s));
+    GOPS_CUDA_TRY(dev_malloc_async((void **)&nch, sizeof(int64_t) * (nbig + 1), s));
     chunk_counts<<<blocks_for(nbig + 1, 256, 4096), 256, 0, s>>>(g->in_rp, b->n_big, nch);
     GOPS_TRY(exclusive_scan_i64(nch, nch, nbig + 1, s));
     int64_t tasks = 0;

@@ -80,7 +80,7 @@ Status exclusive_scan(const T *in, T *out, int64_t n, cudaStream_t s) {
     return Status::ok();
   }
   T *sums = nullptr;
-  GOPS_CUDA_TRY(cudaMallocAsync((void **)&sums, sizeof(T) * tiles, s));
+  GOPS_CUDA_TRY(dev_malloc_async((void **)&sums, sizeof(T) * tiles, s));
   scan_tile_sums<T><<<(unsigned)tiles, kScanThreads, 0, s>>>(in, n, sums);
   Status st = exclusive_scan<T>(sums, sums, tiles, s);
   if (st.code == GOPS_OK) {
@@ -189,7 +189,7 @@ Status radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt,
   if (n >= (int64_t)UINT32_MAX) return Status{GOPS_ERR_INVALID, "radix sort: too many items"};
   const int64_t tiles = ceil_div<int64_t>(n, kSortTile);
   uint32_t *hist = nullptr;
-  GOPS_CUDA_TRY(cudaMallocAsync((void **)&hist, sizeof(uint32_t) * tiles * kRadix, s));
+  GOPS_CUDA_TRY(dev_malloc_async((void **)&hist, sizeof(uint32_t) * tiles * kRadix, s));
   uint32_t *k_in = keys, *v_in = vals, *k_out = keys_alt, *v_out = vals_alt;
   Status st;
   for (int shift = 0; shift < key_bits; shift += 8) {

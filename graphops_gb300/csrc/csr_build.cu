@@ -26,18 +26,33 @@ namespace {
 
 // Per out-row u: out-degree, source id of every entry, and (weighted) the
 // transition weight max(w,0) / sum_u max(w,0) in FP32 with the weighted-
-// dangling bit.  Rows of at most kRowBig entries (nearly all: R-MAT rows
-// average ~16): an 8-lane group per row in a persistent grid, the FP64 sum in
-// a fixed order per group (the shuffles name the group only: groups of a warp
-// run different numbers of rows).  Longer rows (hubs, up to ~1e5 entries): a
-// block per row in out_row_pass_big, a fixed-order block sum; the small pass
-// lists them in big[1..big[0]] (list order varies, per-row results do not).
+// dangling bit, in three passes that keep FP64 instructions (issued at a
+// small fraction of the FP32 rate on this GPU) to one add per entry, one
+// divide per row and one multiply and conversion per entry:
+//  out_row_sums      rows of at most kRowBig entries (nearly all: R-MAT rows
+//                    average ~16): an 8-lane group per row in a persistent
+//                    grid, the FP64 sum in a fixed order per group (the
+//                    shuffles name the group only: groups of a warp run
+//                    different numbers of rows); longer rows are listed in
+//                    big[1..big[0]] (list order varies, per-row results do not)
+//  out_row_sums_big  the listed rows (hubs, up to ~1e5 entries), a block per
+//                    row, a fixed-order block sum
+//  row_inverse       a thread per row: rowsum -> 1/rowsum (0 for an empty or
+//                    zero-weight row) and the dangling bits, a word per warp
+//  edge_weights      a thread per entry: (float)(max(w,0) * inverse of its row)
 constexpr int kRowLanes = 8;
 constexpr int64_t kRowBig = 256;
-__global__ void out_row_pass(int64_t n, const int64_t *__restrict__ rp, const double *__restrict__ w,
-                             uint32_t *__restrict__ src, float *__restrict__ val_out,
-                             float *__restrict__ deg_f, uint32_t *__restrict__ dmask,
-                             uint32_t *__restrict__ big) {
+
+// max(w, 0), 0 for NaN (the maximum ignores a NaN operand), from the bits
+__device__ __forceinline__ double clamp_weight(double w) {
+  const long long b = __double_as_longlong(w);
+  const bool neg_or_nan = b < 0 || b > 0x7ff0000000000000LL;  // sign set, or NaN
+  return neg_or_nan ? 0.0 : w;
+}
+
+__global__ void out_row_sums(int64_t n, const int64_t *__restrict__ rp, const double *__restrict__ w,
+                             uint32_t *__restrict__ src, float *__restrict__ deg_f,
+                             double *__restrict__ rowsum, uint32_t *__restrict__ big) {
   const int lane = threadIdx.x & (kRowLanes - 1);
   const unsigned gmask = ((1u << kRowLanes) - 1u) << ((threadIdx.x & 31) & ~(kRowLanes - 1));
   const int64_t groups = (int64_t)gridDim.x * (blockDim.x / kRowLanes);
@@ -51,23 +66,17 @@ __global__ void out_row_pass(int64_t n, const int64_t *__restrict__ rp, const do
     for (int64_t i = b + lane; i < e; i += kRowLanes) src[i] = (uint32_t)u;
     if (w) {
       double s = 0.0;
-      for (int64_t i = b + lane; i < e; i += kRowLanes) s += fmax(w[i], 0.0);
+      for (int64_t i = b + lane; i < e; i += kRowLanes) s += clamp_weight(w[i]);
 #pragma unroll
       for (int o = kRowLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, kRowLanes);
-      const double inv = s > 0.0 ? 1.0 / s : 0.0;
-      for (int64_t i = b + lane; i < e; i += kRowLanes) {
-        const double wc = fmax(w[i], 0.0);
-        val_out[i] = wc > 0.0 ? (float)(wc * inv) : 0.0f;
-      }
-      if (lane == 0 && s == 0.0) atomicOr(&dmask[u >> 5], 1u << (u & 31));
+      if (lane == 0) rowsum[u] = s;
     }
   }
 }
 
-__global__ void __launch_bounds__(256) out_row_pass_big(int64_t n, const int64_t *__restrict__ rp,
+__global__ void __launch_bounds__(256) out_row_sums_big(const int64_t *__restrict__ rp,
                                                          const double *__restrict__ w, uint32_t *__restrict__ src,
-                                                         float *__restrict__ val_out, float *__restrict__ deg_f,
-                                                         uint32_t *__restrict__ dmask,
+                                                         float *__restrict__ deg_f, double *__restrict__ rowsum,
                                                          const uint32_t *__restrict__ big) {
   __shared__ double sh[256];
   const uint32_t nbig = big[0];
@@ -78,21 +87,39 @@ __global__ void __launch_bounds__(256) out_row_pass_big(int64_t n, const int64_t
     for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) src[i] = (uint32_t)u;
     if (!w) continue;
     double s = 0.0;
-    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) s += fmax(w[i], 0.0);
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) s += clamp_weight(w[i]);
     sh[threadIdx.x] = s;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
       if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
       __syncthreads();
     }
-    const double tot = sh[0];
+    if (threadIdx.x == 0) rowsum[u] = sh[0];
     __syncthreads();
-    const double inv = tot > 0.0 ? 1.0 / tot : 0.0;
-    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-      const double wc = fmax(w[i], 0.0);
-      val_out[i] = wc > 0.0 ? (float)(wc * inv) : 0.0f;
+  }
+}
+
+// Rows 32*j .. 32*j+31 are one warp's: dmask word j is written whole.
+__global__ void row_inverse(int64_t n, double *__restrict__ rowsum, uint32_t *__restrict__ dmask) {
+  const int64_t words = (n + 31) / 32;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < words * 32;
+       u += (int64_t)gridDim.x * blockDim.x) {  // uniform per warp: words * 32 rounds up
+    bool dang = false;
+    if (u < n) {
+      const double s = rowsum[u];
+      dang = !(s > 0.0);
+      rowsum[u] = dang ? 0.0 : 1.0 / s;
     }
-    if (threadIdx.x == 0 && tot == 0.0) atomicOr(&dmask[u >> 5], 1u << (u & 31));
+    const unsigned bits = __ballot_sync(0xffffffffu, dang);
+    if ((threadIdx.x & 31) == 0) dmask[u >> 5] = bits;
+  }
+}
+
+__global__ void edge_weights(int64_t m, const double *__restrict__ w, const uint32_t *__restrict__ src,
+                             const double *__restrict__ inv, float *__restrict__ val_out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const double wc = clamp_weight(w[i]);
+    val_out[i] = __double_as_longlong(wc) > 0 ? (float)(wc * inv[src[i]]) : 0.0f;
   }
 }
 
@@ -285,12 +312,13 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   int32_t *inv_perm = nullptr;
   unsigned *maxdeg = nullptr;
   uint32_t *bigrows = nullptr;
+  double *rowsum = nullptr;
   auto cleanup = [&]() {
     free_async(src, s); free_async(keys, s); free_async(vals, s); free_async(keys2, s);
     free_async(vals2, s); free_async(nk, s); free_async(nv, s); free_async(nk2, s);
     free_async(nv2, s); free_async(dmask_old, s); free_async(val_out, s); free_async(deg_old, s);
     free_async(rp_old, s); free_async(new_deg, s); free_async(small, s); free_async(inv_perm, s);
-    free_async(maxdeg, s); free_async(bigrows, s);
+    free_async(maxdeg, s); free_async(bigrows, s); free_async(rowsum, s);
   };
 #define BUILD_TRY(expr)                                                                     \
   do {                                                                                      \
@@ -319,6 +347,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(dev_malloc_async((void **)&dmask_old, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(cudaMemsetAsync(dmask_old, 0, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(dev_malloc_async((void **)&val_out, sizeof(float) * mm, s));
+    BUILD_TRY(dev_malloc_async((void **)&rowsum, sizeof(double) * nn, s));
   }
   // K1: stable sort of edge ids by destination
   BUILD_TRY(dev_malloc_async((void **)&keys, sizeof(uint32_t) * mm, s));
@@ -342,11 +371,15 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     const int64_t nbig_cap = std::min<int64_t>(n, m / (kRowBig + 1)) + 1;
     BUILD_TRY(dev_malloc_async((void **)&bigrows, sizeof(uint32_t) * nbig_cap, s));
     BUILD_TRY(cudaMemsetAsync(bigrows, 0, sizeof(uint32_t), s));
-    out_row_pass<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
-        n, d_out_rp, d_w, src, val_out, deg_old, dmask_old, bigrows);
-    out_row_pass_big<<<ctx->num_sms * 4, 256, 0, s>>>(n, d_out_rp, d_w, src, val_out, deg_old, dmask_old,
-                                                      bigrows);
+    out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
+        n, d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, d_w, src, deg_old, rowsum, bigrows);
     BUILD_TRY(cudaGetLastError());
+    if (d_w) {
+      row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(n, rowsum, dmask_old);
+      if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, s>>>(m, d_w, src, rowsum, val_out);
+      BUILD_TRY(cudaGetLastError());
+    }
   }
   BUILD_TRY(dev_malloc_async((void **)&rp_old, sizeof(int64_t) * (n + 1), s));
   rp_from_sorted<<<grid_for(m + 1, 256), 256, 0, s>>>(K, m, n, rp_old);

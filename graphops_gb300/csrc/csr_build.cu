@@ -39,7 +39,9 @@ namespace {
 //                    row, a fixed-order block sum
 //  row_inverse       a thread per row: rowsum -> 1/rowsum (0 for an empty or
 //                    zero-weight row) and the dangling bits, a word per warp
-//  edge_weights      a thread per entry: (float)(max(w,0) * inverse of its row)
+//  edge_weights      a thread per entry: (float)(max(w,0) * inverse of its row),
+//                    stored beside the entry's source so that the in-CSR
+//                    scatter gathers both with one 8-byte load
 constexpr int kRowLanes = 8;
 constexpr int64_t kRowBig = 256;
 
@@ -116,10 +118,12 @@ __global__ void row_inverse(int64_t n, double *__restrict__ rowsum, uint32_t *__
 }
 
 __global__ void edge_weights(int64_t m, const double *__restrict__ w, const uint32_t *__restrict__ src,
-                             const double *__restrict__ inv, float *__restrict__ val_out) {
+                             const double *__restrict__ inv, uint2 *__restrict__ src_val) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
     const double wc = clamp_weight(w[i]);
-    val_out[i] = __double_as_longlong(wc) > 0 ? (float)(wc * inv[src[i]]) : 0.0f;
+    const uint32_t u = src[i];
+    const float v = __double_as_longlong(wc) > 0 ? (float)(wc * inv[u]) : 0.0f;
+    src_val[i] = make_uint2(u, __float_as_uint(v));
   }
 }
 
@@ -197,14 +201,19 @@ __global__ void permute_dmask(const int32_t *perm, int64_t n, const uint32_t *ol
 // row inv_perm[K[i]] at the same offset within the row.
 __global__ void scatter_edges(const uint32_t *K, const uint32_t *O, int64_t m, const int64_t *rp_old,
                               const int32_t *inv_perm, const int64_t *rp_new, const uint32_t *src,
-                              const float *val_out, int32_t *in_col, float *in_val) {
+                              const uint2 *src_val, int32_t *in_col, float *in_val) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
        i += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t v = K[i];
     const int64_t pos = rp_new[inv_perm[v]] + (i - rp_old[v]);
     const uint32_t e = O[i];
-    in_col[pos] = inv_perm[src[e]];
-    if (in_val) in_val[pos] = val_out[e];
+    if (src_val) {  // weighted: source and weight in one load
+      const uint2 sv = src_val[e];
+      in_col[pos] = inv_perm[sv.x];
+      in_val[pos] = __uint_as_float(sv.y);
+    } else {
+      in_col[pos] = inv_perm[src[e]];
+    }
   }
 }
 
@@ -307,7 +316,8 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   Status st;
   uint32_t *src = nullptr, *keys = nullptr, *vals = nullptr, *keys2 = nullptr, *vals2 = nullptr;
   uint32_t *nk = nullptr, *nv = nullptr, *nk2 = nullptr, *nv2 = nullptr, *dmask_old = nullptr;
-  float *val_out = nullptr, *deg_old = nullptr;
+  float *deg_old = nullptr;
+  uint2 *src_val = nullptr;
   int64_t *rp_old = nullptr, *new_deg = nullptr, *small = nullptr;
   int32_t *inv_perm = nullptr;
   unsigned *maxdeg = nullptr;
@@ -316,7 +326,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   auto cleanup = [&]() {
     free_async(src, s); free_async(keys, s); free_async(vals, s); free_async(keys2, s);
     free_async(vals2, s); free_async(nk, s); free_async(nv, s); free_async(nk2, s);
-    free_async(nv2, s); free_async(dmask_old, s); free_async(val_out, s); free_async(deg_old, s);
+    free_async(nv2, s); free_async(dmask_old, s); free_async(src_val, s); free_async(deg_old, s);
     free_async(rp_old, s); free_async(new_deg, s); free_async(small, s); free_async(inv_perm, s);
     free_async(maxdeg, s); free_async(bigrows, s); free_async(rowsum, s);
   };
@@ -346,7 +356,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(cudaMemsetAsync(g->dmask_w, 0, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(dev_malloc_async((void **)&dmask_old, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(cudaMemsetAsync(dmask_old, 0, sizeof(uint32_t) * nwords, s));
-    BUILD_TRY(dev_malloc_async((void **)&val_out, sizeof(float) * mm, s));
+    BUILD_TRY(dev_malloc_async((void **)&src_val, sizeof(uint2) * mm, s));
     BUILD_TRY(dev_malloc_async((void **)&rowsum, sizeof(double) * nn, s));
   }
   // K1: stable sort of edge ids by destination
@@ -377,7 +387,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(cudaGetLastError());
     if (d_w) {
       row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(n, rowsum, dmask_old);
-      if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, s>>>(m, d_w, src, rowsum, val_out);
+      if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, s>>>(m, d_w, src, rowsum, src_val);
       BUILD_TRY(cudaGetLastError());
     }
   }
@@ -436,7 +446,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(cudaMemsetAsync(g->in_val, 0, sizeof(float) * ms, s));
   }
   if (m > 0) {
-    scatter_edges<<<grid_for(m, 256), 256, 0, s>>>(K, O, m, rp_old, inv_perm, g->in_rp, src, val_out,
+    scatter_edges<<<grid_for(m, 256), 256, 0, s>>>(K, O, m, rp_old, inv_perm, g->in_rp, src, src_val,
                                                    g->in_col, g->in_val);
     BUILD_TRY(cudaGetLastError());
   }

@@ -105,6 +105,7 @@ constexpr int kSortWarps = kSortThreads / kWarp;
 constexpr int kPerWarp = 512;
 constexpr int kSortTile = kSortWarps * kPerWarp;
 constexpr int kRadix = 256;
+static_assert(kSortThreads == kRadix, "the downsweep gives each thread one digit");
 
 __global__ void radix_upsweep(const uint32_t *keys, int64_t n, int shift, uint32_t *hist,
                               int64_t tiles) {
@@ -120,54 +121,88 @@ __global__ void radix_upsweep(const uint32_t *keys, int64_t n, int shift, uint32
   for (int d = threadIdx.x; d < kRadix; d += kSortThreads) hist[(int64_t)d * tiles + blockIdx.x] = cnt[d];
 }
 
-__global__ void radix_downsweep(const uint32_t *keys, const uint32_t *vals, uint32_t *okeys,
-                                uint32_t *ovals, int64_t n, int shift, const uint32_t *offs,
-                                int64_t tiles) {
+// Per tile: (a) warp-private digit counts (the tile's keys stay in
+// registers), (b) tile-local start of every (warp, digit) and the offset from
+// tile-local to global position per digit, (c) stable scatter into shared
+// memory in digit order, (d) coalesced copy-out: consecutive threads write
+// consecutive positions of a digit's run.
+__global__ void __launch_bounds__(kSortThreads) radix_downsweep(const uint32_t *keys, const uint32_t *vals,
+                                                                uint32_t *okeys, uint32_t *ovals, int64_t n,
+                                                                int shift, const uint32_t *offs, int64_t tiles) {
+  constexpr int kChunks = kPerWarp / kWarp;
   __shared__ uint32_t wcnt[kSortWarps][kRadix];
+  __shared__ uint32_t skeys[kSortTile];
+  __shared__ uint32_t svals[kSortTile];
+  __shared__ uint32_t gdelta[kRadix];  // global - tile-local position (mod 2^32)
+  __shared__ uint32_t wsum[kSortWarps];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) (&wcnt[0][0])[i] = 0;
   __syncthreads();
-  const int64_t wbase = (int64_t)blockIdx.x * kSortTile + (int64_t)w * kPerWarp;
+  const int64_t tbase = (int64_t)blockIdx.x * kSortTile;
+  const int64_t wbase = tbase + (int64_t)w * kPerWarp;
   const unsigned lt_mask = (1u << lane) - 1u;
-  // (a) warp-private digit counts
-  for (int c = 0; c < kPerWarp; c += 32) {
-    int64_t idx = wbase + c + lane;
-    bool valid = idx < n;
-    unsigned dig = valid ? ((keys[idx] >> shift) & 0xFF) : 0x100u;
-    unsigned peers = __match_any_sync(0xffffffffu, dig);
-    int leader = __ffs(peers) - 1;
-    if (valid && lane == leader) wcnt[w][dig] += __popc(peers);
+  uint32_t k[kChunks];
+  // (a)
+#pragma unroll
+  for (int c = 0; c < kChunks; ++c) {
+    const int64_t idx = wbase + c * kWarp + lane;
+    const bool valid = idx < n;
+    k[c] = valid ? keys[idx] : 0u;
+    const unsigned dig = valid ? ((k[c] >> shift) & 0xFF) : 0x100u;
+    const unsigned peers = __match_any_sync(0xffffffffu, dig);
+    if (valid && lane == __ffs(peers) - 1) wcnt[w][dig] += __popc(peers);
     __syncwarp();
   }
   __syncthreads();
-  // (b) turn counts into global positions: tile offset for the digit plus the
-  //     counts of earlier warps of this tile
-  for (int d = threadIdx.x; d < kRadix; d += kSortThreads) {
-    uint32_t run = offs[(int64_t)d * tiles + blockIdx.x];
+  // (b) thread d owns digit d (kSortThreads == kRadix)
+  {
+    const int d = threadIdx.x;
+    uint32_t tot = 0;
+#pragma unroll
     for (int ww = 0; ww < kSortWarps; ++ww) {
-      uint32_t c = wcnt[ww][d];
-      wcnt[ww][d] = run;
-      run += c;
+      const uint32_t c = wcnt[ww][d];
+      wcnt[ww][d] = tot;
+      tot += c;
     }
+    uint32_t incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    uint32_t loc = incl - tot;
+    for (int ww = 0; ww < w; ++ww) loc += wsum[ww];
+#pragma unroll
+    for (int ww = 0; ww < kSortWarps; ++ww) wcnt[ww][d] += loc;
+    gdelta[d] = offs[(int64_t)d * tiles + blockIdx.x] - loc;
   }
   __syncthreads();
-  // (c) stable scatter
-  for (int c = 0; c < kPerWarp; c += 32) {
-    int64_t idx = wbase + c + lane;
-    bool valid = idx < n;
-    uint32_t k = valid ? keys[idx] : 0u;
-    uint32_t v = valid ? vals[idx] : 0u;
-    unsigned dig = valid ? ((k >> shift) & 0xFF) : 0x100u;
-    unsigned peers = __match_any_sync(0xffffffffu, dig);
-    int leader = __ffs(peers) - 1;
-    uint32_t pos = valid ? wcnt[w][dig] + __popc(peers & lt_mask) : 0u;
+  // (c)
+#pragma unroll
+  for (int c = 0; c < kChunks; ++c) {
+    const int64_t idx = wbase + c * kWarp + lane;
+    const bool valid = idx < n;
+    const unsigned dig = valid ? ((k[c] >> shift) & 0xFF) : 0x100u;
+    const unsigned peers = __match_any_sync(0xffffffffu, dig);
+    const uint32_t pos = valid ? wcnt[w][dig] + __popc(peers & lt_mask) : 0u;
     __syncwarp();
     if (valid) {
-      okeys[pos] = k;
-      ovals[pos] = v;
-      if (lane == leader) wcnt[w][dig] += __popc(peers);
+      skeys[pos] = k[c];
+      svals[pos] = vals[idx];
+      if (lane == __ffs(peers) - 1) wcnt[w][dig] += __popc(peers);
     }
     __syncwarp();
+  }
+  __syncthreads();
+  // (d)
+  const int cnt = (int)(n - tbase < (int64_t)kSortTile ? n - tbase : (int64_t)kSortTile);
+  for (int i = threadIdx.x; i < cnt; i += kSortThreads) {
+    const uint32_t kk = skeys[i];
+    const uint32_t pos = (uint32_t)i + gdelta[(kk >> shift) & 0xFF];
+    okeys[pos] = kk;
+    ovals[pos] = svals[i];
   }
 }
 

@@ -127,18 +127,6 @@ __global__ void edge_weights(int64_t m, const double *__restrict__ w, const uint
   }
 }
 
-__global__ void iota_u32(uint32_t *v, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    v[i] = (uint32_t)i;
-}
-
-__global__ void copy_keys(const int32_t *col, uint32_t *keys, int64_t m) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
-       i += (int64_t)gridDim.x * blockDim.x)
-    keys[i] = (uint32_t)col[i];
-}
-
 // rp[v] = first position i of the sorted destination keys K with K[i] >= v.
 __global__ void rp_from_sorted(const uint32_t *K, int64_t m, int64_t n, int64_t *rp) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= m;
@@ -366,11 +354,9 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   BUILD_TRY(dev_malloc_async((void **)&vals2, sizeof(uint32_t) * mm, s));
   uint32_t *K = keys, *O = vals;
   if (m > 0) {
-    copy_keys<<<grid_for(m, 256), 256, 0, s>>>(d_out_col, keys, m);
-    iota_u32<<<grid_for(m, 256), 256, 0, s>>>(vals, m);
-    BUILD_TRY(cudaGetLastError());
-    bool alt = false;
-    BUILD_ST(radix_sort_pairs_u32(keys, vals, keys2, vals2, m, bits_for(n), &alt, s));
+    bool alt = false;  // keys: the destination ids; values: the edge ids
+    BUILD_ST(radix_sort_index_u32(reinterpret_cast<const uint32_t *>(d_out_col), keys, vals, keys2, vals2, m,
+                                  bits_for(n), &alt, s));
     if (alt) { K = keys2; O = vals2; }
   }
   BUILD_TRY(dev_malloc_async((void **)&src, sizeof(uint32_t) * mm, s));

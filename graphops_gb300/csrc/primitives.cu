@@ -126,6 +126,7 @@ __global__ void radix_upsweep(const uint32_t *keys, int64_t n, int shift, uint32
 // tile-local to global position per digit, (c) stable scatter into shared
 // memory in digit order, (d) coalesced copy-out: consecutive threads write
 // consecutive positions of a digit's run.
+// vals == nullptr: the value of item idx is idx.
 __global__ void __launch_bounds__(kSortThreads) radix_downsweep(const uint32_t *keys, const uint32_t *vals,
                                                                 uint32_t *okeys, uint32_t *ovals, int64_t n,
                                                                 int shift, const uint32_t *offs, int64_t tiles) {
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_downsweep(const uint32_t *
     __syncwarp();
     if (valid) {
       skeys[pos] = k[c];
-      svals[pos] = vals[idx];
+      svals[pos] = vals ? vals[idx] : (uint32_t)idx;  // no vals: the input position
       if (lane == __ffs(peers) - 1) wcnt[w][dig] += __popc(peers);
     }
     __syncwarp();
@@ -216,34 +217,68 @@ Status exclusive_scan_u32(const uint32_t *in, uint32_t *out, int64_t n, cudaStre
   return exclusive_scan<uint32_t>(in, out, n, s);
 }
 
-Status radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt,
-                            uint32_t *vals_alt, int64_t n, int key_bits,
-                            bool *result_in_alt, cudaStream_t s) {
+namespace {
+
+__global__ void iota_fill(uint32_t *v, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = (uint32_t)i;
+}
+
+// keys_in/vals_in: the first pass's input (vals_in nullptr: positions);
+// later passes ping-pong between (keys, vals) and (keys_alt, vals_alt).
+Status radix_sort_impl(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys, uint32_t *vals,
+                       uint32_t *keys_alt, uint32_t *vals_alt, int64_t n, int key_bits, bool *result_in_alt,
+                       cudaStream_t s) {
   *result_in_alt = false;
-  if (n <= 1 || key_bits <= 0) return Status::ok();
+  if (n <= 1 || key_bits <= 0) {  // already sorted: the input into (keys, vals)
+    if (n > 0 && keys_in != keys)
+      GOPS_CUDA_TRY(cudaMemcpyAsync(keys, keys_in, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
+    if (n > 0 && !vals_in) {
+      iota_fill<<<1, 256, 0, s>>>(vals, n);
+      GOPS_CUDA_TRY(cudaGetLastError());
+    }
+    return Status::ok();
+  }
   if (n >= (int64_t)UINT32_MAX) return Status{GOPS_ERR_INVALID, "radix sort: too many items"};
   const int64_t tiles = ceil_div<int64_t>(n, kSortTile);
   uint32_t *hist = nullptr;
   GOPS_CUDA_TRY(dev_malloc_async((void **)&hist, sizeof(uint32_t) * tiles * kRadix, s));
-  uint32_t *k_in = keys, *v_in = vals, *k_out = keys_alt, *v_out = vals_alt;
+  uint32_t *bk[2] = {keys, keys_alt}, *bv[2] = {vals, vals_alt};
+  int cur = 0;  // the buffer pair the next pass does not write
+  const uint32_t *k_in = keys_in, *v_in = vals_in;
   Status st;
   for (int shift = 0; shift < key_bits; shift += 8) {
     radix_upsweep<<<(unsigned)tiles, kSortThreads, 0, s>>>(k_in, n, shift, hist, tiles);
     st = exclusive_scan_u32(hist, hist, tiles * kRadix, s);
     if (st.code != GOPS_OK) break;
-    radix_downsweep<<<(unsigned)tiles, kSortThreads, 0, s>>>(k_in, v_in, k_out, v_out, n, shift,
+    radix_downsweep<<<(unsigned)tiles, kSortThreads, 0, s>>>(k_in, v_in, bk[cur ^ 1], bv[cur ^ 1], n, shift,
                                                              hist, tiles);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       st = Status{GOPS_ERR_CUDA, std::string("radix sort: ") + cudaGetErrorString(e)};
       break;
     }
-    std::swap(k_in, k_out);
-    std::swap(v_in, v_out);
-    *result_in_alt = !*result_in_alt;
+    cur ^= 1;
+    k_in = bk[cur];
+    v_in = bv[cur];
   }
+  *result_in_alt = cur == 1;
   free_async(hist, s);
   return st;
+}
+
+}  // namespace
+
+Status radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt,
+                            uint32_t *vals_alt, int64_t n, int key_bits,
+                            bool *result_in_alt, cudaStream_t s) {
+  return radix_sort_impl(keys, vals, keys, vals, keys_alt, vals_alt, n, key_bits, result_in_alt, s);
+}
+
+Status radix_sort_index_u32(const uint32_t *keys_in, uint32_t *keys, uint32_t *vals, uint32_t *keys_alt,
+                            uint32_t *vals_alt, int64_t n, int key_bits, bool *result_in_alt,
+                            cudaStream_t s) {
+  return radix_sort_impl(keys_in, nullptr, keys, vals, keys_alt, vals_alt, n, key_bits, result_in_alt, s);
 }
 
 }  // namespace gops

@@ -19,4 +19,11 @@ Status radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt,
                             uint32_t *vals_alt, int64_t n, int key_bits,
                             bool *result_in_alt, cudaStream_t s);
 
+// The same with the input read from `keys_in` (left unchanged) and the values
+// being the input positions 0..n-1: keys/vals and keys_alt/vals_alt are only
+// written.
+Status radix_sort_index_u32(const uint32_t *keys_in, uint32_t *keys, uint32_t *vals, uint32_t *keys_alt,
+                            uint32_t *vals_alt, int64_t n, int key_bits, bool *result_in_alt,
+                            cudaStream_t s);
+
 }  // namespace gops

@@ -110,6 +110,7 @@ struct BatchState {
   WaveState *hwave = nullptr;             // pinned: two polled copies of the wave record
   cudaEvent_t wev[2] = {nullptr, nullptr};
   std::vector<int32_t> inv_perm;  // host: original id -> relabelled row
+  int32_t *d_inv_perm = nullptr;  // the same on the device
 };
 
 void batch_free(Graph &g) {
@@ -120,6 +121,7 @@ void batch_free(Graph &g) {
   cudaFree(b->acc); cudaFree(b->tail); cudaFree(b->lpart); cudaFree(b->lcnt);
   cudaFree(b->sums); cudaFree(b->cols); cudaFree(b->wave); cudaFree(b->prow);
   cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted); cudaFree(b->x0); cudaFree(b->out);
+  cudaFree(b->d_inv_perm);
   if (b->hstage[0]) cudaFreeHost(b->hstage[0]);
   if (b->hstage[1]) cudaFreeHost(b->hstage[1]);
   if (b->hwave) cudaFreeHost(b->hwave);
@@ -613,6 +615,91 @@ __global__ void batch_finalize(BatchParams p) {
   }
 }
 
+// Tiled forms for 32-column waves.  A warp takes 32 consecutive original
+// node ids u0..u0+31: the warm starts (set-major, original order) are read 32
+// consecutive floats per column, the wave's rows inv_perm[u] (relabelled) are
+// read or written 32 columns at a time, and a 32x32 shared-memory tile turns
+// one into the other, so both sides are coalesced.
+constexpr int kTile = 32;
+
+// batch_init for caller start vectors (p.x0 set); same outputs.
+__global__ void __launch_bounds__(kBThreads) batch_init_x0(BatchParams p, const int32_t *__restrict__ inv_perm) {
+  __shared__ float tile[kBWarps][kTile][kTile + 1];  // [column][node]
+  __shared__ long long bdg[kBWarps][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  long long dang = 0;  // column `lane`
+  if (blockIdx.x == 0 && wid == 0) {  // padding row: gathers of padded edges read zeros
+    const int64_t i = p.n * kCols + lane;
+    p.gdf_out[i] = make_float2(0.f, 0.f);
+    p.gf_out[i] = 0.f;
+    const_cast<float2 *>(p.gdf_in)[i] = make_float2(0.f, 0.f);
+    const_cast<float *>(p.gf_in)[i] = 0.f;
+  }
+  const int64_t step = (int64_t)gridDim.x * kBWarps * kTile;
+  for (int64_t u0 = ((int64_t)blockIdx.x * kBWarps + wid) * kTile; u0 < p.n; u0 += step) {
+    const int64_t u = u0 + lane;
+    const bool u_ok = u < p.n;
+    for (int c = 0; c < kCols; ++c)
+      tile[wid][c][lane] = (c < p.ncols && u_ok) ? p.x0[p.xcol[c] * p.n + u] : 0.f;
+    const int32_t vl = u_ok ? inv_perm[u] : 0;
+    __syncwarp();
+    const int jn = (int)(p.n - u0 < (int64_t)kTile ? p.n - u0 : (int64_t)kTile);
+    for (int j = 0; j < jn; ++j) {
+      const int64_t v = __shfl_sync(0xffffffffu, vl, j);
+      const int64_t i = v * kCols + lane;
+      const df x0 = {tile[wid][lane][j], 0.f};
+      const float dg = p.deg[v];
+      p.acc[i] = make_float2(x0.hi, x0.lo);
+      p.tail[i] = 0.f;
+      const df g = dg > 0.f ? df_div_f(x0, dg) : df{0.f, 0.f};
+      p.gdf_out[i] = make_float2(g.hi, g.lo);
+      p.gf_out[i] = g.hi;
+      if (dg == 0.f) dang += fx_of(x0.hi, p.fx_scale);
+    }
+    __syncwarp();
+  }
+  bdg[wid][lane] = dang;
+  __syncthreads();
+  if (wid == 0) {
+    long long t = 0;
+    for (int w = 0; w < kBWarps; ++w) t += bdg[w][lane];
+    if (t) atomicAdd((unsigned long long *)&p.sums[lane * 4 + 0], (unsigned long long)t);
+  }
+}
+
+// float(a.x + a.y + t) without FP64 (issued at a small fraction of the FP32
+// rate on this GPU): an error-free two-sum of the large terms (Knuth), then
+// the small ones.
+__device__ __forceinline__ float sum3_f(float ax, float ay, float t) {
+  const float s = ax + t;
+  const float bb = s - ax;
+  const float err = (ax - (s - bb)) + (t - bb);
+  return s + (err + ay);
+}
+
+// results of the wave: out[ocol[c] * n + u] = acc + tail of row inv_perm[u]
+__global__ void __launch_bounds__(kBThreads) batch_finalize_t(BatchParams p, const int32_t *__restrict__ inv_perm) {
+  __shared__ float tile[kBWarps][kTile][kTile + 1];  // [node][column]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t step = (int64_t)gridDim.x * kBWarps * kTile;
+  for (int64_t u0 = ((int64_t)blockIdx.x * kBWarps + wid) * kTile; u0 < p.n; u0 += step) {
+    const int64_t u = u0 + lane;
+    const bool u_ok = u < p.n;
+    const int32_t vl = u_ok ? inv_perm[u] : 0;
+    const int jn = (int)(p.n - u0 < (int64_t)kTile ? p.n - u0 : (int64_t)kTile);
+    for (int j = 0; j < jn; ++j) {
+      const int64_t v = __shfl_sync(0xffffffffu, vl, j);
+      const int64_t i = v * kCols + lane;
+      const float2 a = p.acc[i];
+      tile[wid][j][lane] = sum3_f(a.x, a.y, p.tail[i]);
+    }
+    __syncwarp();
+    if (u_ok)
+      for (int c = 0; c < p.ncols; ++c) p.out[p.ocol[c] * p.n + u] = tile[wid][lane][c];
+    __syncwarp();
+  }
+}
+
 __global__ void chunk_counts(const int64_t *rp, int32_t n_big, int64_t *nch) {
   for (int32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= n_big; h += gridDim.x * blockDim.x)
     nch[h] = h < n_big ? ceil_div<int64_t>(rp[h + 1] - rp[h], kSpmmChunk) : 0;
@@ -639,13 +726,22 @@ __global__ void count_big(const int64_t *rp, int64_t n, int64_t *out) {
 
 // prow[v] = first entry whose row >= v (entries sorted by row): a thread per
 // row and a binary search (a wave has a few hundred entries over n rows, so
-// a thread per entry filling its gap would leave one thread ~n writes)
-__global__ void prow_from_sorted(const int32_t *rows, int64_t e, int64_t n, int32_t *prow) {
+// a thread per entry filling its gap would leave one thread ~n writes); the
+// entries are staged in shared memory when they fit (kProwStage)
+constexpr int kProwStage = 4096;
+__global__ void __launch_bounds__(256) prow_from_sorted(const int32_t *rows, int64_t e, int64_t n, int32_t *prow) {
+  __shared__ int32_t srows[kProwStage];
+  const bool staged = e <= kProwStage;
+  if (staged) {
+    for (int i = threadIdx.x; i < (int)e; i += blockDim.x) srows[i] = rows[i];
+    __syncthreads();
+  }
+  const int32_t *r = staged ? srows : rows;
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += (int64_t)gridDim.x * blockDim.x) {
     int64_t lo = 0, hi = e;
     while (lo < hi) {
       const int64_t mid = (lo + hi) >> 1;
-      if ((int64_t)rows[mid] < v) lo = mid + 1;
+      if ((int64_t)r[mid] < v) lo = mid + 1;
       else hi = mid;
     }
     prow[v] = (int32_t)lo;
@@ -706,6 +802,10 @@ Status batch_prepare(Ctx *ctx, Graph *g) {
   GOPS_CUDA_TRY(cudaStreamSynchronize(s));
   b->inv_perm.assign((size_t)n, 0);
   for (int64_t i = 0; i < n; ++i) b->inv_perm[(size_t)perm[(size_t)i]] = (int32_t)i;
+  GOPS_CUDA_TRY(cudaMalloc(&b->d_inv_perm, sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1)));
+  if (n > 0)
+    GOPS_CUDA_TRY(cudaMemcpyAsync(b->d_inv_perm, b->inv_perm.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+  GOPS_CUDA_TRY(cudaStreamSynchronize(s));
   return Status::ok();
 }
 
@@ -881,7 +981,11 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     p.gf_in = b->gf[1];
     p.gdf_out = b->gdf[0];
     p.gf_out = b->gf[0];
-    batch_init<<<grid_rows, kBThreads, 0, st>>>(p);
+    if (kCols == 32 && p.x0)
+      batch_init_x0<<<blocks_for(ceil_div<int64_t>(n, kTile), kBWarps, ctx->num_sms * 8), kBThreads, 0, st>>>(
+          p, b->d_inv_perm);
+    else
+      batch_init<<<grid_rows, kBThreads, 0, st>>>(p);
     GOPS_CUDA_TRY(cudaGetLastError());
     ++launches;
     // ---- steps: chunks of 4 launches; one chunk stays queued ahead of the
@@ -965,7 +1069,11 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     // ---- results of the wave
     p.out = scores_on_device ? scores : b->out;
     if (scores) {
-      batch_finalize<<<grid_rows, kBThreads, 0, st>>>(p);
+      if (kCols == 32)
+        batch_finalize_t<<<blocks_for(ceil_div<int64_t>(n, kTile), kBWarps, ctx->num_sms * 8), kBThreads, 0, st>>>(
+            p, b->d_inv_perm);
+      else
+        batch_finalize<<<grid_rows, kBThreads, 0, st>>>(p);
       GOPS_CUDA_TRY(cudaGetLastError());
       ++launches;
       if (staged) {

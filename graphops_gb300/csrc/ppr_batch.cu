@@ -809,8 +809,9 @@ Status batch_prepare(Ctx *ctx, Graph *g) {
   return Status::ok();
 }
 
-Status ensure_entries(BatchState *b, int64_t e) {
+Status ensure_entries(BatchState *b, int64_t e, cudaStream_t st) {
   if (e <= b->pcap) return Status::ok();
+  GOPS_CUDA_TRY(cudaStreamSynchronize(st));  // earlier waves may still read the old arrays
   cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted);
   b->pslot = nullptr; b->pval = nullptr; b->prows_sorted = nullptr;
   const int64_t cap = std::max<int64_t>(e, 1024);
@@ -881,9 +882,6 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   uint64_t launches = 0, col_iters = 0;
   float spmm_ms = 0.f;
   uint64_t spmm_launches = 0;
-  std::vector<ColState> cols_h(kCols);
-  std::vector<int32_t> erow, eslot;
-  std::vector<float2> eval;
   // host results: each wave's block goes to a pinned buffer in one copy, and
   // host threads scatter its columns to the sets' rows while the GPU runs
   // the next wave (two buffers; a buffer's scatter is joined before reuse)
@@ -910,36 +908,61 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
     return seed_ptr[a + 1] - seed_ptr[a] < seed_ptr[b + 1] - seed_ptr[b];
   });
+  // Host side of a wave (personalization entries, column records), built for
+  // wave w+1 while wave w runs on the device.
+  struct HostWave {
+    int ncols = 0;
+    std::vector<ColState> cols;
+    std::vector<int32_t> erow, eslot;
+    std::vector<float2> eval;
+  } hw[2];
+  auto prep = [&](HostWave &h, int64_t set0) {
+    h.ncols = (int)std::min<int64_t>(kCols, nsets - set0);
+    h.cols.assign(kCols, ColState{});
+    std::map<std::pair<int32_t, int32_t>, double> ent;
+    for (int c = 0; c < kCols; ++c)
+      h.cols[c] = ColState{0, 0.0, c < h.ncols ? 0 : 1, 0, 0, 0,
+                           r1_max && c < h.ncols ? r1_max[order[set0 + c]] : (double)INFINITY};
+    for (int c = 0; c < h.ncols; ++c) {
+      const int64_t a0 = seed_ptr[order[set0 + c]], a1 = seed_ptr[order[set0 + c] + 1];
+      if (a1 == a0) { h.cols[c].uniform = 1; continue; }  // sum <= 0: uniform (src/ppr.rs:108)
+      const double inv = 1.0 / (double)(a1 - a0);
+      for (int64_t k = a0; k < a1; ++k) ent[{b->inv_perm[(size_t)seed_idx[k]], c}] += inv;
+    }
+    h.erow.clear(); h.eslot.clear(); h.eval.clear();
+    for (const auto &kv : ent) {
+      h.erow.push_back(kv.first.first);
+      h.eslot.push_back(kv.first.second);
+      const df w = df_from_double(kv.second);
+      h.eval.push_back(make_float2(w.hi, w.lo));
+    }
+  };
+  // per-column records of every wave stay on the device until the end,
+  // unless host score staging needs a synchronisation per wave anyway
+  const int64_t nwaves = ceil_div<int64_t>(nsets, kCols);
+  ColState *cols_all = nullptr;
+  GOPS_CUDA_TRY(dev_malloc_async((void **)&cols_all, sizeof(ColState) * (size_t)nwaves * kCols, st));
+  struct FreeOnExit {
+    void *p; cudaStream_t s;
+    ~FreeOnExit() { free_async(p, s); }
+  } cols_all_guard{cols_all, st};
+  prep(hw[0], 0);
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], st));
   for (int64_t set0 = 0; set0 < nsets; set0 += kCols) {
-    const int ncols = (int)std::min<int64_t>(kCols, nsets - set0);
+    HostWave &h = hw[(set0 / kCols) & 1];
+    const int ncols = h.ncols;
     p.ncols = ncols;
     for (int c = 0; c < kCols; ++c) {
       const int64_t sid = c < ncols ? order[set0 + c] : 0;
       p.xcol[c] = x0 && !x0_on_device ? c : sid;
       p.ocol[c] = scores && !scores_on_device ? c : sid;
     }
-    // ---- personalization entries of the wave: (row, column, weight)
-    std::map<std::pair<int32_t, int32_t>, double> ent;
-    for (int c = 0; c < kCols; ++c)
-      cols_h[c] = ColState{0, 0.0, c < ncols ? 0 : 1, 0, 0, 0,
-                           r1_max && c < ncols ? r1_max[order[set0 + c]] : (double)INFINITY};
+    std::vector<ColState> &cols_h = h.cols;
+    std::vector<int32_t> &erow = h.erow, &eslot = h.eslot;
+    std::vector<float2> &eval = h.eval;
     double wmax = 1.0;
-    for (int c = 0; c < ncols; ++c) {
-      const int64_t a0 = seed_ptr[order[set0 + c]], a1 = seed_ptr[order[set0 + c] + 1];
-      if (a1 == a0) { cols_h[c].uniform = 1; continue; }  // sum <= 0: uniform (src/ppr.rs:108)
-      const double inv = 1.0 / (double)(a1 - a0);
-      for (int64_t k = a0; k < a1; ++k) ent[{b->inv_perm[(size_t)seed_idx[k]], c}] += inv;
-    }
-    erow.clear(); eslot.clear(); eval.clear();
-    for (const auto &kv : ent) {
-      erow.push_back(kv.first.first);
-      eslot.push_back(kv.first.second);
-      const df w = df_from_double(kv.second);
-      eval.push_back(make_float2(w.hi, w.lo));
-    }
     const int64_t ne = (int64_t)erow.size();
-    GOPS_TRY(ensure_entries(b, ne));
+    GOPS_TRY(ensure_entries(b, ne, st));
     if (ne) {
       GOPS_CUDA_TRY(cudaMemcpyAsync(b->prows_sorted, erow.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, st));
       GOPS_CUDA_TRY(cudaMemcpyAsync(b->pslot, eslot.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, st));
@@ -1035,6 +1058,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       GOPS_TRY(poll_after(q));
       pending[npend++] = q;
     }
+    if (set0 + kCols < nsets) prep(hw[((set0 / kCols) + 1) & 1], set0 + kCols);  // overlaps this wave
     bool finished = false;
     while (npend > 0) {
       const int slot = pending[0];
@@ -1088,8 +1112,9 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
         ctx->stats.d2h_bytes += sizeof(float) * (size_t)ncols * n;
       }
     }
-    GOPS_CUDA_TRY(cudaMemcpyAsync(cols_h.data(), b->cols, sizeof(ColState) * kCols, cudaMemcpyDeviceToHost, st));
-    GOPS_CUDA_TRY(cudaStreamSynchronize(st));
+    GOPS_CUDA_TRY(cudaMemcpyAsync(cols_all + (set0 / kCols) * kCols, b->cols, sizeof(ColState) * kCols,
+                                  cudaMemcpyDeviceToDevice, st));
+    if (staged) GOPS_CUDA_TRY(cudaStreamSynchronize(st));
     if (staged) {  // the block is in the pinned buffer: scatter it in the background
       const int q = (int)((set0 / kCols) & 1);
       const float *src = b->hstage[q];
@@ -1100,10 +1125,18 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
             std::memcpy(scores + ids[c] * n, src + (size_t)c * n, sizeof(float) * (size_t)n);
         });
     }
+  }
+  std::vector<ColState> cols_res((size_t)nwaves * kCols);
+  GOPS_CUDA_TRY(cudaMemcpyAsync(cols_res.data(), cols_all, sizeof(ColState) * cols_res.size(), cudaMemcpyDeviceToHost,
+                                st));
+  GOPS_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int64_t set0 = 0; set0 < nsets; set0 += kCols) {
+    const int ncols = (int)std::min<int64_t>(kCols, nsets - set0);
+    const ColState *cr = cols_res.data() + (set0 / kCols) * kCols;
     for (int c = 0; c < ncols; ++c) {
-      col_iters += cols_h[c].iterations;
-      if (runs) runs[order[set0 + c]] = gops_run{cols_h[c].iterations, cols_h[c].diff_l1, cols_h[c].converged, 0};
-      if (rejected) rejected[order[set0 + c]] = cols_h[c].rejected;
+      col_iters += cr[c].iterations;
+      if (runs) runs[order[set0 + c]] = gops_run{cr[c].iterations, cr[c].diff_l1, cr[c].converged, 0};
+      if (rejected) rejected[order[set0 + c]] = cr[c].rejected;
     }
   }
   scatter.join(0);

@@ -34,6 +34,12 @@ constexpr int kPushThreads = 512;
 constexpr int kMaxSeeds = 1024;  // distinct seeds of a set handled by the push
 constexpr int kMaxL1 = 2048;     // out-edges of a set's seeds handled by the push
 constexpr float kFixF = 1099511627776.0f;  // 2^40 (kWFix)
+
+// A 2^40 fixed-point value as FP32: one rounding (64-bit integer to FP32),
+// then an exact power-of-two scale; the same value as (float)(f / 2^40) in
+// FP64 without FP64 instructions (issued at a small fraction of the FP32 rate
+// on this GPU).
+__device__ __forceinline__ float fix40_to_float(long long f) { return __ll2float_rn(f) * (1.0f / kFixF); }
 constexpr double kCentFix = 1073741824.0;  // 2^30: fixed point of the k-means sums
 
 __host__ __device__ inline uint64_t mix64(uint64_t z) {  // SplitMix64 (Steele, Lea, Flood 2014)
@@ -120,7 +126,7 @@ __global__ void runs_kernel(const int64_t *out_rp, const int32_t *out_col, const
         if (nz) {
           const int64_t pos = base + __popc(mask & ((1u << lane) - 1u));
           ocl[pos] = c;
-          owt[pos] = (float)((double)h[c] / kWFix);
+          owt[pos] = fix40_to_float((long long)h[c]);
         }
         base += __popc(mask);
       }
@@ -249,7 +255,7 @@ __global__ void table_from_runs(const int64_t *out_rp, const int32_t *out_col, c
         atomicAdd(reinterpret_cast<unsigned long long *>(&h[hcl[q]]), (unsigned long long)fx40(hwt[q] * iu));
     }
     __syncwarp();
-    for (int c = lane; c < r; c += 32) T[u * r + c] = (float)((double)h[c] / kWFix);
+    for (int c = lane; c < r; c += 32) T[u * r + c] = fix40_to_float((long long)h[c]);
     __syncwarp();
   }
 }
@@ -679,10 +685,11 @@ __global__ void compose_kernel(long long *push, const float *w, const int32_t *c
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float wi = w[i];
     const int c = cluster[i];
+#pragma unroll 4
     for (int64_t j = 0; j < nsets; ++j) {
       const int64_t q = j * n + i;
       const long long f = __ldcs(&push[q]);
-      float v = (float)((double)f / kWFix);
+      float v = fix40_to_float(f);
       const int o = over[j];
       if (o == 2) v = inv_n;
       else if (o == 0) v += wi * __ldg(&coef[j * r + c]);
@@ -694,9 +701,10 @@ __global__ void compose_kernel(long long *push, const float *w, const int32_t *c
 // t[j][i] = x*[j][i] - local (in place); the caller clears the push scratch
 __global__ void tail_targets(const long long *push, int64_t n, int64_t nsets, float *t) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+#pragma unroll 4
     for (int64_t j = 0; j < nsets; ++j) {
       const int64_t q = j * n + i;
-      t[q] -= (float)((double)__ldcs(&push[q]) / kWFix);
+      t[q] -= fix40_to_float(__ldcs(&push[q]));
     }
 }
 

@@ -251,7 +251,7 @@ def learned_workload(a):
             "tolerance_per_set": 1e-7, "max_iterations": 1000,
             "graph_seed": 3, "train_seed": 31, "eval_seed": 77,
             "model": "2-layer MPNN (hidden 128, BF16 operands, FP32 accumulation) per-node weight, "
-                     "128 k-means clusters of a 16-wide random-projection code, least-squares "
+                     "72 k-means clusters (best of 8 seeded runs) of a 16-wide random-projection code, least-squares "
                      "cluster coupling, exact 3-hop push"}
 
 
@@ -268,7 +268,9 @@ def run_learned(a, ctx, rank, ws):
     t0 = time.perf_counter()
     # the push scratch and the targets hold chunk x n x 12 bytes: keep them to ~8 GB
     chunk = int(max(32, min(512, 8e9 / (12.0 * g.n))))
-    model = warm.WarmStart(dg, g.row_ptr, g.col, warm.default_config(chunk=chunk))
+    # 72 clusters: the best of 64-256 in a sweep on this graph (validation sets
+    # drawn like the evaluation sets); the library default is 128
+    model = warm.WarmStart(dg, g.row_ptr, g.col, warm.default_config(chunk=chunk, clusters=72))
     create_s = time.perf_counter() - t0
     sp_t, si_t = gen.seed_sets(g, a.learned_train, 1, a.learned_size_hi, seed=31)
     t0 = time.perf_counter()

@@ -41,6 +41,7 @@ constexpr float kFixF = 1099511627776.0f;  // 2^40 (kWFix)
 // on this GPU).
 __device__ __forceinline__ float fix40_to_float(long long f) { return __ll2float_rn(f) * (1.0f / kFixF); }
 constexpr double kCentFix = 1073741824.0;  // 2^30: fixed point of the k-means sums
+constexpr int kKmeansRestarts = 8;        // k-means runs per model; the lowest within-cluster sum is kept
 
 __host__ __device__ inline uint64_t mix64(uint64_t z) {  // SplitMix64 (Steele, Lea, Flood 2014)
   z += 0x9E3779B97F4A7C15ull;
@@ -317,7 +318,7 @@ __global__ void chunk_sums(const float *d2, int64_t n, double *out) {
 }
 
 __global__ void km_assign(const float *y, int64_t n, const float *cent, int r, int32_t *a, long long *sums,
-                          int *counts) {
+                          int *counts, float *best_d2) {
   extern __shared__ __align__(16) unsigned char sm[];
   float *cs = reinterpret_cast<float *>(sm);                             // r x kWY
   long long *acc = reinterpret_cast<long long *>(cs + r * kWY);          // r x kWY
@@ -347,6 +348,7 @@ __global__ void km_assign(const float *y, int64_t n, const float *cent, int r, i
       }
     }
     a[i] = bc;
+    if (best_d2) best_d2[i] = best;
     if (sums) {
 #pragma unroll
       for (int k = 0; k < kWY; ++k)
@@ -938,62 +940,80 @@ Status kmeans(WarmModel &w, const float *y) {
   guard.p.push_back(sums);
   GOPS_CUDA_TRY(cudaMalloc(&counts, sizeof(int) * r));
   guard.p.push_back(counts);
-  // k-means++ seeding
-  uint64_t ctr = mix64(w.cfg.seed ^ 0xC1A55EEDull);
-  auto uniform = [&]() { return (double)(mix64(ctr++) >> 11) * (1.0 / 9007199254740992.0); };
-  int64_t idx = (int64_t)(uniform() * (double)n);
-  if (idx >= n) idx = n - 1;
+  int32_t *assign = nullptr;
+  GOPS_CUDA_TRY(cudaMalloc(&assign, sizeof(int32_t) * n));
+  guard.p.push_back(assign);
   std::vector<double> hcs(nch);
   std::vector<float> hd(kChunk);
   const int gb = blocks_for(n, 256, w.ctx->num_sms * 8);
-  for (int t = 0; t < r; ++t) {
-    GOPS_CUDA_TRY(cudaMemcpyAsync(cent + (int64_t)t * kWY, y + idx * kWY, sizeof(float) * kWY,
-                                  cudaMemcpyDeviceToDevice, s));
-    if (t == r - 1) break;
-    kmpp_dist<<<gb, 256, 0, s>>>(y, n, cent + (int64_t)t * kWY, t == 0, d2);
-    chunk_sums<<<(unsigned)nch, 256, 0, s>>>(d2, n, cs);
-    GOPS_CUDA_TRY(cudaMemcpyAsync(hcs.data(), cs, sizeof(double) * nch, cudaMemcpyDeviceToHost, s));
-    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
-    double total = 0.0;
-    for (int64_t c = 0; c < nch; ++c) total += hcs[c];
-    const double u = uniform();
-    if (!(total > 0.0)) {
-      idx = std::min<int64_t>(n - 1, (int64_t)(u * (double)n));
-      continue;
-    }
-    double target = u * total, run = 0.0;
-    int64_t ch = 0;
-    while (ch < nch - 1 && run + hcs[ch] <= target) run += hcs[ch++];
-    const int64_t base = ch * kChunk, len = std::min<int64_t>(kChunk, n - base);
-    GOPS_CUDA_TRY(cudaMemcpyAsync(hd.data(), d2 + base, sizeof(float) * len, cudaMemcpyDeviceToHost, s));
-    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
-    // the same per-thread order as chunk_sums is not needed here: pick the
-    // first node whose running sum passes the target, else the last positive one
-    idx = -1;
-    int64_t last_pos = -1;
-    for (int64_t q = 0; q < len; ++q) {
-      if (hd[q] > 0.f) last_pos = base + q;
-      run += (double)hd[q];
-      if (run > target && hd[q] > 0.f) {
-        idx = base + q;
-        break;
-      }
-    }
-    if (idx < 0) idx = last_pos >= 0 ? last_pos : base;
-  }
-  // Lloyd iterations
   const size_t smem = sizeof(float) * r * kWY + sizeof(long long) * r * kWY + sizeof(int) * r;
   GOPS_CUDA_TRY(cudaFuncSetAttribute(km_assign, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int ab = std::max(1, w.ctx->num_sms);
-  for (int it = 0; it <= w.cfg.kmeans_iters; ++it) {
-    const bool upd = it < w.cfg.kmeans_iters;
-    if (upd) {
-      GOPS_CUDA_TRY(cudaMemsetAsync(sums, 0, sizeof(long long) * r * kWY, s));
-      GOPS_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * r, s));
+  // kKmeansRestarts seeded runs; the one with the smallest within-cluster sum
+  // of squares is kept (ties: the earliest)
+  double best_inertia = INFINITY;
+  for (int rs = 0; rs < kKmeansRestarts; ++rs) {
+    // k-means++ seeding
+    uint64_t ctr = mix64(w.cfg.seed ^ 0xC1A55EEDull ^ (rs ? mix64((uint64_t)rs) : 0ull));
+    auto uniform = [&]() { return (double)(mix64(ctr++) >> 11) * (1.0 / 9007199254740992.0); };
+    int64_t idx = (int64_t)(uniform() * (double)n);
+    if (idx >= n) idx = n - 1;
+    for (int t = 0; t < r; ++t) {
+      GOPS_CUDA_TRY(cudaMemcpyAsync(cent + (int64_t)t * kWY, y + idx * kWY, sizeof(float) * kWY,
+                                    cudaMemcpyDeviceToDevice, s));
+      if (t == r - 1) break;
+      kmpp_dist<<<gb, 256, 0, s>>>(y, n, cent + (int64_t)t * kWY, t == 0, d2);
+      chunk_sums<<<(unsigned)nch, 256, 0, s>>>(d2, n, cs);
+      GOPS_CUDA_TRY(cudaMemcpyAsync(hcs.data(), cs, sizeof(double) * nch, cudaMemcpyDeviceToHost, s));
+      GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+      double total = 0.0;
+      for (int64_t c = 0; c < nch; ++c) total += hcs[c];
+      const double u = uniform();
+      if (!(total > 0.0)) {
+        idx = std::min<int64_t>(n - 1, (int64_t)(u * (double)n));
+        continue;
+      }
+      double target = u * total, run = 0.0;
+      int64_t ch = 0;
+      while (ch < nch - 1 && run + hcs[ch] <= target) run += hcs[ch++];
+      const int64_t base = ch * kChunk, len = std::min<int64_t>(kChunk, n - base);
+      GOPS_CUDA_TRY(cudaMemcpyAsync(hd.data(), d2 + base, sizeof(float) * len, cudaMemcpyDeviceToHost, s));
+      GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+      // the same per-thread order as chunk_sums is not needed here: pick the
+      // first node whose running sum passes the target, else the last positive one
+      idx = -1;
+      int64_t last_pos = -1;
+      for (int64_t q = 0; q < len; ++q) {
+        if (hd[q] > 0.f) last_pos = base + q;
+        run += (double)hd[q];
+        if (run > target && hd[q] > 0.f) {
+          idx = base + q;
+          break;
+        }
+      }
+      if (idx < 0) idx = last_pos >= 0 ? last_pos : base;
     }
-    km_assign<<<ab, 256, smem, s>>>(y, n, cent, r, w.cluster, upd ? sums : nullptr, counts);
-    GOPS_CUDA_TRY(cudaGetLastError());
-    if (upd) km_update<<<(r * kWY + 255) / 256, 256, 0, s>>>(cent, r, sums, counts);
+    // Lloyd iterations; the last pass only assigns and records each node's
+    // squared distance to its centroid
+    for (int it = 0; it <= w.cfg.kmeans_iters; ++it) {
+      const bool upd = it < w.cfg.kmeans_iters;
+      if (upd) {
+        GOPS_CUDA_TRY(cudaMemsetAsync(sums, 0, sizeof(long long) * r * kWY, s));
+        GOPS_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * r, s));
+      }
+      km_assign<<<ab, 256, smem, s>>>(y, n, cent, r, assign, upd ? sums : nullptr, counts, upd ? nullptr : d2);
+      GOPS_CUDA_TRY(cudaGetLastError());
+      if (upd) km_update<<<(r * kWY + 255) / 256, 256, 0, s>>>(cent, r, sums, counts);
+    }
+    chunk_sums<<<(unsigned)nch, 256, 0, s>>>(d2, n, cs);
+    GOPS_CUDA_TRY(cudaMemcpyAsync(hcs.data(), cs, sizeof(double) * nch, cudaMemcpyDeviceToHost, s));
+    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+    double inertia = 0.0;
+    for (int64_t c = 0; c < nch; ++c) inertia += hcs[c];
+    if (inertia < best_inertia || rs == 0) {
+      best_inertia = inertia;
+      GOPS_CUDA_TRY(cudaMemcpyAsync(w.cluster, assign, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+    }
   }
   GOPS_CUDA_TRY(cudaStreamSynchronize(s));
   return Status::ok();

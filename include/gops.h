@@ -266,7 +266,7 @@ int gops_normalize_f64_device(gops_ctx *ctx, double *scores_device, int64_t n);
 typedef struct gops_warm gops_warm;
 
 typedef struct gops_warm_config {
-  int32_t clusters;     /* k-means clusters, 1..256 (default 128) */
+  int32_t clusters;     /* k-means clusters, 1..256 (default 128; best kept of 8 seeded runs) */
   int32_t code_steps;   /* diffusion steps of the 16-wide code (default 10) */
   int32_t kmeans_iters; /* Lloyd iterations after k-means++ seeding (default 20) */
   int32_t minibatch;    /* sets per Adam step, 1..32 (default 32) */

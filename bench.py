@@ -200,6 +200,54 @@ def batch_cpu(g, sp, si, nsets, threads):
     return nsets / dt, dt
 
 
+def run_dense_small(a, ctx, rank):
+    """Plain PageRank on the reference's CPU-sized case: directed Erdos-Renyi
+    n=2000, p=0.005, 1% of nodes forced dangling, given as a dense
+    AdjacencyMatrix (d=0.85, tol 1e-6, max_iterations 100).  Too small for a
+    roofline: latency per solve, device-resident (graph on the device) and
+    end to end through the public API (dense matrix upload, device
+    compaction to CSR, solve, scores back), beside the C restatement of
+    pagerank_run with its O(N^2) neighbour scan on one host thread."""
+    import torch
+    import graphops_gb300 as go
+    from graphops_gb300 import _native, gen
+    g = gen.erdos_renyi(2000, 0.005, 0.01, seed=0)
+    M = gen.dense_adjacency(g)
+    conf = go.PageRankConfig(0.85, 100, 1e-6)
+    dg = _native.DeviceGraph.from_dense(M, ctx=ctx)
+    for _ in range(5):
+        dg.pagerank_run(conf, out=False)
+    reps = 50
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        _, it, _, _ = dg.pagerank_run(conf, out=True)
+    dev_ms = (time.perf_counter() - t0) * 1e3 / reps
+    am = go.AdjacencyMatrix(M)
+    for _ in range(3):
+        go.pagerank_run(am, conf)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        r = go.pagerank_run(am, conf)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
+    out = {"workload": "plain PageRank, directed Erdos-Renyi n=2000 p=0.005, 1% forced dangling, dense "
+                       "AdjacencyMatrix, d=0.85, tol 1e-6, max_iterations 100, seed 0",
+           "edges": int(g.m), "iterations": int(r.iterations),
+           "ms_per_solve_device_resident": round(dev_ms, 4), "ms_per_solve_e2e": round(e2e_ms, 4),
+           "e2e_h2d_bytes": int(M.nbytes), "e2e_d2h_bytes": 8 * 2000}
+    if rank == 0 and not a.no_cpu:
+        from oracle import port  # the C restatement (CPU baseline only)
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < 2.0:
+            port.pagerank_run_dense(M, 0.85, 100, 1e-6)
+            k += 1
+        out["cpu_baseline"] = {"ms_per_solve": round((time.perf_counter() - t0) * 1e3 / k, 3), "cores": 1,
+                               "kind": "port", "sample": f"{k} solves of pagerank_run on the dense matrix, "
+                                                         f"C restatement incl. the O(N^2) neighbour scan"}
+    return out
+
+
 def run_batch(a, ctx, rank, ws):
     """Batched PPR seeds/s: device-resident graph; end to end with the score
     blocks copied back; CPU reference on a sample of the same seed sets."""
@@ -484,6 +532,7 @@ def run_gpu(a):
                "sample": f"{it} iterations of pagerank_weighted_run ({dt:.1f} s), C restatement, "
                          f"FP64, single thread (the reference path is single-threaded)"}
 
+    dense_small = run_dense_small(a, ctx, rank)
     batch = None
     if not a.no_batch:
         batch = run_batch(a, ctx, rank, ws)
@@ -512,6 +561,7 @@ def run_gpu(a):
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
+            "dense_small": dense_small,
             "ppr_batched": batch,
             "ppr_learned": learned,
         }

@@ -32,3 +32,16 @@ def test_valid_after_invalid():
     g = upload([0, 1, 2, 2], [1, 2])
     s, it, diff, conv = g.pagerank_run(go.PageRankConfig())
     assert conv and abs(s.sum() - 1.0) < 1e-9
+
+
+def test_weighted_invalid_then_valid():
+    """The weights travel on a second stream: a rejected upload still waits
+    for that copy before freeing, and the next upload and solve are sound."""
+    w = np.array([0.5, 2.0], np.float64)
+    with pytest.raises(GopsError, match="neighbor index out of range"):
+        go.DeviceGraph.from_csr(np.array([0, 1, 2, 2], np.int64), np.array([1, 7], np.int32), w)
+    with pytest.raises(GopsError, match="row_ptr must be non-decreasing"):
+        go.DeviceGraph.from_csr(np.array([0, 2, 1, 2], np.int64), np.array([1, 2], np.int32), w)
+    g = go.DeviceGraph.from_csr(np.array([0, 1, 2, 2], np.int64), np.array([1, 2], np.int32), w)
+    s, it, diff, conv = g.pagerank_weighted_run(go.PageRankConfig())
+    assert conv and abs(s.sum() - 1.0) < 1e-9

@@ -299,4 +299,98 @@ PageRankRun personalized_pagerank_checked_run(const G &graph, PageRankConfig con
   return personalized_pagerank_run(graph, config, personalization);
 }
 
+// ---- Katz centrality (src/katz.rs:19-210) ----
+struct KatzConfig {
+  double alpha = 0.1;
+  double beta = 1.0;
+  size_t max_iterations = 100;
+  double tolerance = 1e-6;
+  // src/katz.rs:60-86: the library's checks and messages
+  void validate() const {
+    const gops_katz_config c{alpha, beta, static_cast<uint64_t>(max_iterations), tolerance};
+    char msg[256] = {0};
+    if (gops_katz_config_validate(&c, msg, sizeof(msg)) != GOPS_OK) throw InvalidParameter(msg);
+  }
+};
+
+struct KatzRun {  // src/katz.rs:93-104
+  std::vector<double> scores;
+  size_t iterations = 0;
+  double diff_l1 = 0.0;
+  bool converged = true;
+};
+
+template <class G>
+KatzRun katz_centrality_run(const G &graph, KatzConfig config = {}) {
+  const size_t n = graph.node_count();
+  if (n == 0) return KatzRun{};  // src/katz.rs:138-145
+  gops_ctx *ctx = detail::thread_ctx();
+  auto h = detail::upload(ctx, graph, false);
+  const gops_katz_config c{config.alpha, config.beta, static_cast<uint64_t>(config.max_iterations),
+                           config.tolerance};
+  KatzRun out;
+  out.scores.resize(n);
+  gops_run r{};
+  detail::check(ctx, gops_katz_run(ctx, h.get(), &c, out.scores.data(), &r));
+  out.iterations = static_cast<size_t>(r.iterations);
+  out.diff_l1 = r.diff_l1;
+  out.converged = r.converged != 0;
+  return out;
+}
+
+template <class G>
+std::vector<double> katz_centrality(const G &graph, KatzConfig config = {}) {
+  return katz_centrality_run(graph, config).scores;
+}
+
+template <class G>
+std::vector<double> katz_centrality_checked(const G &graph, KatzConfig config = {}) {
+  config.validate();
+  return katz_centrality(graph, config);
+}
+
+// ---- eigenvector centrality (src/eigenvector.rs:13-125) ----
+struct EigenvectorRun {
+  std::vector<double> scores;
+  size_t iterations = 0;
+  double diff_l1 = 0.0;
+  bool converged = true;
+};
+
+template <class G>
+EigenvectorRun eigenvector_centrality_run(const G &graph, size_t max_iterations, double tolerance) {
+  const size_t n = graph.node_count();
+  if (n == 0) return EigenvectorRun{};
+  gops_ctx *ctx = detail::thread_ctx();
+  auto h = detail::upload(ctx, graph, false);
+  EigenvectorRun out;
+  out.scores.resize(n);
+  gops_run r{};
+  detail::check(ctx, gops_eigenvector_run(ctx, h.get(), static_cast<uint64_t>(max_iterations), tolerance,
+                                          out.scores.data(), &r));
+  out.iterations = static_cast<size_t>(r.iterations);
+  out.diff_l1 = r.diff_l1;
+  out.converged = r.converged != 0;
+  return out;
+}
+
+template <class G>
+std::vector<double> eigenvector_centrality(const G &graph) {  // src/eigenvector.rs:26-28
+  return eigenvector_centrality_run(graph, 100, 1e-6).scores;
+}
+
+// ---- HITS (src/centrality.rs:114-166): (hub scores, authority scores) ----
+template <class G>
+std::pair<std::vector<double>, std::vector<double>> hits(const G &graph, size_t max_iter = 100,
+                                                         double tol = 1e-6) {
+  const size_t n = graph.node_count();
+  if (n == 0) return {};
+  gops_ctx *ctx = detail::thread_ctx();
+  auto h = detail::upload(ctx, graph, false);
+  std::vector<double> hub(n), auth(n);
+  gops_run r{};
+  detail::check(ctx, gops_hits_run(ctx, h.get(), static_cast<uint64_t>(max_iter), tol, hub.data(), auth.data(), &r));
+  return {std::move(hub), std::move(auth)};
+}
+
 }  // namespace graphops

@@ -91,6 +91,24 @@ static void cpu_tests() {
         "ppr_checked rejects wrong length");
   check(error_of([&] { personalized_pagerank_checked(g2, PageRankConfig{}, {0.0, 0.0}); }).find("sum") != std::string::npos,
         "ppr_checked rejects zero sum");
+  // src/katz.rs:60-86
+  KatzConfig k;
+  check(error_of([&] { k.validate(); }).empty(), "default Katz config validates");
+  KatzConfig kb = k;
+  kb.alpha = 0.0;
+  check(error_of([&] { kb.validate(); }) == "alpha must be finite and > 0", "Katz alpha message");
+  kb = k;
+  kb.alpha = 1.0;
+  check(error_of([&] { kb.validate(); }).find("alpha must be < 1") == 0, "Katz alpha bound message");
+  kb = k;
+  kb.beta = INFINITY;
+  check(error_of([&] { kb.validate(); }) == "beta must be finite", "Katz beta message");
+  kb = k;
+  kb.max_iterations = 0;
+  check(error_of([&] { kb.validate(); }) == "max_iterations must be > 0", "Katz max_iterations message");
+  kb = k;
+  kb.tolerance = -1.0;
+  check(error_of([&] { kb.validate(); }) == "tolerance must be finite and > 0", "Katz tolerance message");
 }
 
 static void gpu_tests() {
@@ -147,6 +165,22 @@ static void gpu_tests() {
   check(r.iterations == 3 && !r.converged && r.diff_l1 > 0.0, "non-converged run reports max_iterations");
   auto r0 = pagerank_run(AdjacencyMatrix(std::vector<std::vector<double>>{}));
   check(r0.scores.empty() && r0.iterations == 0 && r0.converged, "empty graph");
+  // closed forms on the 3-cycle: Katz x = beta / (1 - alpha); eigenvector and
+  // HITS scores 1/sqrt(3)
+  auto kr = katz_centrality_run(AdjacencyMatrix(cyc));
+  bool kok = kr.converged && kr.scores.size() == 3;
+  for (double x : kr.scores) kok = kok && std::fabs(x - 1.0 / 0.9) < 1e-5;
+  check(kok, "Katz on the 3-cycle");
+  auto ev = eigenvector_centrality(AdjacencyMatrix(cyc));
+  bool eok = ev.size() == 3;
+  for (double x : ev) eok = eok && std::fabs(x - 1.0 / std::sqrt(3.0)) < 1e-9;
+  check(eok, "eigenvector centrality on the 3-cycle");
+  auto ha = hits(AdjacencyMatrix(cyc));
+  bool hok = ha.first.size() == 3 && ha.second.size() == 3;
+  for (size_t i = 0; i < 3 && hok; ++i)
+    hok = std::fabs(ha.first[i] - 1.0 / std::sqrt(3.0)) < 1e-9 && std::fabs(ha.second[i] - 1.0 / std::sqrt(3.0)) < 1e-9;
+  check(hok, "HITS on the 3-cycle");
+  check(katz_centrality_run(AdjacencyMatrix(std::vector<std::vector<double>>{})).scores.empty(), "Katz empty graph");
 }
 
 int main(int argc, char **argv) {

@@ -248,6 +248,27 @@ def run_dense_small(a, ctx, rank):
     return out
 
 
+def batch_roofline(g, st):
+    """The batched step's roofline by the per-step formula 8(N+1) + 4m +
+    8*N*k (row offsets, column indices, the k = 32 columns' block read and
+    written) over the mean CUDA-event duration of the FP32-phase launches
+    (every column of a wave counted active: an upper bound on the bytes)."""
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    n, m = g.n, g.m
+    b = 8 * (n + 1) + 4 * m + 8 * n * 32
+    ms = st.f32_ms / max(1, st.f32_launches)
+    ach = b / (ms * 1e-3) / 1e9 if st.f32_launches else None
+    return {"bound": "hbm", "kernel": "spmm_kernel<BF32>", "bytes_per_launch": int(b),
+            "mean_launch_ms": round(ms, 5), "achieved": round(ach, 1) if ach else None, "peak": peak,
+            "unit": "GB/s", "frac": round(ach / peak, 4) if ach else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"}
+
+
 def run_batch(a, ctx, rank, ws):
     """Batched PPR seeds/s: device-resident graph; end to end with the score
     blocks copied back; CPU reference on a sample of the same seed sets."""
@@ -271,6 +292,7 @@ def run_batch(a, ctx, rank, ws):
            "ms": round(t, 3), "iterations_mean": float(its.mean()), "iterations_max": int(its.max()),
            "all_converged": bool(conv.all()), "kernel_launches": int(st.kernel_launches),
            "spmm_fp32_launch_ms": round(st.f32_ms / max(1, st.f32_launches), 4),
+           "roofline": batch_roofline(g, st),
            "e2e": {"seeds_per_s": round(ws * a.batch_sets / e2e_s, 2),
                    "h2d_bytes_per_step": int(g.row_ptr.nbytes + g.col.nbytes + sp.nbytes + si.nbytes),
                    "d2h_bytes_per_step": int(s.nbytes)}}

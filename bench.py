@@ -179,13 +179,20 @@ def batch_workload(a):
                         f"(0.57/0.19/0.19/0.05, dedup, no self loops), unweighted; {a.batch_sets} seed sets "
                         f"of sizes U[1,64], nodes drawn proportional to out-degree",
             "nodes": 1 << a.batch_scale, "damping": 0.85, "tolerance_per_set": 1e-7,
-            "max_iterations": 1000, "graph_seed": 20, "seed_set_seed": 7}
+            "max_iterations": 1000, "graph_seed": 20, "seed_set_seed": "7 + 1000 * rank"}
 
 
-def batch_inputs(a):
+def shard_seed(base, rank):
+    """Seed of a rank's own seed sets: the sets are the units the batched paths
+    shard (graph replicated, no data-path collective), so every rank solves
+    distinct sets of the same distribution (weak scaling)."""
+    return base + 1000 * rank
+
+
+def batch_inputs(a, rank=0):
     from graphops_gb300 import gen
     g = gen.rmat(a.batch_scale, 16, seed=20)
-    sp, si = gen.seed_sets(g, a.batch_sets, 1, 64, seed=7)
+    sp, si = gen.seed_sets(g, a.batch_sets, 1, 64, seed=shard_seed(7, rank))
     return g, sp, si
 
 
@@ -274,7 +281,7 @@ def run_batch(a, ctx, rank, ws):
     blocks copied back; CPU reference on a sample of the same seed sets."""
     import graphops_gb300 as go
     from graphops_gb300 import _native
-    g, sp, si = batch_inputs(a)
+    g, sp, si = batch_inputs(a, rank)
     conf = go.PageRankConfig(0.85, 1000, 1e-7)
     dg = _native.DeviceGraph.from_csr(g.row_ptr, g.col, ctx=ctx)
     dg.ppr_batch(conf, sp[:33], si[:sp[32]], out=False)  # plan + workspace
@@ -319,7 +326,7 @@ def learned_workload(a):
                         f"drawn proportional to out-degree",
             "nodes": (1 << a.learned_rmat) if a.learned_rmat else a.learned_n, "damping": 0.85,
             "tolerance_per_set": 1e-7, "max_iterations": 1000,
-            "graph_seed": 3, "train_seed": 31, "eval_seed": 77,
+            "graph_seed": 3, "train_seed": 31, "eval_seed": "77 + 1000 * rank",
             "model": "2-layer MPNN (hidden 128, BF16 operands, FP32 accumulation) per-node weight, "
                      "72 k-means clusters (best of 8 seeded runs) of a 16-wide random-projection code, least-squares "
                      "cluster coupling, exact 3-hop push"}
@@ -346,7 +353,7 @@ def run_learned(a, ctx, rank, ws):
     t0 = time.perf_counter()
     tst = model.train(conf, sp_t, si_t)
     train_s = time.perf_counter() - t0
-    sp, si = gen.seed_sets(g, a.learned_sets, 1, a.learned_size_hi, seed=77)
+    sp, si = gen.seed_sets(g, a.learned_sets, 1, a.learned_size_hi, seed=shard_seed(77, rank))
     # warm-up of both paths (plans, workspaces)
     dg.ppr_batch(conf, sp[:65], si[:sp[64]], out=False)
     model.ppr_batch(conf, sp[:65], si[:sp[64]], scores=False)

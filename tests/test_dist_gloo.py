@@ -1,0 +1,58 @@
+"""The multi-rank host path of bench.py on CPU: two gloo ranks (the GPU run
+uses NCCL with one rank per GPU; every box here has one GPU).  The paths
+shard by seed set with no data-path collective, so what runs across ranks
+is the timing protocol: barrier, max over ranks, rank 0 printing one line,
+and distinct seed sets per rank."""
+import json
+import os
+import socket
+import subprocess
+import sys
+from types import SimpleNamespace
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, port, results):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE="2")
+    sys.path.insert(0, ROOT)
+    import bench
+    r, ws = bench.dist_init(SimpleNamespace(impl="reference"))
+    bench.barrier(ws)
+    mx = bench.max_over_ranks(1.5 + r, ws)
+    results[r] = (r, ws, mx, bench.shard_seed(7, r))
+    import torch.distributed as dist
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_timing_protocol():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    port = free_port()
+    with mp.Manager() as m:
+        results = m.dict()
+        mp.spawn(_worker, args=(port, results), nprocs=2, join=True)
+        got = dict(results)
+    assert got[0][:3] == (0, 2, 2.5) and got[1][:3] == (1, 2, 2.5)
+    assert got[0][3] != got[1][3]
+
+
+def test_reference_arm_two_ranks_prints_once():
+    pytest.importorskip("torch")
+    port = free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--scale", "10", "--steps", "1", "--warmup", "3",
+           "--cpu-iters", "2"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1 and lines[0]["impl"] == "reference" and lines[0]["value"] > 0

@@ -86,6 +86,18 @@ def test_clusters_follow_blocks(small):
     assert pure / g.n >= 0.95
 
 
+def test_clusters_reproducible_and_best_of_runs(small):
+    """The clustering (the lowest within-cluster sum of 8 seeded k-means
+    runs, fixed-point centroid sums) is a function of the configuration: a
+    second model with the same seed gets the same assignment."""
+    g, dg, ws = small
+    cfg = warm.default_config(clusters=32, kmeans_iters=10, chunk=256, seed=7)
+    ws2 = warm.WarmStart(dg, g.row_ptr, g.col, cfg)
+    a, b = ws.get(warm.CLUSTERS), ws2.get(warm.CLUSTERS)
+    assert np.array_equal(a, b)
+    assert a.min() >= 0 and a.max() < 32
+
+
 def random_params(seed):
     rng = np.random.default_rng(seed)
     p = np.zeros(wo.P_COUNT, dtype=np.float32)

@@ -18,7 +18,9 @@
  * Build: oracle/build_oracle.py (gcc -O2 -ffp-contract=off, so x86 and Arm
  * give bit-identical FP64 results).
  */
+#define _POSIX_C_SOURCE 200809L
 #include <math.h>
+#include <time.h>
 #include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -491,5 +493,148 @@ int orc_hits_run(int64_t n, const int64_t *row_ptr, const int32_t *col, uint64_t
     run->iterations = iters;
     run->diff_l1 = last;
     run->converged = conv;
+    return 0;
+}
+
+/*
+ * All-cores CPU figure for the weighted PageRank workload (a timing baseline,
+ * not a parity reference): the same iteration as pagerank_weighted_run
+ * (src/pagerank.rs:210-289: uniform start, dangling <=> weight sum 0, mass
+ * spread uniformly, transition max(w,0)/ws, L1 stop with strict <), in pull
+ * form over an in-edge CSR so that `threads` host threads each own a range of
+ * rows; the sums run in a different order than the reference's scatter.  The
+ * in-CSR is built first (not timed); *iter_seconds is the wall time of the
+ * iterations alone.
+ */
+typedef struct {
+    int64_t v0, v1;
+    const int64_t *irp;
+    const int32_t *isrc;
+    const double *ip;
+    const double *ws;
+    double damping, n_f64;
+    double **x, **nx;
+    double *part_l1, *part_dang;
+    int tid;
+    pthread_barrier_t *bar;
+    uint64_t max_iter;
+    double tol;
+    int *stop;
+    uint64_t *iters;
+    double *last_diff;
+    int *converged;
+    int nthreads;
+} pr_mt_job;
+
+static void *pr_mt_worker(void *arg) {
+    pr_mt_job *j = (pr_mt_job *)arg;
+    for (uint64_t it = 0; it < j->max_iter; ++it) {
+        /* dangling mass of x (partials from the previous pass, or initial) */
+        double dsum = 0.0;
+        for (int t = 0; t < j->nthreads; ++t) dsum += j->part_dang[t];
+        const double fill = (1.0 - j->damping) / j->n_f64 + j->damping * dsum / j->n_f64;
+        pthread_barrier_wait(j->bar);  /* everyone has read part_dang */
+        const double *x = *j->x;
+        double *nx = *j->nx;
+        double l1 = 0.0, dg = 0.0;
+        for (int64_t v = j->v0; v < j->v1; ++v) {
+            double s = 0.0;
+            for (int64_t e = j->irp[v]; e < j->irp[v + 1]; ++e) s += x[j->isrc[e]] * j->ip[e];
+            const double nv = fill + j->damping * s;
+            nx[v] = nv;
+            l1 += fabs(x[v] - nv);
+            if (j->ws[v] == 0.0) dg += nv;
+        }
+        j->part_l1[j->tid] = l1;
+        j->part_dang[j->tid] = dg;
+        pthread_barrier_wait(j->bar);
+        if (j->tid == 0) {
+            double diff = 0.0;
+            for (int t = 0; t < j->nthreads; ++t) diff += j->part_l1[t];
+            *j->iters = it + 1;
+            *j->last_diff = diff;
+            double *tmp = *j->x; *j->x = *j->nx; *j->nx = tmp;
+            if (diff < j->tol) { *j->converged = 1; *j->stop = 1; }
+        }
+        pthread_barrier_wait(j->bar);
+        if (*j->stop) break;
+    }
+    return NULL;
+}
+
+int orc_pagerank_weighted_run_mt(int64_t n, const int64_t *row_ptr, const int32_t *col, const double *w,
+                                 orc_config cfg, int threads, double *scores, orc_run *run,
+                                 double *iter_seconds) {
+    *iter_seconds = 0.0;
+    if (n == 0) { empty_run(run); return 0; }
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    const int64_t m = row_ptr[n];
+    double *ws = (double *)calloc((size_t)n, sizeof(double));
+    int64_t *irp = (int64_t *)calloc((size_t)n + 1, sizeof(int64_t));
+    int32_t *isrc = (int32_t *)malloc(sizeof(int32_t) * (size_t)(m > 0 ? m : 1));
+    double *ip = (double *)malloc(sizeof(double) * (size_t)(m > 0 ? m : 1));
+    double *xa = (double *)malloc(sizeof(double) * (size_t)n);
+    double *xb = (double *)malloc(sizeof(double) * (size_t)n);
+    int64_t *fillp = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+    if (!ws || !irp || !isrc || !ip || !xa || !xb || !fillp) {
+        free(ws); free(irp); free(isrc); free(ip); free(xa); free(xb); free(fillp);
+        return -1;
+    }
+    for (int64_t u = 0; u < n; ++u) {
+        double s = 0.0;
+        for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e) s += rust_max(w[e], 0.0);
+        ws[u] = s;
+    }
+    for (int64_t u = 0; u < n; ++u)
+        if (ws[u] > 0.0)
+            for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e)
+                if (rust_max(w[e], 0.0) > 0.0) irp[col[e] + 1] += 1;
+    for (int64_t v = 0; v < n; ++v) irp[v + 1] += irp[v];
+    memcpy(fillp, irp, sizeof(int64_t) * (size_t)n);
+    for (int64_t u = 0; u < n; ++u)
+        if (ws[u] > 0.0)
+            for (int64_t e = row_ptr[u]; e < row_ptr[u + 1]; ++e) {
+                const double we = rust_max(w[e], 0.0);
+                if (we > 0.0) {
+                    const int64_t q = fillp[col[e]]++;
+                    isrc[q] = (int32_t)u;
+                    ip[q] = we / ws[u];
+                }
+            }
+    free(fillp);
+    for (int64_t i = 0; i < n; ++i) xa[i] = 1.0 / (double)n;
+    double part_l1[256], part_dang[256];
+    for (int t = 0; t < threads; ++t) { part_l1[t] = 0.0; part_dang[t] = 0.0; }
+    double d0 = 0.0;
+    for (int64_t i = 0; i < n; ++i)
+        if (ws[i] == 0.0) d0 += xa[i];
+    part_dang[0] = d0;
+    double *xp = xa, *nxp = xb;
+    int stop = 0, converged = 0;
+    uint64_t iters = 0;
+    double last_diff = INFINITY;
+    pthread_barrier_t bar;
+    pthread_barrier_init(&bar, NULL, (unsigned)threads);
+    pr_mt_job jobs[256];
+    pthread_t tid[256];
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int t = 0; t < threads; ++t) {
+        jobs[t] = (pr_mt_job){n * t / threads, n * (t + 1) / threads, irp, isrc, ip, ws, cfg.damping,
+                              (double)n, &xp, &nxp, part_l1, part_dang, t, &bar, cfg.max_iterations,
+                              cfg.tolerance, &stop, &iters, &last_diff, &converged, threads};
+        if (t > 0) pthread_create(&tid[t], NULL, pr_mt_worker, &jobs[t]);
+    }
+    pr_mt_worker(&jobs[0]);
+    for (int t = 1; t < threads; ++t) pthread_join(tid[t], NULL);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    *iter_seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+    pthread_barrier_destroy(&bar);
+    memcpy(scores, xp, sizeof(double) * (size_t)n);
+    free(ws); free(irp); free(isrc); free(ip); free(xa); free(xb);
+    run->iterations = iters;
+    run->diff_l1 = last_diff;
+    run->converged = converged;
     return 0;
 }

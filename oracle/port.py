@@ -47,6 +47,8 @@ def lib():
                                    ctypes.POINTER(OrcRun)]
         l.orc_eigenvector_run.argtypes = [ctypes.c_int64, P, P, ctypes.c_uint64, ctypes.c_double, P,
                                           ctypes.POINTER(OrcRun)]
+        l.orc_pagerank_weighted_run_mt.argtypes = [ctypes.c_int64, P, P, P, OrcConfig, ctypes.c_int, P,
+                                                    ctypes.POINTER(OrcRun), ctypes.POINTER(ctypes.c_double)]
         _lib = l
     return _lib
 
@@ -171,3 +173,21 @@ def hits_run(row_ptr, col, max_iterations=100, tolerance=1e-6):
                           ctypes.byref(r)):
         raise MemoryError
     return hub[:n], auth[:n], int(r.iterations), float(r.diff_l1), bool(r.converged)
+
+
+def pagerank_weighted_run_mt(row_ptr, col, w, damping=0.85, max_iterations=100, tolerance=1e-6, threads=1):
+    """All-cores timing form of pagerank_weighted_run (pull over an in-CSR,
+    rows split over `threads` host threads; a CPU baseline, not a parity
+    reference).  Returns (scores, iterations, diff_l1, converged, seconds of
+    the iterations alone)."""
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    n = row_ptr.shape[0] - 1
+    out = np.empty(max(n, 1))
+    r = OrcRun()
+    secs = ctypes.c_double()
+    if lib().orc_pagerank_weighted_run_mt(n, _p(row_ptr), _p(col), _p(w), _cfg(damping, max_iterations, tolerance),
+                                          int(threads), _p(out), ctypes.byref(r), ctypes.byref(secs)):
+        raise MemoryError
+    return out[:n], int(r.iterations), float(r.diff_l1), bool(r.converged), float(secs.value)

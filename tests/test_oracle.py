@@ -146,3 +146,17 @@ def test_ppr_many_threads_equal_single():
     p = np.zeros(g.n); p[si[sp[3]:sp[4]]] = 1.0
     s, it, _, _ = port.ppr_run(g.row_ptr, g.col, p, tolerance=1e-8)
     assert np.array_equal(a[3], s) and ia[3] == it
+
+
+def test_all_cores_timing_form_matches_serial_restatement():
+    """The pull-form, multi-threaded figure bench.py reports beside the
+    single-threaded restatement runs the same iteration (other summation
+    order): same step count, L1 within rounding."""
+    from graphops_gb300 import gen
+    g = gen.rmat(12, 16, weighted=True, seed=12)
+    w = g.weight.astype(np.float64)
+    a = port.pagerank_weighted_run(g.row_ptr, g.col, w, 0.85, 1000, 1e-8)
+    for t in (1, 3, 8):
+        b = port.pagerank_weighted_run_mt(g.row_ptr, g.col, w, 0.85, 1000, 1e-8, threads=t)
+        assert b[1] == a[1] and b[3] == a[3]
+        assert np.abs(b[0] - a[0]).sum() <= 1e-12

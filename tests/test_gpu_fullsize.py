@@ -85,3 +85,25 @@ def test_batched_ppr_rmat20_linearity():
         mix = (na * x[a] / c[a] + nb * x[b] / c[b]) / (na + nb)
         # each column is within ~1e-7 of its exact vector (tolerance 1e-7 per set)
         assert np.abs(x[u] / c[u] - mix).sum() < 1e-6, q
+
+
+def test_learned_matches_plain_batched_sbm500k():
+    """The learned warm start changes where each set's iteration starts, not
+    what it converges to: on the learned bench graph (SBM n = 500,000) the
+    learned and plain batched results of the same sets agree within what the
+    stopping rule allows (each is within d/(1-d) tol of its fixed point)."""
+    from graphops_gb300 import warm
+    g = gen.sbm(500000, 64, 1.2, 16.0, 4.0, seed=3)
+    conf = go.PageRankConfig(0.85, 1000, 1e-7)
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    model = warm.WarmStart(dg, g.row_ptr, g.col, warm.default_config(chunk=512, clusters=72))
+    sp_t, si_t = gen.seed_sets(g, 2048, 1, 32, seed=31)
+    model.train(conf, sp_t, si_t)
+    sp, si = gen.seed_sets(g, 96, 1, 32, seed=78)
+    lr = model.ppr_batch(conf, sp, si, scores=True)
+    pr = go.ppr_batch(dg, conf, sp, si)
+    assert lr.converged.all() and pr.converged.all()
+    assert (lr.iterations < pr.iterations).mean() > 0.9
+    a, b = lr.scores.astype(np.float64), pr.scores.astype(np.float64)
+    assert a.min() >= 0.0 and np.abs(a.sum(axis=1) - 1.0).max() < 1e-6
+    assert np.abs(a - b).sum(axis=1).max() < 2e-6

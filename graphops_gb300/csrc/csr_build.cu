@@ -52,6 +52,9 @@ __device__ __forceinline__ double clamp_weight(double w) {
   return neg_or_nan ? 0.0 : w;
 }
 
+// Two calls: the structure pass (w == nullptr: out-degree, sources, the list
+// of long rows), which needs no weights and runs while they are still being
+// copied, then the sums pass (w set: row sums only).
 __global__ void out_row_sums(int64_t n, const int64_t *__restrict__ rp, const double *__restrict__ w,
                              uint32_t *__restrict__ src, float *__restrict__ deg_f,
                              double *__restrict__ rowsum, uint32_t *__restrict__ big) {
@@ -61,12 +64,13 @@ __global__ void out_row_sums(int64_t n, const int64_t *__restrict__ rp, const do
   for (int64_t u = (int64_t)blockIdx.x * (blockDim.x / kRowLanes) + threadIdx.x / kRowLanes; u < n; u += groups) {
     const int64_t b = rp[u], e = rp[u + 1];
     if (e - b > kRowBig) {  // the whole group skips: same row
-      if (lane == 0) big[1 + atomicAdd(&big[0], 1u)] = (uint32_t)u;
+      if (!w && lane == 0) big[1 + atomicAdd(&big[0], 1u)] = (uint32_t)u;
       continue;
     }
-    if (lane == 0) deg_f[u] = (float)(e - b);
-    for (int64_t i = b + lane; i < e; i += kRowLanes) src[i] = (uint32_t)u;
-    if (w) {
+    if (!w) {
+      if (lane == 0) deg_f[u] = (float)(e - b);
+      for (int64_t i = b + lane; i < e; i += kRowLanes) src[i] = (uint32_t)u;
+    } else {
       double s = 0.0;
       for (int64_t i = b + lane; i < e; i += kRowLanes) s += clamp_weight(w[i]);
 #pragma unroll
@@ -85,9 +89,11 @@ __global__ void __launch_bounds__(256) out_row_sums_big(const int64_t *__restric
   for (uint32_t k = blockIdx.x; k < nbig; k += gridDim.x) {  // uniform per block
     const int64_t u = big[1 + k];
     const int64_t b = rp[u], e = rp[u + 1];
-    if (threadIdx.x == 0) deg_f[u] = (float)(e - b);
-    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) src[i] = (uint32_t)u;
-    if (!w) continue;
+    if (!w) {  // structure pass
+      if (threadIdx.x == 0) deg_f[u] = (float)(e - b);
+      for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) src[i] = (uint32_t)u;
+      continue;
+    }
     double s = 0.0;
     for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) s += clamp_weight(w[i]);
     sh[threadIdx.x] = s;
@@ -360,22 +366,15 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     if (alt) { K = keys2; O = vals2; }
   }
   BUILD_TRY(dev_malloc_async((void **)&src, sizeof(uint32_t) * mm, s));
-  // the out-row pass is the first reader of the weights
-  if (w_ready) BUILD_TRY(cudaStreamWaitEvent(s, w_ready, 0));
-  if (n > 0) {
+  if (n > 0) {  // structure pass: no weights read
     // rows longer than kRowBig: at most m / (kRowBig + 1) of them
     const int64_t nbig_cap = std::min<int64_t>(n, m / (kRowBig + 1)) + 1;
     BUILD_TRY(dev_malloc_async((void **)&bigrows, sizeof(uint32_t) * nbig_cap, s));
     BUILD_TRY(cudaMemsetAsync(bigrows, 0, sizeof(uint32_t), s));
     out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
-        n, d_out_rp, d_w, src, deg_old, rowsum, bigrows);
-    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+        n, d_out_rp, nullptr, src, deg_old, rowsum, bigrows);
+    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, nullptr, src, deg_old, rowsum, bigrows);
     BUILD_TRY(cudaGetLastError());
-    if (d_w) {
-      row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(n, rowsum, dmask_old);
-      if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, s>>>(m, d_w, src, rowsum, src_val);
-      BUILD_TRY(cudaGetLastError());
-    }
   }
   BUILD_TRY(dev_malloc_async((void **)&rp_old, sizeof(int64_t) * (n + 1), s));
   rp_from_sorted<<<grid_for(m + 1, 256), 256, 0, s>>>(K, m, n, rp_old);
@@ -403,10 +402,6 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     permute_nodes<<<grid_for(n, 256), 256, 0, s>>>(SK, SV, n, maxdeg, g->perm, inv_perm, new_deg,
                                                    deg_old, g->deg);
     BUILD_TRY(cudaGetLastError());
-    if (g->weighted) {
-      permute_dmask<<<(unsigned)ceil_div<int64_t>(n, 256), 256, 0, s>>>(g->perm, n, dmask_old, g->dmask_w);
-      BUILD_TRY(cudaGetLastError());
-    }
   } else {
     BUILD_TRY(cudaMemsetAsync(new_deg, 0, sizeof(int64_t), s));
   }
@@ -430,6 +425,17 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   if (g->weighted) {
     BUILD_TRY(dev_malloc_async(&g->in_val, sizeof(float) * ms, s));
     BUILD_TRY(cudaMemsetAsync(g->in_val, 0, sizeof(float) * ms, s));
+  }
+  // the weights: everything above ran while they were being copied
+  if (w_ready) BUILD_TRY(cudaStreamWaitEvent(s, w_ready, 0));
+  if (d_w && n > 0) {
+    out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
+        n, d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+    row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(n, rowsum, dmask_old);
+    if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, s>>>(m, d_w, src, rowsum, src_val);
+    permute_dmask<<<(unsigned)ceil_div<int64_t>(n, 256), 256, 0, s>>>(g->perm, n, dmask_old, g->dmask_w);
+    BUILD_TRY(cudaGetLastError());
   }
   if (m > 0) {
     scatter_edges<<<grid_for(m, 256), 256, 0, s>>>(K, O, m, rp_old, inv_perm, g->in_rp, src, src_val,

@@ -127,7 +127,7 @@ __global__ void radix_upsweep(const uint32_t *keys, int64_t n, int shift, uint32
 // memory in digit order, (d) coalesced copy-out: consecutive threads write
 // consecutive positions of a digit's run.
 // vals == nullptr: the value of item idx is idx.
-__global__ void __launch_bounds__(kSortThreads) radix_downsweep(const uint32_t *keys, const uint32_t *vals,
+__global__ void __launch_bounds__(kSortThreads, 3) radix_downsweep(const uint32_t *keys, const uint32_t *vals,
                                                                 uint32_t *okeys, uint32_t *ovals, int64_t n,
                                                                 int shift, const uint32_t *offs, int64_t tiles) {
   constexpr int kChunks = kPerWarp / kWarp;
@@ -143,6 +143,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_downsweep(const uint32_t *
   const int64_t wbase = tbase + (int64_t)w * kPerWarp;
   const unsigned lt_mask = (1u << lane) - 1u;
   uint32_t k[kChunks];
+  unsigned pk[kChunks];  // each item's peers (same digit) in its 32-item chunk
   // (a)
 #pragma unroll
   for (int c = 0; c < kChunks; ++c) {
@@ -150,8 +151,8 @@ __global__ void __launch_bounds__(kSortThreads) radix_downsweep(const uint32_t *
     const bool valid = idx < n;
     k[c] = valid ? keys[idx] : 0u;
     const unsigned dig = valid ? ((k[c] >> shift) & 0xFF) : 0x100u;
-    const unsigned peers = __match_any_sync(0xffffffffu, dig);
-    if (valid && lane == __ffs(peers) - 1) wcnt[w][dig] += __popc(peers);
+    pk[c] = __match_any_sync(0xffffffffu, dig);
+    if (valid && lane == __ffs(pk[c]) - 1) wcnt[w][dig] += __popc(pk[c]);
     __syncwarp();
   }
   __syncthreads();
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_downsweep(const uint32_t *
     const int64_t idx = wbase + c * kWarp + lane;
     const bool valid = idx < n;
     const unsigned dig = valid ? ((k[c] >> shift) & 0xFF) : 0x100u;
-    const unsigned peers = __match_any_sync(0xffffffffu, dig);
+    const unsigned peers = pk[c];
     const uint32_t pos = valid ? wcnt[w][dig] + __popc(peers & lt_mask) : 0u;
     __syncwarp();
     if (valid) {

@@ -107,6 +107,7 @@ struct BatchState {
   float *x0 = nullptr;        // warm-start vectors of the wave (set-major, original order)
   float *out = nullptr;       // results of the wave (set-major, original order)
   float *hstage[2] = {nullptr, nullptr};  // pinned host copies of two waves' results
+  cudaEvent_t sev[2] = {nullptr, nullptr};  // after each pinned copy
   WaveState *hwave = nullptr;             // pinned: two polled copies of the wave record
   cudaEvent_t wev[2] = {nullptr, nullptr};
   std::vector<int32_t> inv_perm;  // host: original id -> relabelled row
@@ -124,6 +125,8 @@ void batch_free(Graph &g) {
   cudaFree(b->d_inv_perm);
   if (b->hstage[0]) cudaFreeHost(b->hstage[0]);
   if (b->hstage[1]) cudaFreeHost(b->hstage[1]);
+  for (cudaEvent_t e : b->sev)
+    if (e) cudaEventDestroy(e);
   if (b->hwave) cudaFreeHost(b->hwave);
   for (cudaEvent_t e : b->wev)
     if (e) cudaEventDestroy(e);
@@ -890,6 +893,8 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   if (staged && !b->hstage[0]) {
     GOPS_CUDA_TRY(cudaMallocHost(&b->hstage[0], block_bytes));
     GOPS_CUDA_TRY(cudaMallocHost(&b->hstage[1], block_bytes));
+    GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->sev[0], cudaEventDisableTiming));
+    GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->sev[1], cudaEventDisableTiming));
   }
   constexpr int kScatterThreads = 4;
   struct Scatter {
@@ -901,6 +906,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     }
     ~Scatter() { join(0); join(1); }
   } scatter;
+
   // waves of sets of similar size: a set's step count falls with its size,
   // and a wave runs until its slowest column retires
   std::vector<int64_t> order(nsets);
@@ -908,6 +914,27 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
     return seed_ptr[a + 1] - seed_ptr[a] < seed_ptr[b + 1] - seed_ptr[b];
   });
+  // a wave whose block is being copied to hstage[q] and not yet scattered:
+  // its scatter starts once the copy's event has passed, while the next wave
+  // runs on the device (no stream synchronisation at the wave boundary)
+  struct PendingScatter {
+    int64_t set0 = -1;
+    int ncols = 0, q = 0;
+  } pend;
+  auto start_scatter = [&]() -> Status {
+    if (pend.set0 < 0) return Status::ok();
+    GOPS_CUDA_TRY(cudaEventSynchronize(b->sev[pend.q]));
+    const float *src = b->hstage[pend.q];
+    const int ncols_p = pend.ncols;
+    const std::vector<int64_t> ids(order.begin() + pend.set0, order.begin() + pend.set0 + ncols_p);
+    for (int t = 0; t < kScatterThreads; ++t)
+      scatter.t[pend.q].emplace_back([=]() {
+        for (int c = t; c < ncols_p; c += kScatterThreads)
+          std::memcpy(scores + ids[c] * n, src + (size_t)c * n, sizeof(float) * (size_t)n);
+      });
+    pend.set0 = -1;
+    return Status::ok();
+  };
   // Host side of a wave (personalization entries, column records), built for
   // wave w+1 while wave w runs on the device.
   struct HostWave {
@@ -1058,6 +1085,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       GOPS_TRY(poll_after(q));
       pending[npend++] = q;
     }
+    GOPS_TRY(start_scatter());  // the previous wave's block, while this wave runs
     if (set0 + kCols < nsets) prep(hw[((set0 / kCols) + 1) & 1], set0 + kCols);  // overlaps this wave
     bool finished = false;
     while (npend > 0) {
@@ -1101,10 +1129,15 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       GOPS_CUDA_TRY(cudaGetLastError());
       ++launches;
       if (staged) {
-        scatter.join((int)((set0 / kCols) & 1));
-        GOPS_CUDA_TRY(cudaMemcpyAsync(b->hstage[(set0 / kCols) & 1], b->out, sizeof(float) * (size_t)ncols * n,
+        const int q = (int)((set0 / kCols) & 1);
+        scatter.join(q);  // the scatter of two waves ago read this buffer
+        GOPS_CUDA_TRY(cudaMemcpyAsync(b->hstage[q], b->out, sizeof(float) * (size_t)ncols * n,
                                       cudaMemcpyDeviceToHost, st));
+        GOPS_CUDA_TRY(cudaEventRecord(b->sev[q], st));
         ctx->stats.d2h_bytes += sizeof(float) * (size_t)ncols * n;
+        pend.set0 = set0;
+        pend.ncols = ncols;
+        pend.q = q;
       } else if (!scores_on_device) {
         for (int c = 0; c < ncols; ++c)
           GOPS_CUDA_TRY(cudaMemcpyAsync(scores + order[set0 + c] * n, b->out + (size_t)c * n, sizeof(float) * (size_t)n,
@@ -1114,18 +1147,8 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     }
     GOPS_CUDA_TRY(cudaMemcpyAsync(cols_all + (set0 / kCols) * kCols, b->cols, sizeof(ColState) * kCols,
                                   cudaMemcpyDeviceToDevice, st));
-    if (staged) GOPS_CUDA_TRY(cudaStreamSynchronize(st));
-    if (staged) {  // the block is in the pinned buffer: scatter it in the background
-      const int q = (int)((set0 / kCols) & 1);
-      const float *src = b->hstage[q];
-      const std::vector<int64_t> ids(order.begin() + set0, order.begin() + set0 + ncols);
-      for (int t = 0; t < kScatterThreads; ++t)
-        scatter.t[q].emplace_back([=]() {
-          for (int c = t; c < ncols; c += kScatterThreads)
-            std::memcpy(scores + ids[c] * n, src + (size_t)c * n, sizeof(float) * (size_t)n);
-        });
-    }
   }
+  GOPS_TRY(start_scatter());  // the last wave's block
   std::vector<ColState> cols_res((size_t)nwaves * kCols);
   GOPS_CUDA_TRY(cudaMemcpyAsync(cols_res.data(), cols_all, sizeof(ColState) * cols_res.size(), cudaMemcpyDeviceToHost,
                                 st));

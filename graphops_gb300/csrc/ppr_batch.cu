@@ -921,6 +921,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     int64_t set0 = -1;
     int ncols = 0, q = 0;
   } pend;
+  int pend_copy_q = -1;  // the last wave whose block went to a pinned buffer
   auto start_scatter = [&]() -> Status {
     if (pend.set0 < 0) return Status::ok();
     GOPS_CUDA_TRY(cudaEventSynchronize(b->sev[pend.q]));
@@ -1121,6 +1122,8 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     // ---- results of the wave
     p.out = scores_on_device ? scores : b->out;
     if (scores) {
+      // the previous wave's pinned copy (on the copy stream) has read b->out
+      if (staged && pend_copy_q >= 0) GOPS_CUDA_TRY(cudaStreamWaitEvent(st, b->sev[pend_copy_q], 0));
       if (kCols == 32)
         batch_finalize_t<<<blocks_for(ceil_div<int64_t>(n, kTile), kBWarps, ctx->num_sms * 8), kBThreads, 0, st>>>(
             p, b->d_inv_perm);
@@ -1129,11 +1132,16 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       GOPS_CUDA_TRY(cudaGetLastError());
       ++launches;
       if (staged) {
+        // the copy to the pinned buffer runs on the copy stream, overlapping
+        // the next wave's steps
         const int q = (int)((set0 / kCols) & 1);
         scatter.join(q);  // the scatter of two waves ago read this buffer
+        GOPS_CUDA_TRY(cudaEventRecord(ctx->copy_ev[0], st));
+        GOPS_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[0], 0));
         GOPS_CUDA_TRY(cudaMemcpyAsync(b->hstage[q], b->out, sizeof(float) * (size_t)ncols * n,
-                                      cudaMemcpyDeviceToHost, st));
-        GOPS_CUDA_TRY(cudaEventRecord(b->sev[q], st));
+                                      cudaMemcpyDeviceToHost, ctx->copy_stream));
+        GOPS_CUDA_TRY(cudaEventRecord(b->sev[q], ctx->copy_stream));
+        pend_copy_q = q;
         ctx->stats.d2h_bytes += sizeof(float) * (size_t)ncols * n;
         pend.set0 = set0;
         pend.ncols = ncols;

@@ -1,13 +1,14 @@
 // Graph ingestion on the device.
 //
-//  K1  out-adjacency (adapter order) -> in-edge CSR.  Per out-row: source ids,
-//      out-degree, weight sum sum max(w,0) and transition weights
+//  K1  out-adjacency (adapter order) -> in-edge CSR: a stable radix sort of
+//      edge ids by destination (read from the uploaded columns), so every
+//      in-row lists its sources in ascending source order, the order the
+//      reference scatters in (src/pagerank.rs:154-162); in-row offsets come
+//      from the sorted keys (no atomics on hub destinations).  Per out-row:
+//      source ids and out-degree (structure pass, before the weights have
+//      arrived), then weight sum sum max(w,0) and transition weights
 //      max(w,0)/sum (replacing the neighbor / out_wsum precompute of
-//      src/pagerank.rs:136-137,226-234 and src/ppr.rs:112); then a stable radix
-//      sort of edge ids by destination, so every in-row lists its sources in
-//      ascending source order, the order the reference scatters in
-//      (src/pagerank.rs:154-162).  In-row offsets come from the sorted keys
-//      (no atomics on hub destinations).
+//      src/pagerank.rs:136-137,226-234 and src/ppr.rs:112).
 //  K2  relabelling and the pull kernels' plan: a stable radix sort of nodes by
 //      in-degree (descending) gives perm; the in-edge CSR is rewritten in that
 //      order with relabelled sources; rows then fall into contiguous degree

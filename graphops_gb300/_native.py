@@ -63,6 +63,7 @@ class WarmStats(ctypes.Structure):
 # (name, restype, argtypes) for every symbol include/gops.h declares
 SIGNATURES = [
     ("gops_abi_version", ctypes.c_int, []),
+    ("gops_debug_fail_allocations_after", ctypes.c_int, [ctypes.c_int64]),
     ("gops_ctx_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_p)]),
     ("gops_ctx_destroy", None, [_p]),
     ("gops_last_error", ctypes.c_char_p, [_p]),

@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <new>
 
@@ -43,6 +44,16 @@ cudaMemPool_t library_pool(int device) {
     cudaGetLastError();  // a failed creation leaves the default pool in use
   }
   return g_pool[device];
+}
+
+static std::atomic<int64_t> g_alloc_fail_after{-1};  // < 0: no injection
+
+bool alloc_fault_injected() {
+  int64_t k = g_alloc_fail_after.load(std::memory_order_relaxed);
+  while (k > 0) {  // this allocation still succeeds
+    if (g_alloc_fail_after.compare_exchange_weak(k, k - 1, std::memory_order_relaxed)) return false;
+  }
+  return k == 0;
 }
 
 void library_pool_trim(int device) {
@@ -158,6 +169,11 @@ Status upload_impl(Ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *c
 extern "C" {
 
 int gops_abi_version(void) { return GOPS_ABI_VERSION; }
+
+int gops_debug_fail_allocations_after(int64_t count) {
+  g_alloc_fail_after.store(count < 0 ? -1 : count, std::memory_order_relaxed);
+  return GOPS_OK;
+}
 
 int gops_ctx_create(int device, gops_ctx **out) {
   if (!out) return GOPS_ERR_INVALID;

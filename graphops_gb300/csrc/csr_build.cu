@@ -483,9 +483,10 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     if (e == cudaSuccess && s2.code == GOPS_OK)
       e = cudaMemcpyAsync(&nht, nch + pl.n_hub, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e == cudaSuccess) e = dev_malloc_async(&g->hub_first, sizeof(int32_t) * (pl.n_hub + 1), s);
-    if (e == cudaSuccess) e = dev_malloc_async(&g->hub_task_row, sizeof(int32_t) * std::max<int64_t>(nht, 1), s);
-    if (e == cudaSuccess) {
+    const bool ok = e == cudaSuccess && s2.code == GOPS_OK;  // nch holds offsets only then
+    if (ok) e = dev_malloc_async(&g->hub_first, sizeof(int32_t) * (pl.n_hub + 1), s);
+    if (ok && e == cudaSuccess) e = dev_malloc_async(&g->hub_task_row, sizeof(int32_t) * std::max<int64_t>(nht, 1), s);
+    if (ok && e == cudaSuccess) {
       hub_fill<<<grid_for(pl.n_hub + 1, 256), 256, 0, s>>>(nch, pl.n_hub, g->hub_first, g->hub_task_row);
       e = cudaGetLastError();
     }

@@ -191,7 +191,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
 // library waits for its stream before it returns).
 cudaMemPool_t library_pool(int device);  // nullptr: pool not available
 void library_pool_trim(int device);
+// Host-side fault injection for tests (gops_debug_fail_allocations_after):
+// true when this allocation is to fail as if the device were out of memory.
+bool alloc_fault_injected();
 inline cudaError_t dev_malloc_async(void **p, size_t bytes, cudaStream_t s) {
+  if (alloc_fault_injected()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
   int d = 0;
   cudaError_t e = cudaGetDevice(&d);
   if (e != cudaSuccess) return e;

@@ -645,9 +645,22 @@ void workspace_free(Workspace &ws) {
   ws = Workspace{};
 }
 
+Status workspace_alloc(Ctx *ctx, Graph *g);
+
+// The solve workspace of a graph, allocated on first use; a failed
+// allocation leaves none of it behind.
 Status workspace_ensure(Ctx *ctx, Graph *g) {
+  if (g->ws.sums) return Status::ok();
+  Status st = workspace_alloc(ctx, g);
+  if (st.code != GOPS_OK) {
+    cudaStreamSynchronize(ctx->stream);
+    workspace_free(g->ws);
+  }
+  return st;
+}
+
+Status workspace_alloc(Ctx *ctx, Graph *g) {
   Workspace &ws = g->ws;
-  if (ws.sums) return Status::ok();
   const size_t n = (size_t)std::max<int64_t>(g->n, 1);
   const size_t nht = (size_t)std::max<int32_t>(g->plan.n_hub_tasks, 1);
   const size_t nh = (size_t)std::max<int32_t>(g->plan.n_hub, 1);

@@ -751,8 +751,21 @@ __global__ void __launch_bounds__(256) prow_from_sorted(const int32_t *rows, int
   }
 }
 
+Status batch_prepare_impl(Ctx *ctx, Graph *g);
+
+// The batched plan and workspace of a graph, built on first use; a failed
+// build leaves no partial state behind (the next call builds it again).
 Status batch_prepare(Ctx *ctx, Graph *g) {
   if (g->batch) return Status::ok();
+  Status st = batch_prepare_impl(ctx, g);
+  if (st.code != GOPS_OK) {
+    cudaStreamSynchronize(ctx->stream);
+    batch_free(*g);
+  }
+  return st;
+}
+
+Status batch_prepare_impl(Ctx *ctx, Graph *g) {
   cudaStream_t s = ctx->stream;
   BatchState *b = new BatchState();
   g->batch = b;

@@ -83,6 +83,12 @@ typedef struct gops_stats {
 /* ---- library / context (no reference counterpart: the reference is a pure
  * CPU crate with no device state) ---- */
 int gops_abi_version(void);
+/* Test hook (no reference counterpart): host-side fault injection.  With
+ * count >= 0 the next `count` device allocations of the library's pool
+ * succeed and every later one fails as if the device were out of memory
+ * (GOPS_ERR_OOM from the call that needed it), until called with count < 0.
+ * Lets tests drive every allocation-failure path without a GPU fault. */
+int gops_debug_fail_allocations_after(int64_t count);
 int gops_ctx_create(int device, gops_ctx **out);
 void gops_ctx_destroy(gops_ctx *ctx);
 const char *gops_last_error(const gops_ctx *ctx);

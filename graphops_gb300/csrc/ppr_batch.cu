@@ -830,6 +830,7 @@ Status ensure_entries(BatchState *b, int64_t e, cudaStream_t st) {
   GOPS_CUDA_TRY(cudaStreamSynchronize(st));  // earlier waves may still read the old arrays
   cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted);
   b->pslot = nullptr; b->pval = nullptr; b->prows_sorted = nullptr;
+  b->pcap = 0;  // a failed allocation below leaves no capacity claimed
   const int64_t cap = std::max<int64_t>(e, 1024);
   GOPS_CUDA_TRY(cudaMalloc(&b->pslot, sizeof(int32_t) * cap));
   GOPS_CUDA_TRY(cudaMalloc(&b->pval, sizeof(float2) * cap));

@@ -1207,7 +1207,9 @@ Status ensure_train(WarmModel &w, int64_t chunk) {
   }
   if (!w.gsign) GOPS_CUDA_TRY(cudaMalloc(&w.gsign, sizeof(int8_t) * kWMaxBatch * w.n));
   if (!w.csum) GOPS_CUDA_TRY(cudaMalloc(&w.csum, sizeof(float) * kWMaxBatch * w.r));
-  if (!w.gram) {
+  if (!w.gram || !w.rhs || !w.chol) {  // all three, or none after a failed attempt
+    cudaFree(w.gram); cudaFree(w.rhs); cudaFree(w.chol);
+    w.gram = nullptr; w.rhs = nullptr; w.chol = nullptr;
     GOPS_CUDA_TRY(cudaMalloc(&w.gram, sizeof(double) * F * F));
     GOPS_CUDA_TRY(cudaMalloc(&w.rhs, sizeof(double) * F * w.r));
     GOPS_CUDA_TRY(cudaMalloc(&w.chol, sizeof(double) * ((int64_t)F * F + (int64_t)F * w.r)));

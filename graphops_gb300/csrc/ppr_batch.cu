@@ -61,9 +61,11 @@ constexpr int kSpmmBig = 256;   // rows above this in-degree are chunked
 constexpr int kSpmmChunk = 256; // edges per chunk task
 constexpr int kBThreads = 256;
 constexpr int kBWarps = kBThreads / kWarp;
-constexpr double kBTheta = 1e-1;  // double-float phase while some column has ||r||_1 >= kBTheta
-// with caller warm starts: their first residual is already small (a learned
-// start is typically 0.1-0.3), so the FP32 phase may begin at step 2
+constexpr double kBTheta = 1e-1;  // double-float phase while some column has ||r||_1 >= its theta
+// judged warm starts (a finite r1_max): their first residual is already small
+// (a learned start is typically 0.1-0.3), so the FP32 phase may begin at step
+// 2; a column started from s (no judge, or a learned set over the push
+// budget) keeps the cold threshold, whatever its wave
 constexpr double kBThetaWarm = 5e-1;
 
 struct ColState {
@@ -74,6 +76,7 @@ struct ColState {
   int uniform;   // personalization is uniform (empty seed set)
   int rejected;  // warm start rejected after step 1 (its residual exceeded r1_max)
   double r1_max; // largest first-step residual accepted from a warm start
+  double theta;  // double-float phase while this column's step norm >= theta
 };
 
 struct WaveState {
@@ -164,7 +167,7 @@ struct BatchParams {
   df d, omd, inv_n;
   float fx_scale;
   double fx_inv;
-  double tol, theta;
+  double tol;
   unsigned long long k, max_iter;
 };
 
@@ -433,7 +436,7 @@ __device__ bool batch_prologue(const BatchParams &p, int lane, bool *active, df 
     if (blockIdx.x == 0 && threadIdx.x == 0) p.wave->done = 1;
     return false;
   }
-  const bool big = act && !(diff < p.theta);
+  const bool big = act && !(diff < p.cols[c].theta);
   const bool f32 = k > 1 && (*(volatile int *)&p.wave->f32_phase || !__any_sync(0xffffffffu, big));
   if (f32 == WANT_DF) return false;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -885,7 +888,6 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   p.omd = df_from_double(1.0 - cfg->damping);
   p.inv_n = df_from_double(1.0 / (double)n);
   p.tol = cfg->tolerance;
-  p.theta = x0 ? kBThetaWarm : kBTheta;
   p.max_iter = cfg->max_iterations;
 
   int occ_df = 0, occ_f = 0;
@@ -962,9 +964,11 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     h.ncols = (int)std::min<int64_t>(kCols, nsets - set0);
     h.cols.assign(kCols, ColState{});
     std::map<std::pair<int32_t, int32_t>, double> ent;
-    for (int c = 0; c < kCols; ++c)
-      h.cols[c] = ColState{0, 0.0, c < h.ncols ? 0 : 1, 0, 0, 0,
-                           r1_max && c < h.ncols ? r1_max[order[set0 + c]] : (double)INFINITY};
+    for (int c = 0; c < kCols; ++c) {
+      const double r1 = r1_max && c < h.ncols ? r1_max[order[set0 + c]] : (double)INFINITY;
+      h.cols[c] = ColState{0, 0.0, c < h.ncols ? 0 : 1, 0, 0, 0, r1,
+                           x0 && std::isfinite(r1) ? kBThetaWarm : kBTheta};
+    }
     for (int c = 0; c < h.ncols; ++c) {
       const int64_t a0 = seed_ptr[order[set0 + c]], a1 = seed_ptr[order[set0 + c] + 1];
       if (a1 == a0) { h.cols[c].uniform = 1; continue; }  // sum <= 0: uniform (src/ppr.rs:108)

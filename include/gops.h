@@ -330,7 +330,10 @@ int gops_ppr_batch_learned_device(gops_ctx *ctx, const gops_graph *g, gops_warm 
  * residual L1 norm is not below r1_max[s] (host, optional: NULL accepts every
  * start) is retired after that step and solved again from its
  * personalization vector (rejected[s] = 1).  gops_ppr_batch_learned is
- * gops_warm_predict followed by this call with r1_max = the cold residuals. */
+ * gops_warm_predict followed by this call with r1_max = the cold residuals.
+ * A set with a finite r1_max[s] leaves the double-float phase at a step norm
+ * of 0.5 instead of 0.1 (its first residual is already small); every other
+ * set, here or in gops_ppr_batch, keeps 0.1. */
 int gops_ppr_batch_judged_device(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,
                                  const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0_device,
                                  const double *r1_max, float *scores_device, gops_run *runs, int32_t *rejected);

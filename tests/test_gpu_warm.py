@@ -19,7 +19,7 @@ import torch
 
 import graphops_gb300 as go
 from graphops_gb300 import gen, warm
-from oracle import port
+from oracle import fp64, port
 from oracle import warm_oracle as wo
 
 pytestmark = pytest.mark.gpu
@@ -270,3 +270,44 @@ def test_budget_exceeded_starts_cold(small):
     assert np.abs(lr.scores.astype(np.float64) - ref).sum(1).max() <= 1e-7
     assert np.abs(lr.scores.astype(np.float64) - cold.scores.astype(np.float64)).sum(1).max() <= 5e-8
     assert not lr.rejected.any()
+
+
+def test_mixed_wave_judged_and_unjudged_starts(trained):
+    """One wave holding judged warm starts (finite r1_max: double-float phase
+    until 0.5) and starts from s with no judge (r1_max = inf: until 0.1).
+    The sets started from s follow the reference's own iterates (within 1e-7
+    of the restatement); the warm ones stop at another iterate of the same
+    chain, within the stopping rule's distance of its fixed point."""
+    g, dg, ws, conf, stats = trained
+    ns = 32
+    sp, si = gen.seed_sets(g, ns, 1, 8, seed=9)
+    n = g.n
+    x0 = torch.empty((ns, n), dtype=torch.float32, device="cuda")
+    r1 = ws.predict_device(0.85, sp, si, x0.data_ptr())
+    r1c = np.ascontiguousarray(r1, np.float64).copy()
+    for j in range(1, ns, 2):  # odd sets: start from s, no judge
+        s = np.zeros(n, np.float32)
+        np.add.at(s, si[sp[j]:sp[j + 1]], np.float32(1.0 / (sp[j + 1] - sp[j])))
+        x0[j] = torch.from_numpy(s).cuda()
+        r1c[j] = np.inf
+    out = torch.empty((ns, n), dtype=torch.float32, device="cuda")
+    runs = (go._native.Run * ns)()
+    rej = np.zeros(ns, dtype=np.int32)
+    c = go._native.Config(0.85, 1000, 1e-7)
+    l = dg.ctx._l
+    spp = np.ascontiguousarray(sp, np.int64)
+    sii = np.ascontiguousarray(si, np.int32)
+    dg.ctx.check(l.gops_ppr_batch_judged_device(dg.ctx.handle, dg.handle, ctypes.byref(c), ns,
+                                                go._native.ptr(spp), go._native.ptr(sii),
+                                                ctypes.c_void_p(x0.data_ptr()), go._native.ptr(r1c),
+                                                ctypes.c_void_p(out.data_ptr()),
+                                                ctypes.cast(runs, ctypes.c_void_p), go._native.ptr(rej)))
+    assert all(runs[j].converged for j in range(ns))
+    ref, _ = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-7, threads=8)
+    got = out.cpu().numpy().astype(np.float64)
+    assert np.abs(got[1::2] - ref[1::2]).sum(axis=1).max() <= 1e-7
+    for j in range(0, ns, 2):
+        p = np.zeros(n)
+        np.add.at(p, si[sp[j]:sp[j + 1]], 1.0)
+        x = fp64.fixed_point(n, g.row_ptr, g.col, 0.85, personalization=p)
+        assert np.abs(got[j] - x).sum() <= 1e-6, j

@@ -1,0 +1,48 @@
+"""Host-side helpers of the batched and learned paths and the test hook,
+callable without a device: the CSR form of seed sets, the warm-start
+defaults, Katz validation messages through the library, and the allocation
+fault hook's switch."""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+import graphops_gb300 as go
+from graphops_gb300 import _native, warm
+
+
+def test_seed_sets_to_csr():
+    sp, si = go.seed_sets_to_csr([[3, 1], [], [7, 7, 2]])
+    assert sp.tolist() == [0, 2, 2, 5] and si.tolist() == [3, 1, 7, 7, 2]
+    assert sp.dtype == np.int64 and si.dtype == np.int32
+    sp0, si0 = go.seed_sets_to_csr([])
+    assert sp0.tolist() == [0] and si0.size == 0
+
+
+def test_warm_defaults_and_overrides():
+    c = warm.default_config()
+    assert c.clusters == 128 and c.code_steps == 10 and c.kmeans_iters == 20
+    assert c.minibatch == 32 and c.chunk == 512 and c.epochs == 1
+    assert c.push_budget == 1 << 24 and c.lr > 0 and c.ridge >= 0
+    c2 = warm.default_config(clusters=72, seed=5)
+    assert c2.clusters == 72 and c2.seed == 5
+    with pytest.raises(AttributeError):
+        warm.default_config(no_such_field=1)
+
+
+@pytest.mark.parametrize("kw,msg", [
+    (dict(alpha=0.0), "alpha must be finite and > 0"),
+    (dict(alpha=math.nan), "alpha must be finite and > 0"),
+    (dict(beta=math.inf), "beta must be finite"),
+    (dict(tolerance=0.0), "tolerance must be finite and > 0"),
+])
+def test_katz_validate_messages(kw, msg):
+    with pytest.raises(go.InvalidParameter, match=msg):
+        go.KatzConfig(**kw).validate()
+
+
+def test_allocation_fault_hook_switch():
+    lib = _native.lib()
+    assert lib.gops_debug_fail_allocations_after(ctypes.c_int64(5)) == 0
+    assert lib.gops_debug_fail_allocations_after(ctypes.c_int64(-1)) == 0

@@ -167,6 +167,40 @@ def cpu_sample(g, a, iters):
     return g.m * it / dt / 1e9, it, dt
 
 
+def fp64_residual(row_ptr, col, weights, x, d=0.85, p=None):
+    """||F(x) - x||_1 of the reference's iteration map in FP64 on the host
+    (scipy), an independent check of a GPU result: F(x) = (1-d) p + d A x +
+    d D(x) q with A[v,u] = max(w,0)/ws(u) (weights None: 1/deg(u)), D(x) the
+    mass on dangling nodes, p the uniform vector (q = p) or a personalization
+    (q = p, src/ppr.rs:125-128).  The error of x against the exact fixed
+    point is at most this residual / (1 - d)."""
+    import scipy.sparse as sps
+    n = row_ptr.shape[0] - 1
+    src = np.repeat(np.arange(n), np.diff(row_ptr))
+    w = np.ones(col.shape[0]) if weights is None else np.maximum(np.asarray(weights, np.float64), 0.0)
+    ws = np.bincount(src, weights=w, minlength=n)
+    safe = np.where(ws > 0, ws, 1.0)
+    M = sps.csr_matrix((w / safe[src], col, row_ptr), shape=(n, n))  # M[u, v] = A[v, u]
+    x = np.asarray(x, np.float64)
+    q = np.full(n, 1.0 / n) if p is None else np.asarray(p, np.float64) / np.sum(p)
+    fx = (1.0 - d) * q + d * (M.T @ x) + d * x[ws == 0].sum() * q
+    return float(np.abs(fx - x).sum())
+
+
+def columns_accuracy(g, sp, si, scores, cols, d=0.85):
+    """fp64_residual of a few result columns of a batched solve (seed set c:
+    p = 1 per occurrence of each seed, normalised, src/ppr.rs:48-65); the
+    worst residual and its bound on the L1 distance from the exact vector."""
+    t0 = time.perf_counter()
+    worst = 0.0
+    for c in cols:
+        p = np.zeros(g.n)
+        np.add.at(p, si[sp[c]:sp[c + 1]], 1.0)
+        worst = max(worst, fp64_residual(g.row_ptr, g.col, None, scores[c], d=d, p=p))
+    return {"columns": [int(c) for c in cols], "worst_fp64_residual_l1": worst,
+            "l1_vs_fixed_point_bound": worst / (1.0 - d), "check_s": round(time.perf_counter() - t0, 2)}
+
+
 def cpu_all_cores(g, a):
     """A clearly separate all-cores CPU figure: the same iteration in pull
     form over an in-edge CSR (built first, not timed), rows split over every
@@ -309,11 +343,12 @@ def run_batch(a, ctx, rank, ws):
     dg2 = _native.DeviceGraph.from_csr(g.row_ptr, g.col, ctx=ctx)
     s, _, _, _ = dg2.ppr_batch(conf, sp, si, out=True)
     e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
+    acc = columns_accuracy(g, sp, si, s, (0, a.batch_sets // 2, a.batch_sets - 1)) if rank == 0 else None
     out = {"config": batch_workload(a), "seeds_per_s": round(ws * a.batch_sets / (t * 1e-3), 2),
            "ms": round(t, 3), "iterations_mean": float(its.mean()), "iterations_max": int(its.max()),
            "all_converged": bool(conv.all()), "kernel_launches": int(st.kernel_launches),
            "spmm_fp32_launch_ms": round(st.f32_ms / max(1, st.f32_launches), 4),
-           "roofline": batch_roofline(g, st),
+           "roofline": batch_roofline(g, st), "accuracy": acc,
            "e2e": {"seeds_per_s": round(ws * a.batch_sets / e2e_s, 2),
                    "h2d_bytes_per_step": int(g.row_ptr.nbytes + g.col.nbytes + sp.nbytes + si.nbytes),
                    "d2h_bytes_per_step": int(s.nbytes)}}
@@ -385,6 +420,7 @@ def run_learned(a, ctx, rank, ws):
     s = model.ppr_batch(conf, sp, si, scores=True).scores
     e2e_l = max_over_ranks(time.perf_counter() - t0, ws)
     d2h = int(s.nbytes)
+    acc = columns_accuracy(g, sp, si, s, (0, a.learned_sets // 2, a.learned_sets - 1)) if rank == 0 else None
     del s
     t0 = time.perf_counter()
     s, _, _, _ = dg.ppr_batch(conf, sp, si, out=True)
@@ -398,7 +434,7 @@ def run_learned(a, ctx, rank, ws):
            "learned_ms": round(tl, 3), "plain_ms": round(tp, 3),
            "iterations_mean_learned": float(lr.iterations.mean()),
            "iterations_mean_plain": float(its_p.mean()),
-           "rejected": int(lr.rejected.sum()),
+           "rejected": int(lr.rejected.sum()), "accuracy_learned": acc,
            "all_converged": bool(lr.converged.all() and conv_p.all()),
            "kernel_launches_learned": int(st_l.kernel_launches),
            "train": {"sets": int(tst.sets), "adam_steps": int(tst.steps),
@@ -573,6 +609,17 @@ def run_gpu(a):
     e_ms = max_over_ranks(max(e0.elapsed_time(e1), wall * 1e3), ws)
     e2e_value = ws * m * e_iters / (e_ms * 1e-3) / 1e9
 
+    # ---- accuracy of the timed end-to-end result, checked on the host ----
+    quality = None
+    if rank == 0:
+        t0 = time.perf_counter()
+        res = fp64_residual(g.row_ptr, g.col, g.weight, out_h.numpy(), d=conf.damping)
+        quality = {"fp64_residual_l1": res, "l1_vs_fixed_point_bound": res / (1.0 - conf.damping),
+                   "sum": float(out_h.numpy().sum()), "min": float(out_h.numpy().min()),
+                   "check_s": round(time.perf_counter() - t0, 2),
+                   "how": "||F(x) - x||_1 of the FP64 iteration map (scipy) at the e2e result x; "
+                          "||x - x*||_1 <= residual / (1 - d)"}
+
     # ---- CPU baseline (rank 0, bounded sample) ----
     cpu = None
     if rank == 0 and not a.no_cpu:
@@ -610,6 +657,7 @@ def run_gpu(a):
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
                          "df_phase_mean_ms": round(df_ms / max(1, df_n), 5), "df_launches": df_n},
             "gpu_launches": launches,
+            "accuracy": quality,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
             "dense_small": dense_small,

@@ -119,7 +119,8 @@ def pagerank_run_dense(M, damping=0.85, max_iterations=100, tolerance=1e-6):
 
 def ppr_many(row_ptr, col, seed_ptr, seed_idx, damping=0.85, max_iterations=100,
              tolerance=1e-6, threads=1, want_scores=True):
-    """One reference PPR solve per seed set (p = 1 on each seed); returns
+    """One reference PPR solve per seed set (p = 1 per occurrence of each
+    seed, so a repeated node counts twice); returns
     (scores[nsets, n] or None, iterations[nsets])."""
     rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
     cl = np.ascontiguousarray(col, dtype=np.int32)

@@ -160,3 +160,40 @@ def test_all_cores_timing_form_matches_serial_restatement():
         b = port.pagerank_weighted_run_mt(g.row_ptr, g.col, w, 0.85, 1000, 1e-8, threads=t)
         assert b[1] == a[1] and b[3] == a[3]
         assert np.abs(b[0] - a[0]).sum() <= 1e-12
+
+
+def test_bench_accuracy_check_bounds_the_error():
+    """bench.py's host check of the timed result (||F(x) - x||_1 of the FP64
+    iteration map, scipy) is ~0 at the FP64 fixed point, and residual/(1-d)
+    bounds the L1 distance of a converged restatement iterate from it, for
+    weighted PageRank and for a personalization."""
+    import bench
+    from graphops_gb300 import gen
+    g = gen.rmat(10, 8, weighted=True, seed=3)
+    w = g.weight.astype(np.float64)
+    x = fp64.fixed_point(g.n, g.row_ptr, g.col, 0.85, weights=w)
+    assert bench.fp64_residual(g.row_ptr, g.col, w, x) < 1e-13
+    xr = port.pagerank_weighted_run(g.row_ptr, g.col, w, 0.85, 1000, 1e-8)[0]
+    res = bench.fp64_residual(g.row_ptr, g.col, w, xr)
+    assert 0.0 < res < 1e-8 and np.abs(xr - x).sum() <= res / 0.15
+    p = np.zeros(g.n); p[[3, 5]] = 1.0
+    xp = fp64.fixed_point(g.n, g.row_ptr, g.col, 0.85, personalization=p)
+    assert bench.fp64_residual(g.row_ptr, g.col, None, xp, p=p) < 1e-13
+    # a wrong vector is caught
+    assert bench.fp64_residual(g.row_ptr, g.col, w, np.full(g.n, 1.0 / g.n)) > 1e-3
+
+
+def test_bench_column_accuracy_of_seed_sets():
+    """The batched sections' check: seed set c means p = 1 per occurrence of
+    each seed (a repeated node counts twice); converged restatement columns
+    pass with residual below the tolerance, and swapped columns are caught."""
+    import bench
+    from graphops_gb300 import gen
+    g = gen.rmat(10, 8, seed=4)
+    sp = np.array([0, 2, 5, 6], np.int64)
+    si = np.array([3, 9, 7, 7, 100, 42], np.int32)
+    x, _ = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-9)
+    acc = bench.columns_accuracy(g, sp, si, x, (0, 1, 2))
+    assert acc["worst_fp64_residual_l1"] < 1e-9
+    bad = bench.columns_accuracy(g, sp, si, x[::-1].copy(), (0, 1, 2))
+    assert bad["worst_fp64_residual_l1"] > 1e-2

@@ -46,3 +46,45 @@ def test_allocation_fault_hook_switch():
     lib = _native.lib()
     assert lib.gops_debug_fail_allocations_after(ctypes.c_int64(5)) == 0
     assert lib.gops_debug_fail_allocations_after(ctypes.c_int64(-1)) == 0
+
+
+NULL_EXEMPT = {
+    # no context argument, or a value-returning query with its own null answer
+    "gops_abi_version", "gops_debug_fail_allocations_after", "gops_ctx_create", "gops_config_validate",
+    "gops_weights_validate", "gops_personalization_validate", "gops_katz_config_validate",
+    "gops_warm_config_default", "gops_ctx_destroy", "gops_graph_destroy", "gops_warm_destroy",
+    "gops_last_error", "gops_ctx_stream", "gops_ctx_scores_device", "gops_warm_count",
+}
+
+
+def null_args(argtypes):
+    out = []
+    for t in argtypes:
+        if t in (ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, ctypes.c_size_t):
+            out.append(t(0))
+        elif t is ctypes.c_double:
+            out.append(0.5)
+        else:
+            out.append(None)
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(n for n, r, _ in _native.SIGNATURES if n not in NULL_EXEMPT))
+def test_every_entry_point_rejects_a_null_context(name):
+    """A NULL context (and NULL everything else) is GOPS_ERR_INVALID before
+    any device call, for every status-returning entry point."""
+    lib = _native.lib()
+    fn = getattr(lib, name)
+    assert fn(*null_args(fn.argtypes)) == _native.GOPS_ERR_INVALID, name
+
+
+def test_null_queries_and_destroys_are_safe():
+    lib = _native.lib()
+    lib.gops_ctx_destroy(None)
+    lib.gops_graph_destroy(None)
+    lib.gops_warm_destroy(None)
+    assert lib.gops_last_error(None) == b"null context"
+    assert lib.gops_ctx_stream(None) is None
+    assert lib.gops_ctx_scores_device(None) is None
+    assert lib.gops_warm_count(None, 0) == -1
+    assert lib.gops_graph_info(None, None, None, None) == _native.GOPS_ERR_INVALID

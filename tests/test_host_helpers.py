@@ -88,3 +88,37 @@ def test_null_queries_and_destroys_are_safe():
     assert lib.gops_ctx_scores_device(None) is None
     assert lib.gops_warm_count(None, 0) == -1
     assert lib.gops_graph_info(None, None, None, None) == _native.GOPS_ERR_INVALID
+
+
+def _no_device():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+
+
+def test_no_silent_cpu_fallback_without_a_device():
+    """Without a GPU every solve raises (no CPU code path); only the
+    reference's n == 0 early return needs no device."""
+    _no_device()
+    g = go.CsrAdjacency(np.array([0, 1, 2, 3]), np.array([1, 2, 0], np.int32), np.ones(3))
+    cfg = go.PageRankConfig()
+    for call in (lambda: go.pagerank_run(g, cfg), lambda: go.pagerank_weighted_run(g, cfg),
+                 lambda: go.personalized_pagerank_run(g, cfg, [1.0, 0.0, 0.0]),
+                 lambda: go.katz_centrality_run(g, go.KatzConfig()),
+                 lambda: go.eigenvector_centrality_run(g, 100, 1e-6)):
+        with pytest.raises(go.GopsError) as ei:
+            call()
+        assert ei.value.code == _native.GOPS_ERR_NO_DEVICE
+    empty = go.pagerank_run(go.CsrAdjacency(np.array([0]), np.array([], np.int32)), cfg)
+    assert empty.scores.size == 0 and empty.iterations == 0 and empty.converged
+
+
+def test_bench_gpu_arm_fails_without_a_device():
+    """bench.py's own arm has no CPU path either: no JSON line, non-zero exit."""
+    _no_device()
+    import subprocess
+    import sys
+    from conftest import ROOT
+    r = subprocess.run([sys.executable, "bench.py", "--steps", "1", "--warmup", "3", "--scale", "10", "--no-cpu"],
+                       capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode != 0 and not any(x.startswith("{") for x in r.stdout.splitlines())

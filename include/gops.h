@@ -177,7 +177,8 @@ int gops_ppr_batch_device(gops_ctx *ctx, const gops_graph *g, const gops_config 
                           float *scores_device, gops_run *runs);
 
 /* Device pointer (double, n entries) of the last solve's scores, valid until
- * the next solve on this context. */
+ * the next solve on this context or the destruction of the graph that solve
+ * ran on, whichever comes first (the vector lives in the graph's workspace). */
 const double *gops_ctx_scores_device(const gops_ctx *ctx);
 
 /* gops_pagerank_run without any allocation.  No counterpart in the

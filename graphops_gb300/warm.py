@@ -18,6 +18,10 @@ below the cold start's is rejected and that set is solved again from s.
 from __future__ import annotations
 
 import ctypes
+import hashlib
+import json
+import os
+import struct
 from dataclasses import dataclass
 from typing import Optional
 
@@ -46,6 +50,93 @@ def default_config(**kw) -> WarmConfig:
             raise AttributeError(k)
         setattr(c, k, v)
     return c
+
+
+# ---- checkpoint file: a trained model's parameters and cluster coupling ----
+#
+#   magic "GOPSWARM" | u32 version | u32 header length | header (UTF-8 JSON)
+#   | payload: the arrays, little-endian, each starting on a 16-byte boundary
+#
+# The header holds the model's configuration, the graph's n, m and a SHA-256
+# of its out-adjacency (row_ptr as int64, col as int32), and for each array
+# its name, dtype, count and offset within the payload.  The clusters, the
+# code and the features are not learned: a model created with the same
+# configuration on the same graph rebuilds them (k-means is seeded), and the
+# clusters are stored only to check that it did.
+
+CHECKPOINT_MAGIC = b"GOPSWARM"
+CHECKPOINT_VERSION = 1
+
+
+def config_to_dict(cfg: WarmConfig) -> dict:
+    return {name: getattr(cfg, name) for name, _ in cfg._fields_}
+
+
+def config_from_dict(d: dict) -> WarmConfig:
+    return default_config(**d)
+
+
+def graph_digest(row_ptr, col) -> str:
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(row_ptr, dtype="<i8").tobytes())
+    h.update(np.ascontiguousarray(col, dtype="<i4").tobytes())
+    return h.hexdigest()
+
+
+def write_checkpoint(path, meta: dict, arrays: dict) -> None:
+    """Writes meta (JSON-serialisable) and named 1-D arrays (float32 or int32)
+    to path, through a temporary file renamed into place."""
+    entries, blobs, off = [], [], 0
+    for name, a in arrays.items():
+        a = np.ascontiguousarray(a)
+        dt = {np.dtype(np.float32): "<f4", np.dtype(np.int32): "<i4"}.get(a.dtype)
+        if dt is None or a.ndim != 1:
+            raise ValueError(f"array {name!r}: 1-D float32 or int32 expected")
+        b = a.astype(dt).tobytes()
+        entries.append({"name": name, "dtype": dt, "count": int(a.shape[0]), "offset": off})
+        pad = (-len(b)) % 16
+        blobs.append(b + b"\0" * pad)
+        off += len(b) + pad
+    head = json.dumps(dict(meta, arrays=entries), sort_keys=True).encode()
+    pre = CHECKPOINT_MAGIC + struct.pack("<II", CHECKPOINT_VERSION, len(head)) + head
+    pre += b"\0" * ((-len(pre)) % 16)
+    tmp = f"{os.fspath(path)}.tmp"
+    with open(tmp, "wb") as f:
+        f.write(pre)
+        for b in blobs:
+            f.write(b)
+    os.replace(tmp, path)
+
+
+def read_checkpoint(path):
+    """(meta, {name: array}) of a file written by write_checkpoint; raises
+    ValueError for another format, another version or a truncated file."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if len(data) < 16 or data[:8] != CHECKPOINT_MAGIC:
+        raise ValueError("not a warm-start checkpoint")
+    version, hlen = struct.unpack_from("<II", data, 8)
+    if version != CHECKPOINT_VERSION:
+        raise ValueError(f"checkpoint version {version} is not supported (expected {CHECKPOINT_VERSION})")
+    if 16 + hlen > len(data):
+        raise ValueError("truncated checkpoint")
+    try:
+        meta = json.loads(data[16:16 + hlen].decode())
+        entries = meta.pop("arrays")
+    except (UnicodeDecodeError, json.JSONDecodeError, KeyError, AttributeError) as e:
+        raise ValueError("corrupt checkpoint header") from e
+    base = 16 + hlen + (-(16 + hlen)) % 16
+    arrays = {}
+    for e in entries:
+        if e.get("dtype") not in ("<f4", "<i4"):
+            raise ValueError("corrupt checkpoint header")
+        dt = np.dtype(e["dtype"])
+        lo = base + int(e["offset"])
+        hi = lo + int(e["count"]) * dt.itemsize
+        if lo < base or hi < lo or hi > len(data):
+            raise ValueError("truncated checkpoint")
+        arrays[e["name"]] = np.frombuffer(data[lo:hi], dtype=dt).astype(dt.newbyteorder("="))
+    return meta, arrays
 
 
 @dataclass
@@ -82,6 +173,38 @@ class WarmStart:
                                                      ctypes.byref(cfg), ctypes.byref(h)))
         self.handle = h
         self.config = cfg
+        self._rp, self._col = rp, cc  # for the graph digest of a checkpoint
+
+    def save(self, path) -> None:
+        """Writes the trained parameters and cluster coupling (and what a
+        load checks them against) to a checkpoint file."""
+        meta = {"config": config_to_dict(self.config), "n": int(self.n), "m": int(self._col.shape[0]),
+                "graph_sha256": graph_digest(self._rp, self._col)}
+        write_checkpoint(path, meta, {"params": self.get(PARAMS), "coupling": self.get(COUPLING),
+                                      "clusters": self.get(CLUSTERS)})
+
+    @classmethod
+    def load(cls, path, graph: "_native.DeviceGraph", row_ptr, col) -> "WarmStart":
+        """A model for graph with the parameters and coupling of a checkpoint.
+        The graph must be the one the model was saved for (same out-adjacency);
+        the model is rebuilt with the saved configuration and its clusters are
+        checked against the saved ones before the parameters are set."""
+        meta, arrays = read_checkpoint(path)
+        rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+        cc = np.ascontiguousarray(col, dtype=np.int32)
+        if (meta["n"] != rp.shape[0] - 1 or meta["m"] != cc.shape[0]
+                or meta["graph_sha256"] != graph_digest(rp, cc)):
+            raise ValueError("checkpoint was saved for a different graph")
+        model = cls(graph, rp, cc, config_from_dict(meta["config"]))
+        try:
+            if not np.array_equal(model.get(CLUSTERS), arrays["clusters"]):
+                raise ValueError("rebuilt clusters differ from the checkpoint's")
+            model.set(PARAMS, arrays["params"])
+            model.set(COUPLING, arrays["coupling"])
+        except Exception:
+            model.close()
+            raise
+        return model
 
     def close(self):
         if getattr(self, "handle", None):

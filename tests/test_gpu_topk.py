@@ -65,23 +65,3 @@ def test_normalize_device():
     z = torch.tensor([0.0, 0.0], dtype=torch.float64, device="cuda")
     normalize_device(z.data_ptr(), 2)                       # sum 0: unchanged
     assert (z.cpu().numpy() == 0).all()
-
-
-def test_solve_left_on_device_then_top_k_there():
-    """A solve without a host buffer leaves its scores on the device
-    (gops_ctx_scores_device), where top_k reads them: the same entries as the
-    host copy of the same (bitwise-repeatable) solve.  The context's counters
-    show the one copy to the host."""
-    g = gen.rmat(12, 16, weighted=True, seed=12)
-    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col, g.weight.astype(np.float64))
-    conf = go.PageRankConfig(0.85, 1000, 1e-8)
-    s, it, _, conv = dg.pagerank_weighted_run(conf)
-    st = dg.ctx.stats()
-    assert conv and st.d2h_bytes == 8 * g.n and st.kernel_launches > 0
-    _, it2, _, _ = dg.pagerank_weighted_run(conf, out=False)
-    assert it2 == it and dg.ctx.stats().d2h_bytes == 0
-    ptr = dg.ctx._l.gops_ctx_scores_device(dg.ctx.handle)
-    assert ptr
-    got = top_k_device(ptr, g.n, 100, ctx=dg.ctx)
-    want = ref_top_k(s, 100)
-    assert [i for i, _ in got] == want and [v for _, v in got] == [s[i] for i in want]

@@ -7,8 +7,9 @@ a fixed scratch array inside the library, so its output must equal the
 regular entry point's.  Two calls in a row check that the shared scratch,
 which keeps the previous call's contents, is reset correctly.
 
-This file sorts last so that a run stopping at the first failure has already
-run every other test; it passes alone in a fresh process as well.
+This file sorts after the parity, batch, warm-start and upload tests, so that
+a run stopping at the first failure has already run them; it passes alone in
+a fresh process as well.
 """
 import ctypes
 

@@ -122,3 +122,43 @@ def test_bench_gpu_arm_fails_without_a_device():
     r = subprocess.run([sys.executable, "bench.py", "--steps", "1", "--warmup", "3", "--scale", "10", "--no-cpu"],
                        capture_output=True, text=True, timeout=300, cwd=ROOT)
     assert r.returncode != 0 and not any(x.startswith("{") for x in r.stdout.splitlines())
+
+
+STRUCTS = [("gops_config", "Config"), ("gops_run", "Run"), ("gops_stats", "Stats"),
+           ("gops_katz_config", "KatzConfig"), ("gops_warm_config", "WarmConfig"),
+           ("gops_warm_stats", "WarmStats")]
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every struct the Python binding passes through the ABI has the C
+    header's size, field names, field offsets and field sizes (compiled with
+    the host C compiler against include/gops.h)."""
+    import shutil
+    import subprocess
+    from conftest import ROOT
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "gops.h"', 'int main(void) {']
+    for cname, pyname in STRUCTS:
+        lines.append(f'  printf("{pyname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in getattr(_native, pyname)._fields_:
+            lines.append(f'  printf("{pyname} {fname} %zu %zu\\n", offsetof({cname}, {fname}), '
+                         f'sizeof((({cname} *)0)->{fname}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", f"{ROOT}/include", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln:
+            parts = ln.split()
+            got[tuple(parts[:2])] = tuple(int(x) for x in parts[2:])
+    for _, pyname in STRUCTS:
+        cls = getattr(_native, pyname)
+        assert got[(pyname, "size")] == (ctypes.sizeof(cls),), pyname
+        for fname, ftype in cls._fields_:
+            desc = getattr(cls, fname)
+            assert got[(pyname, fname)] == (desc.offset, ctypes.sizeof(ftype)), (pyname, fname)

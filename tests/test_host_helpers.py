@@ -162,3 +162,44 @@ def test_ctypes_structs_match_the_header(tmp_path):
         for fname, ftype in cls._fields_:
             desc = getattr(cls, fname)
             assert got[(pyname, fname)] == (desc.offset, ctypes.sizeof(ftype)), (pyname, fname)
+
+
+SCALARS = {"int": ctypes.c_int, "int32_t": ctypes.c_int32, "int64_t": ctypes.c_int64, "uint64_t": ctypes.c_uint64,
+           "size_t": ctypes.c_size_t, "double": ctypes.c_double, "float": ctypes.c_float}
+
+
+def header_prototypes():
+    import re
+    from conftest import ROOT
+    src = open(f"{ROOT}/include/gops.h").read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(gops_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src):
+        params = [p.strip() for p in m.group(3).split(",") if p.strip() and p.strip() != "void"]
+        protos[m.group(2)] = (m.group(1).strip(), params)
+    return protos
+
+
+def test_ctypes_signatures_match_the_header():
+    """Arity, and for each parameter pointer-or-scalar (scalars of the same C
+    type), of every binding signature against include/gops.h's prototypes;
+    the return kinds likewise."""
+    protos = header_prototypes()
+    for name, res, args in _native.SIGNATURES:
+        ret, params = protos[name]
+        assert len(params) == len(args), name
+        for p, a in zip(params, args):
+            if "*" in p:
+                assert a in (ctypes.c_void_p, ctypes.c_char_p) or issubclass(a, ctypes._Pointer), (name, p)
+            else:
+                ctype = " ".join(w for w in p.replace("const ", "").split()[:-1])
+                assert SCALARS[ctype] is a or ctypes.sizeof(SCALARS[ctype]) == ctypes.sizeof(a) and \
+                    (SCALARS[ctype] in (ctypes.c_double, ctypes.c_float)) == (a in (ctypes.c_double, ctypes.c_float)), \
+                    (name, p)
+        if ret == "void":
+            assert res is None, name
+        elif "*" in ret:
+            assert res in (ctypes.c_void_p, ctypes.c_char_p), name
+        else:
+            assert res is SCALARS[ret.replace("const ", "").strip()] or \
+                ctypes.sizeof(res) == ctypes.sizeof(SCALARS[ret.strip()]), name

@@ -113,7 +113,7 @@ def random_proptest_graph(rng, n):
     return M
 
 
-def main():
+def build_cases():
     cases = []
     cyc = [[0.0, 1.0, 0.0], [0.0, 0.0, 1.0], [1.0, 0.0, 0.0]]
     cases.append(case("doctest_3cycle", "src/pagerank.rs:103-112", dense_nb(cyc), exact=True))
@@ -135,7 +135,7 @@ def main():
     # multigraph adapter order, duplicates, a self loop, dangling nodes
     multi = [[1, 1, 2, 0], [2], [], [0, 2, 2], [4]]
     cases.append(case("multigraph_plain", "src/graph.rs:26-39 (duplicates counted)", multi))
-    mw = [[0.5, 0.5, 2.0, 1.0], [1.0], [], [-1.0, float("nan") if False else 0.0, 3.0], [0.0]]
+    mw = [[0.5, 0.5, 2.0, 1.0], [1.0], [], [-1.0, 0.0, 3.0], [0.0]]
     cases.append(case("multigraph_weighted_clamps", "src/pagerank.rs:227-261 (max(w,0), w>0)", multi, mw))
     cases.append(case("multigraph_ppr", "src/ppr.rs:90-156", multi, personalization=[0.0, 2.0, 0.0, 1.0, 0.0]))
     cases.append(case("ppr_zero_sum_uniform", "src/ppr.rs:104-109", multi, personalization=[0.0] * 5))
@@ -151,6 +151,11 @@ def main():
     cases.append(case("random40_weighted", "src/pagerank.rs:210-289", nb, ws, tolerance=1e-10, max_iterations=200))
     pers = [float(rng.randrange(0, 3)) for _ in range(40)]
     cases.append(case("random40_ppr", "src/ppr.rs:90-156", nb, personalization=pers, tolerance=1e-10, max_iterations=200))
+    return cases
+
+
+def main():
+    cases = build_cases()
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, f, indent=1)
     print(f"wrote {len(cases)} cases")

@@ -197,3 +197,19 @@ def test_bench_column_accuracy_of_seed_sets():
     assert acc["worst_fp64_residual_l1"] < 1e-9
     bad = bench.columns_accuracy(g, sp, si, x[::-1].copy(), (0, 1, 2))
     assert bad["worst_fp64_residual_l1"] > 1e-2
+
+
+def test_golden_fixture_is_what_its_generator_makes():
+    """tests/golden/golden.json is exactly the output of
+    tests/golden/make_golden.py (pure-Python restatement + exact rationals),
+    so the fixture's provenance is checked on every run."""
+    import importlib.util
+    import json
+    import os
+    from conftest import ROOT
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(ROOT, "tests", "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    made = json.loads(json.dumps({"generator": "tests/golden/make_golden.py", "cases": mg.build_cases()}))
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+        assert json.load(f) == made

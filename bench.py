@@ -16,6 +16,14 @@ GTEPS = m * iterations / time.
             against the measured HBM copy bandwidth.
   cpu_baseline  the oracle's C restatement of pagerank_weighted_run (the
             reference is single-threaded) on a bounded number of iterations.
+  accuracy  ||F(x) - x||_1 of the FP64 iteration map at the end-to-end result
+            x, computed on the host with scipy, and the bound it gives on the
+            L1 distance from the exact fixed point; the batched and learned
+            sections carry the same check for three of their result columns.
+
+The same line carries dense_small (the n = 2000 dense-matrix case, latency),
+ppr_batched (seeds/s on R-MAT 20) and ppr_learned (learned warm start vs
+plain batched seeds/s on the block-model graph).
 
 --impl reference times that CPU restatement alone, in the same JSON shape.
 Multi-GPU: one replica per rank (the solve does not shard without an

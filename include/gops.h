@@ -123,7 +123,7 @@ int gops_personalization_validate(int64_t node_count, int64_t len, const double 
  * device builds the in-edge CSR from it (transpose by stable radix sort),
  * the FP32 transition weights max(w,0)/sum_u max(w,0), and the dangling sets
  * of both the unweighted (deg == 0) and weighted (weight sum == 0) chains.
- * Requires n < 2^31 and m < 2^31. */
+ * Requires n < 2^31 - 1 and m < 2^31 - 1 (int32 indices on the device). */
 int gops_graph_upload(gops_ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *col,
                       const double *weights, gops_graph **out);
 

@@ -195,18 +195,42 @@ def fp64_residual(row_ptr, col, weights, x, d=0.85, p=None):
     return float(np.abs(fx - x).sum())
 
 
-def columns_accuracy(g, sp, si, scores, cols, d=0.85):
-    """fp64_residual of a few result columns of a batched solve (seed set c:
-    p = 1 per occurrence of each seed, normalised, src/ppr.rs:48-65); the
-    worst residual and its bound on the L1 distance from the exact vector."""
+def top_order_matches(a, b, k=100):
+    """The k largest entries of a in the order of b's, ties in b within
+    1e-15 relative counting as equal (top_k sorts unstably, src/topk.rs:40)."""
+    ia = np.argsort(-a, kind="stable")[:k]
+    ib = np.argsort(-b, kind="stable")[:k]
+    return bool(all(x == y or abs(b[x] - b[y]) <= 1e-15 * max(abs(b[x]), 1e-300) for x, y in zip(ia, ib)))
+
+
+def columns_accuracy(g, sp, si, scores, cols, d=0.85, iterations=None):
+    """Checks of a few result columns of a batched solve (seed set c: p = 1
+    per occurrence of each seed, normalised, src/ppr.rs:48-65): the FP64
+    residual ||F(x) - x||_1 and its bound on the distance from the exact
+    vector, and the measured L1 distance from the oracle's C restatement of
+    personalized_pagerank_run on the same sets (with top-100 order and, when
+    `iterations` is given, the step counts)."""
+    from oracle import port
     t0 = time.perf_counter()
     worst = 0.0
     for c in cols:
         p = np.zeros(g.n)
         np.add.at(p, si[sp[c]:sp[c + 1]], 1.0)
         worst = max(worst, fp64_residual(g.row_ptr, g.col, None, scores[c], d=d, p=p))
-    return {"columns": [int(c) for c in cols], "worst_fp64_residual_l1": worst,
-            "l1_vs_fixed_point_bound": worst / (1.0 - d), "check_s": round(time.perf_counter() - t0, 2)}
+    cols = [int(c) for c in cols]
+    sp2 = np.zeros(len(cols) + 1, np.int64)
+    sp2[1:] = np.cumsum([sp[c + 1] - sp[c] for c in cols])
+    si2 = np.concatenate([si[sp[c]:sp[c + 1]] for c in cols]).astype(np.int32)
+    ref, its = port.ppr_many(g.row_ptr, g.col, sp2, si2, d, 1000, 1e-7, threads=len(cols))
+    l1 = [float(np.abs(scores[c].astype(np.float64) - ref[q]).sum()) for q, c in enumerate(cols)]
+    out = {"columns": cols, "worst_fp64_residual_l1": worst, "l1_vs_fixed_point_bound": worst / (1.0 - d),
+           "l1_vs_restatement": l1, "l1_vs_restatement_max": max(l1),
+           "top100_match": all(top_order_matches(scores[c].astype(np.float64), ref[q]) for q, c in enumerate(cols)),
+           "restatement_iterations": [int(x) for x in its]}
+    if iterations is not None:
+        out["iterations"] = [int(iterations[c]) for c in cols]
+    out["check_s"] = round(time.perf_counter() - t0, 2)
+    return out
 
 
 def cpu_all_cores(g, a):
@@ -351,7 +375,8 @@ def run_batch(a, ctx, rank, ws):
     dg2 = _native.DeviceGraph.from_csr(g.row_ptr, g.col, ctx=ctx)
     s, _, _, _ = dg2.ppr_batch(conf, sp, si, out=True)
     e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
-    acc = columns_accuracy(g, sp, si, s, (0, a.batch_sets // 2, a.batch_sets - 1)) if rank == 0 else None
+    acc = (columns_accuracy(g, sp, si, s, (0, a.batch_sets // 2, a.batch_sets - 1), iterations=its)
+           if rank == 0 else None)
     out = {"config": batch_workload(a), "seeds_per_s": round(ws * a.batch_sets / (t * 1e-3), 2),
            "ms": round(t, 3), "iterations_mean": float(its.mean()), "iterations_max": int(its.max()),
            "all_converged": bool(conv.all()), "kernel_launches": int(st.kernel_launches),
@@ -359,7 +384,8 @@ def run_batch(a, ctx, rank, ws):
            "roofline": batch_roofline(g, st), "accuracy": acc,
            "e2e": {"seeds_per_s": round(ws * a.batch_sets / e2e_s, 2),
                    "h2d_bytes_per_step": int(g.row_ptr.nbytes + g.col.nbytes + sp.nbytes + si.nbytes),
-                   "d2h_bytes_per_step": int(s.nbytes)}}
+                   "d2h_bytes_per_step": int(s.nbytes),
+                   "includes": "graph upload and device CSR build, seed sets up, every score block to the host"}}
     del s
     if rank == 0 and not a.no_cpu:
         threads = max(1, os.cpu_count() or 1)
@@ -428,12 +454,24 @@ def run_learned(a, ctx, rank, ws):
     s = model.ppr_batch(conf, sp, si, scores=True).scores
     e2e_l = max_over_ranks(time.perf_counter() - t0, ws)
     d2h = int(s.nbytes)
-    acc = columns_accuracy(g, sp, si, s, (0, a.learned_sets // 2, a.learned_sets - 1)) if rank == 0 else None
+    acc = (columns_accuracy(g, sp, si, s, (0, a.learned_sets // 2, a.learned_sets - 1), iterations=lr.iterations)
+           if rank == 0 else None)
     del s
     t0 = time.perf_counter()
     s, _, _, _ = dg.ppr_batch(conf, sp, si, out=True)
     e2e_p = max_over_ranks(time.perf_counter() - t0, ws)
     del s
+    # what the trained network gains: the same pipeline with the network off
+    # (w = 1 for every node: w3 = b3 = 0; same push, clusters and coupling)
+    params = model.get(warm.PARAMS)
+    off = params.copy()
+    off[warm.P_W3:warm.P_B3 + 1] = 0.0
+    model.set(warm.PARAMS, off)
+    model.ppr_batch(conf, sp[:65], si[:sp[64]], scores=False)  # refreshes w for the new parameters
+    lo = model.ppr_batch(conf, sp, si, scores=False)
+    st_o = ctx.stats()
+    model.set(warm.PARAMS, params)
+    to = max_over_ranks(st_o.solve_ms, ws)
     n_sets = a.learned_sets
     out = {"config": learned_workload(a),
            "learned_seeds_per_s": round(ws * n_sets / (tl * 1e-3), 2),
@@ -443,6 +481,15 @@ def run_learned(a, ctx, rank, ws):
            "iterations_mean_learned": float(lr.iterations.mean()),
            "iterations_mean_plain": float(its_p.mean()),
            "rejected": int(lr.rejected.sum()), "accuracy_learned": acc,
+           "ablation": {"trained_iterations_mean": float(lr.iterations.mean()),
+                        "network_off_iterations_mean": float(lo.iterations.mean()),
+                        "cold_iterations_mean": float(its_p.mean()),
+                        "trained_seeds_per_s": round(ws * n_sets / (tl * 1e-3), 2),
+                        "network_off_seeds_per_s": round(ws * n_sets / (to * 1e-3), 2),
+                        "cold_seeds_per_s": round(ws * n_sets / (tp * 1e-3), 2),
+                        "network_off_rejected": int(lo.rejected.sum()),
+                        "how": "network off = every node's weight w = 1 (w3 = b3 = 0): the same exact push, "
+                               "clusters and least-squares coupling, each cluster's tail mass spread evenly"},
            "all_converged": bool(lr.converged.all() and conv_p.all()),
            "kernel_launches_learned": int(st_l.kernel_launches),
            "train": {"sets": int(tst.sets), "adam_steps": int(tst.steps),
@@ -451,7 +498,9 @@ def run_learned(a, ctx, rank, ws):
                      "wall_s": round(train_s, 2), "model_build_s": round(create_s, 2)},
            "e2e": {"learned_seeds_per_s": round(ws * n_sets / e2e_l, 2),
                    "plain_seeds_per_s": round(ws * n_sets / e2e_p, 2),
-                   "h2d_bytes_per_step": int(sp.nbytes + si.nbytes), "d2h_bytes_per_step": d2h}}
+                   "h2d_bytes_per_step": int(sp.nbytes + si.nbytes), "d2h_bytes_per_step": d2h,
+                   "includes": "seed sets up, inference, every score block to the host; the graph and the "
+                               "trained model stay on the device (built once, before the timed calls)"}}
     if rank == 0 and not a.no_cpu:
         threads = max(1, os.cpu_count() or 1)
         ns = min(n_sets, threads)
@@ -624,19 +673,29 @@ def run_gpu(a):
         res = fp64_residual(g.row_ptr, g.col, g.weight, out_h.numpy(), d=conf.damping)
         quality = {"fp64_residual_l1": res, "l1_vs_fixed_point_bound": res / (1.0 - conf.damping),
                    "sum": float(out_h.numpy().sum()), "min": float(out_h.numpy().min()),
+                   "iterations": int(e_iters // e2e_steps),
                    "check_s": round(time.perf_counter() - t0, 2),
                    "how": "||F(x) - x||_1 of the FP64 iteration map (scipy) at the e2e result x; "
-                          "||x - x*||_1 <= residual / (1 - d)"}
+                          "||x - x*||_1 <= residual / (1 - d); l1_vs_restatement against the oracle's "
+                          "C restatement of pagerank_weighted_run on the same graph"}
 
-    # ---- CPU baseline (rank 0, bounded sample) ----
+    # ---- CPU baseline (rank 0): one full solve of the C restatement on one
+    # thread; its result is also the parity reference of the accuracy object
     cpu = None
     if rank == 0 and not a.no_cpu:
-        ci = cpu_iters_for(g, a)
-        v, it, dt = cpu_sample(g, a, ci)
-        cpu = {"value": round(v, 6), "unit": "GTEPS", "cores": 1, "kind": "port",
-               "sample": f"{it} iterations of pagerank_weighted_run ({dt:.1f} s), C restatement, "
+        from oracle import port
+        t0 = time.perf_counter()
+        ref, rit, _, _ = port.pagerank_weighted_run(g.row_ptr, g.col, g.weight.astype(np.float64), conf.damping,
+                                                    a.max_iter, a.tol)
+        dt = time.perf_counter() - t0
+        cpu = {"value": round(m * rit / dt / 1e9, 6), "unit": "GTEPS", "cores": 1, "kind": "port",
+               "sample": f"a full solve ({rit} iterations, {dt:.1f} s) of pagerank_weighted_run, C restatement, "
                          f"FP64, single thread (the reference path is single-threaded)"}
         cpu["all_cores"] = cpu_all_cores(g, a)
+        quality["l1_vs_restatement"] = float(np.abs(out_h.numpy() - ref).sum())
+        quality["top100_match"] = top_order_matches(out_h.numpy(), ref)
+        quality["restatement_iterations"] = int(rit)
+        del ref
 
     dense_small = run_dense_small(a, ctx, rank)
     batch = None

@@ -196,6 +196,13 @@ int gops_ctx_create(int device, gops_ctx **out) {
     gops_ctx_destroy(c);
     return e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA;
   }
+  // the no-allocation entry point's scratch array: mapped on this device now
+  const Status na = noalloc_attach(device);
+  if (na.code != GOPS_OK) {
+    gops_ctx_destroy(c);
+    return na.code;
+  }
+  x.noalloc_attached = true;
   *out = c;
   return GOPS_OK;
 }
@@ -215,6 +222,7 @@ void gops_ctx_destroy(gops_ctx *ctx) {
   for (cudaEvent_t e : x.tev) cudaEventDestroy(e);
   if (x.stream) cudaStreamDestroy(x.stream);
   library_pool_trim(x.device);  // memory that no live graph or model holds
+  if (x.noalloc_attached) noalloc_detach(x.device);
   delete ctx;
 }
 

@@ -13,13 +13,21 @@
 //
 // Limits: at most kNoAllocMaxNodes nodes and kNoAllocMaxHubTasks hub tasks;
 // larger graphs are rejected with GOPS_ERR_INVALID.  The array (about 13 MB)
-// is held by every GPU that loads this library until the process exits.
-// Every call shares it and it keeps the last call's contents; the solve
-// clears what must start at zero.  Calls that overlap on the GPU (from two
-// contexts or streams at once) race on it and must be serialized by the
-// caller.  The first call on a device looks up the array's device address
-// (cudaGetSymbolAddress, once per device, with that device current), so that
-// first call should come before any stream capture.
+// is held by every GPU that uses this library until the process exits.
+// With CUDA's lazy module loading the array's memory is committed only when
+// this file's module is first loaded on a device, so gops_ctx_create loads
+// it: it looks up the array's device address (cudaGetSymbolAddress, with the
+// device current) for the context's device, and the no-alloc calls that
+// follow need no device memory of their own.  The cached address is dropped
+// when the last context on the device is destroyed and looked up again by
+// the next gops_ctx_create; a device reset while a context lives
+// invalidates it, like every other device object of the library.
+// Every call shares the array and it keeps the last call's contents; the
+// solve clears what must start at zero.  Calls that overlap on the GPU (from
+// two contexts or streams at once) race on it and must be serialized by the
+// caller.  After a no-alloc call, gops_ctx_scores_device points into the
+// array: the next no-alloc call on that device, from any context,
+// overwrites those scores.
 #include <cstdio>
 #include <mutex>
 
@@ -65,16 +73,18 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kLayout.total];
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned char *g_scratch_addr[kMaxDevices] = {};
+int g_live_contexts[kMaxDevices] = {};
 
-// Device address of the scratch array on `device` (which must be current).
-Status scratch_address(int device, unsigned char **out) {
+// Device address of the scratch array on `device` (which must be current),
+// looked up once per device and cached.  The caller holds g_mu.
+Status scratch_address_locked(int device, unsigned char **out) {
   if (device < 0 || device >= kMaxDevices) return Status{GOPS_ERR_INVALID, "device index out of range"};
-  std::lock_guard<std::mutex> lock(g_mu);
   if (!g_scratch_addr[device]) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess)
-      return Status{GOPS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)};
+      return Status{e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA,
+                    std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)};
     g_scratch_addr[device] = static_cast<unsigned char *>(p);
   }
   *out = g_scratch_addr[device];
@@ -100,6 +110,25 @@ Workspace workspace_in(unsigned char *base) {
 }
 
 }  // namespace
+
+// Called by gops_ctx_create with `device` current: loads this file's module
+// on the device (committing the array's memory) and caches its address.
+Status noalloc_attach(int device) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  unsigned char *base = nullptr;
+  GOPS_TRY(scratch_address_locked(device, &base));
+  ++g_live_contexts[device];
+  return Status::ok();
+}
+
+// Called by gops_ctx_destroy: the last context on a device drops the cached
+// address, so a context created after a device reset looks it up again.
+void noalloc_detach(int device) {
+  if (device < 0 || device >= kMaxDevices) return;
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (g_live_contexts[device] > 0 && --g_live_contexts[device] == 0) g_scratch_addr[device] = nullptr;
+}
+
 }  // namespace gops
 
 using namespace gops;
@@ -123,7 +152,11 @@ extern "C" int gops_pagerank_run_noalloc(gops_ctx *ctx, const gops_graph *g, con
   cudaError_t e = cudaSetDevice(c.device);
   if (e != cudaSuccess) return c.set(Status{GOPS_ERR_CUDA, cudaGetErrorString(e)});
   unsigned char *base = nullptr;
-  Status st = scratch_address(c.device, &base);
+  Status st;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    st = scratch_address_locked(c.device, &base);
+  }
   if (st.code != GOPS_OK) return c.set(st);
   Workspace ws = workspace_in(base);
   return c.set(solve_plain_in_workspace(&c, const_cast<Graph *>(&gr), cfg, ws, scores, run));

@@ -33,23 +33,14 @@ struct Plan {
 
 constexpr int kHubChunk = 1024;      // edges per hub task (one warp)
 constexpr int kHubThreshold = 4096;  // rows above this in-degree are hubs
-#ifndef GOPS_PAD4
-#define GOPS_PAD4 1
-#endif
-// With kRowAlign == 4 every in-row is padded to a multiple of four edges
-// (padding: column n, weight 0; entry n of the gathered vectors is 0), so a
-// lane loads four edges with one aligned 16-byte load.
-constexpr int kRowAlign = GOPS_PAD4 ? 4 : 1;
-#ifndef GOPS_ROWS_PER_LANE
-#define GOPS_ROWS_PER_LANE 2
-#endif
-#ifndef GOPS_LANE_EDGES
-#define GOPS_LANE_EDGES 4
-#endif
-// rows interleaved per sub-warp in one warp task
-constexpr int kRowsPerLane = GOPS_ROWS_PER_LANE;
+// Every in-row is padded to a multiple of four edges (padding: column n,
+// weight 0; entry n of the gathered vectors is 0), so a lane loads four edges
+// with one aligned 16-byte load.
+constexpr int kRowAlign = 4;
+// rows interleaved per sub-warp in one warp task of the pull step
+constexpr int kRowsPerLane = 2;
 // target edges per lane when choosing a degree class's sub-warp width
-constexpr int kLaneEdges = GOPS_LANE_EDGES;
+constexpr int kLaneEdges = 4;
 
 // Solver workspace held by a graph (allocated on first solve, reused).
 struct Workspace {
@@ -117,6 +108,7 @@ struct Ctx {
   std::string last_error;
   gops_stats stats{};
   const double *last_scores = nullptr;  // device scores of the last solve
+  bool noalloc_attached = false;        // counted in the no-alloc scratch's live contexts
   int set(const Status &s) {
     if (s.code != GOPS_OK) last_error = s.msg;
     return s.code;
@@ -125,6 +117,10 @@ struct Ctx {
 
 Status solve_plain_in_workspace(Ctx *ctx, Graph *g, const gops_config *cfg, Workspace &ws,
                                 double *scores_host, gops_run *run);
+// the no-allocation entry point's scratch array (csrc/noalloc.cu): mapped on
+// a device with its first context, released with its last
+Status noalloc_attach(int device);
+void noalloc_detach(int device);
 // w_ready (optional): an event after which d_w is complete; the build
 // orders its first read of d_w after it.
 Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_rp,

@@ -45,66 +45,23 @@ enum Mode : int { kPlain = 0, kWeighted = 1, kPpr = 2 };
 
 constexpr int kThreads = 256;  // init / small kernels
 constexpr int kWarps = kThreads / kWarp;
-#ifndef GOPS_BLOCK
-#define GOPS_BLOCK 1024
-#endif
-#ifndef GOPS_GCACHE
-#define GOPS_GCACHE 32768
-#endif
-#ifndef GOPS_GCACHE_U
-#define GOPS_GCACHE_U 0
-#endif
-#ifndef GOPS_L1HINT
-#define GOPS_L1HINT 0
-#endif
-// iteration kernels: threads per block (one block per SM), and how many of
-// the first (hottest, after the in-degree relabelling) entries of the FP32
-// gathered vector each block of the FP32 phase stages in shared memory:
-// kGCache when the step reads transition weights, kGCacheU when it does not
-// (measured at R-MAT 22: a 32 K-entry cache takes the weighted FP32 step from
-// 0.246 to 0.231 ms; it does not pay for the unweighted step, nor for the
-// double-float phase, whose 8-byte entries halve what fits).
-constexpr int kIterThreads = GOPS_BLOCK;
+// Iteration kernels: one 1024-thread block per SM (64 registers per thread
+// fill the register file), and the first kGCache (hottest, after the
+// in-degree relabelling) entries of the FP32 gathered vector staged in shared
+// memory by every block of the weighted FP32 phase.  Measured at R-MAT 22: a
+// 32 K-entry cache takes the weighted FP32 step from 0.246 to 0.231 ms; it
+// does not pay for the unweighted step, nor for the double-float phase,
+// whose 8-byte entries halve what fits.
+constexpr int kIterThreads = 1024;
 constexpr int kIterWarps = kIterThreads / kWarp;
-constexpr int kGCache = GOPS_GCACHE;
-constexpr int kGCacheU = GOPS_GCACHE_U;
-constexpr bool kL1Hint = GOPS_L1HINT != 0;
-#ifndef GOPS_L1POL
-#define GOPS_L1POL 0
-#endif
-#ifndef GOPS_L1HOT
-#define GOPS_L1HOT 49152
-#endif
-// With kL1Policy the streams (columns, weights) and gathers of cold nodes do
-// not allocate in L1, and gathers of the first kL1Hot (hottest) nodes are
-// marked evict-last, so L1 holds the hot prefix of the gathered vector.
-constexpr bool kL1Policy = GOPS_L1POL != 0;
-constexpr int kL1Hot = GOPS_L1HOT;
-#ifndef GOPS_L2STREAM
-#define GOPS_L2STREAM 0
-#endif
-#ifndef GOPS_L2GATHER
-#define GOPS_L2GATHER 0
-#endif
-constexpr bool kL2Stream = GOPS_L2STREAM != 0;
-constexpr bool kL2Gather = GOPS_L2GATHER != 0;
-#ifndef GOPS_UNROLL
-#define GOPS_UNROLL 4
-#endif
-#ifndef GOPS_MINB
-#define GOPS_MINB 1
-#endif
-constexpr int kUnroll = GOPS_UNROLL;   // edges per lane per round and row
-constexpr int kMinBlocks = GOPS_MINB;  // occupancy hint for the iteration kernels
+constexpr int kGCache = 32768;
+constexpr int kUnroll = 4;  // edges per lane per round and row (one 16-byte load)
 // double-float phase while ||r||_1 >= kTheta.  Measured L1 against the FP64
 // fixed point on R-MAT 16-20 (tol 1e-8): 4.5e-9 at 1e-2, 4.8e-9 at 3e-2,
 // 6e-9 at 1e-1, for the same step counts; 1e-1 runs 3-4 fewer double-float
 // steps (2.4 % of a solve at R-MAT 22) but leaves 2.7e-8 on a small dense
 // random graph of the golden fixtures (bar 1e-8), so 1e-2 stays.
-#ifndef GOPS_THETA
-#define GOPS_THETA 1e-2
-#endif
-constexpr double kTheta = GOPS_THETA;
+constexpr double kTheta = 1e-2;
 
 struct IterParams {
   int64_t n;
@@ -134,106 +91,6 @@ struct IterParams {
   unsigned long long k, max_iter;
 };
 
-// Streamed loads (column indices, transition weights): with kL1Hint they do
-// not allocate in L1, which then keeps the hot lines of the gathered vector.
-// L2 policies (kL2Stream / kL2Gather): the edge streams, read once per step,
-// are loaded evict-first and the gathered vector (re-read ~16 times per step)
-// evict-last, so the streams do not push the gathered vector out of L2.
-__device__ __forceinline__ uint64_t l2_evict_first() {
-  uint64_t pol;
-  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-__device__ __forceinline__ uint64_t l2_evict_last() {
-  uint64_t pol;
-  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-__device__ __forceinline__ int4 ld_stream_v4i(const int32_t *a) {
-  int4 v;
-  if constexpr (kL2Stream) {
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.s32 {%0,%1,%2,%3}, [%4], %5;"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(a), "l"(l2_evict_first()));
-  } else if constexpr (kL1Hint || kL1Policy) {
-    asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(a));
-  } else {
-    v = __ldg(reinterpret_cast<const int4 *>(a));
-  }
-  return v;
-}
-__device__ __forceinline__ float4 ld_stream_v4f(const float *a) {
-  float4 v;
-  if constexpr (kL2Stream) {
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
-                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(a), "l"(l2_evict_first()));
-  } else if constexpr (kL1Hint || kL1Policy) {
-    asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
-                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(a));
-  } else {
-    v = __ldg(reinterpret_cast<const float4 *>(a));
-  }
-  return v;
-}
-// gathers under the L1 policy
-__device__ __forceinline__ float ld_gather_f32(const float *base, int32_t u) {
-  if constexpr (kL2Gather) {
-    float v;
-    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(base + u), "l"(l2_evict_last()));
-    return v;
-  } else if constexpr (kL1Policy) {
-    float v;
-    if (u < kL1Hot) asm volatile("ld.global.nc.L1::evict_last.f32 %0, [%1];" : "=f"(v) : "l"(base + u));
-    else asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(base + u));
-    return v;
-  } else {
-    return __ldg(base + u);
-  }
-}
-__device__ __forceinline__ float2 ld_gather_f2(const float2 *base, int32_t u) {
-  if constexpr (kL2Gather) {
-    float2 v;
-    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0,%1}, [%2], %3;"
-                 : "=f"(v.x), "=f"(v.y) : "l"(base + u), "l"(l2_evict_last()));
-    return v;
-  } else if constexpr (kL1Policy) {
-    float2 v;
-    if (u < kL1Hot / 2)
-      asm volatile("ld.global.nc.L1::evict_last.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(base + u));
-    else
-      asm volatile("ld.global.nc.L1::no_allocate.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(base + u));
-    return v;
-  } else {
-    return __ldg(base + u);
-  }
-}
-__device__ __forceinline__ int32_t ld_stream_i32(const int32_t *a) {
-  if constexpr (kL2Stream) {
-    int32_t v;
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(l2_evict_first()));
-    return v;
-  } else if constexpr (kL1Hint || kL1Policy) {
-    int32_t v;
-    asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(a));
-    return v;
-  } else {
-    return __ldg(a);
-  }
-}
-__device__ __forceinline__ float ld_stream_f32(const float *a) {
-  if constexpr (kL2Stream) {
-    float v;
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(l2_evict_first()));
-    return v;
-  } else if constexpr (kL1Hint || kL1Policy) {
-    float v;
-    asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(a));
-    return v;
-  } else {
-    return __ldg(a);
-  }
-}
-
 // --------------------------------------------------------------------------
 // precision policies
 // --------------------------------------------------------------------------
@@ -246,7 +103,7 @@ struct PrecDF {
   static constexpr bool kCache = false;
   template <int NC>
   __device__ static T load_g(const IterParams &p, const void *, int32_t u) {
-    const float2 g = ld_gather_f2(p.gdf_in, u);
+    const float2 g = __ldg(&p.gdf_in[u]);
     return {g.x, g.y};
   }
   template <int NC>
@@ -268,7 +125,7 @@ struct PrecF32 {
   template <int NC>
   __device__ static T load_g(const IterParams &p, const void *cache, int32_t u) {
     if (NC > 0 && u < NC) return reinterpret_cast<const float *>(cache)[u];
-    return ld_gather_f32(p.gf_in, u);
+    return __ldg(&p.gf_in[u]);
   }
   template <int NC>
   __device__ static void stage(const IterParams &p, void *cache) {
@@ -284,7 +141,7 @@ struct PrecF32 {
 // FP32 entries of the gathered vector staged in shared memory per block
 template <class P, int MODE>
 __host__ __device__ constexpr int cache_entries() {
-  return P::kCache ? (MODE == kWeighted ? kGCache : kGCacheU) : 0;
+  return P::kCache && MODE == kWeighted ? kGCache : 0;
 }
 
 struct Acc {
@@ -395,13 +252,15 @@ __device__ bool prologue(const IterParams &p, df *dsum) {
 }
 
 // R rows per sub-warp, their edges interleaved so that every lane keeps
-// R * kUnroll column loads, then R * kUnroll gathers, in flight.  Lane li of
-// a row's sub-warp takes edges eb+li, eb+li+SW, ... and adds them in that
-// order, so a row's sum does not depend on R or kUnroll.
+// R column loads (16 bytes: four edges each), then 4R gathers, in flight.
+// Rows start and end on 4-edge boundaries (padding edges: column n, weight
+// 0), so lane li of a row's sub-warp takes the quads li, li+SW, ... of each
+// row and adds them in that order: a row's sum does not depend on R.
 template <class P, int MODE, int R>
 __device__ __forceinline__ void rows_sum(const IterParams &p, const void *cache,
                                          const int32_t (&eb)[R], const int32_t (&ee)[R], int li,
                                          int SW, typename P::T (&s)[R]) {
+  static_assert(kRowAlign == 4 && kUnroll == 4, "one aligned quad per lane and round");
   constexpr int NC = cache_entries<P, MODE>();
   int32_t len = 0;
 #pragma unroll
@@ -409,77 +268,41 @@ __device__ __forceinline__ void rows_sum(const IterParams &p, const void *cache,
     s[q] = P::zero();
     len = max(len, ee[q] - eb[q]);
   }
-  if constexpr (kRowAlign == 4) {
-    // rows start and end on 4-edge boundaries: lane li takes the quads
-    // li, li+SW, ... of each row, kUnroll / 4 quads (at least one) per round
-    constexpr int QU = kUnroll >= 8 ? kUnroll / 4 : 1;
-    for (int32_t off = 4 * li; off < len; off += 4 * QU * SW) {
-      int4 c[R][QU];
-      float4 w[R][QU];
-      bool ok[R][QU];
+  for (int32_t off = 4 * li; off < len; off += 4 * SW) {
+    int4 c[R];
+    float4 w[R];
+    bool ok[R];
 #pragma unroll
-      for (int q = 0; q < R; ++q)
-#pragma unroll
-        for (int j = 0; j < QU; ++j) {
-          const int32_t e = eb[q] + off + 4 * j * SW;
-          ok[q][j] = e < ee[q];
-          c[q][j] = ok[q][j] ? ld_stream_v4i(&p.col[e]) : make_int4(0, 0, 0, 0);
-          w[q][j] = (MODE == kWeighted && ok[q][j]) ? ld_stream_v4f(&p.val[e])
-                                                     : make_float4(1.f, 1.f, 1.f, 1.f);
-        }
-      typename P::T g[R][QU][4];
-#pragma unroll
-      for (int q = 0; q < R; ++q)
-#pragma unroll
-        for (int j = 0; j < QU; ++j) {
-          g[q][j][0] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j].x) : P::zero();
-          g[q][j][1] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j].y) : P::zero();
-          g[q][j][2] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j].z) : P::zero();
-          g[q][j][3] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j].w) : P::zero();
-        }
-#pragma unroll
-      for (int q = 0; q < R; ++q)
-#pragma unroll
-        for (int j = 0; j < QU; ++j)
-          if (ok[q][j]) {
-            if (MODE == kWeighted) {
-              s[q] = P::add(s[q], P::scale(g[q][j][0], w[q][j].x));
-              s[q] = P::add(s[q], P::scale(g[q][j][1], w[q][j].y));
-              s[q] = P::add(s[q], P::scale(g[q][j][2], w[q][j].z));
-              s[q] = P::add(s[q], P::scale(g[q][j][3], w[q][j].w));
-            } else {
-              s[q] = P::add(s[q], g[q][j][0]);
-              s[q] = P::add(s[q], g[q][j][1]);
-              s[q] = P::add(s[q], g[q][j][2]);
-              s[q] = P::add(s[q], g[q][j][3]);
-            }
-          }
+    for (int q = 0; q < R; ++q) {
+      const int32_t e = eb[q] + off;
+      ok[q] = e < ee[q];
+      c[q] = ok[q] ? __ldg(reinterpret_cast<const int4 *>(&p.col[e])) : make_int4(0, 0, 0, 0);
+      w[q] = (MODE == kWeighted && ok[q]) ? __ldg(reinterpret_cast<const float4 *>(&p.val[e]))
+                                          : make_float4(1.f, 1.f, 1.f, 1.f);
     }
-    return;
-  }
-  for (int32_t off = li; off < len; off += kUnroll * SW) {
-    int32_t c[R][kUnroll];
-    float w[R][kUnroll];
-    bool ok[R][kUnroll];
+    typename P::T g[R][4];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      g[q][0] = ok[q] ? P::template load_g<NC>(p, cache, c[q].x) : P::zero();
+      g[q][1] = ok[q] ? P::template load_g<NC>(p, cache, c[q].y) : P::zero();
+      g[q][2] = ok[q] ? P::template load_g<NC>(p, cache, c[q].z) : P::zero();
+      g[q][3] = ok[q] ? P::template load_g<NC>(p, cache, c[q].w) : P::zero();
+    }
 #pragma unroll
     for (int q = 0; q < R; ++q)
-#pragma unroll
-      for (int j = 0; j < kUnroll; ++j) {
-        const int32_t e = eb[q] + off + j * SW;
-        ok[q][j] = e < ee[q];
-        c[q][j] = ok[q][j] ? ld_stream_i32(&p.col[e]) : 0;
-        w[q][j] = (MODE == kWeighted && ok[q][j]) ? ld_stream_f32(&p.val[e]) : 1.0f;
+      if (ok[q]) {
+        if (MODE == kWeighted) {
+          s[q] = P::add(s[q], P::scale(g[q][0], w[q].x));
+          s[q] = P::add(s[q], P::scale(g[q][1], w[q].y));
+          s[q] = P::add(s[q], P::scale(g[q][2], w[q].z));
+          s[q] = P::add(s[q], P::scale(g[q][3], w[q].w));
+        } else {
+          s[q] = P::add(s[q], g[q][0]);
+          s[q] = P::add(s[q], g[q][1]);
+          s[q] = P::add(s[q], g[q][2]);
+          s[q] = P::add(s[q], g[q][3]);
+        }
       }
-    typename P::T g[R][kUnroll];
-#pragma unroll
-    for (int q = 0; q < R; ++q)
-#pragma unroll
-      for (int j = 0; j < kUnroll; ++j) g[q][j] = ok[q][j] ? P::template load_g<NC>(p, cache, c[q][j]) : P::zero();
-#pragma unroll
-    for (int q = 0; q < R; ++q)
-#pragma unroll
-      for (int j = 0; j < kUnroll; ++j)
-        if (ok[q][j]) s[q] = P::add(s[q], MODE == kWeighted ? P::scale(g[q][j], w[q][j]) : g[q][j]);
   }
 }
 
@@ -545,7 +368,7 @@ __device__ __forceinline__ void hub_task(const IterParams &p, const void *cache,
 }
 
 template <class P, int MODE>
-__global__ void __launch_bounds__(kIterThreads, kMinBlocks) iterate_kernel(IterParams p) {
+__global__ void __launch_bounds__(kIterThreads, 1) iterate_kernel(IterParams p) {
   __shared__ long long bred[2][kIterWarps];
   __shared__ int bbad[kIterWarps];
   extern __shared__ __align__(16) unsigned char gcache[];
@@ -694,8 +517,6 @@ int grid_for_iter(const Ctx *ctx, const Graph *g) {
   int occ = 0;
   if (smem > 0)
     cudaFuncSetAttribute(iterate_kernel<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (kL1Policy && smem == 0)
-    cudaFuncSetAttribute(iterate_kernel<P, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, iterate_kernel<P, MODE>, kIterThreads, smem);
   occ = std::max(1, occ);
   const int64_t blocks_needed = ceil_div<int64_t>(std::max<int32_t>(g->plan.n_tasks, 1), kIterWarps);

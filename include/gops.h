@@ -178,7 +178,10 @@ int gops_ppr_batch_device(gops_ctx *ctx, const gops_graph *g, const gops_config 
 
 /* Device pointer (double, n entries) of the last solve's scores, valid until
  * the next solve on this context or the destruction of the graph that solve
- * ran on, whichever comes first (the vector lives in the graph's workspace). */
+ * ran on, whichever comes first (the vector lives in the graph's workspace).
+ * After gops_pagerank_run_noalloc the vector lives in that entry point's
+ * shared scratch array instead: it is valid only until the next no-alloc
+ * call on the same device, from any context. */
 const double *gops_ctx_scores_device(const gops_ctx *ctx);
 
 /* gops_pagerank_run without any allocation.  No counterpart in the
@@ -192,8 +195,11 @@ const double *gops_ctx_scores_device(const gops_ctx *ctx);
  * 262,144 nodes and 65,536 hub tasks, else GOPS_ERR_INVALID.  The graph must
  * already be uploaded (that call allocates).  All calls share the array:
  * calls that overlap on the GPU race and must be serialized by the caller.
- * The first call on a device looks up the array's address, so make it
- * before any stream capture. */
+ * The array is mapped on a device when the first context on it is created
+ * (gops_ctx_create loads its module and looks up its address, so that no
+ * later call needs device memory for it, also under CUDA's lazy module
+ * loading); the address is dropped with the device's last context.  After
+ * a call, gops_ctx_scores_device points into the shared array. */
 int gops_pagerank_run_noalloc(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg,
                               double *scores, gops_run *run);
 

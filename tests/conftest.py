@@ -40,3 +40,26 @@ def case_csr(c):
     if c["weights"] is not None:
         w = np.array([x for row in c["weights"] for x in row], dtype=np.float64)
     return rp, col, w
+
+
+def top_order_matches(a, b, k=100):
+    """True when the k largest entries of a come in the order of b's k
+    largest, ties in b within 1e-15 relative counting as equal (the
+    reference's top_k sorts by score with an unstable sort, src/topk.rs:40)."""
+    import numpy as np
+    ia = np.argsort(-a, kind="stable")[:k]
+    ib = np.argsort(-b, kind="stable")[:k]
+    for x, y in zip(ia, ib):
+        if x != y and abs(b[x] - b[y]) > 1e-15 * max(abs(b[x]), 1e-300):
+            return False
+    return True
+
+
+def sample_sets(sp, si, idx):
+    """The seed sets idx of (seed_ptr, seed_idx) as a new (seed_ptr, seed_idx)."""
+    import numpy as np
+    lens = np.diff(sp)[idx]
+    sp2 = np.zeros(len(idx) + 1, np.int64)
+    sp2[1:] = np.cumsum(lens)
+    si2 = np.concatenate([si[sp[i]:sp[i + 1]] for i in idx]).astype(np.int32) if len(idx) else np.zeros(0, np.int32)
+    return sp2, si2

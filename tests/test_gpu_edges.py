@@ -1,7 +1,6 @@
 """Entry points at their edges, through the C ABI: node and edge counts at
 the int32 limit refused from the scalars alone, and a solve's scores left on
-the device and read there by top_k.  This file sorts after the other GPU
-tests."""
+the device and read there by top_k."""
 import ctypes
 
 import numpy as np

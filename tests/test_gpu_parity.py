@@ -13,7 +13,7 @@ import pytest
 
 import graphops_gb300 as go
 from graphops_gb300 import gen
-from conftest import case_csr, load_golden
+from conftest import case_csr, load_golden, top_order_matches
 from oracle import fp64, port
 
 pytestmark = pytest.mark.gpu
@@ -30,15 +30,6 @@ DIFF_REL = 1e-2      # diff_l1 of a step taken in the FP32 phase carries accumul
 def cfg(c):
     return go.PageRankConfig(damping=c["damping"], max_iterations=c["max_iterations"],
                              tolerance=c["tolerance"])
-
-
-def top_order_matches(a, b, k=100):
-    ia = np.argsort(-a, kind="stable")[:k]
-    ib = np.argsort(-b, kind="stable")[:k]
-    for x, y in zip(ia, ib):
-        if x != y and abs(b[x] - b[y]) > 1e-15 * max(abs(b[x]), 1e-300):
-            return False
-    return True
 
 
 @pytest.mark.parametrize("c", GOLDEN, ids=[c["name"] for c in GOLDEN])

@@ -1,8 +1,7 @@
 """Save and load of a trained warm-start model (WarmStart.save / load): the
 loaded model has the same parameters, coupling and clusters and predicts the
 same start vectors; a checkpoint is refused for another graph.  The file
-format itself is tested without a device in test_warm_checkpoint.py.  This
-file sorts after the other GPU tests."""
+format itself is tested without a device in test_warm_checkpoint.py."""
 import numpy as np
 import pytest
 import torch

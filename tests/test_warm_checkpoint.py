@@ -1,7 +1,7 @@
 """The warm-start checkpoint file (graphops_gb300.warm.write_checkpoint /
 read_checkpoint) and its configuration and graph fingerprints, without a
 device.  The save/load round trip of a trained model on the GPU is in
-test_zzz_warm_checkpoint_gpu.py."""
+test_gpu_warm_checkpoint.py."""
 import struct
 
 import numpy as np

@@ -1,31 +1,50 @@
-#include <cstring>
-#include <thread>
 // Batched personalized PageRank (K5): many seed sets per pass over the graph.
 //
 // Each seed set is one independent personalized_pagerank_run of the
 // reference (src/ppr.rs:90-156) with personalization 1 on each seed node
 // (repeats count), normalised as src/ppr.rs:104-109 does -- an empty set gives
-// the uniform vector.  Sets run in waves of kCols columns.  Per wave the
-// library keeps row-major n x kCols blocks (relabelled node order) of the
-// gathered step vector, the double-float accumulator and the FP32 tail --
-// the residual form of the single solve (csrc/pagerank.cu), column by column:
+// the uniform vector.  Sets run in waves of KT columns, KT = 32 * CPL with
+// CPL (columns per lane) 1, 2 or 4.  Per wave the library keeps row-major
+// (n+1) x KT blocks (relabelled node order) of the gathered step vector, the
+// double-float accumulator and the FP32 tail -- the residual form of the
+// single solve (csrc/pagerank.cu), column by column:
 //   r_1 = F(x_0) - x_0,  r_{k+1} = A r_k,  x_k = x_0 + sum r,  diff_k = ||r_k||_1
 // with a double-float phase while some column's step norm is >= theta.
 //
-// Kernel layout: a warp owns a row and lane c owns column c, so every
-// gathered in-neighbour row is one coalesced 128-byte load (FP32 phase);
-// 32 column indices are loaded at once and broadcast by shuffles, eight
-// gathers in flight per lane.  Rows with more than kSpmmBig in-edges are split
-// into kSpmmChunk-edge warp tasks combined, in chunk order, by the task that
-// arrives last.  Per-column dangling and L1 sums are exact 64-bit fixed-point
-// integers held per lane, so every column's result is independent of the
-// others and of the schedule.  A column whose step norm fell below tol at step
-// k-1 retires at step k: its values freeze (the reference returns that x) and
-// it stops contributing; the wave ends when every column has retired or
-// max_iterations is reached.
+// Kernel layout: a warp owns a row and lane l owns columns l*CPL .. l*CPL +
+// CPL - 1, so every gathered in-neighbour row is one coalesced KT * 4-byte
+// read (128, 256 or 512 bytes in the FP32 phase), loaded as float / float2 /
+// float4 per lane; the column indices of four edges come in one 16-byte
+// broadcast load, and eight gathers per lane are in flight.  A wider k-tile
+// reads the in-edge index stream once for more sets and moves more bytes per
+// gather latency; the autotuner below picks it per graph.
+//
+// Canonical row sums.  A row's sum is defined independently of how the work
+// is split: its in-edges form base blocks of kBase edges (from the row's
+// first edge), each summed in edge order, and the block sums are added in
+// block order.  Rows with more than `chunk` in-edges are split into chunk
+// tasks (chunk a multiple of kBase) that write their blocks' sums, and the
+// task that arrives last adds them in order.  So every k-tile and chunk size
+// gives bit-identical results, and the autotuner's choice cannot change them.
+//
+// Per-column dangling and L1 sums are exact 64-bit fixed-point integers, so a
+// column's result is independent of the others and of the schedule.  A
+// column whose step norm fell below tol at step k-1 retires at step k: its
+// values freeze (the reference returns that x) and it stops contributing;
+// the wave ends when every column has retired or max_iterations is reached.
+//
+// Launch structure.  The kernels take no per-step or per-wave arguments: the
+// step number comes from the wave record (k = k0 + j + 1 for the j-th step of
+// a chunk; a one-thread kernel advances k0 after each chunk), the ping-pong
+// buffers by its parity, and the per-wave constants from a device struct.  So
+// a chunk of kChunkSteps steps is captured once as a CUDA graph and replayed
+// for every chunk of every wave; the host polls a pinned copy of the wave
+// record after each replay, with one chunk queued ahead.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <map>
+#include <thread>
 #include <vector>
 
 #include "objects.cuh"
@@ -33,35 +52,13 @@
 
 namespace gops {
 
-#ifndef GOPS_BCOLS
-#define GOPS_BCOLS 32
-#endif
-#ifndef GOPS_L2POL
-#define GOPS_L2POL 0
-#endif
-constexpr int kCols = GOPS_BCOLS;  // columns per wave (one lane each; 32/kCols rows per warp)
-constexpr int kRowsPerWarp = 32 / kCols;
-// With kL2Policy gathers of the step block are marked evict-last in L2 and
-// the streamed data (columns, accumulators, written blocks) evict-first, so
-// the gathered block stays L2-resident.
-constexpr bool kL2Policy = GOPS_L2POL != 0;
-#ifndef GOPS_BROWS
-#define GOPS_BROWS 1
-#endif
-#ifndef GOPS_BROWS_DF
-#define GOPS_BROWS_DF 1
-#endif
-#ifndef GOPS_BMINB
-#define GOPS_BMINB 1
-#endif
-constexpr int kBRowsF32 = GOPS_BROWS;   // rows interleaved per warp, FP32 phase
-constexpr int kBRowsDF = GOPS_BROWS_DF; // rows interleaved per warp, double-float phase
-constexpr int kBMinBlocks = GOPS_BMINB;
-constexpr int kSpmmBig = 256;   // rows above this in-degree are chunked
-constexpr int kSpmmChunk = 256; // edges per chunk task
+constexpr int kMaxCPL = 4;
+constexpr int kMaxKT = 32 * kMaxCPL;  // widest k-tile
+constexpr int kBase = 256;            // edges per base block of a row sum
 constexpr int kBThreads = 256;
 constexpr int kBWarps = kBThreads / kWarp;
-constexpr double kBTheta = 1e-1;  // double-float phase while some column has ||r||_1 >= its theta
+constexpr int kChunkSteps = 4;        // steps per launched (captured) chunk
+constexpr double kBTheta = 1e-1;      // double-float phase while some column has ||r||_1 >= its theta
 // judged warm starts (a finite r1_max): their first residual is already small
 // (a learned start is typically 0.1-0.3), so the FP32 phase may begin at step
 // 2; a column started from s (no judge, or a learned set over the push
@@ -77,6 +74,8 @@ struct ColState {
   int rejected;  // warm start rejected after step 1 (its residual exceeded r1_max)
   double r1_max; // largest first-step residual accepted from a warm start
   double theta;  // double-float phase while this column's step norm >= theta
+  int f32;       // in its FP32 phase (from the first step after its norm fell below theta)
+  int pad;
 };
 
 struct WaveState {
@@ -84,24 +83,49 @@ struct WaveState {
   int f32_phase;
   unsigned long long f32_from;
   unsigned long long steps;  // last step that did work
+  unsigned long long k0;     // steps launched before the current chunk
+};
+
+// Per-call and per-wave values, read by the kernels from device memory.
+struct WaveScalars {
+  df d, omd, inv_n;
+  float fx_scale;
+  int ncols;
+  double fx_inv;
+  double tol;
+  unsigned long long max_iter;
+  int has_x0;
+  int kt;  // columns of the wave's blocks (row stride)
+};
+struct WaveConst {
+  WaveScalars s;
+  int64_t xcol[kMaxKT], ocol[kMaxKT];  // set of each column: its row in x0 and in out
 };
 
 struct BatchState {
   int64_t n = 0;
-  // plan: rows [0, n_big) in chunk tasks, then one warp task per row
-  int32_t n_big = 0, n_big_tasks = 0;
-  int64_t n_tasks = 0;
-  int32_t *big_first = nullptr, *big_task_row = nullptr;
-  // wave workspace
+  // tile configuration in use and the workspace's capacity
+  int cpl = 0, chunk = 0;
+  int kt_cap = 0;
+  bool tuned = false;
+  float tune_ms[3][2] = {};  // per (cpl 1/2/4, chunk 256/1024): cost per column-step, 0 = not tried
+  // chunk plan: rows [0, n_big) have more than `chunk` in-edges (rows are in
+  // non-increasing in-degree); row h has tasks big_first[h]..big_first[h+1]-1
+  // and base blocks blk_first[h]..blk_first[h+1]-1
+  int32_t n_big = 0, n_big_tasks = 0, n_blocks = 0;
+  int32_t *big_first = nullptr, *big_task_row = nullptr, *blk_first = nullptr;
+  // wave workspace, kt_cap columns
   float2 *gdf[2] = {nullptr, nullptr};
   float *gf[2] = {nullptr, nullptr};
   float2 *acc = nullptr;
   float *tail = nullptr;
-  float2 *lpart = nullptr;
-  unsigned *lcnt = nullptr;
-  long long *sums = nullptr;  // 3 slots x kCols x {dangling, l1, nonfinite, spare}
-  ColState *cols = nullptr;
+  float2 *lpart = nullptr;   // base-block sums of chunked rows (n_blocks x kt_cap)
+  unsigned *lcnt = nullptr;  // arrivals per chunked row
+  long long *sums = nullptr; // 3 slots x kMaxKT x {dangling, l1, nonfinite, spare}
+  ColState *cols = nullptr;  // kMaxKT
   WaveState *wave = nullptr;
+  WaveConst *wc = nullptr;  // device
+  int grid_df = 1, grid_f = 1;  // step kernel grids of the tile in use
   int32_t *prow = nullptr;    // n + 1
   int32_t *pslot = nullptr;   // seed entries of the wave: column slot
   float2 *pval = nullptr;     //   and normalised weight (double-float)
@@ -109,21 +133,58 @@ struct BatchState {
   int64_t pcap = 0;
   float *x0 = nullptr;        // warm-start vectors of the wave (set-major, original order)
   float *out = nullptr;       // results of the wave (set-major, original order)
+  int64_t x0_cols = 0, out_cols = 0;
   float *hstage[2] = {nullptr, nullptr};  // pinned host copies of two waves' results
+  size_t hstage_bytes = 0;
   cudaEvent_t sev[2] = {nullptr, nullptr};  // after each pinned copy
   WaveState *hwave = nullptr;             // pinned: two polled copies of the wave record
   cudaEvent_t wev[2] = {nullptr, nullptr};
   std::vector<int32_t> inv_perm;  // host: original id -> relabelled row
   int32_t *d_inv_perm = nullptr;  // the same on the device
+  // captured chunks: [0] double-float and FP32 launches, [1] FP32 only
+  cudaGraphExec_t chunk_exec[2] = {nullptr, nullptr};
+  int exec_cpl = 0, exec_chunk = 0;
+  const void *exec_pslot = nullptr;
 };
+
+static void free_graphs(BatchState *b) {
+  for (auto &e : b->chunk_exec)
+    if (e) {
+      cudaGraphExecDestroy(e);
+      e = nullptr;
+    }
+  b->exec_cpl = 0;
+}
+
+static void free_plan(BatchState *b) {
+  cudaFree(b->big_first); cudaFree(b->big_task_row); cudaFree(b->blk_first);
+  cudaFree(b->lpart); cudaFree(b->lcnt);
+  b->big_first = b->big_task_row = b->blk_first = nullptr;
+  b->lpart = nullptr;
+  b->lcnt = nullptr;
+  b->n_big = b->n_big_tasks = b->n_blocks = 0;
+  b->chunk = 0;
+}
+
+static void free_blocks(BatchState *b) {
+  cudaFree(b->gdf[0]); cudaFree(b->gdf[1]); cudaFree(b->gf[0]); cudaFree(b->gf[1]);
+  cudaFree(b->acc); cudaFree(b->tail);
+  b->gdf[0] = b->gdf[1] = nullptr;
+  b->gf[0] = b->gf[1] = nullptr;
+  b->acc = nullptr;
+  b->tail = nullptr;
+  cudaFree(b->lpart);
+  b->lpart = nullptr;
+  b->kt_cap = 0;
+}
 
 void batch_free(Graph &g) {
   BatchState *b = g.batch;
   if (!b) return;
-  cudaFree(b->big_first); cudaFree(b->big_task_row);
-  cudaFree(b->gdf[0]); cudaFree(b->gdf[1]); cudaFree(b->gf[0]); cudaFree(b->gf[1]);
-  cudaFree(b->acc); cudaFree(b->tail); cudaFree(b->lpart); cudaFree(b->lcnt);
-  cudaFree(b->sums); cudaFree(b->cols); cudaFree(b->wave); cudaFree(b->prow);
+  free_graphs(b);
+  free_plan(b);
+  free_blocks(b);
+  cudaFree(b->sums); cudaFree(b->cols); cudaFree(b->wave); cudaFree(b->wc); cudaFree(b->prow);
   cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted); cudaFree(b->x0); cudaFree(b->out);
   cudaFree(b->d_inv_perm);
   if (b->hstage[0]) cudaFreeHost(b->hstage[0]);
@@ -137,21 +198,20 @@ void batch_free(Graph &g) {
   g.batch = nullptr;
 }
 
-struct BatchParams {
+// Kernel arguments: fixed for a tile configuration (pointers only), so the
+// launches of a chunk can be replayed from a captured graph.
+struct StepParams {
   int64_t n;
   const int64_t *rp;
   const int32_t *col;
   const float *deg;
   const int32_t *perm;
-  int32_t n_big, n_big_tasks;
-  int64_t n_tasks;
-  const int32_t *big_first, *big_task_row;
+  int32_t n_big, n_big_tasks, chunk;
+  const int32_t *big_first, *big_task_row, *blk_first;
   const int32_t *prow, *pslot;
   const float2 *pval;
-  const float2 *gdf_in;
-  float2 *gdf_out;
-  const float *gf_in;
-  float *gf_out;
+  float2 *gdf[2];
+  float *gf[2];
   float2 *acc;
   float *tail;
   float2 *lpart;
@@ -159,518 +219,701 @@ struct BatchParams {
   long long *sums;
   ColState *cols;
   WaveState *wave;
-  const float *x0;  // nullable
-  float *out;
-  // set of each column: its row in x0 and in out (set-major, n floats each)
-  int64_t xcol[kCols], ocol[kCols];
-  int ncols;
-  df d, omd, inv_n;
-  float fx_scale;
-  double fx_inv;
-  double tol;
-  unsigned long long k, max_iter;
+  const WaveConst *wc;
+  int j;  // step offset within the chunk
 };
 
 namespace {
 
-__device__ __forceinline__ uint64_t l2_keep() {
-  uint64_t pol;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
+// ---------------------------------------------------------------------------
+// lane values: CPL consecutive columns
+// ---------------------------------------------------------------------------
+template <int CPL>
+struct FV {
+  float v[CPL];
+};
+template <int CPL>
+struct DV {
+  df v[CPL];
+};
 
-__device__ __forceinline__ float ld_keep_f32(const float *a, uint64_t pol) {
-  float v;
-  asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
-  return v;
-}
-
-__device__ __forceinline__ float2 ld_keep_f2(const float2 *a, uint64_t pol) {
-  float2 v;
-  asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0,%1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(a), "l"(pol));
-  return v;
-}
-
-struct BDF {
-  using T = df;
-  static constexpr bool kDF = true;
-  __device__ static T zero() { return {0.0f, 0.0f}; }
-  __device__ static T add(T a, T b) { return df_add(a, b); }
-  __device__ static T load(const BatchParams &p, int64_t i, uint64_t pol) {
-    float2 v;
-    if constexpr (kL2Policy) v = ld_keep_f2(&p.gdf_in[i], pol);
-    else v = __ldg(&p.gdf_in[i]);
-    return {v.x, v.y};
+template <int CPL>
+__device__ __forceinline__ FV<CPL> ld_fv(const float *a) {
+  FV<CPL> r;
+  if constexpr (CPL == 1) {
+    r.v[0] = __ldg(a);
+  } else if constexpr (CPL == 2) {
+    const float2 t = __ldg(reinterpret_cast<const float2 *>(a));
+    r.v[0] = t.x; r.v[1] = t.y;
+  } else {
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(a));
+    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
   }
-  __device__ static float2 pack(T v) { return make_float2(v.hi, v.lo); }
-  __device__ static T unpack(float2 v) { return {v.x, v.y}; }
-};
-
-struct BF32 {
-  using T = float;
-  static constexpr bool kDF = false;
-  __device__ static T zero() { return 0.0f; }
-  __device__ static T add(T a, T b) { return a + b; }
-  __device__ static T load(const BatchParams &p, int64_t i, uint64_t pol) {
-    if constexpr (kL2Policy) return ld_keep_f32(&p.gf_in[i], pol);
-    else return __ldg(&p.gf_in[i]);
-  }
-  __device__ static float2 pack(T v) { return make_float2(v, 0.0f); }
-  __device__ static T unpack(float2 v) { return v.x; }
-};
-
-// personalization entry of (row v, column lane), double-float
-__device__ __forceinline__ df red_of(const BatchParams &p, int64_t v, int lane, bool uniform) {
-  if (uniform) return p.inv_n;
-  df red = {0.0f, 0.0f};
-  const int pb = __ldg(&p.prow[v]), pe = __ldg(&p.prow[v + 1]);
-  for (int e = pb; e < pe; ++e)
-    if (__ldg(&p.pslot[e]) == lane) {
-      const float2 w = __ldg(&p.pval[e]);
-      red = {w.x, w.y};
-    }
-  return red;
+  return r;
 }
 
-struct LaneAcc {
-  long long l1 = 0, dang = 0;
-  int bad = 0;
-};
+template <int CPL>
+__device__ __forceinline__ void st_fv(float *a, const FV<CPL> &r) {
+  if constexpr (CPL == 1) {
+    *a = r.v[0];
+  } else if constexpr (CPL == 2) {
+    *reinterpret_cast<float2 *>(a) = make_float2(r.v[0], r.v[1]);
+  } else {
+    *reinterpret_cast<float4 *>(a) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+  }
+}
 
-// Gathered sum of row edges [eb, ee) for column c of this lane's sub-group
-// (kCols lanes, shuffle mask gmask).
-template <class P>
-__device__ __forceinline__ typename P::T gather_sum(const BatchParams &p, int eb, int ee, int c,
-                                                    unsigned gmask, uint64_t pol) {
-  using T = typename P::T;
-  T s = P::zero();
-  for (int base = eb; base < ee; base += kCols) {
-    const int cnt = min(kCols, ee - base);
-    const int my = base + c;
-    const int32_t cidx = my < ee ? __ldg(&p.col[my]) : (int32_t)p.n;
-    for (int j = 0; j < cnt; j += 8) {
-      T g[8];
+// CPL double-float values stored as CPL float2 (hi, lo)
+template <int CPL>
+__device__ __forceinline__ DV<CPL> ld_dv(const float2 *a, bool cached) {
+  DV<CPL> r;
+  if constexpr (CPL == 1) {
+    const float2 t = cached ? __ldg(a) : *a;
+    r.v[0] = {t.x, t.y};
+  } else {
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int32_t u = __shfl_sync(gmask, cidx, (j + q) & (kCols - 1), kCols);
-        g[q] = (j + q < cnt) ? P::load(p, (int64_t)u * kCols + c, pol) : P::zero();
-      }
-#pragma unroll
-      for (int q = 0; q < 8; ++q)
-        if (j + q < cnt) s = P::add(s, g[q]);
+    for (int q = 0; q < CPL / 2; ++q) {
+      const float4 t = cached ? __ldg(reinterpret_cast<const float4 *>(a) + q) : reinterpret_cast<const float4 *>(a)[q];
+      r.v[2 * q] = {t.x, t.y};
+      r.v[2 * q + 1] = {t.z, t.w};
     }
+  }
+  return r;
+}
+
+template <int CPL>
+__device__ __forceinline__ void st_dv(float2 *a, const DV<CPL> &r) {
+  if constexpr (CPL == 1) {
+    *a = make_float2(r.v[0].hi, r.v[0].lo);
+  } else {
+#pragma unroll
+    for (int q = 0; q < CPL / 2; ++q)
+      reinterpret_cast<float4 *>(a)[q] = make_float4(r.v[2 * q].hi, r.v[2 * q].lo, r.v[2 * q + 1].hi, r.v[2 * q + 1].lo);
+  }
+}
+
+// FP32 step of one column (shared by both kernels, with explicit roundings
+// so that the two compute the same bits): r = d (s + dsum * red).
+__device__ __forceinline__ float f32_step(float s, float dsum, float red, float d) {
+  return __fmul_rn(d, __fmaf_rn(dsum, red, s));
+}
+
+// ---------------------------------------------------------------------------
+// The FP32 step (every active column in its FP32 phase): gathers KT * 4-byte
+// rows of the FP32 block.
+// ---------------------------------------------------------------------------
+template <int CPL>
+__device__ __forceinline__ void f32_add(FV<CPL> &s, const FV<CPL> &g) {
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) s.v[q] += g.v[q];
+}
+
+template <int CPL>
+__device__ __forceinline__ FV<CPL> f32_zero() {
+  FV<CPL> r;
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) r.v[q] = 0.0f;
+  return r;
+}
+
+// Sum over edges [eb, ee) of one base block, in edge order.  Rows are
+// padded to multiples of 4 edges and start 16-byte aligned; padding edges
+// point at row n, whose gathered entries are 0.
+template <int CPL>
+__device__ __forceinline__ FV<CPL> f32_block(const StepParams &p, int in, int kt, int eb, int ee, int lane) {
+  constexpr int U = 8;  // gathers in flight per lane
+  const float *gb = p.gf[in] + lane * CPL;
+  FV<CPL> s = f32_zero<CPL>();
+  int e = eb;
+  for (; e + U <= ee; e += U) {
+    const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
+    const int4 b = __ldg(reinterpret_cast<const int4 *>(p.col + e + 4));
+    const int32_t u[U] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    FV<CPL> g[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) g[q] = ld_fv<CPL>(gb + (int64_t)u[q] * kt);
+#pragma unroll
+    for (int q = 0; q < U; ++q) f32_add(s, g[q]);
+  }
+  if (e < ee) {
+    const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
+    const int32_t u[4] = {a.x, a.y, a.z, a.w};
+    FV<CPL> g[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) g[q] = ld_fv<CPL>(gb + (int64_t)u[q] * kt);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) f32_add(s, g[q]);
   }
   return s;
 }
 
-// Per-(row, column) epilogue inputs, loaded before the row's gathers.
+// ---------------------------------------------------------------------------
+// The mixed step (some active column still in its double-float phase).
+// A lane with a column in the double-float phase gathers its 8-byte (hi, lo)
+// entries of the double-float block and keeps, per column, both the
+// double-float sum and the FP32 sum of the hi words; a lane whose columns are
+// all in the FP32 phase gathers the FP32 block like the FP32 step.  A column
+// in its FP32 phase thus computes exactly what the FP32 step would, whatever
+// its neighbours in the wave do, so every column's result depends on its own
+// history alone (not on the sets it shares a wave with, nor on the k-tile).
+// ---------------------------------------------------------------------------
+template <int CPL>
+struct MixSum {
+  DV<CPL> d;  // double-float sums (lanes in the double-float phase)
+  FV<CPL> f;  // FP32 sums of the hi words (or of the FP32 block)
+};
+
+template <int CPL>
+__device__ __forceinline__ MixSum<CPL> mix_zero() {
+  MixSum<CPL> r;
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) r.d.v[q] = {0.0f, 0.0f};
+  r.f = f32_zero<CPL>();
+  return r;
+}
+
+// A lane's entry of row u: the double-float lanes read 8 * CPL bytes of the
+// double-float block (interleaved hi, lo per column), the others 4 * CPL
+// bytes of the FP32 block; one load covers the first 4 * CPL bytes of either.
+template <int CPL>
+struct Raw {
+  float a[2 * CPL];
+};
+
+template <int CPL>
+__device__ __forceinline__ Raw<CPL> mix_load(const float *base_df, const float *base_f, int64_t off_df, int64_t off_f,
+                                             bool ldf) {
+  Raw<CPL> r;
+  const float *a = ldf ? base_df + off_df : base_f + off_f;
+  const FV<CPL> x = ld_fv<CPL>(a);
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) r.a[q] = x.v[q];
+  if (ldf) {
+    const FV<CPL> y = ld_fv<CPL>(a + CPL);
+#pragma unroll
+    for (int q = 0; q < CPL; ++q) r.a[CPL + q] = y.v[q];
+  } else {
+#pragma unroll
+    for (int q = 0; q < CPL; ++q) r.a[CPL + q] = 0.0f;
+  }
+  return r;
+}
+
+template <int CPL>
+__device__ __forceinline__ void mix_add(MixSum<CPL> &s, const Raw<CPL> &r, bool ldf) {
+  if (ldf) {
+#pragma unroll
+    for (int q = 0; q < CPL; ++q) {
+      const df g = {r.a[2 * q], r.a[2 * q + 1]};
+      s.d.v[q] = df_add(s.d.v[q], g);
+      s.f.v[q] += g.hi;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < CPL; ++q) s.f.v[q] += r.a[q];
+  }
+}
+
+template <int CPL>
+__device__ __forceinline__ MixSum<CPL> mix_block(const StepParams &p, int in, int kt, int eb, int ee, int lane,
+                                                 bool ldf) {
+  constexpr int U = CPL == 4 ? 4 : 8;
+  const float *bdf = reinterpret_cast<const float *>(p.gdf[in]) + 2 * lane * CPL;
+  const float *bf = p.gf[in] + lane * CPL;
+  MixSum<CPL> s = mix_zero<CPL>();
+  for (int e = eb; e < ee; e += U) {  // ee - eb is a multiple of 4 and of U when U == 4
+    int32_t u[U];
+    const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
+    u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
+    bool ok2 = true;
+    if constexpr (U == 8) {
+      ok2 = e + 4 < ee;
+      const int4 b = ok2 ? __ldg(reinterpret_cast<const int4 *>(p.col + e + 4)) : make_int4(0, 0, 0, 0);
+      u[4] = b.x; u[5] = b.y; u[6] = b.z; u[7] = b.w;
+    }
+    Raw<CPL> g[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q)
+      if (q < 4 || ok2) g[q] = mix_load<CPL>(bdf, bf, (int64_t)u[q] * 2 * kt, (int64_t)u[q] * kt, ldf);
+#pragma unroll
+    for (int q = 0; q < U; ++q)
+      if (q < 4 || ok2) mix_add<CPL>(s, g[q], ldf);
+  }
+  return s;
+}
+
+struct Lane {
+  // per column of this lane
+  bool act[kMaxCPL];
+  bool f32[kMaxCPL];  // in its FP32 phase
+  bool uni[kMaxCPL];
+  df dsum[kMaxCPL];
+  bool any;  // some column active
+  bool ldf;  // some active column in its double-float phase
+};
+
+template <int CPL>
+struct LaneAcc {
+  long long l1[CPL], dang[CPL];
+  int bad;
+  __device__ LaneAcc() {
+#pragma unroll
+    for (int q = 0; q < CPL; ++q) l1[q] = dang[q] = 0;
+    bad = 0;
+  }
+};
+
+// Per-(row, lane) epilogue inputs, loaded before the row's gathers.
+template <int CPL>
 struct BIn {
-  df red;
-  float2 x;  // acc (double-float phase) or (tail, 0)
+  df red[CPL];
+  FV<CPL> tail;
+  DV<CPL> acc;  // double-float lanes only
   float deg;
 };
 
-template <class P>
-__device__ __forceinline__ BIn b_in(const BatchParams &p, int64_t v, int c, bool uniform) {
-  BIn in;
-  in.red = red_of(p, v, c, uniform);
+template <int CPL>
+__device__ __forceinline__ BIn<CPL> b_in(const StepParams &p, const WaveScalars &wc, int64_t v, int lane,
+                                         const Lane &ln, bool want_acc) {
+  BIn<CPL> in;
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) in.red[q] = ln.uni[q] ? wc.inv_n : df{0.0f, 0.0f};
+  const int pb = __ldg(&p.prow[v]), pe = __ldg(&p.prow[v + 1]);
+  for (int e = pb; e < pe; ++e) {
+    const int q = __ldg(&p.pslot[e]) - lane * CPL;
+    if (q >= 0 && q < CPL) {
+      const float2 w = __ldg(&p.pval[e]);
+#pragma unroll
+      for (int qq = 0; qq < CPL; ++qq)
+        if (qq == q) in.red[qq] = {w.x, w.y};
+    }
+  }
   in.deg = __ldg(&p.deg[v]);
-  const int64_t i = v * kCols + c;
-  if constexpr (P::kDF) in.x = p.acc[i];
-  else in.x = make_float2(p.tail[i], 0.f);
+  const int64_t i = v * wc.kt + lane * CPL;
+  in.tail = ld_fv<CPL>(p.tail + i);
+  if (want_acc) in.acc = ld_dv<CPL>(p.acc + i, false);
   return in;
 }
 
-template <class P>
-__device__ __forceinline__ void col_epilogue_in(const BatchParams &p, int64_t v, typename P::T s, df dsum,
-                                                const BIn &in, LaneAcc &a, int c) {
-  const df red = in.red;
+// FP32 step epilogue: every active column of the lane in its FP32 phase.
+template <int CPL>
+__device__ __forceinline__ void f32_epilogue(const StepParams &p, const WaveScalars &wc, int64_t v, const FV<CPL> &s,
+                                             const BIn<CPL> &in, const Lane &ln, int out, LaneAcc<CPL> &a, int lane) {
+  const int64_t i = v * wc.kt + lane * CPL;
   const float dg = in.deg;
-  const int64_t i = v * kCols + c;
-  if constexpr (P::kDF) {
-    const float2 ao = in.x;
-    df r = df_mul(p.d, df_add(s, df_mul(dsum, red)));
-    if (p.k == 1) r = df_add(df_add(df_mul(p.omd, red), r), df_neg({ao.x, ao.y}));  // F(x_0) - x_0
-    const df an = df_add({ao.x, ao.y}, r);
-    p.acc[i] = make_float2(an.hi, an.lo);
-    const df ar = r.hi < 0.0f ? df_neg(r) : r;
-    a.l1 += fx_of(ar.hi, p.fx_scale) + fx_of(ar.lo, p.fx_scale);
-    a.bad |= !isfinite(r.hi);
-    if (dg == 0.0f) a.dang += fx_of(r.hi, p.fx_scale) + fx_of(r.lo, p.fx_scale);
-    const df g = dg > 0.0f ? df_div_f(r, dg) : df{0.0f, 0.0f};
-    p.gdf_out[i] = make_float2(g.hi, g.lo);
-    p.gf_out[i] = g.hi;
-  } else {
-    const float r = p.d.hi * (s + dsum.hi * red.hi);
-    p.tail[i] = in.x.x + r;
-    a.l1 += fx_of(fabsf(r), p.fx_scale);
-    a.bad |= !isfinite(r);
-    if (dg == 0.0f) a.dang += fx_of(r, p.fx_scale);
-    p.gf_out[i] = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
+  FV<CPL> tn, gh;
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) {
+    const float r = ln.act[q] ? f32_step(s.v[q], ln.dsum[q].hi, in.red[q].hi, wc.d.hi) : 0.0f;
+    tn.v[q] = in.tail.v[q] + r;
+    a.l1[q] += fx_of(fabsf(r), wc.fx_scale);
+    a.bad |= (!isfinite(r)) << q;
+    if (dg == 0.0f) a.dang[q] += fx_of(r, wc.fx_scale);
+    gh.v[q] = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
   }
+  st_fv<CPL>(p.tail + i, tn);
+  st_fv<CPL>(p.gf[out] + i, gh);
 }
 
-// Gathered sum over edges [eb, ee) when in-rows are padded to multiples of 4
-// edges and start 16-byte aligned: every lane loads the same 4 column indices
-// (one broadcast 16-byte load per 4 edges), padding edges point at the zero
-// row n, so no per-edge predicate is needed; two groups are in flight.
-template <class P>
-__device__ __forceinline__ typename P::T gather_sum_q(const BatchParams &p, int eb, int ee, int c,
-                                                      uint64_t pol) {
-  using T = typename P::T;
-  T s = P::zero();
-  int e = eb;
-  for (; e + 8 <= ee; e += 8) {
-    const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
-    const int4 b = __ldg(reinterpret_cast<const int4 *>(p.col + e + 4));
-    const T g0 = P::load(p, (int64_t)a.x * kCols + c, pol), g1 = P::load(p, (int64_t)a.y * kCols + c, pol);
-    const T g2 = P::load(p, (int64_t)a.z * kCols + c, pol), g3 = P::load(p, (int64_t)a.w * kCols + c, pol);
-    const T g4 = P::load(p, (int64_t)b.x * kCols + c, pol), g5 = P::load(p, (int64_t)b.y * kCols + c, pol);
-    const T g6 = P::load(p, (int64_t)b.z * kCols + c, pol), g7 = P::load(p, (int64_t)b.w * kCols + c, pol);
-    s = P::add(s, g0); s = P::add(s, g1); s = P::add(s, g2); s = P::add(s, g3);
-    s = P::add(s, g4); s = P::add(s, g5); s = P::add(s, g6); s = P::add(s, g7);
+// Mixed step epilogue: a column in its double-float phase takes the
+// double-float step on s.d (x in acc), one in its FP32 phase the FP32 step on
+// s.f (x in tail), exactly as f32_epilogue computes it.
+template <int CPL>
+__device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScalars &wc, int64_t v,
+                                             const MixSum<CPL> &s, const BIn<CPL> &in, const Lane &ln, int out,
+                                             unsigned long long k, LaneAcc<CPL> &a, int lane) {
+  if (!ln.ldf) {
+    f32_epilogue<CPL>(p, wc, v, s.f, in, ln, out, a, lane);
+    return;
   }
-  if (e < ee) {  // one group of 4 left
-    const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
-    const T g0 = P::load(p, (int64_t)a.x * kCols + c, pol), g1 = P::load(p, (int64_t)a.y * kCols + c, pol);
-    const T g2 = P::load(p, (int64_t)a.z * kCols + c, pol), g3 = P::load(p, (int64_t)a.w * kCols + c, pol);
-    s = P::add(s, g0); s = P::add(s, g1); s = P::add(s, g2); s = P::add(s, g3);
-  }
-  return s;
-}
-
-template <class P>
-__device__ __forceinline__ void col_epilogue(const BatchParams &p, int64_t v, typename P::T s, df dsum,
-                                             bool uniform, LaneAcc &a, int c) {
-  const BIn in = b_in<P>(p, v, c, uniform);
-  col_epilogue_in<P>(p, v, s, dsum, in, a, c);
-}
-
-// Rows [v0, v0 + R) at once (kCols == 32: lane c is column c).  All R rows'
-// column indices, then all their gathers (8 per row per round) are issued
-// before any is consumed, and the epilogue inputs are loaded up front.
-template <class P, int R>
-__device__ __forceinline__ void rows_task(const BatchParams &p, int64_t v0, int64_t vend, int c,
-                                          bool active, bool uniform, df dsum, LaneAcc &a, uint64_t pol) {
-  using T = typename P::T;
-  int eb[R], ee[R];
-  BIn in[R];
-  const int64_t rl = (int64_t)c < (int64_t)R + 1 && v0 + c <= vend ? v0 + c : vend;
-  const int rpv = (int)__ldg(&p.rp[rl]);  // lane q holds rp[v0 + q]
+  const int64_t i = v * wc.kt + lane * CPL;
+  const float dg = in.deg;
+  DV<CPL> an, g;
+  FV<CPL> tn, gh;
 #pragma unroll
-  for (int q = 0; q < R; ++q) {
-    const bool ok = v0 + q < vend;
-    eb[q] = ok ? __shfl_sync(0xffffffffu, rpv, q) : 0;
-    ee[q] = ok ? __shfl_sync(0xffffffffu, rpv, q + 1) : 0;
-    if (ok && active) in[q] = b_in<P>(p, v0 + q, c, uniform);
-  }
-  int len = 0;
-#pragma unroll
-  for (int q = 0; q < R; ++q) len = max(len, ee[q] - eb[q]);
-  T s[R];
-#pragma unroll
-  for (int q = 0; q < R; ++q) s[q] = P::zero();
-  for (int base = 0; base < len; base += 32) {
-    int32_t cidx[R];
-    int cnt[R];
-#pragma unroll
-    for (int q = 0; q < R; ++q) {
-      const int e = eb[q] + base + c;
-      cidx[q] = e < ee[q] ? __ldg(&p.col[e]) : (int32_t)p.n;
-      cnt[q] = min(32, max(0, ee[q] - eb[q] - base));
-    }
-    for (int j = 0; j < 32; j += 8) {
-      T g[R][8];
-#pragma unroll
-      for (int q = 0; q < R; ++q)
-#pragma unroll
-        for (int qq = 0; qq < 8; ++qq) {
-          const int32_t u = __shfl_sync(0xffffffffu, cidx[q], j + qq);
-          g[q][qq] = (j + qq < cnt[q]) ? P::load(p, (int64_t)u * kCols + c, pol) : P::zero();
-        }
-#pragma unroll
-      for (int q = 0; q < R; ++q)
-#pragma unroll
-        for (int qq = 0; qq < 8; ++qq)
-          if (j + qq < cnt[q]) s[q] = P::add(s[q], g[q][qq]);
+  for (int q = 0; q < CPL; ++q) {
+    const df red = in.red[q];
+    an.v[q] = in.acc.v[q];
+    tn.v[q] = in.tail.v[q];
+    if (ln.act[q] && ln.f32[q]) {
+      const float r = f32_step(s.f.v[q], ln.dsum[q].hi, red.hi, wc.d.hi);
+      tn.v[q] = in.tail.v[q] + r;
+      a.l1[q] += fx_of(fabsf(r), wc.fx_scale);
+      a.bad |= (!isfinite(r)) << q;
+      if (dg == 0.0f) a.dang[q] += fx_of(r, wc.fx_scale);
+      gh.v[q] = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
+      g.v[q] = {gh.v[q], 0.0f};
+    } else if (ln.act[q]) {
+      const df ao = in.acc.v[q];
+      df r = df_mul(wc.d, df_add(s.d.v[q], df_mul(ln.dsum[q], red)));
+      if (k == 1) r = df_add(df_add(df_mul(wc.omd, red), r), df_neg(ao));  // F(x_0) - x_0
+      an.v[q] = df_add(ao, r);
+      const df ar = r.hi < 0.0f ? df_neg(r) : r;
+      a.l1[q] += fx_of(ar.hi, wc.fx_scale) + fx_of(ar.lo, wc.fx_scale);
+      a.bad |= (!isfinite(r.hi)) << q;
+      if (dg == 0.0f) a.dang[q] += fx_of(r.hi, wc.fx_scale) + fx_of(r.lo, wc.fx_scale);
+      g.v[q] = dg > 0.0f ? df_div_f(r, dg) : df{0.0f, 0.0f};
+      gh.v[q] = g.v[q].hi;
+    } else {
+      g.v[q] = {0.0f, 0.0f};
+      gh.v[q] = 0.0f;
     }
   }
-#pragma unroll
-  for (int q = 0; q < R; ++q)
-    if (v0 + q < vend && active) col_epilogue_in<P>(p, v0 + q, s[q], dsum, in[q], a, c);
+  st_dv<CPL>(p.acc + i, an);
+  st_fv<CPL>(p.tail + i, tn);
+  st_dv<CPL>(p.gdf[out] + i, g);
+  st_fv<CPL>(p.gf[out] + i, gh);
 }
 
-// Per-column view of step k: which columns are still active, their dangling
-// sums, and whether this kernel's precision is the active one.  Returns false
+// Per-column view of step k: which columns are still active, which are in
+// their FP32 phase (sticky: from the first step after their step norm fell
+// below their theta), their dangling sums, and whether this kernel (the
+// mixed step: WANT_MIX, or the FP32 step) is the one to run.  Returns false
 // when the block should exit.  Every warp evaluates it identically.
-template <bool WANT_DF>
-__device__ bool batch_prologue(const BatchParams &p, int lane, bool *active, df *dsum, bool *uniform) {
-  const unsigned long long k = p.k;
+template <bool WANT_MIX, int CPL>
+__device__ bool batch_prologue(const StepParams &p, const WaveScalars &wc, unsigned long long k, int lane, Lane *ln) {
   if (*(volatile int *)&p.wave->done) return false;
   const int prev = (int)((k - 1) % 3);
-  const int c = lane & (kCols - 1);
-  const bool col_ok = c < p.ncols;
-  const int retired0 = col_ok ? *(volatile int *)&p.cols[c].retired : 1;
-  double diff = INFINITY;
-  if (k > 1) {
-    const long long raw = *(volatile long long *)&p.sums[(prev * kCols + c) * 4 + 1];
-    const long long badc = *(volatile long long *)&p.sums[(prev * kCols + c) * 4 + 2];
-    diff = badc ? NAN : (double)raw * p.fx_inv;
+  bool lane_act = false, lane_df = false;
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) {
+    const int c = lane * CPL + q;
+    const bool col_ok = c < wc.ncols;
+    const int retired0 = col_ok ? *(volatile int *)&p.cols[c].retired : 1;
+    double diff = INFINITY;
+    if (k > 1) {
+      const long long raw = *(volatile long long *)&p.sums[(prev * kMaxKT + c) * 4 + 1];
+      const long long badc = *(volatile long long *)&p.sums[(prev * kMaxKT + c) * 4 + 2];
+      diff = badc ? NAN : (double)raw * wc.fx_inv;
+    }
+    // a warm start is judged by its first residual: one that does not drop
+    // below the cold start's (or is not finite) retires the column, and the
+    // caller solves that set again from the personalization vector
+    const bool rej = !retired0 && k == 2 && wc.has_x0 && !(diff <= p.cols[c].r1_max);
+    const bool conv = !retired0 && !rej && k > 1 && diff < wc.tol;
+    const bool cap = !retired0 && !rej && !conv && k - 1 >= wc.max_iter;
+    const bool act = !retired0 && !rej && !conv && !cap;
+    const bool f32 = act && k > 1 && (*(volatile int *)&p.cols[c].f32 || diff < p.cols[c].theta);
+    if (blockIdx.x == 0 && threadIdx.x < 32) {
+      if (conv || cap || rej) {
+        p.cols[c].retired = 1;
+        p.cols[c].converged = conv ? 1 : 0;
+        p.cols[c].rejected = rej ? 1 : 0;
+        p.cols[c].iterations = k - 1;
+        p.cols[c].diff_l1 = diff;
+      }
+      if (f32) p.cols[c].f32 = 1;
+    }
+    ln->act[q] = act;
+    ln->f32[q] = f32;
+    ln->uni[q] = col_ok && p.cols[c].uniform;
+    lane_act |= act;
+    lane_df |= act && !f32;
   }
-  // a warm start is judged by its first residual: one that does not drop
-  // below the cold start's (or is not finite) retires the column, and the
-  // caller solves that set again from the personalization vector
-  const bool rej = !retired0 && k == 2 && p.x0 && !(diff <= p.cols[c].r1_max);
-  const bool conv = !retired0 && !rej && k > 1 && diff < p.tol;
-  const bool cap = !retired0 && !rej && !conv && k - 1 >= p.max_iter;
-  const bool act = !retired0 && !rej && !conv && !cap;
-  if (blockIdx.x == 0 && threadIdx.x < kCols && (conv || cap || rej)) {
-    p.cols[c].retired = 1;
-    p.cols[c].converged = conv ? 1 : 0;
-    p.cols[c].rejected = rej ? 1 : 0;
-    p.cols[c].iterations = k - 1;
-    p.cols[c].diff_l1 = diff;
-  }
-  const unsigned any = __ballot_sync(0xffffffffu, act);
-  if (!any) {
+  ln->any = lane_act;
+  ln->ldf = lane_df;
+  if (!__any_sync(0xffffffffu, lane_act)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) p.wave->done = 1;
     return false;
   }
-  const bool big = act && !(diff < p.cols[c].theta);
-  const bool f32 = k > 1 && (*(volatile int *)&p.wave->f32_phase || !__any_sync(0xffffffffu, big));
-  if (f32 == WANT_DF) return false;
+  const bool all_f32 = k > 1 && (*(volatile int *)&p.wave->f32_phase || !__any_sync(0xffffffffu, lane_df));
+  if (all_f32 == WANT_MIX) return false;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    p.wave->f32_phase = f32 ? 1 : 0;
-    if (f32 && p.wave->f32_from == 0) p.wave->f32_from = k;
+    p.wave->f32_phase = all_f32 ? 1 : 0;
+    if (all_f32 && p.wave->f32_from == 0) p.wave->f32_from = k;
     p.wave->steps = k;
   }
-  if (blockIdx.x == 0 && threadIdx.x < kCols) {
+  if (blockIdx.x == 0 && threadIdx.x < kMaxKT) {
     const int nxt = (int)((k + 1) % 3);
-    for (int i = 0; i < 4; ++i) p.sums[(nxt * kCols + c) * 4 + i] = 0;
+    for (int i = 0; i < 4; ++i) p.sums[(nxt * kMaxKT + threadIdx.x) * 4 + i] = 0;
   }
-  *active = act;
-  *uniform = col_ok && p.cols[c].uniform;
-  const long long draw = *(volatile long long *)&p.sums[(prev * kCols + c) * 4 + 0];
-  *dsum = df_from_double((double)draw * p.fx_inv);
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) {
+    const long long draw = *(volatile long long *)&p.sums[(prev * kMaxKT + lane * CPL + q) * 4 + 0];
+    ln->dsum[q] = df_from_double((double)draw * wc.fx_inv);
+  }
   return true;
 }
 
-template <class P>
-__global__ void __launch_bounds__(kBThreads, kBMinBlocks) spmm_kernel(BatchParams p) {
-  using T = typename P::T;
-  __shared__ long long bl1[kBWarps][32], bdg[kBWarps][32];
-  __shared__ int bbad[kBWarps][32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int sub = lane / kCols, c = lane & (kCols - 1);
-  const unsigned gmask = kCols == 32 ? 0xffffffffu : (((1u << kCols) - 1u) << (sub * kCols));
-  bool active = false, uniform = false;
-  df dsum;
-  if (!batch_prologue<P::kDF>(p, lane, &active, &dsum, &uniform)) return;
-  uint64_t pol = 0;
-  if constexpr (kL2Policy) pol = l2_keep();
-  LaneAcc a;
-  const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
-  if constexpr (kCols == 32) {
-    // warp tasks: the chunk tasks, then groups of R consecutive rows
-    constexpr int R = P::kDF ? kBRowsDF : kBRowsF32;
-    const int64_t nrows = p.n - p.n_big;
-    const int64_t nwt = p.n_big_tasks + ceil_div<int64_t>(nrows, R);
-    for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
-      if (w < p.n_big_tasks) {
-        const int64_t t = w;
-        const int h = __ldg(&p.big_task_row[t]);
-        const int first = __ldg(&p.big_first[h]);
-        const int nch = __ldg(&p.big_first[h + 1]) - first;
-        const int rb = (int)__ldg(&p.rp[h]), re = (int)__ldg(&p.rp[h + 1]);
-        const int cs = rb + ((int)t - first) * kSpmmChunk;
-        const int ce = min(re, cs + kSpmmChunk);
-        // a retired column's lane gathers nothing (its sectors are not read)
-        T s = P::zero();
-        if (kRowAlign != 4) s = gather_sum<P>(p, cs, ce, c, gmask, pol);
-        else if (active) s = gather_sum_q<P>(p, cs, ce, c, pol);
-        p.lpart[t * kCols + c] = P::pack(s);
-        __threadfence();
-        __syncwarp();
-        unsigned tk = 0;
-        if (c == 0) tk = atomicAdd(&p.lcnt[h], 1u);
-        tk = __shfl_sync(0xffffffffu, tk, 0);
-        if (tk == (unsigned)(nch - 1)) {
-          __threadfence();
-          T all = P::zero();
-          for (int q = 0; q < nch; ++q) all = P::add(all, P::unpack(__ldcg(&p.lpart[(int64_t)(first + q) * kCols + c])));
-          if (c == 0) p.lcnt[h] = 0;
-          if (active) col_epilogue<P>(p, h, all, dsum, uniform, a, c);
-        }
-      } else if (kRowAlign == 4 && R == 1) {
-        const int64_t v = p.n_big + (w - p.n_big_tasks);
-        BIn in;
-        if (active) in = b_in<P>(p, v, c, uniform);
-        if (active) {  // a retired column's lane gathers nothing
-          const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
-          const T s = gather_sum_q<P>(p, eb, ee, c, pol);
-          col_epilogue_in<P>(p, v, s, dsum, in, a, c);
-        }
-      } else {
-        const int64_t v0 = p.n_big + (w - p.n_big_tasks) * R;
-        rows_task<P, R>(p, v0, p.n, c, active, uniform, dsum, a, pol);
-      }
-    }
-  } else {
-  // unit u: chunk task (u < n_big_tasks) or row n_big + (u - n_big_tasks);
-  // a warp task covers kRowsPerWarp consecutive units, one per sub-group
-  const int64_t nwt = ceil_div<int64_t>(p.n_tasks, kRowsPerWarp);
-  for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
-    const int64_t t = w * kRowsPerWarp + sub;
-    if (t >= p.n_tasks) continue;
-    if (t < p.n_big_tasks) {
-      const int h = __ldg(&p.big_task_row[t]);
-      const int first = __ldg(&p.big_first[h]);
-      const int nch = __ldg(&p.big_first[h + 1]) - first;
-      const int rb = (int)__ldg(&p.rp[h]), re = (int)__ldg(&p.rp[h + 1]);
-      const int cs = rb + ((int)t - first) * kSpmmChunk;
-      const int ce = min(re, cs + kSpmmChunk);
-      const T s = gather_sum<P>(p, cs, ce, c, gmask, pol);
-      p.lpart[t * kCols + c] = P::pack(s);
-      __threadfence();
-      __syncwarp(gmask);
-      unsigned tk = 0;
-      if (c == 0) tk = atomicAdd(&p.lcnt[h], 1u);
-      tk = __shfl_sync(gmask, tk, 0, kCols);
-      if (tk == (unsigned)(nch - 1)) {
-        __threadfence();
-        T all = P::zero();
-        for (int q = 0; q < nch; ++q) all = P::add(all, P::unpack(__ldcg(&p.lpart[(int64_t)(first + q) * kCols + c])));
-        if (c == 0) p.lcnt[h] = 0;
-        if (active) col_epilogue<P>(p, h, all, dsum, uniform, a, c);
-      }
-    } else {
-      const int64_t v = p.n_big + (t - p.n_big_tasks);
-      const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
-      const T s = gather_sum<P>(p, eb, ee, c, gmask, pol);
-      if (active) col_epilogue<P>(p, v, s, dsum, uniform, a, c);
-    }
+// The block's per-column fixed-point sums -> one atomic per column.
+template <int CPL>
+__device__ __forceinline__ void block_sums(const StepParams &p, int kt, unsigned long long k, const LaneAcc<CPL> &a,
+                                           int lane, int wid, long long (*bl1)[kMaxKT], long long (*bdg)[kMaxKT],
+                                           int (*bbad)[32]) {
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) {
+    bl1[wid][lane * CPL + q] = a.l1[q];
+    bdg[wid][lane * CPL + q] = a.dang[q];
   }
-  }
-  bl1[wid][lane] = a.l1;
-  bdg[wid][lane] = a.dang;
   bbad[wid][lane] = a.bad;
   __syncthreads();
-  if (wid == 0 && lane < kCols) {
+  if (threadIdx.x < kt) {
+    const int c = threadIdx.x;
     long long t1 = 0, t2 = 0;
     int tb = 0;
-    for (int w = 0; w < kBWarps; ++w)
-      for (int q = lane; q < 32; q += kCols) { t1 += bl1[w][q]; t2 += bdg[w][q]; tb |= bbad[w][q]; }
-    const int cur = (int)(p.k % 3);
-    long long *sl = &p.sums[(cur * kCols + lane) * 4];
+    for (int w = 0; w < kBWarps; ++w) {
+      t1 += bl1[w][c];
+      t2 += bdg[w][c];
+      tb |= (bbad[w][c / CPL] >> (c % CPL)) & 1;
+    }
+    const int cur = (int)(k % 3);
+    long long *sl = &p.sums[(cur * kMaxKT + c) * 4];
     if (t1) atomicAdd((unsigned long long *)&sl[1], (unsigned long long)t1);
     if (t2) atomicAdd((unsigned long long *)&sl[0], (unsigned long long)t2);
     if (tb) atomicAdd((unsigned long long *)&sl[2], 1ull);
   }
 }
 
-// x_0 (p, or the warm start), acc = x_0, tail = 0, gathered vector for step 1,
-// per-column dangling sums of x_0; zero padding row n of the gathered blocks.
-__global__ void __launch_bounds__(kBThreads) batch_init(BatchParams p) {
-  __shared__ long long bdg[kBWarps][32];
+// Chunk task t of a row with more than `chunk` in-edges: its row h, the
+// row's tasks and base blocks, and the task's edge range [cs, ce).  The
+// task writes the sums of its base blocks to lpart; chunk_arrive returns
+// true for the task that arrives last, which adds the row's blocks in order
+// and runs the epilogue.
+__device__ __forceinline__ void chunk_row(const StepParams &p, int t, int *h, int *first, int *nch, int *b0, int *nb,
+                                          int *cs, int *ce, int *rb) {
+  *h = __ldg(&p.big_task_row[t]);
+  *first = __ldg(&p.big_first[*h]);
+  *nch = __ldg(&p.big_first[*h + 1]) - *first;
+  *b0 = __ldg(&p.blk_first[*h]);
+  *nb = __ldg(&p.blk_first[*h + 1]) - *b0;
+  *rb = (int)__ldg(&p.rp[*h]);
+  const int re = (int)__ldg(&p.rp[*h + 1]);
+  *cs = *rb + (t - *first) * p.chunk;
+  *ce = min(re, *cs + p.chunk);
+}
+
+__device__ __forceinline__ bool chunk_arrive(const StepParams &p, int h, int nch, int lane) {
+  __threadfence();
+  __syncwarp();
+  unsigned tk = 0;
+  if (lane == 0) tk = atomicAdd(&p.lcnt[h], 1u);
+  tk = __shfl_sync(0xffffffffu, tk, 0);
+  if (tk != (unsigned)(nch - 1)) return false;
+  __threadfence();
+  if (lane == 0) p.lcnt[h] = 0;
+  return true;
+}
+
+template <int CPL>
+__global__ void __launch_bounds__(kBThreads) spmm_f32(StepParams p) {
+  __shared__ long long bl1[kBWarps][kMaxKT], bdg[kBWarps][kMaxKT];
+  __shared__ int bbad[kBWarps][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int sub = lane / kCols, c = lane & (kCols - 1);
-  const bool col_ok = c < p.ncols;
-  const bool uniform = col_ok && p.cols[c].uniform;
-  long long dang = 0;
-  const int64_t step = (int64_t)gridDim.x * kBWarps * kRowsPerWarp;
-  for (int64_t v = ((int64_t)blockIdx.x * kBWarps + wid) * kRowsPerWarp + sub; v <= p.n; v += step) {
-    const int64_t i = v * kCols + c;
-    if (v == p.n) {  // padding row: gathers of padded edges read zeros
-      p.gdf_out[i] = make_float2(0.f, 0.f);
-      p.gf_out[i] = 0.f;
-      const_cast<float2 *>(p.gdf_in)[i] = make_float2(0.f, 0.f);
-      const_cast<float *>(p.gf_in)[i] = 0.f;
+  const WaveScalars wc = p.wc->s;
+  const unsigned long long k = *(volatile unsigned long long *)&p.wave->k0 + (unsigned long long)p.j + 1ull;
+  Lane ln;
+  if (!batch_prologue<false, CPL>(p, wc, k, lane, &ln)) return;
+  const int in = (int)((k - 1) & 1), out = (int)(k & 1);
+  const int kt = wc.kt;
+  LaneAcc<CPL> a;
+  const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
+  const int64_t nwt = p.n_big_tasks + (p.n - p.n_big);
+  for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
+    if (w < p.n_big_tasks) {
+      int h, first, nch, b0, nb, cs, ce, rb;
+      chunk_row(p, (int)w, &h, &first, &nch, &b0, &nb, &cs, &ce, &rb);
+      // a lane whose columns have all retired gathers nothing
+      if (ln.any)
+        for (int b = cs; b < ce; b += kBase) {
+          const FV<CPL> s = f32_block<CPL>(p, in, kt, b, min(ce, b + kBase), lane);
+          DV<CPL> pk;
+#pragma unroll
+          for (int q = 0; q < CPL; ++q) pk.v[q] = {s.v[q], 0.0f};
+          st_dv<CPL>(p.lpart + (int64_t)(b0 + (b - rb) / kBase) * kt + lane * CPL, pk);
+        }
+      if (chunk_arrive(p, h, nch, lane) && ln.any) {
+        const BIn<CPL> bi = b_in<CPL>(p, wc, h, lane, ln, false);
+        FV<CPL> all = f32_zero<CPL>();
+        for (int q = 0; q < nb; ++q) {
+          const DV<CPL> d = ld_dv<CPL>(p.lpart + (int64_t)(b0 + q) * kt + lane * CPL, false);
+#pragma unroll
+          for (int j = 0; j < CPL; ++j) all.v[j] = q == 0 ? d.v[j].hi : all.v[j] + d.v[j].hi;
+        }
+        f32_epilogue<CPL>(p, wc, h, all, bi, ln, out, a, lane);
+      }
+    } else if (ln.any) {
+      const int64_t v = p.n_big + (w - p.n_big_tasks);
+      const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, false);
+      const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
+      // canonical row sum: base blocks from eb, added in order
+      FV<CPL> tot = f32_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane);
+      for (int b = eb + kBase; b < ee; b += kBase) f32_add(tot, f32_block<CPL>(p, in, kt, b, min(ee, b + kBase), lane));
+      f32_epilogue<CPL>(p, wc, v, tot, bi, ln, out, a, lane);
+    }
+  }
+  block_sums<CPL>(p, kt, k, a, lane, wid, bl1, bdg, bbad);
+}
+
+template <int CPL>
+__global__ void __launch_bounds__(kBThreads, 2) spmm_mixed(StepParams p) {
+  __shared__ long long bl1[kBWarps][kMaxKT], bdg[kBWarps][kMaxKT];
+  __shared__ int bbad[kBWarps][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const WaveScalars wc = p.wc->s;
+  const unsigned long long k = *(volatile unsigned long long *)&p.wave->k0 + (unsigned long long)p.j + 1ull;
+  Lane ln;
+  if (!batch_prologue<true, CPL>(p, wc, k, lane, &ln)) return;
+  const int in = (int)((k - 1) & 1), out = (int)(k & 1);
+  const int kt = wc.kt;
+  LaneAcc<CPL> a;
+  const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
+  const int64_t nwt = p.n_big_tasks + (p.n - p.n_big);
+  for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
+    if (w < p.n_big_tasks) {
+      int h, first, nch, b0, nb, cs, ce, rb;
+      chunk_row(p, (int)w, &h, &first, &nch, &b0, &nb, &cs, &ce, &rb);
+      if (ln.any)
+        for (int b = cs; b < ce; b += kBase) {
+          const MixSum<CPL> s = mix_block<CPL>(p, in, kt, b, min(ce, b + kBase), lane, ln.ldf);
+          // per column: the double-float sum, or the FP32 sum as (s, 0)
+          DV<CPL> pk;
+#pragma unroll
+          for (int q = 0; q < CPL; ++q) pk.v[q] = (ln.ldf && !ln.f32[q]) ? s.d.v[q] : df{s.f.v[q], 0.0f};
+          st_dv<CPL>(p.lpart + (int64_t)(b0 + (b - rb) / kBase) * kt + lane * CPL, pk);
+        }
+      if (chunk_arrive(p, h, nch, lane) && ln.any) {
+        const BIn<CPL> bi = b_in<CPL>(p, wc, h, lane, ln, ln.ldf);
+        MixSum<CPL> all = mix_zero<CPL>();
+        for (int q = 0; q < nb; ++q) {
+          const DV<CPL> d = ld_dv<CPL>(p.lpart + (int64_t)(b0 + q) * kt + lane * CPL, false);
+#pragma unroll
+          for (int j = 0; j < CPL; ++j) {
+            all.d.v[j] = q == 0 ? d.v[j] : df_add(all.d.v[j], d.v[j]);
+            all.f.v[j] = q == 0 ? d.v[j].hi : all.f.v[j] + d.v[j].hi;
+          }
+        }
+        mix_epilogue<CPL>(p, wc, h, all, bi, ln, out, k, a, lane);
+      }
+    } else if (ln.any) {
+      const int64_t v = p.n_big + (w - p.n_big_tasks);
+      const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, ln.ldf);
+      const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
+      MixSum<CPL> tot = mix_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane, ln.ldf);
+      for (int b = eb + kBase; b < ee; b += kBase) {
+        const MixSum<CPL> s = mix_block<CPL>(p, in, kt, b, min(ee, b + kBase), lane, ln.ldf);
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) {
+          tot.d.v[j] = df_add(tot.d.v[j], s.d.v[j]);
+          tot.f.v[j] += s.f.v[j];
+        }
+      }
+      mix_epilogue<CPL>(p, wc, v, tot, bi, ln, out, k, a, lane);
+    }
+  }
+  block_sums<CPL>(p, kt, k, a, lane, wid, bl1, bdg, bbad);
+}
+
+// the wave record's step counter after a chunk
+__global__ void advance_kernel(WaveState *wave) { wave->k0 += kChunkSteps; }
+
+// personalization entry of (row v, column c), double-float
+__device__ __forceinline__ df red_of(const StepParams &p, const WaveScalars &wc, int64_t v, int c, bool uniform) {
+  if (uniform) return wc.inv_n;
+  df red = {0.0f, 0.0f};
+  const int pb = __ldg(&p.prow[v]), pe = __ldg(&p.prow[v + 1]);
+  for (int e = pb; e < pe; ++e)
+    if (__ldg(&p.pslot[e]) == c) {
+      const float2 w = __ldg(&p.pval[e]);
+      red = {w.x, w.y};
+    }
+  return red;
+}
+
+// x_0 = p, acc = x_0, tail = 0, gathered blocks for step 1, per-column
+// dangling sums of x_0; zero padding row n of both gathered blocks.  One
+// thread per (row, column) entry, columns fastest.
+__global__ void __launch_bounds__(kBThreads) batch_init(StepParams p) {
+  __shared__ long long bdg[kMaxKT];
+  const WaveScalars wc = p.wc->s;
+  const int kt = wc.kt;
+  for (int c = threadIdx.x; c < kt; c += blockDim.x) bdg[c] = 0;
+  __syncthreads();
+  const int64_t total = (p.n + 1) * kt;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = i / kt;
+    const int c = (int)(i - v * kt);
+    if (v == p.n) {
+      p.gdf[0][i] = p.gdf[1][i] = make_float2(0.f, 0.f);
+      p.gf[0][i] = p.gf[1][i] = 0.f;
       continue;
     }
-    df x0 = {0.f, 0.f};
-    if (col_ok) x0 = p.x0 ? df_make(p.x0[p.xcol[c] * p.n + p.perm[v]]) : red_of(p, v, c, uniform);
+    const bool col_ok = c < wc.ncols;
+    const df x0 = col_ok ? red_of(p, wc, v, c, p.cols[c].uniform != 0) : df{0.f, 0.f};
     const float dg = p.deg[v];
     p.acc[i] = make_float2(x0.hi, x0.lo);
     p.tail[i] = 0.f;
     const df g = dg > 0.f ? df_div_f(x0, dg) : df{0.f, 0.f};
-    p.gdf_out[i] = make_float2(g.hi, g.lo);
-    p.gf_out[i] = g.hi;
-    if (dg == 0.f) dang += fx_of(x0.hi, p.fx_scale) + fx_of(x0.lo, p.fx_scale);
-  }
-  bdg[wid][lane] = dang;
-  __syncthreads();
-  if (wid == 0 && lane < kCols) {
-    long long t = 0;
-    for (int w = 0; w < kBWarps; ++w)
-      for (int q = lane; q < 32; q += kCols) t += bdg[w][q];
-    if (t) atomicAdd((unsigned long long *)&p.sums[lane * 4 + 0], (unsigned long long)t);
-  }
-}
-
-// results of the wave: out[c * n + perm[v]] = acc + tail (FP32)
-__global__ void batch_finalize(BatchParams p) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int sub = lane / kCols, c = lane & (kCols - 1);
-  const int64_t step = (int64_t)gridDim.x * (blockDim.x >> 5) * kRowsPerWarp;
-  for (int64_t v = ((int64_t)blockIdx.x * (blockDim.x >> 5) + wid) * kRowsPerWarp + sub; v < p.n; v += step) {
-    const int64_t i = v * kCols + c;
-    if (c < p.ncols) {
-      const float2 a = p.acc[i];
-      p.out[p.ocol[c] * p.n + p.perm[v]] = (float)((double)a.x + (double)a.y + (double)p.tail[i]);
+    p.gdf[0][i] = make_float2(g.hi, g.lo);
+    p.gf[0][i] = g.hi;
+    if (dg == 0.f && col_ok) {
+      const long long t = fx_of(x0.hi, wc.fx_scale) + fx_of(x0.lo, wc.fx_scale);
+      if (t) atomicAdd((unsigned long long *)&bdg[c], (unsigned long long)t);
     }
   }
+  __syncthreads();
+  for (int c = threadIdx.x; c < kt; c += blockDim.x)
+    if (bdg[c]) atomicAdd((unsigned long long *)&p.sums[c * 4 + 0], (unsigned long long)bdg[c]);
 }
 
-// Tiled forms for 32-column waves.  A warp takes 32 consecutive original
-// node ids u0..u0+31: the warm starts (set-major, original order) are read 32
-// consecutive floats per column, the wave's rows inv_perm[u] (relabelled) are
-// read or written 32 columns at a time, and a 32x32 shared-memory tile turns
-// one into the other, so both sides are coalesced.
+// Tiled forms for caller start vectors and for the results.  A warp takes 32
+// consecutive original node ids u0..u0+31 and one group of 32 columns: the
+// set-major vectors (original order) are read or written 32 consecutive
+// floats per column, the wave's rows inv_perm[u] (relabelled) 32 columns at
+// a time, and a 32x32 shared-memory tile turns one into the other, so both
+// sides are coalesced.
 constexpr int kTile = 32;
 
-// batch_init for caller start vectors (p.x0 set); same outputs.
-__global__ void __launch_bounds__(kBThreads) batch_init_x0(BatchParams p, const int32_t *__restrict__ inv_perm) {
+// batch_init for caller start vectors (wc.has_x0; x0 set-major, original order)
+__global__ void __launch_bounds__(kBThreads) batch_init_x0(StepParams p, const float *__restrict__ x0,
+                                                           const int32_t *__restrict__ inv_perm) {
   __shared__ float tile[kBWarps][kTile][kTile + 1];  // [column][node]
-  __shared__ long long bdg[kBWarps][32];
+  __shared__ long long bdg[kMaxKT];
+  const WaveScalars wc = p.wc->s;
+  const int64_t *xcol = p.wc->xcol;
+  const int kt = wc.kt, groups = kt / kTile;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  long long dang = 0;  // column `lane`
+  for (int c = threadIdx.x; c < kt; c += blockDim.x) bdg[c] = 0;
+  __syncthreads();
   if (blockIdx.x == 0 && wid == 0) {  // padding row: gathers of padded edges read zeros
-    const int64_t i = p.n * kCols + lane;
-    p.gdf_out[i] = make_float2(0.f, 0.f);
-    p.gf_out[i] = 0.f;
-    const_cast<float2 *>(p.gdf_in)[i] = make_float2(0.f, 0.f);
-    const_cast<float *>(p.gf_in)[i] = 0.f;
+    for (int c = lane; c < kt; c += 32) {
+      const int64_t i = p.n * kt + c;
+      p.gdf[0][i] = p.gdf[1][i] = make_float2(0.f, 0.f);
+      p.gf[0][i] = p.gf[1][i] = 0.f;
+    }
   }
-  const int64_t step = (int64_t)gridDim.x * kBWarps * kTile;
-  for (int64_t u0 = ((int64_t)blockIdx.x * kBWarps + wid) * kTile; u0 < p.n; u0 += step) {
+  const int64_t ntiles = ceil_div<int64_t>(p.n, kTile) * groups;
+  long long dang = 0;  // column gr * 32 + lane of the tiles this warp handled (one group per warp pass)
+  for (int64_t tw = (int64_t)blockIdx.x * kBWarps + wid; tw < ntiles; tw += (int64_t)gridDim.x * kBWarps) {
+    const int gr = (int)(tw % groups);
+    const int64_t u0 = (tw / groups) * kTile;
     const int64_t u = u0 + lane;
     const bool u_ok = u < p.n;
-    for (int c = 0; c < kCols; ++c)
-      tile[wid][c][lane] = (c < p.ncols && u_ok) ? p.x0[p.xcol[c] * p.n + u] : 0.f;
+    for (int c = 0; c < kTile; ++c) {
+      const int cc = gr * kTile + c;
+      tile[wid][c][lane] = (cc < wc.ncols && u_ok) ? x0[xcol[cc] * p.n + u] : 0.f;
+    }
     const int32_t vl = u_ok ? inv_perm[u] : 0;
     __syncwarp();
     const int jn = (int)(p.n - u0 < (int64_t)kTile ? p.n - u0 : (int64_t)kTile);
+    dang = 0;
     for (int j = 0; j < jn; ++j) {
       const int64_t v = __shfl_sync(0xffffffffu, vl, j);
-      const int64_t i = v * kCols + lane;
-      const df x0 = {tile[wid][lane][j], 0.f};
+      const int64_t i = v * kt + gr * kTile + lane;
+      const df xv = {tile[wid][lane][j], 0.f};
       const float dg = p.deg[v];
-      p.acc[i] = make_float2(x0.hi, x0.lo);
+      p.acc[i] = make_float2(xv.hi, xv.lo);
       p.tail[i] = 0.f;
-      const df g = dg > 0.f ? df_div_f(x0, dg) : df{0.f, 0.f};
-      p.gdf_out[i] = make_float2(g.hi, g.lo);
-      p.gf_out[i] = g.hi;
-      if (dg == 0.f) dang += fx_of(x0.hi, p.fx_scale);
+      const df g = dg > 0.f ? df_div_f(xv, dg) : df{0.f, 0.f};
+      p.gdf[0][i] = make_float2(g.hi, g.lo);
+      p.gf[0][i] = g.hi;
+      if (dg == 0.f) dang += fx_of(xv.hi, wc.fx_scale);
     }
+    if (dang) atomicAdd((unsigned long long *)&bdg[gr * kTile + lane], (unsigned long long)dang);
     __syncwarp();
   }
-  bdg[wid][lane] = dang;
   __syncthreads();
-  if (wid == 0) {
-    long long t = 0;
-    for (int w = 0; w < kBWarps; ++w) t += bdg[w][lane];
-    if (t) atomicAdd((unsigned long long *)&p.sums[lane * 4 + 0], (unsigned long long)t);
-  }
+  for (int c = threadIdx.x; c < kt; c += blockDim.x)
+    if (bdg[c]) atomicAdd((unsigned long long *)&p.sums[c * 4 + 0], (unsigned long long)bdg[c]);
 }
 
 // float(a.x + a.y + t) without FP64 (issued at a small fraction of the FP32
@@ -684,47 +927,62 @@ __device__ __forceinline__ float sum3_f(float ax, float ay, float t) {
 }
 
 // results of the wave: out[ocol[c] * n + u] = acc + tail of row inv_perm[u]
-__global__ void __launch_bounds__(kBThreads) batch_finalize_t(BatchParams p, const int32_t *__restrict__ inv_perm) {
+__global__ void __launch_bounds__(kBThreads) batch_finalize_t(StepParams p, float *__restrict__ out,
+                                                              const int32_t *__restrict__ inv_perm) {
   __shared__ float tile[kBWarps][kTile][kTile + 1];  // [node][column]
+  const WaveScalars wc = p.wc->s;
+  const int64_t *ocol = p.wc->ocol;
+  const int kt = wc.kt, groups = kt / kTile;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t step = (int64_t)gridDim.x * kBWarps * kTile;
-  for (int64_t u0 = ((int64_t)blockIdx.x * kBWarps + wid) * kTile; u0 < p.n; u0 += step) {
+  const int64_t ntiles = ceil_div<int64_t>(p.n, kTile) * groups;
+  for (int64_t tw = (int64_t)blockIdx.x * kBWarps + wid; tw < ntiles; tw += (int64_t)gridDim.x * kBWarps) {
+    const int gr = (int)(tw % groups);
+    if (gr * kTile >= wc.ncols) continue;
+    const int64_t u0 = (tw / groups) * kTile;
     const int64_t u = u0 + lane;
     const bool u_ok = u < p.n;
     const int32_t vl = u_ok ? inv_perm[u] : 0;
     const int jn = (int)(p.n - u0 < (int64_t)kTile ? p.n - u0 : (int64_t)kTile);
     for (int j = 0; j < jn; ++j) {
       const int64_t v = __shfl_sync(0xffffffffu, vl, j);
-      const int64_t i = v * kCols + lane;
+      const int64_t i = v * kt + gr * kTile + lane;
       const float2 a = p.acc[i];
       tile[wid][j][lane] = sum3_f(a.x, a.y, p.tail[i]);
     }
     __syncwarp();
-    if (u_ok)
-      for (int c = 0; c < p.ncols; ++c) p.out[p.ocol[c] * p.n + u] = tile[wid][lane][c];
+    if (u_ok) {
+      const int cn = min(kTile, wc.ncols - gr * kTile);
+      for (int c = 0; c < cn; ++c) out[ocol[gr * kTile + c] * p.n + u] = tile[wid][lane][c];
+    }
     __syncwarp();
   }
 }
 
-__global__ void chunk_counts(const int64_t *rp, int32_t n_big, int64_t *nch) {
-  for (int32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= n_big; h += gridDim.x * blockDim.x)
-    nch[h] = h < n_big ? ceil_div<int64_t>(rp[h + 1] - rp[h], kSpmmChunk) : 0;
+// chunk plan: tasks and base blocks per row with more than `chunk` in-edges
+__global__ void chunk_counts(const int64_t *rp, int32_t n_big, int chunk, int64_t *nch, int64_t *nbl) {
+  for (int32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= n_big; h += gridDim.x * blockDim.x) {
+    const int64_t d = h < n_big ? rp[h + 1] - rp[h] : 0;
+    nch[h] = ceil_div<int64_t>(d, chunk);
+    nbl[h] = ceil_div<int64_t>(d, kBase);
+  }
 }
 
-__global__ void chunk_fill(const int64_t *first64, int32_t n_big, int32_t *first, int32_t *task_row) {
+__global__ void chunk_fill(const int64_t *first64, const int64_t *blk64, int32_t n_big, int32_t *first,
+                           int32_t *task_row, int32_t *blk) {
   for (int32_t h = blockIdx.x * blockDim.x + threadIdx.x; h <= n_big; h += gridDim.x * blockDim.x) {
     first[h] = (int32_t)first64[h];
+    blk[h] = (int32_t)blk64[h];
     if (h < n_big)
       for (int64_t t = first64[h]; t < first64[h + 1]; ++t) task_row[t] = h;
   }
 }
 
-// first row with in-degree <= kSpmmBig (rows are in non-increasing degree)
-__global__ void count_big(const int64_t *rp, int64_t n, int64_t *out) {
+// first row with in-degree <= chunk (rows are in non-increasing degree)
+__global__ void count_big(const int64_t *rp, int64_t n, int chunk, int64_t *out) {
   int64_t lo = 0, hi = n;
   while (lo < hi) {
     const int64_t mid = (lo + hi) / 2;
-    if (rp[mid + 1] - rp[mid] > kSpmmBig) lo = mid + 1;
+    if (rp[mid + 1] - rp[mid] > chunk) lo = mid + 1;
     else hi = mid;
   }
   *out = lo;
@@ -754,10 +1012,19 @@ __global__ void __launch_bounds__(256) prow_from_sorted(const int32_t *rows, int
   }
 }
 
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int cpl_index(int cpl) { return cpl == 1 ? 0 : (cpl == 2 ? 1 : 2); }
+
+size_t block_bytes_per_col(int64_t n) {  // gdf x2, gf x2, acc, tail
+  return (size_t)(n + 1) * (2 * sizeof(float2) + 2 * sizeof(float) + sizeof(float2) + sizeof(float));
+}
+
 Status batch_prepare_impl(Ctx *ctx, Graph *g);
 
-// The batched plan and workspace of a graph, built on first use; a failed
-// build leaves no partial state behind (the next call builds it again).
+// The batched state of a graph (everything but the tile workspace), built
+// on first use; a failed build leaves no partial state behind.
 Status batch_prepare(Ctx *ctx, Graph *g) {
   if (g->batch) return Status::ok();
   Status st = batch_prepare_impl(ctx, g);
@@ -777,44 +1044,11 @@ Status batch_prepare_impl(Ctx *ctx, Graph *g) {
   GOPS_CUDA_TRY(cudaMallocHost(&b->hwave, 2 * sizeof(WaveState)));
   GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->wev[0], cudaEventDisableTiming));
   GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->wev[1], cudaEventDisableTiming));
-  int64_t *tmp = nullptr;
-  GOPS_CUDA_TRY(dev_malloc_async((void **)&tmp, sizeof(int64_t) * 2, s));
-  count_big<<<1, 1, 0, s>>>(g->in_rp, n, tmp);
-  int64_t nbig = 0;
-  GOPS_CUDA_TRY(cudaMemcpyAsync(&nbig, tmp, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-  GOPS_CUDA_TRY(cudaStreamSynchronize(s));
-  free_async(tmp, s);
-  b->n_big = (int32_t)nbig;
-  if (nbig > 0) {
-    int64_t *nch = nullptr;
-    GOPS_CUDA_TRY(dev_malloc_async((void **)&nch, sizeof(int64_t) * (nbig + 1), s));
-    chunk_counts<<<blocks_for(nbig + 1, 256, 4096), 256, 0, s>>>(g->in_rp, b->n_big, nch);
-    GOPS_TRY(exclusive_scan_i64(nch, nch, nbig + 1, s));
-    int64_t tasks = 0;
-    GOPS_CUDA_TRY(cudaMemcpyAsync(&tasks, nch + nbig, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
-    GOPS_CUDA_TRY(cudaMalloc(&b->big_first, sizeof(int32_t) * (nbig + 1)));
-    GOPS_CUDA_TRY(cudaMalloc(&b->big_task_row, sizeof(int32_t) * std::max<int64_t>(tasks, 1)));
-    chunk_fill<<<blocks_for(nbig + 1, 256, 4096), 256, 0, s>>>(nch, b->n_big, b->big_first, b->big_task_row);
-    GOPS_CUDA_TRY(cudaGetLastError());
-    free_async(nch, s);
-    b->n_big_tasks = (int32_t)tasks;
-  }
-  b->n_tasks = b->n_big_tasks + (n - nbig);
-  const size_t blk = (size_t)(n + 1) * kCols;
-  GOPS_CUDA_TRY(cudaMalloc(&b->gdf[0], sizeof(float2) * blk));
-  GOPS_CUDA_TRY(cudaMalloc(&b->gdf[1], sizeof(float2) * blk));
-  GOPS_CUDA_TRY(cudaMalloc(&b->gf[0], sizeof(float) * blk));
-  GOPS_CUDA_TRY(cudaMalloc(&b->gf[1], sizeof(float) * blk));
-  GOPS_CUDA_TRY(cudaMalloc(&b->acc, sizeof(float2) * blk));
-  GOPS_CUDA_TRY(cudaMalloc(&b->tail, sizeof(float) * blk));
-  GOPS_CUDA_TRY(cudaMalloc(&b->lpart, sizeof(float2) * (size_t)std::max<int32_t>(b->n_big_tasks, 1) * kCols));
-  GOPS_CUDA_TRY(cudaMalloc(&b->lcnt, sizeof(unsigned) * (size_t)std::max<int32_t>(b->n_big, 1)));
-  GOPS_CUDA_TRY(cudaMalloc(&b->sums, sizeof(long long) * 3 * kCols * 4));
-  GOPS_CUDA_TRY(cudaMalloc(&b->cols, sizeof(ColState) * kCols));
+  GOPS_CUDA_TRY(cudaMalloc(&b->sums, sizeof(long long) * 3 * kMaxKT * 4));
+  GOPS_CUDA_TRY(cudaMalloc(&b->cols, sizeof(ColState) * kMaxKT));
   GOPS_CUDA_TRY(cudaMalloc(&b->wave, sizeof(WaveState)));
+  GOPS_CUDA_TRY(cudaMalloc(&b->wc, sizeof(WaveConst)));
   GOPS_CUDA_TRY(cudaMalloc(&b->prow, sizeof(int32_t) * (n + 1)));
-  GOPS_CUDA_TRY(cudaMalloc(&b->out, sizeof(float) * (size_t)n * kCols));
   // host copy of the relabelling, inverted
   std::vector<int32_t> perm((size_t)n);
   GOPS_CUDA_TRY(cudaMemcpyAsync(perm.data(), g->perm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
@@ -828,13 +1062,90 @@ Status batch_prepare_impl(Ctx *ctx, Graph *g) {
   return Status::ok();
 }
 
+template <int CPL>
+void set_grids(const Ctx *ctx, BatchState *b);
+
+// The chunk plan for `chunk` and the blocks for k-tile 32 * cpl (kept when
+// they already serve it).
+Status ensure_tile(Ctx *ctx, Graph *g, int cpl, int chunk) {
+  BatchState *b = g->batch;
+  cudaStream_t s = ctx->stream;
+  const int64_t n = g->n;
+  const int kt = 32 * cpl;
+  if (b->chunk != chunk) {
+    free_graphs(b);
+    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+    free_plan(b);
+    int64_t *tmp = nullptr;
+    GOPS_CUDA_TRY(dev_malloc_async((void **)&tmp, sizeof(int64_t) * 2, s));
+    count_big<<<1, 1, 0, s>>>(g->in_rp, n, chunk, tmp);
+    int64_t nbig = 0;
+    GOPS_CUDA_TRY(cudaMemcpyAsync(&nbig, tmp, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+    free_async(tmp, s);
+    int64_t tasks = 0, blocks = 0;
+    GOPS_CUDA_TRY(cudaMalloc(&b->big_first, sizeof(int32_t) * (nbig + 1)));
+    GOPS_CUDA_TRY(cudaMalloc(&b->blk_first, sizeof(int32_t) * (nbig + 1)));
+    if (nbig > 0) {
+      int64_t *nch = nullptr, *nbl = nullptr;
+      GOPS_CUDA_TRY(dev_malloc_async((void **)&nch, sizeof(int64_t) * (nbig + 1), s));
+      GOPS_CUDA_TRY(dev_malloc_async((void **)&nbl, sizeof(int64_t) * (nbig + 1), s));
+      chunk_counts<<<blocks_for(nbig + 1, 256, 4096), 256, 0, s>>>(g->in_rp, (int32_t)nbig, chunk, nch, nbl);
+      GOPS_TRY(exclusive_scan_i64(nch, nch, nbig + 1, s));
+      GOPS_TRY(exclusive_scan_i64(nbl, nbl, nbig + 1, s));
+      GOPS_CUDA_TRY(cudaMemcpyAsync(&tasks, nch + nbig, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+      GOPS_CUDA_TRY(cudaMemcpyAsync(&blocks, nbl + nbig, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+      GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+      GOPS_CUDA_TRY(cudaMalloc(&b->big_task_row, sizeof(int32_t) * std::max<int64_t>(tasks, 1)));
+      chunk_fill<<<blocks_for(nbig + 1, 256, 4096), 256, 0, s>>>(nch, nbl, (int32_t)nbig, b->big_first,
+                                                                  b->big_task_row, b->blk_first);
+      GOPS_CUDA_TRY(cudaGetLastError());
+      free_async(nch, s);
+      free_async(nbl, s);
+    } else {
+      GOPS_CUDA_TRY(cudaMemsetAsync(b->big_first, 0, sizeof(int32_t), s));
+      GOPS_CUDA_TRY(cudaMemsetAsync(b->blk_first, 0, sizeof(int32_t), s));
+      GOPS_CUDA_TRY(cudaMalloc(&b->big_task_row, sizeof(int32_t)));
+    }
+    GOPS_CUDA_TRY(cudaMalloc(&b->lcnt, sizeof(unsigned) * (size_t)std::max<int64_t>(nbig, 1)));
+    GOPS_CUDA_TRY(cudaMemsetAsync(b->lcnt, 0, sizeof(unsigned) * (size_t)std::max<int64_t>(nbig, 1), s));
+    b->n_big = (int32_t)nbig;
+    b->n_big_tasks = (int32_t)tasks;
+    b->n_blocks = (int32_t)blocks;
+    b->chunk = chunk;
+    cudaFree(b->lpart);  // sized by the blocks of this plan
+    b->lpart = nullptr;
+  }
+  if (b->kt_cap < kt) {
+    free_graphs(b);
+    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+    free_blocks(b);
+    const size_t blk = (size_t)(n + 1) * kt;
+    GOPS_CUDA_TRY(cudaMalloc(&b->gdf[0], sizeof(float2) * blk));
+    GOPS_CUDA_TRY(cudaMalloc(&b->gdf[1], sizeof(float2) * blk));
+    GOPS_CUDA_TRY(cudaMalloc(&b->gf[0], sizeof(float) * blk));
+    GOPS_CUDA_TRY(cudaMalloc(&b->gf[1], sizeof(float) * blk));
+    GOPS_CUDA_TRY(cudaMalloc(&b->acc, sizeof(float2) * blk));
+    GOPS_CUDA_TRY(cudaMalloc(&b->tail, sizeof(float) * blk));
+    b->kt_cap = kt;
+  }
+  if (!b->lpart)
+    GOPS_CUDA_TRY(cudaMalloc(&b->lpart, sizeof(float2) * (size_t)std::max<int32_t>(b->n_blocks, 1) * b->kt_cap));
+  b->cpl = cpl;
+  if (cpl == 1) set_grids<1>(ctx, b);
+  else if (cpl == 2) set_grids<2>(ctx, b);
+  else set_grids<4>(ctx, b);
+  return Status::ok();
+}
+
 Status ensure_entries(BatchState *b, int64_t e, cudaStream_t st) {
   if (e <= b->pcap) return Status::ok();
   GOPS_CUDA_TRY(cudaStreamSynchronize(st));  // earlier waves may still read the old arrays
+  free_graphs(b);                            // the captured chunks name the old arrays
   cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted);
   b->pslot = nullptr; b->pval = nullptr; b->prows_sorted = nullptr;
   b->pcap = 0;  // a failed allocation below leaves no capacity claimed
-  const int64_t cap = std::max<int64_t>(e, 1024);
+  const int64_t cap = std::max<int64_t>(e, 4096);
   GOPS_CUDA_TRY(cudaMalloc(&b->pslot, sizeof(int32_t) * cap));
   GOPS_CUDA_TRY(cudaMalloc(&b->pval, sizeof(float2) * cap));
   GOPS_CUDA_TRY(cudaMalloc(&b->prows_sorted, sizeof(int32_t) * cap));
@@ -842,7 +1153,252 @@ Status ensure_entries(BatchState *b, int64_t e, cudaStream_t st) {
   return Status::ok();
 }
 
+StepParams step_params(const Graph *g, const BatchState *b) {
+  StepParams p{};
+  p.n = g->n;
+  p.rp = g->in_rp;
+  p.col = g->in_col;
+  p.deg = g->deg;
+  p.perm = g->perm;
+  p.n_big = b->n_big;
+  p.n_big_tasks = b->n_big_tasks;
+  p.chunk = b->chunk;
+  p.big_first = b->big_first;
+  p.big_task_row = b->big_task_row;
+  p.blk_first = b->blk_first;
+  p.prow = b->prow;
+  p.pslot = b->pslot;
+  p.pval = b->pval;
+  p.gdf[0] = b->gdf[0];
+  p.gdf[1] = b->gdf[1];
+  p.gf[0] = b->gf[0];
+  p.gf[1] = b->gf[1];
+  p.acc = b->acc;
+  p.tail = b->tail;
+  p.lpart = b->lpart;
+  p.lcnt = b->lcnt;
+  p.sums = b->sums;
+  p.cols = b->cols;
+  p.wave = b->wave;
+  p.wc = b->wc;
+  return p;
+}
+
+template <class K>
+int spmm_grid(const Ctx *ctx, const BatchState *b, K kernel) {
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kBThreads, 0);
+  const int64_t need = ceil_div<int64_t>(std::max<int64_t>(b->n_big_tasks + (b->n - b->n_big), 1), kBWarps);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * std::max(occ, 1)));
+}
+
+template <int CPL>
+void set_grids(const Ctx *ctx, BatchState *b) {
+  b->grid_df = spmm_grid(ctx, b, spmm_mixed<CPL>);
+  b->grid_f = spmm_grid(ctx, b, spmm_f32<CPL>);
+}
+
+// One step of the wave at offset j of the chunk, in the precision phase P.
+template <int CPL>
+Status launch_step(const BatchState *b, StepParams p, int j, bool df, cudaStream_t st) {
+  p.j = j;
+  if (df) {
+    spmm_mixed<CPL><<<b->grid_df, kBThreads, 0, st>>>(p);
+  } else {
+    spmm_f32<CPL><<<b->grid_f, kBThreads, 0, st>>>(p);
+  }
+  GOPS_CUDA_TRY(cudaGetLastError());
+  return Status::ok();
+}
+
+Status launch_step_cpl(const Ctx *, const BatchState *b, const StepParams &p, int j, bool df, cudaStream_t st) {
+  switch (b->cpl) {
+    case 1: return launch_step<1>(b, p, j, df, st);
+    case 2: return launch_step<2>(b, p, j, df, st);
+    default: return launch_step<4>(b, p, j, df, st);
+  }
+}
+
+// The captured chunk: kChunkSteps steps (a double-float and an FP32 launch
+// each for variant 0, FP32 only for variant 1), then the step counter.
+Status ensure_chunk_graph(Ctx *ctx, Graph *g, int variant) {
+  BatchState *b = g->batch;
+  if (b->exec_cpl != b->cpl || b->exec_chunk != b->chunk || b->exec_pslot != b->pslot) free_graphs(b);
+  if (b->chunk_exec[variant]) return Status::ok();
+  cudaStream_t st = ctx->stream;
+  const StepParams p = step_params(g, b);
+  cudaGraph_t graph = nullptr;
+  GOPS_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  Status cs;
+  for (int j = 0; j < kChunkSteps && cs.code == GOPS_OK; ++j) {
+    if (variant == 0) cs = launch_step_cpl(ctx, b, p, j, true, st);
+    if (cs.code == GOPS_OK) cs = launch_step_cpl(ctx, b, p, j, false, st);
+  }
+  if (cs.code == GOPS_OK) {
+    advance_kernel<<<1, 1, 0, st>>>(b->wave);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) cs = Status{GOPS_ERR_CUDA, cudaGetErrorString(e)};
+  }
+  const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+  GOPS_TRY(cs);
+  GOPS_CUDA_TRY(ee);
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  GOPS_CUDA_TRY(ei);
+  b->chunk_exec[variant] = exec;
+  b->exec_cpl = b->cpl;
+  b->exec_chunk = b->chunk;
+  b->exec_pslot = b->pslot;
+  return Status::ok();
+}
+
+void fill_wave_const(WaveScalars &w, const gops_config *cfg, int64_t n, int kt, int ncols, bool has_x0, double wmax) {
+  w.d = df_from_double(cfg->damping);
+  w.omd = df_from_double(1.0 - cfg->damping);
+  w.inv_n = df_from_double(1.0 / (double)n);
+  w.tol = cfg->tolerance;
+  w.max_iter = cfg->max_iterations;
+  w.ncols = ncols;
+  w.has_x0 = has_x0 ? 1 : 0;
+  w.kt = kt;
+  // fixed-point range: a start of L1 norm up to wmax keeps every partial
+  // sum far below 2^63; larger or non-finite starts are flagged by the
+  // nonfinite counter and the column does not converge
+  int e = 0;
+  while (e < 20 && std::ldexp(1.0, e) < wmax) ++e;
+  const int F = 58 - 2 * e;
+  w.fx_scale = std::ldexp(1.0f, F);
+  w.fx_inv = std::ldexp(1.0, -F);
+}
+
+// ---------------------------------------------------------------------------
+// autotuner: the k-tile (columns per lane) and the chunk size of long rows,
+// picked per graph from timed steps on a probe wave (uniform personalization
+// in every column, never converging) with the workspace the choice needs.
+// Cost of a candidate: its time per column-step, 3/4 FP32 and 1/4
+// double-float steps.  Results do not depend on the choice (canonical row
+// sums), only the time does.
+// ---------------------------------------------------------------------------
+Status probe_tile(Ctx *ctx, Graph *g, int cpl, int chunk, float *cost) {
+  BatchState *b = g->batch;
+  cudaStream_t st = ctx->stream;
+  GOPS_TRY(ensure_tile(ctx, g, cpl, chunk));
+  const int kt = 32 * cpl;
+  gops_config cfg{0.85, 1000000, 0.0};
+  WaveConst w{};
+  fill_wave_const(w.s, &cfg, g->n, kt, kt, false, 1.0);
+  std::vector<ColState> cols(kMaxKT, ColState{0, 0.0, 1, 0, 1, 0, (double)INFINITY, (double)INFINITY});
+  for (int c = 0; c < kt; ++c) cols[c].retired = 0;
+  GOPS_CUDA_TRY(cudaMemcpyAsync(b->wc, &w, sizeof(WaveConst), cudaMemcpyHostToDevice, st));
+  GOPS_CUDA_TRY(cudaMemcpyAsync(b->cols, cols.data(), sizeof(ColState) * kMaxKT, cudaMemcpyHostToDevice, st));
+  GOPS_CUDA_TRY(cudaMemsetAsync(b->wave, 0, sizeof(WaveState), st));
+  GOPS_CUDA_TRY(cudaMemsetAsync(b->sums, 0, sizeof(long long) * 3 * kMaxKT * 4, st));
+  GOPS_CUDA_TRY(cudaMemsetAsync(b->prow, 0, sizeof(int32_t) * (g->n + 1), st));
+  GOPS_CUDA_TRY(cudaMemsetAsync(b->lcnt, 0, sizeof(unsigned) * (size_t)std::max<int32_t>(b->n_big, 1), st));
+  StepParams p = step_params(g, b);
+  batch_init<<<blocks_for((g->n + 1) * kt, kBThreads, ctx->num_sms * 8), kBThreads, 0, st>>>(p);
+  GOPS_CUDA_TRY(cudaGetLastError());
+  // step 1 (double-float), then FP32 steps (theta = inf: FP32 from step 2)
+  constexpr int kF = 3;
+  cudaEvent_t ev[2 * (kF + 1)];
+  for (auto &e : ev) GOPS_CUDA_TRY(cudaEventCreate(&e));
+  struct EvGuard {
+    cudaEvent_t *e; int n;
+    ~EvGuard() { for (int i = 0; i < n; ++i) cudaEventDestroy(e[i]); }
+  } guard{ev, 2 * (kF + 1)};
+  GOPS_CUDA_TRY(cudaEventRecord(ev[0], st));
+  GOPS_TRY(launch_step_cpl(ctx, b, p, 0, true, st));
+  GOPS_CUDA_TRY(cudaEventRecord(ev[1], st));
+  for (int i = 0; i < kF; ++i) {
+    GOPS_CUDA_TRY(cudaEventRecord(ev[2 + 2 * i], st));
+    GOPS_TRY(launch_step_cpl(ctx, b, p, 1 + i, false, st));
+    GOPS_CUDA_TRY(cudaEventRecord(ev[3 + 2 * i], st));
+  }
+  GOPS_CUDA_TRY(cudaStreamSynchronize(st));
+  float t_df = 0.f;
+  cudaEventElapsedTime(&t_df, ev[0], ev[1]);
+  std::vector<float> tf(kF);
+  for (int i = 0; i < kF; ++i) cudaEventElapsedTime(&tf[i], ev[2 + 2 * i], ev[3 + 2 * i]);
+  std::sort(tf.begin(), tf.end());
+  *cost = (0.75f * tf[kF / 2] + 0.25f * t_df) / (float)kt;
+  return Status::ok();
+}
+
+Status batch_tune(Ctx *ctx, Graph *g) {
+  BatchState *b = g->batch;
+  if (b->tuned) return Status::ok();
+  const int chunks[2] = {256, 1024};
+  int cpls[3] = {1, 2, 4};
+  // the wave workspace may take ~40 % of the device memory free now
+  size_t free_b = 0, total_b = 0;
+  GOPS_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+  const size_t budget = (size_t)(0.4 * (double)free_b);
+  float best = INFINITY;
+  int best_cpl = 1, best_chunk = 256;
+  for (int cpl : cpls) {
+    if (cpl > 1 && block_bytes_per_col(g->n) * 32 * cpl > budget) continue;
+    for (int ch : chunks) {
+      float c = 0.f;
+      GOPS_TRY(probe_tile(ctx, g, cpl, ch, &c));
+      b->tune_ms[cpl_index(cpl)][ch == 256 ? 0 : 1] = c;
+      if (c < best) {
+        best = c;
+        best_cpl = cpl;
+        best_chunk = ch;
+      }
+    }
+  }
+  // keep only the workspace the choice needs
+  if (b->kt_cap > 32 * best_cpl) {
+    free_graphs(b);
+    GOPS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    free_blocks(b);
+  }
+  b->chunk = 0;  // rebuild the plan for the chosen chunk
+  free_plan(b);
+  GOPS_TRY(ensure_tile(ctx, g, best_cpl, best_chunk));
+  b->tuned = true;
+  return Status::ok();
+}
+
 }  // namespace
+
+// Choose (cols > 0) or autotune (cols == 0) the k-tile and chunk size.
+Status batch_set_tile(Ctx *ctx, Graph *g, int cols, int chunk) {
+  GOPS_TRY(batch_prepare(ctx, g));
+  BatchState *b = g->batch;
+  if (cols == 0) {
+    b->tuned = false;
+    return batch_tune(ctx, g);
+  }
+  if (cols != 32 && cols != 64 && cols != 128) return Status{GOPS_ERR_INVALID, "cols must be 0, 32, 64 or 128"};
+  if (chunk < kBase || chunk % kBase) return Status{GOPS_ERR_INVALID, "chunk must be a positive multiple of 256"};
+  if (b->kt_cap > cols) {
+    free_graphs(b);
+    GOPS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    free_blocks(b);
+  }
+  GOPS_TRY(ensure_tile(ctx, g, cols / 32, chunk));
+  b->tuned = true;
+  return Status::ok();
+}
+
+Status batch_get_tile(Graph *g, int *cols, int *chunk, float *cost) {
+  BatchState *b = g->batch;
+  if (!b || !b->tuned) {
+    *cols = 0;
+    *chunk = 0;
+    if (cost)
+      for (int i = 0; i < 6; ++i) cost[i] = 0.f;
+    return Status::ok();
+  }
+  *cols = 32 * b->cpl;
+  *chunk = b->chunk;
+  if (cost)
+    for (int i = 0; i < 6; ++i) cost[i] = b->tune_ms[i / 2][i % 2];
+  return Status::ok();
+}
 
 // nsets seed sets -> scores (host or device, set-major, original node order)
 Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, const int64_t *seed_ptr,
@@ -861,56 +1417,47 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   for (int64_t k = seed_ptr[0]; k < seed_ptr[nsets]; ++k)
     if (seed_idx[k] < 0 || seed_idx[k] >= n) return Status{GOPS_ERR_INVALID, "seed index out of range"};
   GOPS_TRY(batch_prepare(ctx, g));
+  GOPS_TRY(batch_tune(ctx, g));
   BatchState *b = g->batch;
   cudaStream_t st = ctx->stream;
-  if (x0 && !x0_on_device && !b->x0) GOPS_CUDA_TRY(cudaMalloc(&b->x0, sizeof(float) * (size_t)n * kCols));
-
-  BatchParams p{};
-  p.n = n;
-  p.rp = g->in_rp;
-  p.col = g->in_col;
-  p.deg = g->deg;
-  p.perm = g->perm;
-  p.n_big = b->n_big;
-  p.n_big_tasks = b->n_big_tasks;
-  p.n_tasks = b->n_tasks;
-  p.big_first = b->big_first;
-  p.big_task_row = b->big_task_row;
-  p.prow = b->prow;
-  p.acc = b->acc;
-  p.tail = b->tail;
-  p.lpart = b->lpart;
-  p.lcnt = b->lcnt;
-  p.sums = b->sums;
-  p.cols = b->cols;
-  p.wave = b->wave;
-  p.d = df_from_double(cfg->damping);
-  p.omd = df_from_double(1.0 - cfg->damping);
-  p.inv_n = df_from_double(1.0 / (double)n);
-  p.tol = cfg->tolerance;
-  p.max_iter = cfg->max_iterations;
-
-  int occ_df = 0, occ_f = 0;
-  GOPS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_df, spmm_kernel<BDF>, kBThreads, 0));
-  GOPS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, spmm_kernel<BF32>, kBThreads, 0));
-  const int64_t need = ceil_div<int64_t>(ceil_div<int64_t>(std::max<int64_t>(b->n_tasks, 1), kRowsPerWarp), kBWarps);
-  const int grid_df = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * std::max(occ_df, 1)));
-  const int grid_f = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * std::max(occ_f, 1)));
-  const int grid_rows = blocks_for(n + 1, kBWarps * kRowsPerWarp, ctx->num_sms * 16);
+  const int KT = 32 * b->cpl;
+  if (x0 && !x0_on_device && b->x0_cols < KT) {
+    cudaFree(b->x0);
+    b->x0 = nullptr;
+    b->x0_cols = 0;
+    GOPS_CUDA_TRY(cudaMalloc(&b->x0, sizeof(float) * (size_t)n * KT));
+    b->x0_cols = KT;
+  }
+  if (scores && !scores_on_device && b->out_cols < KT) {
+    cudaFree(b->out);
+    b->out = nullptr;
+    b->out_cols = 0;
+    GOPS_CUDA_TRY(cudaMalloc(&b->out, sizeof(float) * (size_t)n * KT));
+    b->out_cols = KT;
+  }
 
   uint64_t launches = 0, col_iters = 0;
-  float spmm_ms = 0.f;
-  uint64_t spmm_launches = 0;
+  float spmm_ms = 0.f, df_ms = 0.f;
+  uint64_t spmm_launches = 0, df_launches = 0;
   // host results: each wave's block goes to a pinned buffer in one copy, and
   // host threads scatter its columns to the sets' rows while the GPU runs
   // the next wave (two buffers; a buffer's scatter is joined before reuse)
-  const size_t block_bytes = sizeof(float) * (size_t)kCols * (size_t)n;
-  const bool staged = scores && !scores_on_device && block_bytes <= (size_t(1) << 30);
-  if (staged && !b->hstage[0]) {
+  const size_t block_bytes = sizeof(float) * (size_t)KT * (size_t)n;
+  const bool staged = scores && !scores_on_device && block_bytes <= (size_t(1) << 31);
+  if (staged && b->hstage_bytes < block_bytes) {
+    for (auto &h : b->hstage)
+      if (h) {
+        cudaFreeHost(h);
+        h = nullptr;
+      }
+    b->hstage_bytes = 0;
     GOPS_CUDA_TRY(cudaMallocHost(&b->hstage[0], block_bytes));
     GOPS_CUDA_TRY(cudaMallocHost(&b->hstage[1], block_bytes));
-    GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->sev[0], cudaEventDisableTiming));
-    GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->sev[1], cudaEventDisableTiming));
+    b->hstage_bytes = block_bytes;
+    if (!b->sev[0]) {
+      GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->sev[0], cudaEventDisableTiming));
+      GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->sev[1], cudaEventDisableTiming));
+    }
   }
   constexpr int kScatterThreads = 4;
   struct Scatter {
@@ -927,8 +1474,8 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   // and a wave runs until its slowest column retires
   std::vector<int64_t> order(nsets);
   for (int64_t q = 0; q < nsets; ++q) order[q] = q;
-  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
-    return seed_ptr[a + 1] - seed_ptr[a] < seed_ptr[b + 1] - seed_ptr[b];
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t c) {
+    return seed_ptr[a + 1] - seed_ptr[a] < seed_ptr[c + 1] - seed_ptr[c];
   });
   // a wave whose block is being copied to hstage[q] and not yet scattered:
   // its scatter starts once the copy's event has passed, while the next wave
@@ -961,10 +1508,10 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     std::vector<float2> eval;
   } hw[2];
   auto prep = [&](HostWave &h, int64_t set0) {
-    h.ncols = (int)std::min<int64_t>(kCols, nsets - set0);
-    h.cols.assign(kCols, ColState{});
+    h.ncols = (int)std::min<int64_t>(KT, nsets - set0);
+    h.cols.assign(kMaxKT, ColState{});
     std::map<std::pair<int32_t, int32_t>, double> ent;
-    for (int c = 0; c < kCols; ++c) {
+    for (int c = 0; c < kMaxKT; ++c) {
       const double r1 = r1_max && c < h.ncols ? r1_max[order[set0 + c]] : (double)INFINITY;
       h.cols[c] = ColState{0, 0.0, c < h.ncols ? 0 : 1, 0, 0, 0, r1,
                            x0 && std::isfinite(r1) ? kBThetaWarm : kBTheta};
@@ -983,114 +1530,109 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       h.eval.push_back(make_float2(w.hi, w.lo));
     }
   };
-  // per-column records of every wave stay on the device until the end,
-  // unless host score staging needs a synchronisation per wave anyway
-  const int64_t nwaves = ceil_div<int64_t>(nsets, kCols);
+  // per-column records of every wave stay on the device until the end
+  const int64_t nwaves = ceil_div<int64_t>(nsets, KT);
   ColState *cols_all = nullptr;
-  GOPS_CUDA_TRY(dev_malloc_async((void **)&cols_all, sizeof(ColState) * (size_t)nwaves * kCols, st));
+  GOPS_CUDA_TRY(dev_malloc_async((void **)&cols_all, sizeof(ColState) * (size_t)nwaves * KT, st));
   struct FreeOnExit {
     void *p; cudaStream_t s;
     ~FreeOnExit() { free_async(p, s); }
   } cols_all_guard{cols_all, st};
+  // the largest entry count of any wave, so that the entry arrays (named by
+  // the captured chunks) are sized once per call
+  {
+    int64_t emax = 0;
+    for (int64_t set0 = 0; set0 < nsets; set0 += KT) {
+      int64_t e = 0;
+      for (int64_t q = set0; q < std::min<int64_t>(nsets, set0 + KT); ++q) e += seed_ptr[order[q] + 1] - seed_ptr[order[q]];
+      emax = std::max(emax, e);
+    }
+    GOPS_TRY(ensure_entries(b, emax, st));
+  }
+  const bool use_graphs = !ctx->timing;
+  if (use_graphs) {
+    GOPS_TRY(ensure_chunk_graph(ctx, g, 0));
+    GOPS_TRY(ensure_chunk_graph(ctx, g, 1));
+  }
+  StepParams p = step_params(g, b);
   prep(hw[0], 0);
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], st));
-  for (int64_t set0 = 0; set0 < nsets; set0 += kCols) {
-    HostWave &h = hw[(set0 / kCols) & 1];
+  for (int64_t set0 = 0; set0 < nsets; set0 += KT) {
+    HostWave &h = hw[(set0 / KT) & 1];
     const int ncols = h.ncols;
-    p.ncols = ncols;
-    for (int c = 0; c < kCols; ++c) {
+    // ---- per-wave constants (a small pageable copy: staged at the call)
+    WaveConst w{};
+    fill_wave_const(w.s, cfg, n, KT, ncols, x0 != nullptr, x0 ? 8.0 : 1.0);
+    for (int c = 0; c < kMaxKT; ++c) {
       const int64_t sid = c < ncols ? order[set0 + c] : 0;
-      p.xcol[c] = x0 && !x0_on_device ? c : sid;
-      p.ocol[c] = scores && !scores_on_device ? c : sid;
+      w.xcol[c] = x0 && !x0_on_device ? c : sid;
+      w.ocol[c] = scores && !scores_on_device ? c : sid;
     }
-    std::vector<ColState> &cols_h = h.cols;
-    std::vector<int32_t> &erow = h.erow, &eslot = h.eslot;
-    std::vector<float2> &eval = h.eval;
-    double wmax = 1.0;
-    const int64_t ne = (int64_t)erow.size();
-    GOPS_TRY(ensure_entries(b, ne, st));
+    const int64_t ne = (int64_t)h.erow.size();
     if (ne) {
-      GOPS_CUDA_TRY(cudaMemcpyAsync(b->prows_sorted, erow.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, st));
-      GOPS_CUDA_TRY(cudaMemcpyAsync(b->pslot, eslot.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, st));
-      GOPS_CUDA_TRY(cudaMemcpyAsync(b->pval, eval.data(), sizeof(float2) * ne, cudaMemcpyHostToDevice, st));
+      GOPS_CUDA_TRY(cudaMemcpyAsync(b->prows_sorted, h.erow.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, st));
+      GOPS_CUDA_TRY(cudaMemcpyAsync(b->pslot, h.eslot.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, st));
+      GOPS_CUDA_TRY(cudaMemcpyAsync(b->pval, h.eval.data(), sizeof(float2) * ne, cudaMemcpyHostToDevice, st));
       ctx->stats.h2d_bytes += (sizeof(int32_t) * 2 + sizeof(float2)) * ne;
     }
     prow_from_sorted<<<blocks_for(n + 1, 256, ctx->num_sms * 8), 256, 0, st>>>(b->prows_sorted, ne, n, b->prow);
     ++launches;
-    p.pslot = b->pslot;
-    p.pval = b->pval;
     // ---- warm start of the wave
-    p.x0 = nullptr;
+    const float *x0w = nullptr;
     if (x0) {
       if (x0_on_device) {
-        p.x0 = x0;
+        x0w = x0;
       } else {
         for (int c = 0; c < ncols; ++c)
           GOPS_CUDA_TRY(cudaMemcpyAsync(b->x0 + (size_t)c * n, x0 + order[set0 + c] * n, sizeof(float) * (size_t)n,
                                         cudaMemcpyHostToDevice, st));
         ctx->stats.h2d_bytes += sizeof(float) * (size_t)ncols * n;
-        p.x0 = b->x0;
+        x0w = b->x0;
       }
-      // fixed-point range: a warm start of L1 norm up to 8 keeps every partial
-      // sum far below 2^63; larger or non-finite starts are flagged by the
-      // nonfinite counter and the column does not converge
-      wmax = 8.0;
     }
-    int e = 0;
-    while (e < 20 && std::ldexp(1.0, e) < wmax) ++e;
-    const int F = 58 - 2 * e;
-    p.fx_scale = std::ldexp(1.0f, F);
-    p.fx_inv = std::ldexp(1.0, -F);
-    GOPS_CUDA_TRY(cudaMemcpyAsync(b->cols, cols_h.data(), sizeof(ColState) * kCols, cudaMemcpyHostToDevice, st));
+    GOPS_CUDA_TRY(cudaMemcpyAsync(b->wc, &w, sizeof(WaveConst), cudaMemcpyHostToDevice, st));
+    GOPS_CUDA_TRY(cudaMemcpyAsync(b->cols, h.cols.data(), sizeof(ColState) * kMaxKT, cudaMemcpyHostToDevice, st));
     GOPS_CUDA_TRY(cudaMemsetAsync(b->wave, 0, sizeof(WaveState), st));
-    GOPS_CUDA_TRY(cudaMemsetAsync(b->sums, 0, sizeof(long long) * 3 * kCols * 4, st));
-    GOPS_CUDA_TRY(cudaMemsetAsync(b->lcnt, 0, sizeof(unsigned) * std::max<int32_t>(b->n_big, 1), st));
-    p.k = 0;
-    p.gdf_in = b->gdf[1];
-    p.gf_in = b->gf[1];
-    p.gdf_out = b->gdf[0];
-    p.gf_out = b->gf[0];
-    if (kCols == 32 && p.x0)
-      batch_init_x0<<<blocks_for(ceil_div<int64_t>(n, kTile), kBWarps, ctx->num_sms * 8), kBThreads, 0, st>>>(
-          p, b->d_inv_perm);
+    GOPS_CUDA_TRY(cudaMemsetAsync(b->sums, 0, sizeof(long long) * 3 * kMaxKT * 4, st));
+    if (x0w)
+      batch_init_x0<<<blocks_for(ceil_div<int64_t>(n, kTile) * (KT / kTile), kBWarps, ctx->num_sms * 8), kBThreads, 0,
+                      st>>>(p, x0w, b->d_inv_perm);
     else
-      batch_init<<<grid_rows, kBThreads, 0, st>>>(p);
+      batch_init<<<blocks_for((n + 1) * KT, kBThreads, ctx->num_sms * 8), kBThreads, 0, st>>>(p);
     GOPS_CUDA_TRY(cudaGetLastError());
     ++launches;
-    // ---- steps: chunks of 4 launches; one chunk stays queued ahead of the
-    // host's poll of the wave record, so the GPU does not wait for the host
-    // between chunks (a step launched after the wave is done returns in its
-    // prologue)
+    // ---- steps: chunks of kChunkSteps launches; one chunk stays queued
+    // ahead of the host's poll of the wave record, so the GPU does not wait
+    // for the host between chunks (a step launched after the wave is done
+    // returns in its prologue)
     bool f32_known = false;
-    unsigned long long k = 1;
+    unsigned long long k = 1;  // next step to launch
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evs;
+    std::vector<std::pair<unsigned long long, bool>> evk;
     auto launch_chunk = [&]() -> Status {
-      for (int j = 0; j < 4 && k - 1 <= cfg->max_iterations; ++j, ++k) {
-        p.k = k;
-        p.gdf_in = b->gdf[(k - 1) & 1];
-        p.gf_in = b->gf[(k - 1) & 1];
-        p.gdf_out = b->gdf[k & 1];
-        p.gf_out = b->gf[k & 1];
-        if (!f32_known) {
-          spmm_kernel<BDF><<<grid_df, kBThreads, 0, st>>>(p);
-          ++launches;
-        }
-        if (k >= 2) {
-          cudaEvent_t e0 = nullptr, e1 = nullptr;
-          if (ctx->timing) {
+      if (use_graphs) {
+        GOPS_CUDA_TRY(cudaGraphLaunch(b->chunk_exec[f32_known ? 1 : 0], st));
+        launches += (f32_known ? 1 : 2) * kChunkSteps + 1;
+      } else {
+        for (int j = 0; j < kChunkSteps; ++j) {
+          for (int v = f32_known ? 1 : 0; v < 2; ++v) {
+            const bool isdf = v == 0;
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
             GOPS_CUDA_TRY(cudaEventCreate(&e0));
             GOPS_CUDA_TRY(cudaEventCreate(&e1));
             GOPS_CUDA_TRY(cudaEventRecord(e0, st));
-          }
-          spmm_kernel<BF32><<<grid_f, kBThreads, 0, st>>>(p);
-          if (ctx->timing) {
+            GOPS_TRY(launch_step_cpl(ctx, b, p, j, isdf, st));
             GOPS_CUDA_TRY(cudaEventRecord(e1, st));
             evs.push_back({e0, e1});
+            evk.push_back({k + j, isdf});
+            ++launches;
           }
-          ++launches;
         }
+        advance_kernel<<<1, 1, 0, st>>>(b->wave);
+        GOPS_CUDA_TRY(cudaGetLastError());
+        ++launches;
       }
-      GOPS_CUDA_TRY(cudaGetLastError());
+      k += kChunkSteps;
       return Status::ok();
     };
     auto poll_after = [&](int slot) -> Status {
@@ -1105,7 +1647,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       pending[npend++] = q;
     }
     GOPS_TRY(start_scatter());  // the previous wave's block, while this wave runs
-    if (set0 + kCols < nsets) prep(hw[((set0 / kCols) + 1) & 1], set0 + kCols);  // overlaps this wave
+    if (set0 + KT < nsets) prep(hw[((set0 / KT) + 1) & 1], set0 + KT);  // overlaps this wave
     bool finished = false;
     while (npend > 0) {
       const int slot = pending[0];
@@ -1115,14 +1657,17 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       const WaveState ws = b->hwave[slot];
       if (ws.done) {
         GOPS_CUDA_TRY(cudaStreamSynchronize(st));
-        // time the FP32-phase launches that did work (step >= f32_from and <= steps)
+        // time the launches that did work (their step <= steps, in their phase)
         for (size_t i = 0; i < evs.size(); ++i) {
-          const unsigned long long kk = i + 2;  // F32 launches start at step 2
-          if (ws.f32_from && kk >= ws.f32_from && kk <= ws.steps) {
+          const unsigned long long kk = evk[i].first;
+          const bool isdf = evk[i].second;
+          const bool did = kk <= ws.steps &&
+                           (isdf ? (ws.f32_from == 0 || kk < ws.f32_from) : (ws.f32_from && kk >= ws.f32_from));
+          if (did) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, evs[i].first, evs[i].second);
-            spmm_ms += ms;
-            ++spmm_launches;
+            if (isdf) { df_ms += ms; ++df_launches; }
+            else { spmm_ms += ms; ++spmm_launches; }
           }
         }
         for (auto &pr : evs) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
@@ -1138,21 +1683,18 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     }
     if (!finished) return Status{GOPS_ERR_INTERNAL, "wave did not finish"};
     // ---- results of the wave
-    p.out = scores_on_device ? scores : b->out;
     if (scores) {
+      float *outw = scores_on_device ? scores : b->out;
       // the previous wave's pinned copy (on the copy stream) has read b->out
       if (staged && pend_copy_q >= 0) GOPS_CUDA_TRY(cudaStreamWaitEvent(st, b->sev[pend_copy_q], 0));
-      if (kCols == 32)
-        batch_finalize_t<<<blocks_for(ceil_div<int64_t>(n, kTile), kBWarps, ctx->num_sms * 8), kBThreads, 0, st>>>(
-            p, b->d_inv_perm);
-      else
-        batch_finalize<<<grid_rows, kBThreads, 0, st>>>(p);
+      batch_finalize_t<<<blocks_for(ceil_div<int64_t>(n, kTile) * (KT / kTile), kBWarps, ctx->num_sms * 8), kBThreads,
+                         0, st>>>(p, outw, b->d_inv_perm);
       GOPS_CUDA_TRY(cudaGetLastError());
       ++launches;
       if (staged) {
         // the copy to the pinned buffer runs on the copy stream, overlapping
         // the next wave's steps
-        const int q = (int)((set0 / kCols) & 1);
+        const int q = (int)((set0 / KT) & 1);
         scatter.join(q);  // the scatter of two waves ago read this buffer
         GOPS_CUDA_TRY(cudaEventRecord(ctx->copy_ev[0], st));
         GOPS_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[0], 0));
@@ -1171,17 +1713,17 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
         ctx->stats.d2h_bytes += sizeof(float) * (size_t)ncols * n;
       }
     }
-    GOPS_CUDA_TRY(cudaMemcpyAsync(cols_all + (set0 / kCols) * kCols, b->cols, sizeof(ColState) * kCols,
+    GOPS_CUDA_TRY(cudaMemcpyAsync(cols_all + (set0 / KT) * KT, b->cols, sizeof(ColState) * KT,
                                   cudaMemcpyDeviceToDevice, st));
   }
   GOPS_TRY(start_scatter());  // the last wave's block
-  std::vector<ColState> cols_res((size_t)nwaves * kCols);
+  std::vector<ColState> cols_res((size_t)nwaves * KT);
   GOPS_CUDA_TRY(cudaMemcpyAsync(cols_res.data(), cols_all, sizeof(ColState) * cols_res.size(), cudaMemcpyDeviceToHost,
                                 st));
   GOPS_CUDA_TRY(cudaStreamSynchronize(st));
-  for (int64_t set0 = 0; set0 < nsets; set0 += kCols) {
-    const int ncols = (int)std::min<int64_t>(kCols, nsets - set0);
-    const ColState *cr = cols_res.data() + (set0 / kCols) * kCols;
+  for (int64_t set0 = 0; set0 < nsets; set0 += KT) {
+    const int ncols = (int)std::min<int64_t>(KT, nsets - set0);
+    const ColState *cr = cols_res.data() + (set0 / KT) * KT;
     for (int c = 0; c < ncols; ++c) {
       col_iters += cr[c].iterations;
       if (runs) runs[order[set0 + c]] = gops_run{cr[c].iterations, cr[c].diff_l1, cr[c].converged, 0};
@@ -1199,6 +1741,8 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   ctx->stats.iterations = col_iters;
   ctx->stats.f32_ms = spmm_ms;
   ctx->stats.f32_launches = spmm_launches;
+  ctx->stats.df_ms = df_ms;
+  ctx->stats.df_launches = df_launches;
   return Status::ok();
 }
 

@@ -156,7 +156,9 @@ int gops_personalized_pagerank_run(gops_ctx *ctx, const gops_graph *g, const gop
                                    const double *personalization, double *scores, gops_run *run);
 
 /* Batched personalized PageRank: nsets independent personalized_pagerank_run
- * calls (src/ppr.rs:90-156) in one pass per wave of 32 sets.  Set s is
+ * calls (src/ppr.rs:90-156) in one pass per wave of 32, 64 or 128 sets (the
+ * k-tile, chosen per graph by an autotuner on the first call; see
+ * gops_ppr_batch_set_tile).  Set s is
  * seed_idx[seed_ptr[s] .. seed_ptr[s+1]) (node ids; a repeated node counts
  * twice); its personalization vector is 1 on each seed, normalised as
  * src/ppr.rs:104-109 does, and an empty set means the uniform vector.  Each
@@ -175,6 +177,20 @@ int gops_ppr_batch(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, i
 int gops_ppr_batch_device(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,
                           const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0_device,
                           float *scores_device, gops_run *runs);
+
+/* The batched path's tile of a graph: cols = sets per wave (32, 64 or 128)
+ * and chunk = the in-degree above which a row is split into chunks of that
+ * many edges (a multiple of 256).  cols == 0 re-runs the autotuner, which
+ * times a few steps of each candidate (k-tile x chunk 256 / 1024, within 40 %
+ * of the free device memory) and keeps the fastest per set-step.  The tile
+ * changes the time only: every choice gives bit-identical results (a row's
+ * sum is fixed as in-order sums of 256-edge blocks added in order).  No
+ * reference counterpart (the reference solves one set per call). */
+int gops_ppr_batch_set_tile(gops_ctx *ctx, const gops_graph *g, int32_t cols, int32_t chunk);
+/* The tile in use (0, 0 before the first batched call), and with cost != NULL
+ * the autotuner's measured cost per set-step in ms for (cols 32, 64, 128) x
+ * (chunk 256, 1024), 6 floats, 0 where not tried. */
+int gops_ppr_batch_tile(const gops_graph *g, int32_t *cols, int32_t *chunk, float *cost);
 
 /* Device pointer (double, n entries) of the last solve's scores, valid until
  * the next solve on this context or the destruction of the graph that solve

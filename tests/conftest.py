@@ -42,17 +42,27 @@ def case_csr(c):
     return rp, col, w
 
 
-def top_order_matches(a, b, k=100):
+def top_order_matches(a, b, k=100, tie=0.0):
     """True when the k largest entries of a come in the order of b's k
     largest, ties in b within 1e-15 relative counting as equal (the
-    reference's top_k sorts by score with an unstable sort, src/topk.rs:40)."""
+    reference's top_k sorts by score with an unstable sort, src/topk.rs:40).
+    `tie` (absolute) widens the ties for results that cannot order entries
+    more finely than their own error: the FP32 score blocks of the batched
+    path pass tie = 2 max|a - b|, so two entries may swap only when their
+    reference scores differ by less than the result's largest error."""
     import numpy as np
     ia = np.argsort(-a, kind="stable")[:k]
     ib = np.argsort(-b, kind="stable")[:k]
     for x, y in zip(ia, ib):
-        if x != y and abs(b[x] - b[y]) > 1e-15 * max(abs(b[x]), 1e-300):
+        if x != y and abs(b[x] - b[y]) > max(1e-15 * max(abs(b[x]), 1e-300), tie):
             return False
     return True
+
+
+def fp32_tie(a, b):
+    """The tie width of top_order_matches for an FP32 result a against b."""
+    import numpy as np
+    return 2.0 * float(np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64)).max())
 
 
 def sample_sets(sp, si, idx):

@@ -132,3 +132,46 @@ def test_device_pointers_variant():
                                             _native.ptr(np.ascontiguousarray(si)), None,
                                             ctypes.c_void_p(out.data_ptr()), ctypes.cast(runs, ctypes.c_void_p)))
     assert np.array_equal(out.cpu().numpy(), host.scores)
+
+
+def test_every_tile_gives_the_same_bits():
+    """The autotuner may pick any k-tile (32, 64 or 128 sets per wave) and
+    chunk size of long rows (256 or 1024 edges).  A row's sum is fixed as
+    in-order sums of 256-edge blocks added in order, so every choice gives
+    bit-identical scores and step counts, cold and from caller start
+    vectors, and every choice matches the oracle set by set."""
+    g = gen.rmat(14, 16, seed=12)  # hub rows of several thousand in-edges
+    assert np.diff(g.row_ptr).max() > 1024
+    sp, si = gen.seed_sets(g, 150, 1, 48, seed=13)  # 2 waves of 128, 5 of 32
+    sets = [list(si[sp[q]:sp[q + 1]]) if q % 37 else [] for q in range(150)]  # some empty (uniform)
+    sp, si = go.seed_sets_to_csr(sets)
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    conf = go.PageRankConfig(0.85, 1000, 1e-7)
+    rng = np.random.default_rng(3)
+    x0 = rng.random((150, g.n)).astype(np.float32)
+    x0 /= x0.sum(axis=1, keepdims=True)
+    ref, its = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-7, threads=8)
+    first = None
+    for cols in (32, 64, 128):
+        for chunk in (256, 1024):
+            dg.set_batch_tile(cols, chunk)
+            assert dg.batch_tile()[:2] == (cols, chunk)
+            r = go.ppr_batch(dg, conf, sp, si)
+            w = go.ppr_batch(dg, conf, sp, si, x0=x0)
+            assert r.converged.all() and w.converged.all()
+            if first is None:
+                first = (r, w)
+                l1 = np.abs(r.scores.astype(np.float64) - ref).sum(axis=1)
+                assert l1.max() <= L1_TARGET, l1.max()
+                assert np.array_equal(r.iterations, its.astype(np.int64))
+            else:
+                assert np.array_equal(r.scores, first[0].scores), (cols, chunk)
+                assert np.array_equal(r.iterations, first[0].iterations), (cols, chunk)
+                assert np.array_equal(w.scores, first[1].scores), (cols, chunk)
+                assert np.array_equal(w.iterations, first[1].iterations), (cols, chunk)
+    dg.set_batch_tile(0)  # autotune: one of the candidates, each tried one timed
+    cols, chunk, cost = dg.batch_tile()
+    assert cols in (32, 64, 128) and chunk in (256, 1024)
+    assert (cost[0] > 0).all() and cost[{32: 0, 64: 1, 128: 2}[cols], {256: 0, 1024: 1}[chunk]] == cost[cost > 0].min()
+    r = go.ppr_batch(dg, conf, sp, si)
+    assert np.array_equal(r.scores, first[0].scores)

@@ -349,79 +349,37 @@ __device__ __forceinline__ FV<CPL> f32_block(const StepParams &p, int in, int kt
 
 // ---------------------------------------------------------------------------
 // The mixed step (some active column still in its double-float phase).
-// A lane with a column in the double-float phase gathers its 8-byte (hi, lo)
-// entries of the double-float block and keeps, per column, both the
-// double-float sum and the FP32 sum of the hi words; a lane whose columns are
-// all in the FP32 phase gathers the FP32 block like the FP32 step.  A column
-// in its FP32 phase thus computes exactly what the FP32 step would, whatever
-// its neighbours in the wave do, so every column's result depends on its own
-// history alone (not on the sets it shares a wave with, nor on the k-tile).
+// Every lane gathers its 8-byte (hi, lo) entries of the double-float block.
+// A column in its double-float phase adds them in double-float arithmetic; a
+// column already in its FP32 phase adds only the hi words in FP32 (its sum
+// kept in the hi word), which is exactly what the FP32 step computes from the
+// FP32 block (the double-float step writes hi there).  So every column's
+// result depends on its own history alone: not on the sets that share its
+// wave, nor on the k-tile.
 // ---------------------------------------------------------------------------
 template <int CPL>
-struct MixSum {
-  DV<CPL> d;  // double-float sums (lanes in the double-float phase)
-  FV<CPL> f;  // FP32 sums of the hi words (or of the FP32 block)
-};
-
-template <int CPL>
-__device__ __forceinline__ MixSum<CPL> mix_zero() {
-  MixSum<CPL> r;
+__device__ __forceinline__ DV<CPL> dv_zero() {
+  DV<CPL> r;
 #pragma unroll
-  for (int q = 0; q < CPL; ++q) r.d.v[q] = {0.0f, 0.0f};
-  r.f = f32_zero<CPL>();
+  for (int q = 0; q < CPL; ++q) r.v[q] = {0.0f, 0.0f};
   return r;
 }
 
-// A lane's entry of row u: the double-float lanes read 8 * CPL bytes of the
-// double-float block (interleaved hi, lo per column), the others 4 * CPL
-// bytes of the FP32 block; one load covers the first 4 * CPL bytes of either.
+// s += g column by column: FP32 on the hi words where bit q of fmask is set
 template <int CPL>
-struct Raw {
-  float a[2 * CPL];
-};
-
-template <int CPL>
-__device__ __forceinline__ Raw<CPL> mix_load(const float *base_df, const float *base_f, int64_t off_df, int64_t off_f,
-                                             bool ldf) {
-  Raw<CPL> r;
-  const float *a = ldf ? base_df + off_df : base_f + off_f;
-  const FV<CPL> x = ld_fv<CPL>(a);
+__device__ __forceinline__ void mix_add(DV<CPL> &s, const DV<CPL> &g, unsigned fmask) {
 #pragma unroll
-  for (int q = 0; q < CPL; ++q) r.a[q] = x.v[q];
-  if (ldf) {
-    const FV<CPL> y = ld_fv<CPL>(a + CPL);
-#pragma unroll
-    for (int q = 0; q < CPL; ++q) r.a[CPL + q] = y.v[q];
-  } else {
-#pragma unroll
-    for (int q = 0; q < CPL; ++q) r.a[CPL + q] = 0.0f;
-  }
-  return r;
+  for (int q = 0; q < CPL; ++q)
+    s.v[q] = ((fmask >> q) & 1u) ? df{s.v[q].hi + g.v[q].hi, 0.0f} : df_add(s.v[q], g.v[q]);
 }
 
 template <int CPL>
-__device__ __forceinline__ void mix_add(MixSum<CPL> &s, const Raw<CPL> &r, bool ldf) {
-  if (ldf) {
-#pragma unroll
-    for (int q = 0; q < CPL; ++q) {
-      const df g = {r.a[2 * q], r.a[2 * q + 1]};
-      s.d.v[q] = df_add(s.d.v[q], g);
-      s.f.v[q] += g.hi;
-    }
-  } else {
-#pragma unroll
-    for (int q = 0; q < CPL; ++q) s.f.v[q] += r.a[q];
-  }
-}
-
-template <int CPL>
-__device__ __forceinline__ MixSum<CPL> mix_block(const StepParams &p, int in, int kt, int eb, int ee, int lane,
-                                                 bool ldf) {
+__device__ __forceinline__ DV<CPL> mix_block(const StepParams &p, int in, int kt, int eb, int ee, int lane,
+                                             unsigned fmask) {
   constexpr int U = CPL == 4 ? 4 : 8;
-  const float *bdf = reinterpret_cast<const float *>(p.gdf[in]) + 2 * lane * CPL;
-  const float *bf = p.gf[in] + lane * CPL;
-  MixSum<CPL> s = mix_zero<CPL>();
-  for (int e = eb; e < ee; e += U) {  // ee - eb is a multiple of 4 and of U when U == 4
+  const float2 *gb = p.gdf[in] + lane * CPL;
+  DV<CPL> s = dv_zero<CPL>();
+  for (int e = eb; e < ee; e += U) {  // ee - eb is a multiple of 4
     int32_t u[U];
     const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
     u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
@@ -431,13 +389,13 @@ __device__ __forceinline__ MixSum<CPL> mix_block(const StepParams &p, int in, in
       const int4 b = ok2 ? __ldg(reinterpret_cast<const int4 *>(p.col + e + 4)) : make_int4(0, 0, 0, 0);
       u[4] = b.x; u[5] = b.y; u[6] = b.z; u[7] = b.w;
     }
-    Raw<CPL> g[U];
+    DV<CPL> g[U];
 #pragma unroll
     for (int q = 0; q < U; ++q)
-      if (q < 4 || ok2) g[q] = mix_load<CPL>(bdf, bf, (int64_t)u[q] * 2 * kt, (int64_t)u[q] * kt, ldf);
+      if (q < 4 || ok2) g[q] = ld_dv<CPL>(gb + (int64_t)u[q] * kt, true);
 #pragma unroll
     for (int q = 0; q < U; ++q)
-      if (q < 4 || ok2) mix_add<CPL>(s, g[q], ldf);
+      if (q < 4 || ok2) mix_add<CPL>(s, g[q], fmask);
   }
   return s;
 }
@@ -448,8 +406,8 @@ struct Lane {
   bool f32[kMaxCPL];  // in its FP32 phase
   bool uni[kMaxCPL];
   df dsum[kMaxCPL];
-  bool any;  // some column active
-  bool ldf;  // some active column in its double-float phase
+  bool any;        // some column active
+  unsigned fmask;  // bit q: column q active and in its FP32 phase
 };
 
 template <int CPL>
@@ -474,7 +432,7 @@ struct BIn {
 
 template <int CPL>
 __device__ __forceinline__ BIn<CPL> b_in(const StepParams &p, const WaveScalars &wc, int64_t v, int lane,
-                                         const Lane &ln, bool want_acc) {
+                                         const Lane &ln, bool want_acc, bool want_tail) {
   BIn<CPL> in;
 #pragma unroll
   for (int q = 0; q < CPL; ++q) in.red[q] = ln.uni[q] ? wc.inv_n : df{0.0f, 0.0f};
@@ -490,7 +448,7 @@ __device__ __forceinline__ BIn<CPL> b_in(const StepParams &p, const WaveScalars 
   }
   in.deg = __ldg(&p.deg[v]);
   const int64_t i = v * wc.kt + lane * CPL;
-  in.tail = ld_fv<CPL>(p.tail + i);
+  if (want_tail) in.tail = ld_fv<CPL>(p.tail + i);
   if (want_acc) in.acc = ld_dv<CPL>(p.acc + i, false);
   return in;
 }
@@ -516,16 +474,14 @@ __device__ __forceinline__ void f32_epilogue(const StepParams &p, const WaveScal
 }
 
 // Mixed step epilogue: a column in its double-float phase takes the
-// double-float step on s.d (x in acc), one in its FP32 phase the FP32 step on
-// s.f (x in tail), exactly as f32_epilogue computes it.
+// double-float step on its double-float sum (x in acc), one in its FP32
+// phase the FP32 step on the hi word of its sum (x in tail), exactly as
+// f32_epilogue computes it.  The tail is read and written only by lanes with
+// such a column.
 template <int CPL>
-__device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScalars &wc, int64_t v,
-                                             const MixSum<CPL> &s, const BIn<CPL> &in, const Lane &ln, int out,
-                                             unsigned long long k, LaneAcc<CPL> &a, int lane) {
-  if (!ln.ldf) {
-    f32_epilogue<CPL>(p, wc, v, s.f, in, ln, out, a, lane);
-    return;
-  }
+__device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScalars &wc, int64_t v, const DV<CPL> &s,
+                                             const BIn<CPL> &in, const Lane &ln, int out, unsigned long long k,
+                                             LaneAcc<CPL> &a, int lane) {
   const int64_t i = v * wc.kt + lane * CPL;
   const float dg = in.deg;
   DV<CPL> an, g;
@@ -534,9 +490,9 @@ __device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScal
   for (int q = 0; q < CPL; ++q) {
     const df red = in.red[q];
     an.v[q] = in.acc.v[q];
-    tn.v[q] = in.tail.v[q];
+    tn.v[q] = ln.fmask ? in.tail.v[q] : 0.0f;
     if (ln.act[q] && ln.f32[q]) {
-      const float r = f32_step(s.f.v[q], ln.dsum[q].hi, red.hi, wc.d.hi);
+      const float r = f32_step(s.v[q].hi, ln.dsum[q].hi, red.hi, wc.d.hi);
       tn.v[q] = in.tail.v[q] + r;
       a.l1[q] += fx_of(fabsf(r), wc.fx_scale);
       a.bad |= (!isfinite(r)) << q;
@@ -545,7 +501,7 @@ __device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScal
       g.v[q] = {gh.v[q], 0.0f};
     } else if (ln.act[q]) {
       const df ao = in.acc.v[q];
-      df r = df_mul(wc.d, df_add(s.d.v[q], df_mul(ln.dsum[q], red)));
+      df r = df_mul(wc.d, df_add(s.v[q], df_mul(ln.dsum[q], red)));
       if (k == 1) r = df_add(df_add(df_mul(wc.omd, red), r), df_neg(ao));  // F(x_0) - x_0
       an.v[q] = df_add(ao, r);
       const df ar = r.hi < 0.0f ? df_neg(r) : r;
@@ -560,7 +516,7 @@ __device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScal
     }
   }
   st_dv<CPL>(p.acc + i, an);
-  st_fv<CPL>(p.tail + i, tn);
+  if (ln.fmask) st_fv<CPL>(p.tail + i, tn);
   st_dv<CPL>(p.gdf[out] + i, g);
   st_fv<CPL>(p.gf[out] + i, gh);
 }
@@ -575,6 +531,7 @@ __device__ bool batch_prologue(const StepParams &p, const WaveScalars &wc, unsig
   if (*(volatile int *)&p.wave->done) return false;
   const int prev = (int)((k - 1) % 3);
   bool lane_act = false, lane_df = false;
+  unsigned fmask = 0;
 #pragma unroll
   for (int q = 0; q < CPL; ++q) {
     const int c = lane * CPL + q;
@@ -609,9 +566,10 @@ __device__ bool batch_prologue(const StepParams &p, const WaveScalars &wc, unsig
     ln->uni[q] = col_ok && p.cols[c].uniform;
     lane_act |= act;
     lane_df |= act && !f32;
+    fmask |= (act && f32 ? 1u : 0u) << q;
   }
   ln->any = lane_act;
-  ln->ldf = lane_df;
+  ln->fmask = fmask;
   if (!__any_sync(0xffffffffu, lane_act)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) p.wave->done = 1;
     return false;
@@ -722,7 +680,7 @@ __global__ void __launch_bounds__(kBThreads) spmm_f32(StepParams p) {
           st_dv<CPL>(p.lpart + (int64_t)(b0 + (b - rb) / kBase) * kt + lane * CPL, pk);
         }
       if (chunk_arrive(p, h, nch, lane) && ln.any) {
-        const BIn<CPL> bi = b_in<CPL>(p, wc, h, lane, ln, false);
+        const BIn<CPL> bi = b_in<CPL>(p, wc, h, lane, ln, false, true);
         FV<CPL> all = f32_zero<CPL>();
         for (int q = 0; q < nb; ++q) {
           const DV<CPL> d = ld_dv<CPL>(p.lpart + (int64_t)(b0 + q) * kt + lane * CPL, false);
@@ -733,7 +691,7 @@ __global__ void __launch_bounds__(kBThreads) spmm_f32(StepParams p) {
       }
     } else if (ln.any) {
       const int64_t v = p.n_big + (w - p.n_big_tasks);
-      const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, false);
+      const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, false, true);
       const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
       // canonical row sum: base blocks from eb, added in order
       FV<CPL> tot = f32_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane);
@@ -763,40 +721,23 @@ __global__ void __launch_bounds__(kBThreads, 2) spmm_mixed(StepParams p) {
       int h, first, nch, b0, nb, cs, ce, rb;
       chunk_row(p, (int)w, &h, &first, &nch, &b0, &nb, &cs, &ce, &rb);
       if (ln.any)
-        for (int b = cs; b < ce; b += kBase) {
-          const MixSum<CPL> s = mix_block<CPL>(p, in, kt, b, min(ce, b + kBase), lane, ln.ldf);
-          // per column: the double-float sum, or the FP32 sum as (s, 0)
-          DV<CPL> pk;
-#pragma unroll
-          for (int q = 0; q < CPL; ++q) pk.v[q] = (ln.ldf && !ln.f32[q]) ? s.d.v[q] : df{s.f.v[q], 0.0f};
-          st_dv<CPL>(p.lpart + (int64_t)(b0 + (b - rb) / kBase) * kt + lane * CPL, pk);
-        }
+        for (int b = cs; b < ce; b += kBase)
+          st_dv<CPL>(p.lpart + (int64_t)(b0 + (b - rb) / kBase) * kt + lane * CPL,
+                     mix_block<CPL>(p, in, kt, b, min(ce, b + kBase), lane, ln.fmask));
       if (chunk_arrive(p, h, nch, lane) && ln.any) {
-        const BIn<CPL> bi = b_in<CPL>(p, wc, h, lane, ln, ln.ldf);
-        MixSum<CPL> all = mix_zero<CPL>();
-        for (int q = 0; q < nb; ++q) {
-          const DV<CPL> d = ld_dv<CPL>(p.lpart + (int64_t)(b0 + q) * kt + lane * CPL, false);
-#pragma unroll
-          for (int j = 0; j < CPL; ++j) {
-            all.d.v[j] = q == 0 ? d.v[j] : df_add(all.d.v[j], d.v[j]);
-            all.f.v[j] = q == 0 ? d.v[j].hi : all.f.v[j] + d.v[j].hi;
-          }
-        }
+        const BIn<CPL> bi = b_in<CPL>(p, wc, h, lane, ln, true, ln.fmask != 0);
+        DV<CPL> all = ld_dv<CPL>(p.lpart + (int64_t)b0 * kt + lane * CPL, false);
+        for (int q = 1; q < nb; ++q) mix_add<CPL>(all, ld_dv<CPL>(p.lpart + (int64_t)(b0 + q) * kt + lane * CPL, false),
+                                                  ln.fmask);
         mix_epilogue<CPL>(p, wc, h, all, bi, ln, out, k, a, lane);
       }
     } else if (ln.any) {
       const int64_t v = p.n_big + (w - p.n_big_tasks);
-      const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, ln.ldf);
+      const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, true, ln.fmask != 0);
       const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
-      MixSum<CPL> tot = mix_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane, ln.ldf);
-      for (int b = eb + kBase; b < ee; b += kBase) {
-        const MixSum<CPL> s = mix_block<CPL>(p, in, kt, b, min(ee, b + kBase), lane, ln.ldf);
-#pragma unroll
-        for (int j = 0; j < CPL; ++j) {
-          tot.d.v[j] = df_add(tot.d.v[j], s.d.v[j]);
-          tot.f.v[j] += s.f.v[j];
-        }
-      }
+      DV<CPL> tot = mix_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane, ln.fmask);
+      for (int b = eb + kBase; b < ee; b += kBase)
+        mix_add<CPL>(tot, mix_block<CPL>(p, in, kt, b, min(ee, b + kBase), lane, ln.fmask), ln.fmask);
       mix_epilogue<CPL>(p, wc, v, tot, bi, ln, out, k, a, lane);
     }
   }

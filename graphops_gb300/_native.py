@@ -75,6 +75,7 @@ SIGNATURES = [
     ("gops_personalization_validate", ctypes.c_int, [_i64, _i64, _p, ctypes.c_char_p, ctypes.c_size_t]),
     ("gops_graph_upload", ctypes.c_int, [_p, _i64, _p, _p, _p, ctypes.POINTER(_p)]),
     ("gops_graph_from_dense", ctypes.c_int, [_p, _i64, _p, ctypes.POINTER(_p)]),
+    ("gops_graph_from_edges", ctypes.c_int, [_p, _i64, _i64, _p, _p, _p, ctypes.POINTER(_p)]),
     ("gops_graph_destroy", None, [_p]),
     ("gops_graph_info", ctypes.c_int, [_p, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i32)]),
     ("gops_pagerank_run", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, ctypes.POINTER(Run)]),
@@ -224,6 +225,26 @@ class DeviceGraph:
             raise ValueError("adjacency matrix must be square")
         h = _p()
         ctx.check(ctx._l.gops_graph_from_dense(ctx.handle, n, ptr(M), ctypes.byref(h)))
+        nn, mm, ww = _i64(), _i64(), _i32()
+        ctx._l.gops_graph_info(h, ctypes.byref(nn), ctypes.byref(mm), ctypes.byref(ww))
+        return cls(ctx, h, nn.value, mm.value, bool(ww.value))
+
+    @classmethod
+    def from_edges(cls, n, src, dst, weights=None, ctx: Context | None = None):
+        """A petgraph-style raw edge list (edge e: src[e] -> dst[e], in edge
+        order) built on the device into the adapter's out-adjacency: rows
+        newest edge first, each parallel u->v entry weighted like the newest."""
+        ctx = ctx or default_context()
+        s = np.ascontiguousarray(src, dtype=np.int32)
+        d = np.ascontiguousarray(dst, dtype=np.int32)
+        if s.shape != d.shape:
+            raise ValueError("src and dst must have the same length")
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        if w is not None and w.shape != s.shape:
+            raise ValueError("weights must have one entry per edge")
+        h = _p()
+        ctx.check(ctx._l.gops_graph_from_edges(ctx.handle, int(n), int(s.shape[0]), ptr(s), ptr(d), ptr(w),
+                                               ctypes.byref(h)))
         nn, mm, ww = _i64(), _i64(), _i32()
         ctx._l.gops_graph_info(h, ctypes.byref(nn), ctypes.byref(mm), ctypes.byref(ww))
         return cls(ctx, h, nn.value, mm.value, bool(ww.value))

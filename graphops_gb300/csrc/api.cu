@@ -14,6 +14,8 @@ Status solve(Ctx *ctx, Graph *g, const gops_config *cfg, int mode, const double 
              double *scores_host, gops_run *run);
 Status dense_to_out_csr_device(Ctx *ctx, int64_t n, const double *d_M, int64_t **d_rp,
                                int32_t **d_col, double **d_w, int64_t *m_out);
+Status edges_to_out_csr_device(Ctx *ctx, int64_t n, int64_t m, const int32_t *d_src, const int32_t *d_dst,
+                               const double *d_w, int64_t **d_rp, int32_t **d_col, double **d_wout);
 Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, const int64_t *seed_ptr,
                  const int32_t *seed_idx, const float *x0, bool x0_on_device, float *scores,
                  bool scores_on_device, gops_run *runs, const double *r1_max, int32_t *rejected);
@@ -346,6 +348,68 @@ int gops_graph_from_dense(gops_ctx *ctx, int64_t n, const double *matrix, gops_g
     free_async(d_col, s);
   }
   free_async(d_w, s);
+  cudaStreamSynchronize(s);
+  if (st.code != GOPS_OK) {
+    graph_free_device(g->impl);
+    delete g;
+    return c.set(st);
+  }
+  *out = g;
+  return GOPS_OK;
+}
+
+int gops_graph_from_edges(gops_ctx *ctx, int64_t n, int64_t m, const int32_t *src, const int32_t *dst,
+                          const double *weights, gops_graph **out) {
+  if (!ctx || !out) return GOPS_ERR_INVALID;
+  *out = nullptr;
+  Ctx &c = ctx->impl;
+  cudaSetDevice(c.device);
+  c.stats = gops_stats{};
+  if (n < 0 || n >= INT32_MAX) return c.set(Status{GOPS_ERR_INVALID, "node count out of range"});
+  if (m < 0 || m >= INT32_MAX) return c.set(Status{GOPS_ERR_INVALID, "edge count out of range"});
+  if (m > 0 && (!src || !dst)) return c.set(Status{GOPS_ERR_INVALID, "edge list is NULL"});
+  if (m > 0 && n == 0) return c.set(Status{GOPS_ERR_INVALID, "edge endpoint out of range"});
+  gops_graph *g = new (std::nothrow) gops_graph();
+  if (!g) return c.set(Status{GOPS_ERR_OOM, "host allocation failed"});
+  g->impl.ctx = &c;
+  g->impl.device = c.device;
+  cudaStream_t s = c.stream;
+  int32_t *d_src = nullptr, *d_dst = nullptr;
+  double *d_w = nullptr, *d_wout = nullptr;
+  int64_t *d_rp = nullptr;
+  int32_t *d_col = nullptr;
+  const size_t mm = (size_t)std::max<int64_t>(m, 1);
+  cudaError_t e = dev_malloc_async((void **)&d_src, sizeof(int32_t) * mm, s);
+  if (e == cudaSuccess) e = dev_malloc_async((void **)&d_dst, sizeof(int32_t) * mm, s);
+  if (e == cudaSuccess && weights) e = dev_malloc_async((void **)&d_w, sizeof(double) * mm, s);
+  if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(d_src, src, sizeof(int32_t) * m, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(d_dst, dst, sizeof(int32_t) * m, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && weights && m > 0)
+    e = cudaMemcpyAsync(d_w, weights, sizeof(double) * m, cudaMemcpyHostToDevice, s);
+  Status st;
+  if (e != cudaSuccess)
+    st = Status{e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA,
+                std::string("edge list upload: ") + cudaGetErrorString(e)};
+  if (st.code == GOPS_OK) {
+    c.stats.h2d_bytes += (2 * sizeof(int32_t) + (weights ? sizeof(double) : 0)) * (size_t)m;
+    st = edges_to_out_csr_device(&c, n, m, d_src, d_dst, d_w, &d_rp, &d_col, &d_wout);
+  }
+  if (st.code == GOPS_OK) {
+    g->impl.n = n;
+    g->impl.m = m;
+    st = graph_build_from_out_csr_device(&c, &g->impl, d_rp, d_col, d_wout);
+  }
+  free_async(d_src, s);
+  free_async(d_dst, s);
+  free_async(d_w, s);
+  if (st.code == GOPS_OK) {
+    g->impl.out_rp = d_rp;
+    g->impl.out_col = d_col;
+  } else {
+    free_async(d_rp, s);
+    free_async(d_col, s);
+  }
+  free_async(d_wout, s);
   cudaStreamSynchronize(s);
   if (st.code != GOPS_OK) {
     graph_free_device(g->impl);

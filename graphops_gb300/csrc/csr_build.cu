@@ -278,6 +278,64 @@ __global__ void dense_rows(int64_t n, const double *__restrict__ M, int64_t *cou
   if (!rp && lane == 0) counts[u] = cnt;
 }
 
+// ---- edge-list ingestion (a petgraph Graph's raw edges, in edge order) ----
+
+// keys[i] = src[m - 1 - i] (the edge list reversed), with the range checks
+__global__ void reversed_sources(const int32_t *src, const int32_t *dst, int64_t m, int64_t n, uint32_t *keys,
+                                 int *bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = m - 1 - i;
+    const int32_t a = src[e], b = dst[e];
+    if (a < 0 || a >= n || b < 0 || b >= n) *bad = 1;
+    keys[i] = (uint32_t)min(max(a, 0), (int32_t)(n - 1));
+  }
+}
+
+// out-CSR entry k: the edge at position vals[k] of the reversed list
+__global__ void edges_gather(const uint32_t *vals, const int32_t *dst, const double *w, int64_t m, int32_t *col,
+                             double *wraw, uint32_t *colkey) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = m - 1 - (int64_t)vals[k];
+    col[k] = dst[e];
+    colkey[k] = (uint32_t)dst[e];
+    if (w) wraw[k] = w[e];
+  }
+}
+
+// keys2[i] = source row of out-CSR entry pos[i]
+__global__ void row_of_positions(const uint32_t *rows, const uint32_t *pos, int64_t m, uint32_t *keys2) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    keys2[i] = rows[pos[i]];
+}
+
+// Entries ordered by (row, target), ties in row order: start[i] = 1 where a
+// (row, target) run begins.
+__global__ void run_starts(const uint32_t *rows, const uint32_t *pos, const int32_t *col, int64_t m, int64_t *start) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t p = pos[i];
+    bool st = i == 0;
+    if (!st) {
+      const uint32_t q = pos[i - 1];
+      st = rows[p] != rows[q] || col[p] != col[q];
+    }
+    start[i] = st ? 1 : 0;
+  }
+}
+
+// find_edge's weight: every entry of a run gets the weight of the run's
+// first entry in row order (petgraph's walk meets the newest edge first)
+__global__ void run_weights(const int64_t *run_excl, const int64_t *start, const uint32_t *pos, const double *wraw,
+                            int64_t m, double *first_w, double *wout, int pass) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t run = run_excl[i] + start[i] - 1;
+    if (pass == 0) {
+      if (start[i]) first_w[run] = wraw[pos[i]];
+    } else {
+      wout[pos[i]] = first_w[run];
+    }
+  }
+}
+
 int grid_for(int64_t work, int threads) {
   int64_t b = ceil_div<int64_t>(work, threads);
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, 1 << 20));
@@ -530,6 +588,125 @@ Status dense_to_out_csr_device(Ctx *ctx, int64_t n, const double *d_M, int64_t *
     GOPS_CUDA_TRY(cudaGetLastError());
   }
   return Status::ok();
+}
+
+// A petgraph Graph<_, f64, Directed>'s raw edge list (edge e: src[e] ->
+// dst[e], weight w[e], in edge-index order) -> the out-CSR its adapter
+// exposes (src/graph.rs:144-212): row u lists the targets of u's outgoing
+// edges newest first (petgraph walks a node's edge list from its last
+// added edge; parallel edges are repeated), and with weights, every entry
+// u -> v carries the weight find_edge(u, v) returns, that of the newest
+// u -> v edge.  A stable radix sort of the reversed edge list by source gives
+// the rows; a stable sort of the entries by (source, target) groups the
+// parallel edges, and each group takes the weight of its first entry.
+Status edges_to_out_csr_device(Ctx *ctx, int64_t n, int64_t m, const int32_t *d_src, const int32_t *d_dst,
+                               const double *d_w, int64_t **d_rp, int32_t **d_col, double **d_wout) {
+  cudaStream_t s = ctx->stream;
+  *d_rp = nullptr; *d_col = nullptr; *d_wout = nullptr;
+  const int64_t mm = std::max<int64_t>(m, 1);
+  uint32_t *kin = nullptr, *k1 = nullptr, *v1 = nullptr, *k2 = nullptr, *v2 = nullptr, *colkey = nullptr;
+  double *wraw = nullptr, *first_w = nullptr;
+  int64_t *start = nullptr, *excl = nullptr;
+  int *bad = nullptr;
+  auto cleanup = [&]() {
+    free_async(kin, s); free_async(k1, s); free_async(v1, s); free_async(k2, s); free_async(v2, s);
+    free_async(colkey, s); free_async(wraw, s); free_async(first_w, s); free_async(start, s); free_async(excl, s);
+    free_async(bad, s);
+  };
+  auto fail_all = [&](Status st) {
+    cleanup();
+    free_async(*d_rp, s); free_async(*d_col, s); free_async(*d_wout, s);
+    *d_rp = nullptr; *d_col = nullptr; *d_wout = nullptr;
+    return st;
+  };
+#define EDGE_TRY(expr)                                                                           \
+  do {                                                                                           \
+    cudaError_t _e = (expr);                                                                     \
+    if (_e != cudaSuccess)                                                                       \
+      return fail_all(Status{_e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA,      \
+                             std::string("edge list: ") + cudaGetErrorString(_e)});              \
+  } while (0)
+#define EDGE_ST(expr)                          \
+  do {                                         \
+    Status _s = (expr);                        \
+    if (_s.code != GOPS_OK) return fail_all(_s); \
+  } while (0)
+  EDGE_TRY(dev_malloc_async((void **)d_rp, sizeof(int64_t) * (n + 1), s));
+  EDGE_TRY(dev_malloc_async((void **)d_col, sizeof(int32_t) * mm, s));
+  EDGE_TRY(dev_malloc_async((void **)&kin, sizeof(uint32_t) * mm, s));
+  EDGE_TRY(dev_malloc_async((void **)&k1, sizeof(uint32_t) * mm, s));
+  EDGE_TRY(dev_malloc_async((void **)&v1, sizeof(uint32_t) * mm, s));
+  EDGE_TRY(dev_malloc_async((void **)&k2, sizeof(uint32_t) * mm, s));
+  EDGE_TRY(dev_malloc_async((void **)&v2, sizeof(uint32_t) * mm, s));
+  EDGE_TRY(dev_malloc_async((void **)&colkey, sizeof(uint32_t) * mm, s));
+  EDGE_TRY(dev_malloc_async((void **)&bad, sizeof(int), s));
+  EDGE_TRY(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  if (m > 0) {
+    reversed_sources<<<grid_for(m, 256), 256, 0, s>>>(d_src, d_dst, m, n, kin, bad);
+    EDGE_TRY(cudaGetLastError());
+  }
+  int hbad = 0;
+  EDGE_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  EDGE_TRY(cudaStreamSynchronize(s));
+  if (hbad) return fail_all(Status{GOPS_ERR_INVALID, "edge endpoint out of range"});
+  // rows: sources ascending, each source's edges newest first
+  bool alt = false;
+  const int bits = std::max(1, bits_for(n));
+  EDGE_ST(radix_sort_index_u32(kin, k1, v1, k2, v2, m, bits, &alt, s));
+  const uint32_t *rows = alt ? k2 : k1;
+  const uint32_t *pos_rev = alt ? v2 : v1;
+  rp_from_sorted<<<grid_for(m + 1, 256), 256, 0, s>>>(rows, m, n, *d_rp);
+  EDGE_TRY(cudaGetLastError());
+  if (d_w) {
+    EDGE_TRY(dev_malloc_async((void **)&wraw, sizeof(double) * mm, s));
+    EDGE_TRY(dev_malloc_async((void **)d_wout, sizeof(double) * mm, s));
+  }
+  if (m > 0) {
+    edges_gather<<<grid_for(m, 256), 256, 0, s>>>(pos_rev, d_dst, d_w, m, *d_col, wraw, colkey);
+    EDGE_TRY(cudaGetLastError());
+  }
+  if (d_w && m > 0) {
+    // the row keys move out of the sort buffers, which the next sorts reuse
+    uint32_t *rowk = kin;
+    EDGE_TRY(cudaMemcpyAsync(rowk, rows, sizeof(uint32_t) * m, cudaMemcpyDeviceToDevice, s));
+    // entries by target (stable), then by row (stable): (row, target) order, ties in row order
+    EDGE_ST(radix_sort_index_u32(colkey, k1, v1, k2, v2, m, bits, &alt, s));
+    const uint32_t *pos_t = alt ? v2 : v1;
+    uint32_t *kb = alt ? k1 : k2, *vb = alt ? v1 : v2;  // the buffers not holding the result
+    uint32_t *keys2 = colkey;                           // colkey is no longer needed
+    row_of_positions<<<grid_for(m, 256), 256, 0, s>>>(rowk, pos_t, m, keys2);
+    EDGE_TRY(cudaGetLastError());
+    uint32_t *vin = kb;
+    EDGE_TRY(cudaMemcpyAsync(vin, pos_t, sizeof(uint32_t) * m, cudaMemcpyDeviceToDevice, s));
+    uint32_t *kk1 = nullptr, *vv1 = nullptr;
+    EDGE_TRY(dev_malloc_async((void **)&kk1, sizeof(uint32_t) * mm, s));
+    EDGE_TRY(dev_malloc_async((void **)&vv1, sizeof(uint32_t) * mm, s));
+    bool alt2 = false;
+    Status st2 = radix_sort_pairs_u32(keys2, vin, kk1, vv1, m, bits, &alt2, s);
+    const uint32_t *pos = alt2 ? vv1 : vin;
+    (void)vb;
+    EDGE_TRY(dev_malloc_async((void **)&start, sizeof(int64_t) * (m + 1), s));
+    EDGE_TRY(dev_malloc_async((void **)&excl, sizeof(int64_t) * (m + 1), s));
+    EDGE_TRY(dev_malloc_async((void **)&first_w, sizeof(double) * mm, s));
+    if (st2.code == GOPS_OK) {
+      run_starts<<<grid_for(m, 256), 256, 0, s>>>(rowk, pos, *d_col, m, start);
+      st2 = cudaGetLastError() == cudaSuccess ? Status::ok() : Status{GOPS_ERR_CUDA, "run_starts"};
+    }
+    if (st2.code == GOPS_OK) st2 = exclusive_scan_i64(start, excl, m, s);
+    if (st2.code == GOPS_OK) {
+      run_weights<<<grid_for(m, 256), 256, 0, s>>>(excl, start, pos, wraw, m, first_w, *d_wout, 0);
+      run_weights<<<grid_for(m, 256), 256, 0, s>>>(excl, start, pos, wraw, m, first_w, *d_wout, 1);
+      st2 = cudaGetLastError() == cudaSuccess ? Status::ok() : Status{GOPS_ERR_CUDA, "run_weights"};
+    }
+    free_async(kk1, s);
+    free_async(vv1, s);
+    EDGE_ST(st2);
+  }
+  EDGE_TRY(cudaStreamSynchronize(s));
+  cleanup();
+  return Status::ok();
+#undef EDGE_TRY
+#undef EDGE_ST
 }
 
 }  // namespace gops

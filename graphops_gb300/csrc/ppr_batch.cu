@@ -358,27 +358,45 @@ __device__ __forceinline__ FV<CPL> f32_block(const StepParams &p, int in, int kt
 // wave, nor on the k-tile.
 // ---------------------------------------------------------------------------
 template <int CPL>
-__device__ __forceinline__ DV<CPL> dv_zero() {
-  DV<CPL> r;
+struct MixSum {
+  DV<CPL> d;  // double-float sums (columns in the double-float phase)
+  FV<CPL> f;  // FP32 sums of the hi words (columns in the FP32 phase)
+};
+
+template <int CPL>
+__device__ __forceinline__ MixSum<CPL> mix_zero() {
+  MixSum<CPL> r;
 #pragma unroll
-  for (int q = 0; q < CPL; ++q) r.v[q] = {0.0f, 0.0f};
+  for (int q = 0; q < CPL; ++q) {
+    r.d.v[q] = {0.0f, 0.0f};
+    r.f.v[q] = 0.0f;
+  }
   return r;
 }
 
-// s += g column by column: FP32 on the hi words where bit q of fmask is set
 template <int CPL>
-__device__ __forceinline__ void mix_add(DV<CPL> &s, const DV<CPL> &g, unsigned fmask) {
+__device__ __forceinline__ void mix_add(MixSum<CPL> &s, const DV<CPL> &g) {
 #pragma unroll
-  for (int q = 0; q < CPL; ++q)
-    s.v[q] = ((fmask >> q) & 1u) ? df{s.v[q].hi + g.v[q].hi, 0.0f} : df_add(s.v[q], g.v[q]);
+  for (int q = 0; q < CPL; ++q) {
+    s.d.v[q] = df_add(s.d.v[q], g.v[q]);
+    s.f.v[q] += g.v[q].hi;
+  }
 }
 
 template <int CPL>
-__device__ __forceinline__ DV<CPL> mix_block(const StepParams &p, int in, int kt, int eb, int ee, int lane,
-                                             unsigned fmask) {
+__device__ __forceinline__ void mix_add(MixSum<CPL> &s, const MixSum<CPL> &t) {
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) {
+    s.d.v[q] = df_add(s.d.v[q], t.d.v[q]);
+    s.f.v[q] += t.f.v[q];
+  }
+}
+
+template <int CPL>
+__device__ __forceinline__ MixSum<CPL> mix_block(const StepParams &p, int in, int kt, int eb, int ee, int lane) {
   constexpr int U = CPL == 4 ? 4 : 8;
   const float2 *gb = p.gdf[in] + lane * CPL;
-  DV<CPL> s = dv_zero<CPL>();
+  MixSum<CPL> s = mix_zero<CPL>();
   for (int e = eb; e < ee; e += U) {  // ee - eb is a multiple of 4
     int32_t u[U];
     const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
@@ -395,7 +413,7 @@ __device__ __forceinline__ DV<CPL> mix_block(const StepParams &p, int in, int kt
       if (q < 4 || ok2) g[q] = ld_dv<CPL>(gb + (int64_t)u[q] * kt, true);
 #pragma unroll
     for (int q = 0; q < U; ++q)
-      if (q < 4 || ok2) mix_add<CPL>(s, g[q], fmask);
+      if (q < 4 || ok2) mix_add<CPL>(s, g[q]);
   }
   return s;
 }
@@ -410,14 +428,17 @@ struct Lane {
   unsigned fmask;  // bit q: column q active and in its FP32 phase
 };
 
+// A lane's exact fixed-point partial sums (L1 norm and dangling mass per
+// column, and a nonfinite bit per column), kept in its warp's shared-memory
+// slots rather than in registers; block_sums adds them up per column.
 template <int CPL>
 struct LaneAcc {
-  long long l1[CPL], dang[CPL];
-  int bad;
-  __device__ LaneAcc() {
+  long long *l1, *dang;
+  int *bad;
+  __device__ LaneAcc(long long *l, long long *d, int *b) : l1(l), dang(d), bad(b) {
 #pragma unroll
     for (int q = 0; q < CPL; ++q) l1[q] = dang[q] = 0;
-    bad = 0;
+    *bad = 0;
   }
 };
 
@@ -465,7 +486,7 @@ __device__ __forceinline__ void f32_epilogue(const StepParams &p, const WaveScal
     const float r = ln.act[q] ? f32_step(s.v[q], ln.dsum[q].hi, in.red[q].hi, wc.d.hi) : 0.0f;
     tn.v[q] = in.tail.v[q] + r;
     a.l1[q] += fx_of(fabsf(r), wc.fx_scale);
-    a.bad |= (!isfinite(r)) << q;
+    *a.bad |= (!isfinite(r)) << q;
     if (dg == 0.0f) a.dang[q] += fx_of(r, wc.fx_scale);
     gh.v[q] = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
   }
@@ -479,7 +500,7 @@ __device__ __forceinline__ void f32_epilogue(const StepParams &p, const WaveScal
 // f32_epilogue computes it.  The tail is read and written only by lanes with
 // such a column.
 template <int CPL>
-__device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScalars &wc, int64_t v, const DV<CPL> &s,
+__device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScalars &wc, int64_t v, const MixSum<CPL> &s,
                                              const BIn<CPL> &in, const Lane &ln, int out, unsigned long long k,
                                              LaneAcc<CPL> &a, int lane) {
   const int64_t i = v * wc.kt + lane * CPL;
@@ -492,21 +513,21 @@ __device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScal
     an.v[q] = in.acc.v[q];
     tn.v[q] = ln.fmask ? in.tail.v[q] : 0.0f;
     if (ln.act[q] && ln.f32[q]) {
-      const float r = f32_step(s.v[q].hi, ln.dsum[q].hi, red.hi, wc.d.hi);
+      const float r = f32_step(s.f.v[q], ln.dsum[q].hi, red.hi, wc.d.hi);
       tn.v[q] = in.tail.v[q] + r;
       a.l1[q] += fx_of(fabsf(r), wc.fx_scale);
-      a.bad |= (!isfinite(r)) << q;
+      *a.bad |= (!isfinite(r)) << q;
       if (dg == 0.0f) a.dang[q] += fx_of(r, wc.fx_scale);
       gh.v[q] = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
       g.v[q] = {gh.v[q], 0.0f};
     } else if (ln.act[q]) {
       const df ao = in.acc.v[q];
-      df r = df_mul(wc.d, df_add(s.v[q], df_mul(ln.dsum[q], red)));
+      df r = df_mul(wc.d, df_add(s.d.v[q], df_mul(ln.dsum[q], red)));
       if (k == 1) r = df_add(df_add(df_mul(wc.omd, red), r), df_neg(ao));  // F(x_0) - x_0
       an.v[q] = df_add(ao, r);
       const df ar = r.hi < 0.0f ? df_neg(r) : r;
       a.l1[q] += fx_of(ar.hi, wc.fx_scale) + fx_of(ar.lo, wc.fx_scale);
-      a.bad |= (!isfinite(r.hi)) << q;
+      *a.bad |= (!isfinite(r.hi)) << q;
       if (dg == 0.0f) a.dang[q] += fx_of(r.hi, wc.fx_scale) + fx_of(r.lo, wc.fx_scale);
       g.v[q] = dg > 0.0f ? df_div_f(r, dg) : df{0.0f, 0.0f};
       gh.v[q] = g.v[q].hi;
@@ -595,15 +616,8 @@ __device__ bool batch_prologue(const StepParams &p, const WaveScalars &wc, unsig
 
 // The block's per-column fixed-point sums -> one atomic per column.
 template <int CPL>
-__device__ __forceinline__ void block_sums(const StepParams &p, int kt, unsigned long long k, const LaneAcc<CPL> &a,
-                                           int lane, int wid, long long (*bl1)[kMaxKT], long long (*bdg)[kMaxKT],
-                                           int (*bbad)[32]) {
-#pragma unroll
-  for (int q = 0; q < CPL; ++q) {
-    bl1[wid][lane * CPL + q] = a.l1[q];
-    bdg[wid][lane * CPL + q] = a.dang[q];
-  }
-  bbad[wid][lane] = a.bad;
+__device__ __forceinline__ void block_sums(const StepParams &p, int kt, unsigned long long k,
+                                           long long (*bl1)[kMaxKT], long long (*bdg)[kMaxKT], int (*bbad)[32]) {
   __syncthreads();
   if (threadIdx.x < kt) {
     const int c = threadIdx.x;
@@ -663,7 +677,7 @@ __global__ void __launch_bounds__(kBThreads) spmm_f32(StepParams p) {
   if (!batch_prologue<false, CPL>(p, wc, k, lane, &ln)) return;
   const int in = (int)((k - 1) & 1), out = (int)(k & 1);
   const int kt = wc.kt;
-  LaneAcc<CPL> a;
+  LaneAcc<CPL> a(&bl1[wid][lane * CPL], &bdg[wid][lane * CPL], &bbad[wid][lane]);
   const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
   const int64_t nwt = p.n_big_tasks + (p.n - p.n_big);
   for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
@@ -699,7 +713,7 @@ __global__ void __launch_bounds__(kBThreads) spmm_f32(StepParams p) {
       f32_epilogue<CPL>(p, wc, v, tot, bi, ln, out, a, lane);
     }
   }
-  block_sums<CPL>(p, kt, k, a, lane, wid, bl1, bdg, bbad);
+  block_sums<CPL>(p, kt, k, bl1, bdg, bbad);
 }
 
 template <int CPL>
@@ -713,7 +727,7 @@ __global__ void __launch_bounds__(kBThreads, 2) spmm_mixed(StepParams p) {
   if (!batch_prologue<true, CPL>(p, wc, k, lane, &ln)) return;
   const int in = (int)((k - 1) & 1), out = (int)(k & 1);
   const int kt = wc.kt;
-  LaneAcc<CPL> a;
+  LaneAcc<CPL> a(&bl1[wid][lane * CPL], &bdg[wid][lane * CPL], &bbad[wid][lane]);
   const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
   const int64_t nwt = p.n_big_tasks + (p.n - p.n_big);
   for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
@@ -721,27 +735,37 @@ __global__ void __launch_bounds__(kBThreads, 2) spmm_mixed(StepParams p) {
       int h, first, nch, b0, nb, cs, ce, rb;
       chunk_row(p, (int)w, &h, &first, &nch, &b0, &nb, &cs, &ce, &rb);
       if (ln.any)
-        for (int b = cs; b < ce; b += kBase)
-          st_dv<CPL>(p.lpart + (int64_t)(b0 + (b - rb) / kBase) * kt + lane * CPL,
-                     mix_block<CPL>(p, in, kt, b, min(ce, b + kBase), lane, ln.fmask));
+        for (int b = cs; b < ce; b += kBase) {
+          // per column: the double-float sum, or the FP32 sum as (s, 0)
+          const MixSum<CPL> s = mix_block<CPL>(p, in, kt, b, min(ce, b + kBase), lane);
+          DV<CPL> pk;
+#pragma unroll
+          for (int q = 0; q < CPL; ++q) pk.v[q] = ((ln.fmask >> q) & 1u) ? df{s.f.v[q], 0.0f} : s.d.v[q];
+          st_dv<CPL>(p.lpart + (int64_t)(b0 + (b - rb) / kBase) * kt + lane * CPL, pk);
+        }
       if (chunk_arrive(p, h, nch, lane) && ln.any) {
         const BIn<CPL> bi = b_in<CPL>(p, wc, h, lane, ln, true, ln.fmask != 0);
-        DV<CPL> all = ld_dv<CPL>(p.lpart + (int64_t)b0 * kt + lane * CPL, false);
-        for (int q = 1; q < nb; ++q) mix_add<CPL>(all, ld_dv<CPL>(p.lpart + (int64_t)(b0 + q) * kt + lane * CPL, false),
-                                                  ln.fmask);
+        MixSum<CPL> all = mix_zero<CPL>();
+        for (int q = 0; q < nb; ++q) {
+          const DV<CPL> d = ld_dv<CPL>(p.lpart + (int64_t)(b0 + q) * kt + lane * CPL, false);
+#pragma unroll
+          for (int j = 0; j < CPL; ++j) {
+            all.d.v[j] = q == 0 ? d.v[j] : df_add(all.d.v[j], d.v[j]);
+            all.f.v[j] = q == 0 ? d.v[j].hi : all.f.v[j] + d.v[j].hi;
+          }
+        }
         mix_epilogue<CPL>(p, wc, h, all, bi, ln, out, k, a, lane);
       }
     } else if (ln.any) {
       const int64_t v = p.n_big + (w - p.n_big_tasks);
       const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, true, ln.fmask != 0);
       const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
-      DV<CPL> tot = mix_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane, ln.fmask);
-      for (int b = eb + kBase; b < ee; b += kBase)
-        mix_add<CPL>(tot, mix_block<CPL>(p, in, kt, b, min(ee, b + kBase), lane, ln.fmask), ln.fmask);
+      MixSum<CPL> tot = mix_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane);
+      for (int b = eb + kBase; b < ee; b += kBase) mix_add<CPL>(tot, mix_block<CPL>(p, in, kt, b, min(ee, b + kBase), lane));
       mix_epilogue<CPL>(p, wc, v, tot, bi, ln, out, k, a, lane);
     }
   }
-  block_sums<CPL>(p, kt, k, a, lane, wid, bl1, bdg, bbad);
+  block_sums<CPL>(p, kt, k, bl1, bdg, bbad);
 }
 
 // the wave record's step counter after a chunk

@@ -81,17 +81,34 @@ class CsrAdjacency:
 
 
 class DiGraph:
-    """A directed multigraph with petgraph's adapter semantics."""
+    """A directed multigraph with petgraph's adapter semantics.  It keeps its
+    edges in insertion order, like petgraph's edge storage, so the operators
+    upload it in bulk (raw_edges -> gops_graph_from_edges, which builds the
+    adapter's out-adjacency on the device) instead of walking neighbors()."""
 
     def __init__(self, n: int = 0):
         self._out: List[List[tuple]] = [[] for _ in range(n)]
+        self._src: List[int] = []
+        self._dst: List[int] = []
+        self._w: List[float] = []
 
     def add_node(self) -> int:
         self._out.append([])
         return len(self._out) - 1
 
     def add_edge(self, a: int, b: int, weight: float = 1.0) -> None:
+        if not (0 <= a < len(self._out) and 0 <= b < len(self._out)):
+            raise IndexError("edge endpoint out of range")
         self._out[a].append((b, float(weight)))
+        self._src.append(a)
+        self._dst.append(b)
+        self._w.append(float(weight))
+
+    def raw_edges(self):
+        """(src, dst, weight) arrays in edge-index (insertion) order, as
+        petgraph's Graph::raw_edges() exposes them."""
+        return (np.asarray(self._src, dtype=np.int32), np.asarray(self._dst, dtype=np.int32),
+                np.asarray(self._w, dtype=np.float64))
 
     def node_count(self) -> int:
         return len(self._out)

@@ -19,7 +19,7 @@ from typing import List, Sequence
 import numpy as np
 
 from . import _native
-from .graph import AdjacencyMatrix, extract
+from .graph import AdjacencyMatrix, DiGraph, extract
 
 
 class GraphopsError(Exception):
@@ -65,6 +65,9 @@ def _device_graph(graph, weighted: bool) -> "_native.DeviceGraph":
         return graph
     if isinstance(graph, AdjacencyMatrix):
         return _native.DeviceGraph.from_dense(graph.matrix)
+    if isinstance(graph, DiGraph):  # bulk: the raw edge list, built on the device
+        src, dst, w = graph.raw_edges()
+        return _native.DeviceGraph.from_edges(graph.node_count(), src, dst, w if weighted else None)
     rp, col, w = extract(graph, weighted)
     return _native.DeviceGraph.from_csr(rp, col, w)
 

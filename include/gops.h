@@ -132,6 +132,20 @@ int gops_graph_upload(gops_ctx *ctx, int64_t n, const int64_t *row_ptr, const in
  * device. */
 int gops_graph_from_dense(gops_ctx *ctx, int64_t n, const double *matrix, gops_graph **out);
 
+/* The petgraph adapters in bulk (src/graph.rs:144-212, feature petgraph):
+ * instead of calling neighbors(u) and find_edge per node (one Vec per node,
+ * src/graph.rs:163-197), a Rust caller passes the raw edge list of its
+ * petgraph::Graph<_, f64, Directed> as stored (edge e: src[e] -> dst[e],
+ * weights[e] optional; graph.raw_edges() in edge-index order), and the device
+ * builds the out-adjacency the adapter exposes: row u lists the targets of
+ * u's outgoing edges newest first (petgraph's neighbors order; parallel
+ * edges repeated), and with weights every u -> v entry carries the weight
+ * find_edge(u, v) returns, the newest u -> v edge's.  Then as
+ * gops_graph_upload.  n, m < 2^31 - 1; an endpoint outside [0, n) is
+ * refused. */
+int gops_graph_from_edges(gops_ctx *ctx, int64_t n, int64_t m, const int32_t *src, const int32_t *dst,
+                          const double *weights, gops_graph **out);
+
 void gops_graph_destroy(gops_graph *g);
 int gops_graph_info(const gops_graph *g, int64_t *n, int64_t *m, int32_t *weighted);
 

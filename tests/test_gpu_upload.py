@@ -45,3 +45,69 @@ def test_weighted_invalid_then_valid():
     g = go.DeviceGraph.from_csr(np.array([0, 1, 2, 2], np.int64), np.array([1, 2], np.int32), w)
     s, it, diff, conv = g.pagerank_weighted_run(go.PageRankConfig())
     assert conv and abs(s.sum() - 1.0) < 1e-9
+
+
+def _random_multigraph(n, m, seed):
+    rng = np.random.default_rng(seed)
+    src = rng.integers(0, n, size=m).astype(np.int32)
+    dst = rng.integers(0, n, size=m).astype(np.int32)
+    # hubs, parallel edges and self loops
+    src[: m // 10] = rng.integers(0, 4, size=m // 10)
+    dst[m // 10: m // 5] = src[m // 10: m // 5]
+    w = rng.uniform(0.1, 1.0, size=m)
+    w[::17] = 0.0
+    return src, dst, w
+
+
+def test_edge_list_upload_matches_the_adapter_walk():
+    """gops_graph_from_edges (petgraph's raw edge list, built on the device)
+    against the out-adjacency walked on the host (tests/edges_ref.py, equal to
+    the adapter walk over neighbors() / find_edge): the same graph, so
+    bit-identical weighted, unweighted and personalized solves; and the
+    oracle's restatement on the walked arrays within the parity bars."""
+    from edges_ref import out_csr_from_edges
+    from oracle import port
+    n, m = 3000, 60000
+    src, dst, w = _random_multigraph(n, m, 5)
+    rp, col, ww = out_csr_from_edges(n, src, dst, w)
+    bulk = go.DeviceGraph.from_edges(n, src, dst, w)
+    walked = go.DeviceGraph.from_csr(rp, col, ww)
+    conf = go.PageRankConfig(0.85, 1000, 1e-9)
+    a = bulk.pagerank_weighted_run(conf)
+    b = walked.pagerank_weighted_run(conf)
+    assert np.array_equal(a[0], b[0]) and a[1:] == b[1:]
+    ref = port.pagerank_weighted_run(rp, col, ww, 0.85, 1000, 1e-9)
+    assert np.abs(a[0] - ref[0]).sum() <= 1e-7 and abs(a[1] - ref[1]) <= 1
+    bu = go.DeviceGraph.from_edges(n, src, dst)
+    wu = go.DeviceGraph.from_csr(rp, col)
+    assert np.array_equal(bu.pagerank_run(conf)[0], wu.pagerank_run(conf)[0])
+    p = np.zeros(n)
+    p[[3, 77, 1500]] = 1.0
+    x = go.personalized_pagerank_run(bu, conf, p)
+    y = go.personalized_pagerank_run(wu, conf, p)
+    assert np.array_equal(x.scores, y.scores)
+
+
+def test_edge_list_upload_through_the_digraph_adapter():
+    """The operators take a DiGraph through the bulk path; the result equals
+    the one from its walked out-adjacency."""
+    from graphops_gb300.graph import extract
+    g = go.DiGraph(500)
+    src, dst, w = _random_multigraph(500, 8000, 9)
+    for a, b, x in zip(src, dst, w):
+        g.add_edge(int(a), int(b), float(x))
+    rp, col, ww = extract(g, weighted=True)
+    conf = go.PageRankConfig(0.85, 1000, 1e-9)
+    r = go.pagerank_weighted_run(g, conf)
+    q = go.pagerank_weighted_run(go.CsrAdjacency(rp, col, ww), conf)
+    assert np.array_equal(r.scores, q.scores) and r.iterations == q.iterations
+
+
+def test_edge_list_checks():
+    with pytest.raises(GopsError, match="edge endpoint out of range"):
+        go.DeviceGraph.from_edges(4, np.array([0, 1], np.int32), np.array([1, 4], np.int32))
+    with pytest.raises(GopsError, match="edge endpoint out of range"):
+        go.DeviceGraph.from_edges(4, np.array([-1], np.int32), np.array([1], np.int32))
+    e = go.DeviceGraph.from_edges(5, np.zeros(0, np.int32), np.zeros(0, np.int32))
+    s, it, _, conv = e.pagerank_run(go.PageRankConfig())
+    assert np.allclose(s, 0.2) and conv  # no edges: every node dangling, uniform

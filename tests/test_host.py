@@ -224,3 +224,25 @@ def test_generator_digests():
         "sbm": _digest(gen.sbm(1000, 8, seed=3)),
     }
     assert got == GEN_DIGESTS, got
+
+
+def test_digraph_raw_edges_restate_the_adapter_walk():
+    """The bulk path's expected out-adjacency (tests/edges_ref.py, what the
+    device builds from raw_edges) equals the adapter walk over neighbors()
+    and edge_weight() on a multigraph with parallel edges and self loops."""
+    from edges_ref import out_csr_from_edges
+    from graphops_gb300.graph import extract
+    rng = np.random.default_rng(11)
+    g = go.DiGraph(40)
+    for _ in range(400):
+        a, b = rng.integers(0, 40, size=2)
+        g.add_edge(int(a), int(b), float(rng.choice([0.0, 0.5, 1.5, rng.random()])))
+    for _ in range(30):  # parallel edges with their own weights
+        a, b = rng.integers(0, 5, size=2)
+        g.add_edge(int(a), int(b), float(rng.random()))
+    src, dst, w = g.raw_edges()
+    rp, col, ww = out_csr_from_edges(g.node_count(), src, dst, w)
+    rp2, col2, ww2 = extract(g, weighted=True)
+    assert np.array_equal(rp, rp2) and np.array_equal(col, col2) and np.array_equal(ww, ww2)
+    with pytest.raises(IndexError):
+        g.add_edge(0, 40)

@@ -372,7 +372,7 @@ def batch_roofline(g, st, kt):
     # against the same peak shows how far the gathers are from the copy rate
     gb = b + 4 * m * kt
     achg = gb / (ms * 1e-3) / 1e9 if st.f32_launches else None
-    return {"bound": "hbm", "kernel": f"spmm_f32<{kt // 32}> ({kt} columns per wave)",
+    return {"bound": "hbm", "kernel": f"spmm_f32 ({kt} columns per wave)",
             "bytes_per_launch": int(b), "mean_launch_ms": round(ms, 5),
             "achieved": round(ach, 1) if ach else None, "peak": peak,
             "unit": "GB/s", "frac": round(ach / peak, 4) if ach else None,
@@ -386,10 +386,12 @@ def batch_roofline(g, st, kt):
 def tile_info(dg):
     """The batched path's autotuned tile: sets per wave (k-tile), the chunk
     size of long rows, and the tuner's measured cost of every candidate."""
-    kt, chunk, cost = dg.batch_tile()
+    kt, chunk, l2, cost, cost_l2 = dg.batch_tile()
     names = [f"cols{32 << i}_chunk{c}" for i in range(3) for c in (256, 1024)]
-    return kt, {"cols": kt, "chunk": chunk,
-                "tuner_us_per_set_step": {nm: round(float(v) * 1e3, 3) for nm, v in zip(names, cost.ravel()) if v > 0}}
+    tuned = {nm: round(float(v) * 1e3, 3) for nm, v in zip(names, cost.ravel()) if v > 0}
+    if cost_l2 > 0:
+        tuned[f"cols{kt}_chunk{chunk}_l2hints"] = round(cost_l2 * 1e3, 3)
+    return kt, {"cols": kt, "chunk": chunk, "l2_hints": l2, "tuner_us_per_set_step": tuned}
 
 
 def run_batch(a, ctx, rank, ws):

@@ -85,8 +85,8 @@ SIGNATURES = [
     ("gops_pagerank_run_noalloc", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _p, ctypes.POINTER(Run)]),
     ("gops_ppr_batch", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
     ("gops_ppr_batch_device", ctypes.c_int, [_p, _p, ctypes.POINTER(Config), _i64, _p, _p, _p, _p, _p]),
-    ("gops_ppr_batch_set_tile", ctypes.c_int, [_p, _p, ctypes.c_int32, ctypes.c_int32]),
-    ("gops_ppr_batch_tile", ctypes.c_int, [_p, _p, _p, _p]),
+    ("gops_ppr_batch_set_tile", ctypes.c_int, [_p, _p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    ("gops_ppr_batch_tile", ctypes.c_int, [_p, _p, _p, _p, _p]),
     ("gops_katz_config_validate", ctypes.c_int, [ctypes.POINTER(KatzConfig), ctypes.c_char_p, ctypes.c_size_t]),
     ("gops_katz_run", ctypes.c_int, [_p, _p, ctypes.POINTER(KatzConfig), _p, ctypes.POINTER(Run)]),
     ("gops_eigenvector_run", ctypes.c_int, [_p, _p, _u64, _dbl, _p, ctypes.POINTER(Run)]),
@@ -293,19 +293,23 @@ class DeviceGraph:
         conv = np.array([bool(runs[i].converged) for i in range(ns)])
         return scores, its, diffs, conv
 
-    def set_batch_tile(self, cols=0, chunk=256):
-        """Fix the batched path's k-tile (sets per wave: 32, 64 or 128) and the
-        chunk size of long rows, or re-run the autotuner (cols=0)."""
-        self.ctx.check(self.ctx._l.gops_ppr_batch_set_tile(self.ctx.handle, self.handle, int(cols), int(chunk)))
+    def set_batch_tile(self, cols=0, chunk=256, l2_hints=False):
+        """Fix the batched path's k-tile (sets per wave: 32, 64 or 128), the
+        chunk size of long rows and the FP32 step's L2 hints, or re-run the
+        autotuner (cols=0)."""
+        self.ctx.check(self.ctx._l.gops_ppr_batch_set_tile(self.ctx.handle, self.handle, int(cols), int(chunk),
+                                                           int(bool(l2_hints))))
 
     def batch_tile(self):
-        """(cols, chunk, cost) of the batched path: cost[i, j] is the
-        autotuner's ms per set-step for cols 32/64/128 (i) and chunk
-        256/1024 (j), 0 where not tried."""
-        c, ch = ctypes.c_int32(), ctypes.c_int32()
-        cost = np.zeros(6, dtype=np.float32)
-        self.ctx.check(self.ctx._l.gops_ppr_batch_tile(self.handle, ctypes.byref(c), ctypes.byref(ch), ptr(cost)))
-        return int(c.value), int(ch.value), cost.reshape(3, 2)
+        """(cols, chunk, l2_hints, cost) of the batched path: cost[i, j] is
+        the autotuner's ms per set-step for cols 32/64/128 (i) and chunk
+        256/1024 (j) without L2 hints, cost_l2 that of the chosen tile with
+        them; 0 where not tried."""
+        c, ch, l2 = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        cost = np.zeros(7, dtype=np.float32)
+        self.ctx.check(self.ctx._l.gops_ppr_batch_tile(self.handle, ctypes.byref(c), ctypes.byref(ch),
+                                                       ctypes.byref(l2), ptr(cost)))
+        return int(c.value), int(ch.value), bool(l2.value), cost[:6].reshape(3, 2), float(cost[6])
 
     def katz_run(self, alpha, beta, max_iterations, tolerance, out=True):
         c = KatzConfig(float(alpha), float(beta), int(max_iterations), float(tolerance))

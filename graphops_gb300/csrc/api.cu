@@ -19,8 +19,8 @@ Status edges_to_out_csr_device(Ctx *ctx, int64_t n, int64_t m, const int32_t *d_
 Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, const int64_t *seed_ptr,
                  const int32_t *seed_idx, const float *x0, bool x0_on_device, float *scores,
                  bool scores_on_device, gops_run *runs, const double *r1_max, int32_t *rejected);
-Status batch_set_tile(Ctx *ctx, Graph *g, int cols, int chunk);
-Status batch_get_tile(Graph *g, int *cols, int *chunk, float *cost);
+Status batch_set_tile(Ctx *ctx, Graph *g, int cols, int chunk, int l2_hints);
+Status batch_get_tile(Graph *g, int *cols, int *chunk, int *l2_hints, float *cost);
 
 constexpr int kMaxDevices = 64;
 static std::mutex g_pool_mu;
@@ -488,22 +488,23 @@ int gops_ppr_batch_device(gops_ctx *ctx, const gops_graph *g, const gops_config 
   return batch_common(ctx, g, cfg, nsets, seed_ptr, seed_idx, x0_device, scores_device, runs, true);
 }
 
-int gops_ppr_batch_set_tile(gops_ctx *ctx, const gops_graph *g, int32_t cols, int32_t chunk) {
+int gops_ppr_batch_set_tile(gops_ctx *ctx, const gops_graph *g, int32_t cols, int32_t chunk, int32_t l2_hints) {
   if (!ctx) return GOPS_ERR_INVALID;
   Ctx &c = ctx->impl;
   if (!g) return c.set(Status{GOPS_ERR_INVALID, "null argument"});
   if (g->impl.ctx != &c) return c.set(Status{GOPS_ERR_INVALID, "graph belongs to another context"});
   if (g->impl.n == 0) return GOPS_OK;
   cudaSetDevice(c.device);
-  return c.set(batch_set_tile(&c, const_cast<Graph *>(&g->impl), cols, chunk));
+  return c.set(batch_set_tile(&c, const_cast<Graph *>(&g->impl), cols, chunk, l2_hints));
 }
 
-int gops_ppr_batch_tile(const gops_graph *g, int32_t *cols, int32_t *chunk, float *cost) {
-  if (!g || !cols || !chunk) return GOPS_ERR_INVALID;
-  int c = 0, ch = 0;
-  batch_get_tile(const_cast<Graph *>(&g->impl), &c, &ch, cost);
+int gops_ppr_batch_tile(const gops_graph *g, int32_t *cols, int32_t *chunk, int32_t *l2_hints, float *cost) {
+  if (!g || !cols || !chunk || !l2_hints) return GOPS_ERR_INVALID;
+  int c = 0, ch = 0, l2 = 0;
+  batch_get_tile(const_cast<Graph *>(&g->impl), &c, &ch, &l2, cost);
   *cols = c;
   *chunk = ch;
+  *l2_hints = l2;
   return GOPS_OK;
 }
 

@@ -109,6 +109,9 @@ struct BatchState {
   int kt_cap = 0;
   bool tuned = false;
   float tune_ms[3][2] = {};  // per (cpl 1/2/4, chunk 256/1024): cost per column-step, 0 = not tried
+  float tune_l2 = 0.f;       // cost of the chosen tile with L2 eviction hints (0 = not tried)
+  bool l2h = false;          // FP32 step with L2 eviction hints
+  int l2_bytes = 0;          // the device's L2 size
   // chunk plan: rows [0, n_big) have more than `chunk` in-edges (rows are in
   // non-increasing in-degree); row h has tasks big_first[h]..big_first[h+1]-1
   // and base blocks blk_first[h]..blk_first[h+1]-1
@@ -125,7 +128,7 @@ struct BatchState {
   ColState *cols = nullptr;  // kMaxKT
   WaveState *wave = nullptr;
   WaveConst *wc = nullptr;  // device
-  int grid_df = 1, grid_f = 1;  // step kernel grids of the tile in use
+  int grid_df = 1, grid_f[2] = {1, 1};  // step kernel grids of the tile in use (FP32: without / with L2 hints)
   int32_t *prow = nullptr;    // n + 1
   int32_t *pslot = nullptr;   // seed entries of the wave: column slot
   float2 *pval = nullptr;     //   and normalised weight (double-float)
@@ -143,7 +146,7 @@ struct BatchState {
   int32_t *d_inv_perm = nullptr;  // the same on the device
   // captured chunks: [0] double-float and FP32 launches, [1] FP32 only
   cudaGraphExec_t chunk_exec[2] = {nullptr, nullptr};
-  int exec_cpl = 0, exec_chunk = 0;
+  int exec_cpl = 0, exec_chunk = 0, exec_l2h = -1;
   const void *exec_pslot = nullptr;
 };
 
@@ -207,6 +210,7 @@ struct StepParams {
   const float *deg;
   const int32_t *perm;
   int32_t n_big, n_big_tasks, chunk;
+  int32_t hot;  // rows [0, hot) of the gathered block kept in L2 (FP32 step with L2 hints)
   const int32_t *big_first, *big_task_row, *blk_first;
   const int32_t *prow, *pslot;
   const float2 *pval;
@@ -261,6 +265,54 @@ __device__ __forceinline__ void st_fv(float *a, const FV<CPL> &r) {
   } else {
     *reinterpret_cast<float4 *>(a) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
   }
+}
+
+// L2 eviction priorities (createpolicy / cache_hint): evict_last for the
+// rows of the gathered block that most in-edges read (the first rows after
+// the in-degree relabelling), evict_first for everything streamed once.
+__device__ __forceinline__ uint64_t pol_first() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t pol_last() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+template <int CPL>
+__device__ __forceinline__ FV<CPL> ld_fv_pol(const float *a, uint64_t pol) {
+  FV<CPL> r;
+  if constexpr (CPL == 1) {
+    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(r.v[0]) : "l"(a), "l"(pol));
+  } else if constexpr (CPL == 2) {
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0,%1}, [%2], %3;" : "=f"(r.v[0]), "=f"(r.v[1]) : "l"(a), "l"(pol));
+  } else {
+    asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]) : "l"(a), "l"(pol));
+  }
+  return r;
+}
+
+template <int CPL>
+__device__ __forceinline__ void st_fv_pol(float *a, const FV<CPL> &r, uint64_t pol) {
+  if constexpr (CPL == 1) {
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(a), "f"(r.v[0]), "l"(pol) : "memory");
+  } else if constexpr (CPL == 2) {
+    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1,%2}, %3;" ::"l"(a), "f"(r.v[0]), "f"(r.v[1]), "l"(pol)
+                 : "memory");
+  } else {
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1,%2,%3,%4}, %5;" ::"l"(a), "f"(r.v[0]), "f"(r.v[1]),
+                 "f"(r.v[2]), "f"(r.v[3]), "l"(pol) : "memory");
+  }
+}
+
+__device__ __forceinline__ int4 ld_i4_pol(const int32_t *a, uint64_t pol) {
+  int4 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.s32 {%0,%1,%2,%3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(a), "l"(pol));
+  return v;
 }
 
 // CPL double-float values stored as CPL float2 (hi, lo)
@@ -319,28 +371,42 @@ __device__ __forceinline__ FV<CPL> f32_zero() {
 // Sum over edges [eb, ee) of one base block, in edge order.  Rows are
 // padded to multiples of 4 edges and start 16-byte aligned; padding edges
 // point at row n, whose gathered entries are 0.
-template <int CPL>
+// With L2H the column indices stream evict-first and the gathers of rows
+// below p.hot are marked evict-last.
+template <int CPL, bool L2H>
+__device__ __forceinline__ FV<CPL> gather_fv(const StepParams &p, const float *gb, int32_t u, int kt) {
+  if constexpr (L2H) return ld_fv_pol<CPL>(gb + (int64_t)u * kt, u < p.hot ? pol_last() : pol_first());
+  else return ld_fv<CPL>(gb + (int64_t)u * kt);
+}
+
+template <bool L2H>
+__device__ __forceinline__ int4 col_quad(const StepParams &p, int e) {
+  if constexpr (L2H) return ld_i4_pol(p.col + e, pol_first());
+  else return __ldg(reinterpret_cast<const int4 *>(p.col + e));
+}
+
+template <int CPL, bool L2H>
 __device__ __forceinline__ FV<CPL> f32_block(const StepParams &p, int in, int kt, int eb, int ee, int lane) {
   constexpr int U = 8;  // gathers in flight per lane
   const float *gb = p.gf[in] + lane * CPL;
   FV<CPL> s = f32_zero<CPL>();
   int e = eb;
   for (; e + U <= ee; e += U) {
-    const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
-    const int4 b = __ldg(reinterpret_cast<const int4 *>(p.col + e + 4));
+    const int4 a = col_quad<L2H>(p, e);
+    const int4 b = col_quad<L2H>(p, e + 4);
     const int32_t u[U] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     FV<CPL> g[U];
 #pragma unroll
-    for (int q = 0; q < U; ++q) g[q] = ld_fv<CPL>(gb + (int64_t)u[q] * kt);
+    for (int q = 0; q < U; ++q) g[q] = gather_fv<CPL, L2H>(p, gb, u[q], kt);
 #pragma unroll
     for (int q = 0; q < U; ++q) f32_add(s, g[q]);
   }
   if (e < ee) {
-    const int4 a = __ldg(reinterpret_cast<const int4 *>(p.col + e));
+    const int4 a = col_quad<L2H>(p, e);
     const int32_t u[4] = {a.x, a.y, a.z, a.w};
     FV<CPL> g[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) g[q] = ld_fv<CPL>(gb + (int64_t)u[q] * kt);
+    for (int q = 0; q < 4; ++q) g[q] = gather_fv<CPL, L2H>(p, gb, u[q], kt);
 #pragma unroll
     for (int q = 0; q < 4; ++q) f32_add(s, g[q]);
   }
@@ -451,7 +517,7 @@ struct BIn {
   float deg;
 };
 
-template <int CPL>
+template <int CPL, bool L2H = false>
 __device__ __forceinline__ BIn<CPL> b_in(const StepParams &p, const WaveScalars &wc, int64_t v, int lane,
                                          const Lane &ln, bool want_acc, bool want_tail) {
   BIn<CPL> in;
@@ -469,13 +535,16 @@ __device__ __forceinline__ BIn<CPL> b_in(const StepParams &p, const WaveScalars 
   }
   in.deg = __ldg(&p.deg[v]);
   const int64_t i = v * wc.kt + lane * CPL;
-  if (want_tail) in.tail = ld_fv<CPL>(p.tail + i);
+  if (want_tail) {
+    if constexpr (L2H) in.tail = ld_fv_pol<CPL>(p.tail + i, pol_first());
+    else in.tail = ld_fv<CPL>(p.tail + i);
+  }
   if (want_acc) in.acc = ld_dv<CPL>(p.acc + i, false);
   return in;
 }
 
 // FP32 step epilogue: every active column of the lane in its FP32 phase.
-template <int CPL>
+template <int CPL, bool L2H = false>
 __device__ __forceinline__ void f32_epilogue(const StepParams &p, const WaveScalars &wc, int64_t v, const FV<CPL> &s,
                                              const BIn<CPL> &in, const Lane &ln, int out, LaneAcc<CPL> &a, int lane) {
   const int64_t i = v * wc.kt + lane * CPL;
@@ -490,8 +559,13 @@ __device__ __forceinline__ void f32_epilogue(const StepParams &p, const WaveScal
     if (dg == 0.0f) a.dang[q] += fx_of(r, wc.fx_scale);
     gh.v[q] = dg > 0.0f ? __fdiv_rn(r, dg) : 0.0f;
   }
-  st_fv<CPL>(p.tail + i, tn);
-  st_fv<CPL>(p.gf[out] + i, gh);
+  if constexpr (L2H) {
+    st_fv_pol<CPL>(p.tail + i, tn, pol_first());
+    st_fv_pol<CPL>(p.gf[out] + i, gh, v < p.hot ? pol_last() : pol_first());
+  } else {
+    st_fv<CPL>(p.tail + i, tn);
+    st_fv<CPL>(p.gf[out] + i, gh);
+  }
 }
 
 // Mixed step epilogue: a column in its double-float phase takes the
@@ -666,7 +740,7 @@ __device__ __forceinline__ bool chunk_arrive(const StepParams &p, int h, int nch
   return true;
 }
 
-template <int CPL>
+template <int CPL, bool L2H>
 __global__ void __launch_bounds__(kBThreads) spmm_f32(StepParams p) {
   __shared__ long long bl1[kBWarps][kMaxKT], bdg[kBWarps][kMaxKT];
   __shared__ int bbad[kBWarps][32];
@@ -687,30 +761,31 @@ __global__ void __launch_bounds__(kBThreads) spmm_f32(StepParams p) {
       // a lane whose columns have all retired gathers nothing
       if (ln.any)
         for (int b = cs; b < ce; b += kBase) {
-          const FV<CPL> s = f32_block<CPL>(p, in, kt, b, min(ce, b + kBase), lane);
+          const FV<CPL> s = f32_block<CPL, L2H>(p, in, kt, b, min(ce, b + kBase), lane);
           DV<CPL> pk;
 #pragma unroll
           for (int q = 0; q < CPL; ++q) pk.v[q] = {s.v[q], 0.0f};
           st_dv<CPL>(p.lpart + (int64_t)(b0 + (b - rb) / kBase) * kt + lane * CPL, pk);
         }
       if (chunk_arrive(p, h, nch, lane) && ln.any) {
-        const BIn<CPL> bi = b_in<CPL>(p, wc, h, lane, ln, false, true);
+        const BIn<CPL> bi = b_in<CPL, L2H>(p, wc, h, lane, ln, false, true);
         FV<CPL> all = f32_zero<CPL>();
         for (int q = 0; q < nb; ++q) {
           const DV<CPL> d = ld_dv<CPL>(p.lpart + (int64_t)(b0 + q) * kt + lane * CPL, false);
 #pragma unroll
           for (int j = 0; j < CPL; ++j) all.v[j] = q == 0 ? d.v[j].hi : all.v[j] + d.v[j].hi;
         }
-        f32_epilogue<CPL>(p, wc, h, all, bi, ln, out, a, lane);
+        f32_epilogue<CPL, L2H>(p, wc, h, all, bi, ln, out, a, lane);
       }
     } else if (ln.any) {
       const int64_t v = p.n_big + (w - p.n_big_tasks);
-      const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, false, true);
+      const BIn<CPL> bi = b_in<CPL, L2H>(p, wc, v, lane, ln, false, true);
       const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
       // canonical row sum: base blocks from eb, added in order
-      FV<CPL> tot = f32_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane);
-      for (int b = eb + kBase; b < ee; b += kBase) f32_add(tot, f32_block<CPL>(p, in, kt, b, min(ee, b + kBase), lane));
-      f32_epilogue<CPL>(p, wc, v, tot, bi, ln, out, a, lane);
+      FV<CPL> tot = f32_block<CPL, L2H>(p, in, kt, eb, min(ee, eb + kBase), lane);
+      for (int b = eb + kBase; b < ee; b += kBase)
+        f32_add(tot, f32_block<CPL, L2H>(p, in, kt, b, min(ee, b + kBase), lane));
+      f32_epilogue<CPL, L2H>(p, wc, v, tot, bi, ln, out, a, lane);
     }
   }
   block_sums<CPL>(p, kt, k, bl1, bdg, bbad);
@@ -1006,6 +1081,7 @@ Status batch_prepare_impl(Ctx *ctx, Graph *g) {
   g->batch = b;
   const int64_t n = g->n;
   b->n = n;
+  GOPS_CUDA_TRY(cudaDeviceGetAttribute(&b->l2_bytes, cudaDevAttrL2CacheSize, g->device));
   GOPS_CUDA_TRY(cudaMallocHost(&b->hwave, 2 * sizeof(WaveState)));
   GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->wev[0], cudaEventDisableTiming));
   GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->wev[1], cudaEventDisableTiming));
@@ -1128,6 +1204,9 @@ StepParams step_params(const Graph *g, const BatchState *b) {
   p.n_big = b->n_big;
   p.n_big_tasks = b->n_big_tasks;
   p.chunk = b->chunk;
+  // the hottest rows of both gathered blocks (read and written) fit in half of L2
+  const int kt = 32 * std::max(b->cpl, 1);
+  p.hot = (int32_t)std::min<double>((double)g->n, 0.5 * (double)b->l2_bytes / (2.0 * kt * sizeof(float)));
   p.big_first = b->big_first;
   p.big_task_row = b->big_task_row;
   p.blk_first = b->blk_first;
@@ -1160,7 +1239,8 @@ int spmm_grid(const Ctx *ctx, const BatchState *b, K kernel) {
 template <int CPL>
 void set_grids(const Ctx *ctx, BatchState *b) {
   b->grid_df = spmm_grid(ctx, b, spmm_mixed<CPL>);
-  b->grid_f = spmm_grid(ctx, b, spmm_f32<CPL>);
+  b->grid_f[0] = spmm_grid(ctx, b, spmm_f32<CPL, false>);
+  b->grid_f[1] = spmm_grid(ctx, b, spmm_f32<CPL, true>);
 }
 
 // One step of the wave at offset j of the chunk, in the precision phase P.
@@ -1170,7 +1250,8 @@ Status launch_step(const BatchState *b, StepParams p, int j, bool df, cudaStream
   if (df) {
     spmm_mixed<CPL><<<b->grid_df, kBThreads, 0, st>>>(p);
   } else {
-    spmm_f32<CPL><<<b->grid_f, kBThreads, 0, st>>>(p);
+    if (b->l2h) spmm_f32<CPL, true><<<b->grid_f[1], kBThreads, 0, st>>>(p);
+    else spmm_f32<CPL, false><<<b->grid_f[0], kBThreads, 0, st>>>(p);
   }
   GOPS_CUDA_TRY(cudaGetLastError());
   return Status::ok();
@@ -1188,7 +1269,8 @@ Status launch_step_cpl(const Ctx *, const BatchState *b, const StepParams &p, in
 // each for variant 0, FP32 only for variant 1), then the step counter.
 Status ensure_chunk_graph(Ctx *ctx, Graph *g, int variant) {
   BatchState *b = g->batch;
-  if (b->exec_cpl != b->cpl || b->exec_chunk != b->chunk || b->exec_pslot != b->pslot) free_graphs(b);
+  if (b->exec_cpl != b->cpl || b->exec_chunk != b->chunk || b->exec_pslot != b->pslot || b->exec_l2h != (int)b->l2h)
+    free_graphs(b);
   if (b->chunk_exec[variant]) return Status::ok();
   cudaStream_t st = ctx->stream;
   const StepParams p = step_params(g, b);
@@ -1214,6 +1296,7 @@ Status ensure_chunk_graph(Ctx *ctx, Graph *g, int variant) {
   b->chunk_exec[variant] = exec;
   b->exec_cpl = b->cpl;
   b->exec_chunk = b->chunk;
+  b->exec_l2h = (int)b->l2h;
   b->exec_pslot = b->pslot;
   return Status::ok();
 }
@@ -1240,10 +1323,12 @@ void fill_wave_const(WaveScalars &w, const gops_config *cfg, int64_t n, int kt, 
 // ---------------------------------------------------------------------------
 // autotuner: the k-tile (columns per lane) and the chunk size of long rows,
 // picked per graph from timed steps on a probe wave (uniform personalization
-// in every column, never converging) with the workspace the choice needs.
-// Cost of a candidate: its time per column-step, 3/4 FP32 and 1/4
+// in every column, never converging) with the workspace the choice needs;
+// then, for the chosen tile, the FP32 step with and without L2 eviction
+// hints.  Cost of a candidate: its time per column-step, 3/4 FP32 and 1/4
 // double-float steps.  Results do not depend on the choice (canonical row
-// sums), only the time does.
+// sums, per-column precision phases; cache hints change no value), only the
+// time does.
 // ---------------------------------------------------------------------------
 Status probe_tile(Ctx *ctx, Graph *g, int cpl, int chunk, float *cost) {
   BatchState *b = g->batch;
@@ -1323,14 +1408,20 @@ Status batch_tune(Ctx *ctx, Graph *g) {
   b->chunk = 0;  // rebuild the plan for the chosen chunk
   free_plan(b);
   GOPS_TRY(ensure_tile(ctx, g, best_cpl, best_chunk));
+  // the chosen tile's FP32 step with L2 eviction hints
+  b->l2h = true;
+  float c2 = 0.f;
+  GOPS_TRY(probe_tile(ctx, g, best_cpl, best_chunk, &c2));
+  b->tune_l2 = c2;
+  b->l2h = c2 < best;
   b->tuned = true;
   return Status::ok();
 }
 
 }  // namespace
 
-// Choose (cols > 0) or autotune (cols == 0) the k-tile and chunk size.
-Status batch_set_tile(Ctx *ctx, Graph *g, int cols, int chunk) {
+// Choose (cols > 0) or autotune (cols == 0) the k-tile, chunk size and L2 hints.
+Status batch_set_tile(Ctx *ctx, Graph *g, int cols, int chunk, int l2_hints) {
   GOPS_TRY(batch_prepare(ctx, g));
   BatchState *b = g->batch;
   if (cols == 0) {
@@ -1345,23 +1436,28 @@ Status batch_set_tile(Ctx *ctx, Graph *g, int cols, int chunk) {
     free_blocks(b);
   }
   GOPS_TRY(ensure_tile(ctx, g, cols / 32, chunk));
+  b->l2h = l2_hints != 0;
   b->tuned = true;
   return Status::ok();
 }
 
-Status batch_get_tile(Graph *g, int *cols, int *chunk, float *cost) {
+Status batch_get_tile(Graph *g, int *cols, int *chunk, int *l2_hints, float *cost) {
   BatchState *b = g->batch;
   if (!b || !b->tuned) {
     *cols = 0;
     *chunk = 0;
+    *l2_hints = 0;
     if (cost)
-      for (int i = 0; i < 6; ++i) cost[i] = 0.f;
+      for (int i = 0; i < 7; ++i) cost[i] = 0.f;
     return Status::ok();
   }
   *cols = 32 * b->cpl;
   *chunk = b->chunk;
-  if (cost)
+  *l2_hints = b->l2h ? 1 : 0;
+  if (cost) {
     for (int i = 0; i < 6; ++i) cost[i] = b->tune_ms[i / 2][i % 2];
+    cost[6] = b->tune_l2;
+  }
   return Status::ok();
 }
 

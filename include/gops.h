@@ -192,19 +192,23 @@ int gops_ppr_batch_device(gops_ctx *ctx, const gops_graph *g, const gops_config 
                           const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0_device,
                           float *scores_device, gops_run *runs);
 
-/* The batched path's tile of a graph: cols = sets per wave (32, 64 or 128)
- * and chunk = the in-degree above which a row is split into chunks of that
- * many edges (a multiple of 256).  cols == 0 re-runs the autotuner, which
- * times a few steps of each candidate (k-tile x chunk 256 / 1024, within 40 %
- * of the free device memory) and keeps the fastest per set-step.  The tile
+/* The batched path's tile of a graph: cols = sets per wave (32, 64 or 128),
+ * chunk = the in-degree above which a row is split into chunks of that many
+ * edges (a multiple of 256), l2_hints = the FP32 step marks the hottest rows
+ * of the gathered block evict-last in L2 and its streams evict-first.
+ * cols == 0 re-runs the autotuner, which times a few steps of each k-tile x
+ * chunk 256 / 1024 (within 40 % of the free device memory), keeps the
+ * fastest per set-step, then times that tile with L2 hints.  The tile
  * changes the time only: every choice gives bit-identical results (a row's
- * sum is fixed as in-order sums of 256-edge blocks added in order).  No
- * reference counterpart (the reference solves one set per call). */
-int gops_ppr_batch_set_tile(gops_ctx *ctx, const gops_graph *g, int32_t cols, int32_t chunk);
-/* The tile in use (0, 0 before the first batched call), and with cost != NULL
- * the autotuner's measured cost per set-step in ms for (cols 32, 64, 128) x
- * (chunk 256, 1024), 6 floats, 0 where not tried. */
-int gops_ppr_batch_tile(const gops_graph *g, int32_t *cols, int32_t *chunk, float *cost);
+ * sum is fixed as in-order sums of 256-edge blocks added in order, and each
+ * set's precision phases depend on its own step norms only).  No reference
+ * counterpart (the reference solves one set per call). */
+int gops_ppr_batch_set_tile(gops_ctx *ctx, const gops_graph *g, int32_t cols, int32_t chunk, int32_t l2_hints);
+/* The tile in use (0, 0, 0 before the first batched call), and with
+ * cost != NULL the autotuner's measured cost per set-step in ms: 7 floats,
+ * (cols 32, 64, 128) x (chunk 256, 1024) without L2 hints, then the chosen
+ * tile with them; 0 where not tried. */
+int gops_ppr_batch_tile(const gops_graph *g, int32_t *cols, int32_t *chunk, int32_t *l2_hints, float *cost);
 
 /* Device pointer (double, n entries) of the last solve's scores, valid until
  * the next solve on this context or the destruction of the graph that solve

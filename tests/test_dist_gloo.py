@@ -100,7 +100,7 @@ class _FakeDeviceGraph:
 
     def batch_tile(self):
         import numpy as np
-        return 128, 256, np.zeros((3, 2), np.float32)
+        return 128, 256, False, np.zeros((3, 2), np.float32), 0.0
 
 
 def _batch_worker(rank, port, results):

@@ -135,8 +135,8 @@ def test_device_pointers_variant():
 
 
 def test_every_tile_gives_the_same_bits():
-    """The autotuner may pick any k-tile (32, 64 or 128 sets per wave) and
-    chunk size of long rows (256 or 1024 edges).  A row's sum is fixed as
+    """The autotuner may pick any k-tile (32, 64 or 128 sets per wave), chunk
+    size of long rows (256 or 1024 edges) and L2 hints on or off.  A row's sum is fixed as
     in-order sums of 256-edge blocks added in order, so every choice gives
     bit-identical scores and step counts, cold and from caller start
     vectors, and every choice matches the oracle set by set."""
@@ -152,26 +152,27 @@ def test_every_tile_gives_the_same_bits():
     x0 /= x0.sum(axis=1, keepdims=True)
     ref, its = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-7, threads=8)
     first = None
-    for cols in (32, 64, 128):
-        for chunk in (256, 1024):
-            dg.set_batch_tile(cols, chunk)
-            assert dg.batch_tile()[:2] == (cols, chunk)
-            r = go.ppr_batch(dg, conf, sp, si)
-            w = go.ppr_batch(dg, conf, sp, si, x0=x0)
-            assert r.converged.all() and w.converged.all()
-            if first is None:
-                first = (r, w)
-                l1 = np.abs(r.scores.astype(np.float64) - ref).sum(axis=1)
-                assert l1.max() <= L1_TARGET, l1.max()
-                assert np.array_equal(r.iterations, its.astype(np.int64))
-            else:
-                assert np.array_equal(r.scores, first[0].scores), (cols, chunk)
-                assert np.array_equal(r.iterations, first[0].iterations), (cols, chunk)
-                assert np.array_equal(w.scores, first[1].scores), (cols, chunk)
-                assert np.array_equal(w.iterations, first[1].iterations), (cols, chunk)
-    dg.set_batch_tile(0)  # autotune: one of the candidates, each tried one timed
-    cols, chunk, cost = dg.batch_tile()
+    tiles = [(c, ch, False) for c in (32, 64, 128) for ch in (256, 1024)] + [(64, 256, True), (128, 1024, True)]
+    for cols, chunk, l2 in tiles:
+        dg.set_batch_tile(cols, chunk, l2)
+        assert dg.batch_tile()[:3] == (cols, chunk, l2)
+        r = go.ppr_batch(dg, conf, sp, si)
+        w = go.ppr_batch(dg, conf, sp, si, x0=x0)
+        assert r.converged.all() and w.converged.all()
+        if first is None:
+            first = (r, w)
+            l1 = np.abs(r.scores.astype(np.float64) - ref).sum(axis=1)
+            assert l1.max() <= L1_TARGET, l1.max()
+            assert np.array_equal(r.iterations, its.astype(np.int64))
+        else:
+            assert np.array_equal(r.scores, first[0].scores), (cols, chunk, l2)
+            assert np.array_equal(r.iterations, first[0].iterations), (cols, chunk, l2)
+            assert np.array_equal(w.scores, first[1].scores), (cols, chunk, l2)
+            assert np.array_equal(w.iterations, first[1].iterations), (cols, chunk, l2)
+    dg.set_batch_tile(0)  # autotune: the fastest candidate, then L2 hints on it if they pay
+    cols, chunk, l2, cost, cost_l2 = dg.batch_tile()
     assert cols in (32, 64, 128) and chunk in (256, 1024)
     assert (cost[0] > 0).all() and cost[{32: 0, 64: 1, 128: 2}[cols], {256: 0, 1024: 1}[chunk]] == cost[cost > 0].min()
+    assert cost_l2 > 0 and l2 == (cost_l2 < cost[cost > 0].min())
     r = go.ppr_batch(dg, conf, sp, si)
     assert np.array_equal(r.scores, first[0].scores)

@@ -5,14 +5,19 @@
 // scores are not normalised to sum 1 (Katz grows with beta and the walk
 // counts), so FP32 cannot reproduce the reference's iteration counts.  The
 // per-edge work is one FP64 add, far below the GPU's FP64 rate at these
-// gather-bound speeds.  Every sum is taken in a fixed order (per sub-warp, per
-// block, then over blocks), so results are bit-reproducible.
+// gather-bound speeds.  Rows with at most kLong edges are summed by 8-lane
+// groups; longer rows (power-law hubs, in- or out-degree) in kChunkE-edge
+// chunks of a block each, whose sums are added in chunk order, so no hub row
+// leaves a few lanes running long after the rest.  Every sum is taken in a
+// fixed order (per sub-warp or chunk, per block, then over blocks), so
+// results are bit-reproducible.
 #include <cmath>
 #include <cstdio>
 #include <utility>
 #include <vector>
 
 #include "objects.cuh"
+#include "primitives.cuh"
 
 namespace gops {
 namespace {
@@ -20,6 +25,8 @@ namespace {
 constexpr int kCThreads = 256;
 constexpr int kSub = 8;  // lanes per row
 constexpr int kCBlocks = 1024;
+constexpr int64_t kLong = 2048;    // rows with more edges are summed in chunks, a block each
+constexpr int64_t kChunkE = 8192;  // edges per chunk
 
 // sum over the kSub lanes of this lane's group.  The mask names the group
 // only: the groups of a warp run different numbers of rows (a group past the
@@ -44,52 +51,139 @@ __device__ __forceinline__ void block_part(double v, double *sh, double *part, i
   __syncthreads();
 }
 
-// Katz step over the relabelled, padded in-edge CSR (x has n + 1 entries,
-// x[n] = 0 for the padding edges): y[v] = beta + alpha * sum_{u -> v} x[u]
-// (src/katz.rs:166-173); part[b] = this block's sum of |x - y|.
-__global__ void __launch_bounds__(kCThreads) katz_step(const int64_t *__restrict__ rp, const int32_t *__restrict__ col,
-                                                       int64_t n, double alpha, double beta,
+// Per-row updates of the three pulls: y[v] from the row's own x[v] and its
+// gathered sum s, and the contributions to the step's global sums.
+struct KatzOp {  // y[v] = beta + alpha * sum_{u -> v} x[u] (src/katz.rs:166-173); sum |x - y|
+  static constexpr int kSlots = 1;
+  double alpha, beta;
+  __device__ double y(double xv, double s) const { return beta + alpha * s; }
+  __device__ void add(double xv, double yv, double (&acc)[2]) const { acc[0] += fabs(xv - yv); }
+};
+struct EigOp {  // y[v] = x[v] + sum_{u in neighbors(v)} x[u] (src/eigenvector.rs:72-81); sum y^2, sum y
+  static constexpr int kSlots = 2;
+  __device__ double y(double xv, double s) const { return xv + s; }
+  __device__ void add(double, double yv, double (&acc)[2]) const {
+    acc[0] += yv * yv;
+    acc[1] += yv;
+  }
+};
+struct SumOp {  // HITS: y[v] = sum over the row's edges (no self term); sum y^2
+  static constexpr int kSlots = 1;
+  __device__ double y(double, double s) const { return s; }
+  __device__ void add(double, double yv, double (&acc)[2]) const { acc[0] += yv * yv; }
+};
+
+// Rows with at most kLong edges: kSub lanes per row, four gathers in flight
+// per lane (each lane adds its edges e, e + kSub, ... in order).  Longer rows
+// are skipped here and summed in chunks (chunk_sums / long_rows).  x has
+// n + 1 entries when the rows are the padded in-edge CSR (x[n] = 0 for the
+// padding edges).  part[b * kSlots + j]: this block's global sums.
+template <class Op>
+__global__ void __launch_bounds__(kCThreads) short_rows(const int64_t *__restrict__ rp, const int32_t *__restrict__ col,
+                                                        int64_t n, Op op, const double *__restrict__ x,
+                                                        double *__restrict__ y, double *__restrict__ part) {
+  __shared__ double sh[kCThreads];
+  const int lane = threadIdx.x & (kSub - 1);
+  const int64_t groups = (int64_t)gridDim.x * (kCThreads / kSub);
+  double acc[2] = {0.0, 0.0};
+  for (int64_t v = (int64_t)blockIdx.x * (kCThreads / kSub) + threadIdx.x / kSub; v < n; v += groups) {
+    const int64_t eb = rp[v], ee = rp[v + 1];
+    if (ee - eb > kLong) continue;  // a long row: chunk_sums / long_rows
+    double s = 0.0;
+    int64_t e = eb + lane;
+    for (; e + 3 * kSub < ee; e += 4 * kSub) {
+      const int32_t c0 = col[e], c1 = col[e + kSub], c2 = col[e + 2 * kSub], c3 = col[e + 3 * kSub];
+      const double g0 = x[c0], g1 = x[c1], g2 = x[c2], g3 = x[c3];
+      s += g0;
+      s += g1;
+      s += g2;
+      s += g3;
+    }
+    for (; e < ee; e += kSub) s += x[col[e]];
+    s = sub_sum(s);
+    if (lane == 0) {
+      const double yv = op.y(x[v], s);
+      y[v] = yv;
+      op.add(x[v], yv, acc);
+    }
+  }
+  for (int j = 0; j < Op::kSlots; ++j) block_part(acc[j], sh, part, Op::kSlots, j);
+}
+
+// One block per chunk of kChunkE edges of a long row: cpart[t] = the sum of
+// x over the chunk (per thread in edge order, then a fixed tree).
+__global__ void __launch_bounds__(kCThreads) chunk_sums(const int64_t *__restrict__ rp, const int32_t *__restrict__ col,
+                                                        const int32_t *__restrict__ rows,
+                                                        const int64_t *__restrict__ first,
+                                                        const int32_t *__restrict__ task_row,
+                                                        const double *__restrict__ x, double *__restrict__ cpart) {
+  __shared__ double sh[kCThreads];
+  const int64_t t = blockIdx.x;
+  const int32_t i = task_row[t];
+  const int64_t v = rows[i];
+  const int64_t eb = rp[v] + (t - first[i]) * kChunkE;
+  const int64_t ee = min(rp[v + 1], eb + kChunkE);
+  double s = 0.0;
+  int64_t e = eb + threadIdx.x;
+  for (; e + 3 * kCThreads < ee; e += 4 * kCThreads) {
+    const int32_t c0 = col[e], c1 = col[e + kCThreads], c2 = col[e + 2 * kCThreads], c3 = col[e + 3 * kCThreads];
+    const double g0 = x[c0], g1 = x[c1], g2 = x[c2], g3 = x[c3];
+    s += g0;
+    s += g1;
+    s += g2;
+    s += g3;
+  }
+  for (; e < ee; e += kCThreads) s += x[col[e]];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = kCThreads / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cpart[t] = sh[0];
+}
+
+// Long rows, one thread each: the row's chunk sums added in chunk order,
+// then the update; part[b * kSlots + j]: this block's global sums.
+template <class Op>
+__global__ void __launch_bounds__(kCThreads) long_rows(int64_t n_long, const int32_t *__restrict__ rows,
+                                                       const int64_t *__restrict__ first,
+                                                       const double *__restrict__ cpart, Op op,
                                                        const double *__restrict__ x, double *__restrict__ y,
                                                        double *__restrict__ part) {
   __shared__ double sh[kCThreads];
-  const int lane = threadIdx.x & (kSub - 1);
-  const int64_t groups = (int64_t)gridDim.x * (kCThreads / kSub);
-  double dl = 0.0;
-  for (int64_t v = (int64_t)blockIdx.x * (kCThreads / kSub) + threadIdx.x / kSub; v < n; v += groups) {
+  double acc[2] = {0.0, 0.0};
+  const int64_t i = (int64_t)blockIdx.x * kCThreads + threadIdx.x;
+  if (i < n_long) {
     double s = 0.0;
-    for (int64_t e = rp[v] + lane; e < rp[v + 1]; e += kSub) s += x[col[e]];
-    s = sub_sum(s);
-    const double yv = beta + alpha * s;
-    if (lane == 0) {
-      y[v] = yv;
-      dl += fabs(x[v] - yv);
-    }
+    for (int64_t t = first[i]; t < first[i + 1]; ++t) s += cpart[t];
+    const int64_t v = rows[i];
+    const double yv = op.y(x[v], s);
+    y[v] = yv;
+    op.add(x[v], yv, acc);
   }
-  block_part(dl, sh, part, 1, 0);
+  for (int j = 0; j < Op::kSlots; ++j) block_part(acc[j], sh, part, Op::kSlots, j);
 }
 
-// Eigenvector step over the out-adjacency (original ids): y[v] = x[v] +
-// sum_{u in neighbors(v)} x[u] (src/eigenvector.rs:72-81); part[b] = (sum y^2, sum y).
-__global__ void __launch_bounds__(kCThreads) eig_step(const int64_t *__restrict__ rp, const int32_t *__restrict__ col,
-                                                      int64_t n, const double *__restrict__ x, double *__restrict__ y,
-                                                      double *__restrict__ part) {
-  __shared__ double sh[kCThreads];
-  const int lane = threadIdx.x & (kSub - 1);
-  const int64_t groups = (int64_t)gridDim.x * (kCThreads / kSub);
-  double sq = 0.0, su = 0.0;
-  for (int64_t v = (int64_t)blockIdx.x * (kCThreads / kSub) + threadIdx.x / kSub; v < n; v += groups) {
-    double s = 0.0;
-    for (int64_t e = rp[v] + lane; e < rp[v + 1]; e += kSub) s += x[col[e]];
-    s = sub_sum(s);
-    const double yv = x[v] + s;
-    if (lane == 0) {
-      y[v] = yv;
-      sq += yv * yv;
-      su += yv;
+// ---- plan of the long rows of a CSR: the rows, their chunks
+__global__ void long_flags(const int64_t *rp, int64_t n, int64_t *flag) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += (int64_t)gridDim.x * blockDim.x)
+    flag[v] = v < n && rp[v + 1] - rp[v] > kLong ? 1 : 0;
+}
+
+__global__ void long_compact(const int64_t *rp, int64_t n, const int64_t *pos, int32_t *rows, int64_t *nch) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t d = rp[v + 1] - rp[v];
+    if (d > kLong) {
+      rows[pos[v]] = (int32_t)v;
+      nch[pos[v]] = (d + kChunkE - 1) / kChunkE;
     }
   }
-  block_part(sq, sh, part, 2, 0);
-  block_part(su, sh, part, 2, 1);
+}
+
+__global__ void long_tasks(const int64_t *first, int64_t n_long, int32_t *task_row) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_long; i += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t t = first[i]; t < first[i + 1]; ++t) task_row[t] = (int32_t)i;
 }
 
 // out[j] = sum over blocks of part[b * stride + j] (one block, fixed order)
@@ -127,28 +221,6 @@ __global__ void __launch_bounds__(kCThreads) eig_scale(int64_t n, const double *
     dl += fabs(x[v] - yv);
   }
   block_part(dl, sh, part, 1, 0);
-}
-
-// HITS: y[v] = sum over the row's edges of x[col] (no self term); part[b] =
-// this block's sum of y^2.  Rows of the relabelled in-CSR (x has n+1 entries,
-// x[n] = 0) or of the out-adjacency.
-__global__ void __launch_bounds__(kCThreads) pull_sum(const int64_t *__restrict__ rp, const int32_t *__restrict__ col,
-                                                      int64_t n, const double *__restrict__ x, double *__restrict__ y,
-                                                      double *__restrict__ part) {
-  __shared__ double sh[kCThreads];
-  const int lane = threadIdx.x & (kSub - 1);
-  const int64_t groups = (int64_t)gridDim.x * (kCThreads / kSub);
-  double sq = 0.0;
-  for (int64_t v = (int64_t)blockIdx.x * (kCThreads / kSub) + threadIdx.x / kSub; v < n; v += groups) {
-    double s = 0.0;
-    for (int64_t e = rp[v] + lane; e < rp[v + 1]; e += kSub) s += x[col[e]];
-    s = sub_sum(s);
-    if (lane == 0) {
-      y[v] = s;
-      sq += s * s;
-    }
-  }
-  block_part(sq, sh, part, 1, 0);
 }
 
 // HITS l2_normalize (src/centrality.rs:168-175) of y in place (skipped when
@@ -199,6 +271,65 @@ int grid_rows(int64_t n) {
   return blocks_for(n, kCThreads / kSub, kCBlocks);
 }
 
+// The long rows of a CSR (more than kLong edges) and their kChunkE-edge
+// chunks, built once per call.
+struct LongPlan {
+  int64_t n_long = 0, n_chunks = 0;
+  int32_t *rows = nullptr, *task_row = nullptr;
+  int64_t *first = nullptr;
+  double *cpart = nullptr;
+  ~LongPlan() {
+    cudaFree(rows); cudaFree(task_row); cudaFree(first); cudaFree(cpart);
+  }
+};
+
+Status build_long_plan(cudaStream_t s, const int64_t *rp, int64_t n, LongPlan &lp) {
+  int64_t *pos = nullptr;
+  GOPS_CUDA_TRY(cudaMalloc(&pos, sizeof(int64_t) * (n + 1)));
+  struct Free {
+    int64_t *p;
+    ~Free() { cudaFree(p); }
+  } fp{pos};
+  long_flags<<<blocks_for(n + 1, 256, 4096), 256, 0, s>>>(rp, n, pos);
+  GOPS_CUDA_TRY(cudaGetLastError());
+  GOPS_TRY(exclusive_scan_i64(pos, pos, n + 1, s));
+  GOPS_CUDA_TRY(cudaMemcpyAsync(&lp.n_long, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+  if (lp.n_long == 0) return Status::ok();
+  GOPS_CUDA_TRY(cudaMalloc(&lp.rows, sizeof(int32_t) * lp.n_long));
+  GOPS_CUDA_TRY(cudaMalloc(&lp.first, sizeof(int64_t) * (lp.n_long + 1)));
+  GOPS_CUDA_TRY(cudaMemsetAsync(lp.first + lp.n_long, 0, sizeof(int64_t), s));
+  long_compact<<<blocks_for(n, 256, 4096), 256, 0, s>>>(rp, n, pos, lp.rows, lp.first);
+  GOPS_CUDA_TRY(cudaGetLastError());
+  GOPS_TRY(exclusive_scan_i64(lp.first, lp.first, lp.n_long + 1, s));
+  GOPS_CUDA_TRY(cudaMemcpyAsync(&lp.n_chunks, lp.first + lp.n_long, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+  GOPS_CUDA_TRY(cudaMalloc(&lp.task_row, sizeof(int32_t) * lp.n_chunks));
+  GOPS_CUDA_TRY(cudaMalloc(&lp.cpart, sizeof(double) * lp.n_chunks));
+  long_tasks<<<blocks_for(lp.n_long, 256, 4096), 256, 0, s>>>(lp.first, lp.n_long, lp.task_row);
+  GOPS_CUDA_TRY(cudaGetLastError());
+  return Status::ok();
+}
+
+// Blocks of part[] one pull writes: the short-row blocks, then the long-row blocks.
+int pull_blocks(int64_t n, const LongPlan &lp) {
+  return grid_rows(n) + (lp.n_long ? (int)ceil_div<int64_t>(lp.n_long, kCThreads) : 0);
+}
+
+// y = the pull of x over the rows of (rp, col) with the update op; part gets
+// pull_blocks(n, lp) blocks of Op::kSlots sums.  Returns the launches.
+template <class Op>
+int pull(cudaStream_t s, const int64_t *rp, const int32_t *col, int64_t n, const LongPlan &lp, Op op,
+         const double *x, double *y, double *part) {
+  const int nb = grid_rows(n);
+  short_rows<Op><<<nb, kCThreads, 0, s>>>(rp, col, n, op, x, y, part);
+  if (lp.n_long == 0) return 1;
+  chunk_sums<<<(unsigned)lp.n_chunks, kCThreads, 0, s>>>(rp, col, lp.rows, lp.first, lp.task_row, x, lp.cpart);
+  long_rows<Op><<<(unsigned)ceil_div<int64_t>(lp.n_long, kCThreads), kCThreads, 0, s>>>(
+      lp.n_long, lp.rows, lp.first, lp.cpart, op, x, y, part + (int64_t)nb * Op::kSlots);
+  return 3;
+}
+
 }  // namespace
 
 Status katz_run(Ctx *ctx, const Graph *g, const gops_katz_config *cfg, double *scores, gops_run *run) {
@@ -208,7 +339,9 @@ Status katz_run(Ctx *ctx, const Graph *g, const gops_katz_config *cfg, double *s
   if (n == 0) return Status::ok();  // src/katz.rs:138-145
   cudaStream_t s = ctx->stream;
   Bufs b;
-  const int nb = grid_rows(n);
+  LongPlan lp;
+  GOPS_TRY(build_long_plan(s, g->in_rp, n, lp));
+  const int nb = pull_blocks(n, lp);
   GOPS_CUDA_TRY(cudaMalloc(&b.x, sizeof(double) * (n + 1)));
   GOPS_CUDA_TRY(cudaMalloc(&b.y, sizeof(double) * (n + 1)));
   GOPS_CUDA_TRY(cudaMalloc(&b.part, sizeof(double) * nb));
@@ -223,9 +356,9 @@ Status katz_run(Ctx *ctx, const Graph *g, const gops_katz_config *cfg, double *s
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   for (uint64_t k = 0; k < cfg->max_iterations; ++k) {
     ++it;
-    katz_step<<<nb, kCThreads, 0, s>>>(g->in_rp, g->in_col, n, cfg->alpha, cfg->beta, b.x, b.y, b.part);
+    launches += pull(s, g->in_rp, g->in_col, n, lp, KatzOp{cfg->alpha, cfg->beta}, b.x, b.y, b.part);
     sum_blocks<<<1, kCThreads, 0, s>>>(b.part, nb, 1, b.sums);
-    launches += 2;
+    launches += 1;
     double d = 0.0;
     GOPS_CUDA_TRY(cudaMemcpyAsync(&d, b.sums, sizeof(double), cudaMemcpyDeviceToHost, s));
     GOPS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -262,7 +395,9 @@ Status eigenvector_run(Ctx *ctx, const Graph *g, uint64_t max_iterations, double
   if (!g->out_rp) return Status{GOPS_ERR_INTERNAL, "graph has no out-adjacency"};
   cudaStream_t s = ctx->stream;
   Bufs b;
-  const int nb = grid_rows(n);
+  LongPlan lp;
+  GOPS_TRY(build_long_plan(s, g->out_rp, n, lp));
+  const int nb = pull_blocks(n, lp);
   const int nbs = blocks_for(n, 256, kCBlocks);
   GOPS_CUDA_TRY(cudaMalloc(&b.x, sizeof(double) * n));
   GOPS_CUDA_TRY(cudaMalloc(&b.y, sizeof(double) * n));
@@ -275,11 +410,11 @@ Status eigenvector_run(Ctx *ctx, const Graph *g, uint64_t max_iterations, double
   GOPS_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   for (uint64_t k = 0; k < max_iterations; ++k) {
     it = k + 1;
-    eig_step<<<nb, kCThreads, 0, s>>>(g->out_rp, g->out_col, n, b.x, b.y, b.part);
+    launches += pull(s, g->out_rp, g->out_col, n, lp, EigOp{}, b.x, b.y, b.part);
     sum_blocks<<<1, kCThreads, 0, s>>>(b.part, nb, 2, b.sums);
     eig_scale<<<nbs, kCThreads, 0, s>>>(n, b.sums, b.x, b.y, b.part);
     sum_blocks<<<1, kCThreads, 0, s>>>(b.part, nbs, 1, b.sums);
-    launches += 4;
+    launches += 3;
     double d = 0.0;
     GOPS_CUDA_TRY(cudaMemcpyAsync(&d, b.sums, sizeof(double), cudaMemcpyDeviceToHost, s));
     GOPS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -329,7 +464,11 @@ Status hits_run(Ctx *ctx, const Graph *g, uint64_t max_iterations, double tolera
       cudaFree(part); cudaFree(sums);
     }
   } h;
-  const int nb = grid_rows(n), nbs = blocks_for(n, 256, kCBlocks);
+  LongPlan lpi, lpo;
+  GOPS_TRY(build_long_plan(s, g->in_rp, n, lpi));
+  GOPS_TRY(build_long_plan(s, g->out_rp, n, lpo));
+  const int nbi = pull_blocks(n, lpi), nbo = pull_blocks(n, lpo), nbs = blocks_for(n, 256, kCBlocks);
+  const int nb = std::max(nbi, nbo);
   GOPS_CUDA_TRY(cudaMalloc(&h.hub, sizeof(double) * n));
   GOPS_CUDA_TRY(cudaMalloc(&h.auth, sizeof(double) * n));
   GOPS_CUDA_TRY(cudaMalloc(&h.nhub, sizeof(double) * n));
@@ -349,17 +488,17 @@ Status hits_run(Ctx *ctx, const Graph *g, uint64_t max_iterations, double tolera
     it = k + 1;
     // authority: pull over the in-edge rows (relabelled), back to original order
     permute_to_rows<<<blocks_for(n + 1, 256, 4096), 256, 0, s>>>(h.hub, g->perm, n, h.hub_r);
-    pull_sum<<<nb, kCThreads, 0, s>>>(g->in_rp, g->in_col, n, h.hub_r, h.nauth_r, h.part);
-    sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nb, 1, h.sums);
+    launches += pull(s, g->in_rp, g->in_col, n, lpi, SumOp{}, h.hub_r, h.nauth_r, h.part);
+    sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nbi, 1, h.sums);
     l2_scale<<<nbs, kCThreads, 0, s>>>(n, h.sums, h.auth, g->perm, h.nauth_r, h.part);
     sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nbs, 1, h.sums + 2);
     unpermute_f64<<<blocks_for(n, 256, 4096), 256, 0, s>>>(h.nauth_r, g->perm, n, h.nauth);
     // hub: pull over the out-adjacency (original order)
-    pull_sum<<<nb, kCThreads, 0, s>>>(g->out_rp, g->out_col, n, h.nauth, h.nhub, h.part);
-    sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nb, 1, h.sums);
+    launches += pull(s, g->out_rp, g->out_col, n, lpo, SumOp{}, h.nauth, h.nhub, h.part);
+    sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nbo, 1, h.sums);
     l2_scale<<<nbs, kCThreads, 0, s>>>(n, h.sums, h.hub, nullptr, h.nhub, h.part);
     sum_blocks<<<1, kCThreads, 0, s>>>(h.part, nbs, 1, h.sums + 3);
-    launches += 10;
+    launches += 8;
     double d[2] = {0.0, 0.0};
     GOPS_CUDA_TRY(cudaMemcpyAsync(d, h.sums + 2, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
     GOPS_CUDA_TRY(cudaStreamSynchronize(s));

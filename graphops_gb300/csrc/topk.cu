@@ -5,11 +5,19 @@
 // unspecified; here equal scores are ordered by index, which selects the same
 // set and makes the output deterministic.
 //
-// One CTA per row: an MSB-first radix select on the value's bit pattern
-// (finite positive IEEE values order like their bits) finds the k-th largest
-// key in 4 (FP32) or 8 (FP64) passes of 8 bits over the row; a collection
-// pass takes every key above it and the lowest-index keys equal to it; a
-// bitonic sort in shared memory orders the at most k survivors.
+// One CTA per segment of a row: an MSB-first radix select on the value's bit
+// pattern (finite positive IEEE values order like their bits) finds the k-th
+// largest key in 4 (FP32) or 8 (FP64) passes of 8 bits over the segment; a
+// collection pass takes every key above it and the lowest-index keys equal
+// to it; a bitonic sort in shared memory orders the at most k survivors.
+// Rows longer than two segments run in two stages, so that a row spreads
+// over many SMs: every segment's top k (stage 1), then the top k of the
+// row's candidates (stage 2).  The result is the same: every key of the
+// row's top k is in its segment's top k (fewer than k keys of the row exceed
+// the k-th largest, and each segment keeps its lowest-index equal keys up to
+// k), and the candidates come in segment order, each segment's sorted by
+// index among equal keys, so the lowest candidate position among equal keys
+// is the lowest row index.
 #include <cstdint>
 
 #include "objects.cuh"
@@ -19,6 +27,8 @@ namespace {
 
 constexpr int kTThreads = 512;
 constexpr int kMaxK = 1024;
+constexpr int64_t kSegLen = 32768;        // entries per segment of a long row
+constexpr int64_t kRowsPerLaunch = 16384;  // rows per launch (grid size = rows x segments)
 
 template <class V>
 struct KeyOf;
@@ -37,8 +47,15 @@ struct KeyOf<double> {
   }
 };
 
+// Block (r, b) = blockIdx.x = r * nseg + b takes entries [b * seg_len,
+// min(n, (b + 1) * seg_len)) of row r (rows row_stride apart) and writes k
+// entries at blockIdx.x * k: the top `take` by (key desc, index asc), their
+// row indices (through idx_map when given), then padding (value 0: not a
+// key; index -1); count_out[blockIdx.x] = take.
 template <class V>
-__global__ void __launch_bounds__(kTThreads) topk_rows(const V *__restrict__ x, int64_t n, int k,
+__global__ void __launch_bounds__(kTThreads) topk_rows(const V *__restrict__ x, int64_t row_stride, int64_t seg_len,
+                                                       int64_t n_row, int nseg, int k,
+                                                       const int64_t *__restrict__ idx_map,
                                                        int64_t *__restrict__ idx_out, V *__restrict__ val_out,
                                                        int64_t *__restrict__ count_out) {
   using KO = KeyOf<V>;
@@ -51,7 +68,11 @@ __global__ void __launch_bounds__(kTThreads) topk_rows(const V *__restrict__ x, 
   __shared__ int64_t sidx[kMaxK];
   __shared__ int s_cnt;
   __shared__ int s_eqbase;
-  const V *row = x + (int64_t)blockIdx.x * n;
+  const int64_t r = blockIdx.x / nseg, seg = blockIdx.x % nseg;
+  const int64_t off = r * row_stride + seg * seg_len;
+  const V *row = x + off;
+  const int64_t n = min(seg_len, n_row - seg * seg_len);
+  const int64_t o = (int64_t)blockIdx.x * k;
   // number of valid keys (capped at k): the answer holds min(k, valid) entries
   if (threadIdx.x == 0) s_valid = 0;
   __syncthreads();
@@ -63,6 +84,10 @@ __global__ void __launch_bounds__(kTThreads) topk_rows(const V *__restrict__ x, 
   __syncthreads();
   const int take = s_valid < k ? s_valid : k;
   if (take == 0) {
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+      idx_out[o + i] = -1;
+      val_out[o + i] = (V)0;
+    }
     if (threadIdx.x == 0) count_out[blockIdx.x] = 0;
     return;
   }
@@ -165,14 +190,36 @@ __global__ void __launch_bounds__(kTThreads) topk_rows(const V *__restrict__ x, 
       __syncthreads();
     }
   }
-  for (int i = threadIdx.x; i < take; i += blockDim.x) {
-    idx_out[(int64_t)blockIdx.x * k + i] = sidx[i];
-    val_out[(int64_t)blockIdx.x * k + i] = row[sidx[i]];
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    if (i < take) {
+      idx_out[o + i] = idx_map ? idx_map[off + sidx[i]] : seg * seg_len + sidx[i];
+      val_out[o + i] = row[sidx[i]];
+    } else {
+      idx_out[o + i] = -1;
+      val_out[o + i] = (V)0;
+    }
   }
   if (threadIdx.x == 0) count_out[blockIdx.x] = take;
 }
 
-// normalize (src/topk.rs:53-61): divide by the sum when the sum > 0
+// normalize (src/topk.rs:53-61): divide by the sum when the sum > 0.  The
+// sum in a fixed order: per block of the grid (strided, then a tree), then
+// the block sums by one block.
+constexpr int kSumBlocks = 1024;
+__global__ void sum_f64_part(const double *x, int64_t n, double *part) {
+  __shared__ double sh[256];
+  double t = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    t += x[i];
+  sh[threadIdx.x] = t;
+  __syncthreads();
+  for (int q = blockDim.x / 2; q > 0; q >>= 1) {
+    if ((int)threadIdx.x < q) sh[threadIdx.x] += sh[threadIdx.x + q];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
 __global__ void sum_f64(const double *x, int64_t n, double *out) {
   __shared__ double sh[1024];
   double t = 0.0;
@@ -203,31 +250,47 @@ Status topk_impl(Ctx *ctx, const V *x, int64_t rows, int64_t n, int64_t k, int64
     return Status::ok();
   }
   cudaStream_t s = ctx->stream;
-  int64_t *d_idx = nullptr, *d_cnt = nullptr;
-  V *d_val = nullptr;
+  int64_t *d_idx = nullptr, *d_cnt = nullptr, *c_idx = nullptr, *c_cnt = nullptr;
+  V *d_val = nullptr, *c_val = nullptr;
   Status st;
   auto fail = [&](cudaError_t e) {
     return Status{e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA, cudaGetErrorString(e)};
   };
-  cudaError_t e = cudaMalloc(&d_idx, sizeof(int64_t) * rows * k);
-  if (e == cudaSuccess) e = cudaMalloc(&d_val, sizeof(V) * rows * k);
-  if (e == cudaSuccess) e = cudaMalloc(&d_cnt, sizeof(int64_t) * rows);
-  if (e == cudaSuccess) {
-    for (int64_t r0 = 0; r0 < rows && e == cudaSuccess; r0 += 65535) {
-      const int64_t nr = rows - r0 < 65535 ? rows - r0 : 65535;
-      topk_rows<V><<<(unsigned)nr, kTThreads, 0, s>>>(x + r0 * n, n, (int)k, d_idx + r0 * k, d_val + r0 * k,
-                                                       d_cnt + r0);
-      e = cudaGetLastError();
+  const int64_t nseg = n > 2 * kSegLen ? ceil_div<int64_t>(n, kSegLen) : 1;
+  cudaError_t e = dev_malloc_async((void **)&d_idx, sizeof(int64_t) * rows * k, s);
+  if (e == cudaSuccess) e = dev_malloc_async((void **)&d_val, sizeof(V) * rows * k, s);
+  if (e == cudaSuccess) e = dev_malloc_async((void **)&d_cnt, sizeof(int64_t) * rows, s);
+  if (nseg > 1) {
+    if (e == cudaSuccess) e = dev_malloc_async((void **)&c_idx, sizeof(int64_t) * rows * nseg * k, s);
+    if (e == cudaSuccess) e = dev_malloc_async((void **)&c_val, sizeof(V) * rows * nseg * k, s);
+    if (e == cudaSuccess) e = dev_malloc_async((void **)&c_cnt, sizeof(int64_t) * rows * nseg, s);
+  }
+  for (int64_t r0 = 0; r0 < rows && e == cudaSuccess; r0 += kRowsPerLaunch) {
+    const int64_t nr = rows - r0 < kRowsPerLaunch ? rows - r0 : kRowsPerLaunch;
+    if (nseg == 1) {
+      topk_rows<V><<<(unsigned)nr, kTThreads, 0, s>>>(x + r0 * n, n, n, n, 1, (int)k, nullptr, d_idx + r0 * k,
+                                                       d_val + r0 * k, d_cnt + r0);
+    } else {
+      const int64_t nc = nseg * k;  // candidates per row
+      topk_rows<V><<<(unsigned)(nr * nseg), kTThreads, 0, s>>>(x + r0 * n, n, kSegLen, n, (int)nseg, (int)k, nullptr,
+                                                                c_idx + r0 * nc, c_val + r0 * nc, c_cnt + r0 * nseg);
+      topk_rows<V><<<(unsigned)nr, kTThreads, 0, s>>>(c_val + r0 * nc, nc, nc, nc, 1, (int)k, c_idx + r0 * nc,
+                                                       d_idx + r0 * k, d_val + r0 * k, d_cnt + r0);
     }
+    e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(idx, d_idx, sizeof(int64_t) * rows * k, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(val, d_val, sizeof(V) * rows * k, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d_cnt, sizeof(int64_t) * rows, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) st = fail(e);
-  cudaFree(d_idx);
-  cudaFree(d_val);
-  cudaFree(d_cnt);
+  free_async(d_idx, s);
+  free_async(d_val, s);
+  free_async(d_cnt, s);
+  free_async(c_idx, s);
+  free_async(c_val, s);
+  free_async(c_cnt, s);
+  cudaStreamSynchronize(s);
   return st;
 }
 
@@ -264,14 +327,17 @@ int gops_normalize_f64_device(gops_ctx *ctx, double *scores_device, int64_t n) {
   if (n == 0) return GOPS_OK;
   cudaSetDevice(c.device);
   double *d_sum = nullptr;
-  cudaError_t e = cudaMalloc(&d_sum, sizeof(double));
+  const int nb = blocks_for(n, 256, kSumBlocks);
+  cudaError_t e = dev_malloc_async((void **)&d_sum, sizeof(double) * (nb + 1), c.stream);
   if (e == cudaSuccess) {
-    sum_f64<<<1, 1024, 0, c.stream>>>(scores_device, n, d_sum);
+    sum_f64_part<<<nb, 256, 0, c.stream>>>(scores_device, n, d_sum + 1);
+    sum_f64<<<1, 1024, 0, c.stream>>>(d_sum + 1, nb, d_sum);
     div_f64<<<blocks_for(n, 256, 4096), 256, 0, c.stream>>>(scores_device, n, d_sum);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
-  cudaFree(d_sum);
+  free_async(d_sum, c.stream);
+  cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return c.set(Status{GOPS_ERR_CUDA, cudaGetErrorString(e)});
   return GOPS_OK;
 }

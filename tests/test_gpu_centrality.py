@@ -135,3 +135,41 @@ def test_hits_rmat_matches_oracle(scale):
     dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
     _, _, it, d, conv = dg.hits_run(200, 1e-9)
     assert abs(it - rit) <= 1 and conv == rconv
+
+
+def test_long_rows_summed_in_chunks_match_oracle():
+    """Hub rows above 2,048 edges are summed in 8,192-edge chunks (a block
+    each) and the chunk sums added in order: Katz, eigenvector centrality
+    and HITS on a graph whose hubs have ~20,000 in- and out-edges (several
+    chunks, the last partial) against the oracle, and R-MAT scale 17 (hubs of
+    a few thousand edges)."""
+    rng = np.random.default_rng(7)
+    n = 20000
+    src = [np.zeros(n - 1, np.int64), np.arange(1, n), rng.integers(0, n, 60000)]
+    dst = [np.arange(1, n), np.full(n - 1, 1), rng.integers(0, n, 60000)]
+    u = np.concatenate(src)
+    v = np.concatenate(dst)
+    o = np.argsort(u, kind="stable")
+    u, v = u[o], v[o]
+    rp = np.zeros(n + 1, np.int64)
+    np.add.at(rp, u + 1, 1)
+    rp = np.cumsum(rp)
+    col = v.astype(np.int32)
+    assert np.diff(rp).max() > 2 * 8192 and np.bincount(col, minlength=n).max() > 2 * 8192
+    g = gen.rmat(17, 16, seed=17)
+    for rp_, col_ in ((rp, col), (g.row_ptr, g.col)):
+        dg = go.DeviceGraph.from_csr(rp_, col_)
+        indeg = np.bincount(col_, minlength=len(rp_) - 1)
+        alpha = 0.5 / max(int(indeg.max()), 1)
+        r = go.katz_centrality_run(dg, go.KatzConfig(alpha, 1.0, 1000, 1e-9))
+        s, it, diff, conv = port.katz_run(rp_, col_, alpha, 1.0, 1000, 1e-9)
+        assert r.iterations == it and r.converged == conv
+        assert rel_l1(r.scores, s) <= REL
+        r = go.eigenvector_centrality_run(dg, 200, 1e-9)
+        s, it, diff, conv = port.eigenvector_run(rp_, col_, 200, 1e-9)
+        assert r.iterations == it and r.converged == conv
+        assert rel_l1(r.scores, s) <= REL
+        hub, auth, it, d, conv = dg.hits_run(200, 1e-9)
+        rh, ra, rit, rd, rconv = port.hits_run(rp_, col_, 200, 1e-9)
+        assert abs(it - rit) <= 1 and conv == rconv
+        assert rel_l1(hub, rh) <= 1e-10 and rel_l1(auth, ra) <= 1e-10

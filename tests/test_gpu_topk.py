@@ -65,3 +65,38 @@ def test_normalize_device():
     z = torch.tensor([0.0, 0.0], dtype=torch.float64, device="cuda")
     normalize_device(z.data_ptr(), 2)                       # sum 0: unchanged
     assert (z.cpu().numpy() == 0).all()
+
+
+def test_long_rows_two_stage_ties_across_segments():
+    """Rows longer than two 32,768-entry segments run as every segment's top
+    k, then the top k of the candidates: the same entries and order as one
+    pass, including ties of the k-th value spread over many segments (the
+    lowest indices win) and more equal maxima than k."""
+    rng = np.random.default_rng(1)
+    n = 300000
+    x = rng.random(n)
+    x[rng.integers(0, n, 5000)] = 2.0            # 5,000 equal maxima over every segment
+    x[rng.integers(0, n, 3000)] = np.nan
+    got = top_k_device(torch.tensor(x, device="cuda").data_ptr(), n, 1024)
+    assert [i for i, _ in got] == ref_top_k(x, 1024)
+    y = np.floor(rng.random(n) * 40) / 40.0      # 40 levels: the k-th value tied across segments
+    got = top_k_device(torch.tensor(y, device="cuda").data_ptr(), n, 700)
+    assert [i for i, _ in got] == ref_top_k(y, 700)
+    rows = (np.floor(rng.random((5, 200000)) * 1000) / 1000).astype(np.float32)
+    rows[2] = -1.0                               # no valid entry
+    rows[3, :150000] = 0.5
+    block = torch.tensor(rows, device="cuda")
+    idx, val, cnt = top_k_rows_device(block.data_ptr(), 5, 200000, 100)
+    for r in range(5):
+        want = ref_top_k(rows[r].astype(np.float64), 100)
+        assert cnt[r] == len(want) and idx[r, :cnt[r]].tolist() == want
+        assert val[r, :cnt[r]].tolist() == [float(rows[r, i]) for i in want]
+
+
+def test_normalize_long_vector():
+    rng = np.random.default_rng(2)
+    x = rng.random(3_000_000)
+    t = torch.tensor(x, device="cuda")
+    normalize_device(t.data_ptr(), x.shape[0])
+    y = t.cpu().numpy()
+    assert np.abs(y - x / x.sum()).max() <= 1e-15 * np.abs(x / x.sum()).max() * 4

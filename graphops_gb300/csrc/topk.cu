@@ -102,9 +102,16 @@ __global__ void __launch_bounds__(kTThreads) topk_rows(const V *__restrict__ x, 
     for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
     __syncthreads();
     const K prefix = s_prefix;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-      const K kk = KO::key(row[i]);
-      if (kk != 0 && (kk & mask) == prefix) atomicAdd(&hist[(unsigned)((kk >> shift) & 0xFF)], 1u);
+    // warp-aggregated increments: the keys of a row often share their high
+    // bytes, so one atomic per distinct bin per warp instead of per key
+    const int lane = threadIdx.x & 31;
+    for (int64_t base = 0; base < n; base += blockDim.x) {
+      const int64_t i = base + threadIdx.x;
+      const K kk = i < n ? KO::key(row[i]) : (K)0;
+      const bool hit = kk != 0 && (kk & mask) == prefix;
+      const unsigned bin = hit ? (unsigned)((kk >> shift) & 0xFF) : 256u + (unsigned)lane;  // misses: unique keys
+      const unsigned peers = __match_any_sync(0xffffffffu, bin);
+      if (hit && lane == __ffs(peers) - 1) atomicAdd(&hist[bin], (unsigned)__popc(peers));
     }
     __syncthreads();
     if (threadIdx.x == 0) {

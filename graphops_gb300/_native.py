@@ -64,6 +64,7 @@ class WarmStats(ctypes.Structure):
 SIGNATURES = [
     ("gops_abi_version", ctypes.c_int, []),
     ("gops_debug_fail_allocations_after", ctypes.c_int, [ctypes.c_int64]),
+    ("gops_debug_tc_gemm", ctypes.c_int, [_p, ctypes.c_int, _p, _p, _p, _i64, _p, _p, _p, _p, _p]),
     ("gops_ctx_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_p)]),
     ("gops_ctx_destroy", None, [_p]),
     ("gops_last_error", ctypes.c_char_p, [_p]),

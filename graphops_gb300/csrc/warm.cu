@@ -874,6 +874,7 @@ WarmModel::~WarmModel() {
                   rhs, chol, lpart, x0};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  if (tc_err_h) cudaFreeHost(tc_err_h);
 }
 
 namespace {
@@ -1412,11 +1413,13 @@ Status warm_train(WarmModel &w, const gops_config *cfg, int64_t nsets, const int
         ++st.steps;
       }
       GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+      GOPS_TRY(nn_check(w));
       t_fit += wall_ms() - tb;
     }
   }
   GOPS_TRY(nn_forward(w));
   GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+  GOPS_TRY(nn_check(w));
   st.target_ms = t_targets;
   st.fit_ms = t_fit;
   if (stats) *stats = st;
@@ -1426,7 +1429,11 @@ Status warm_train(WarmModel &w, const gops_config *cfg, int64_t nsets, const int
 Status warm_predict(WarmModel &w, double damping, int64_t nsets, const int64_t *seed_ptr, const int32_t *seed_idx,
                     float *x0, double *r1_cold) {
   cudaStream_t s = w.ctx->stream;
-  if (!w.weights_fresh) GOPS_TRY(nn_forward(w));
+  if (!w.weights_fresh) {
+    GOPS_TRY(nn_forward(w));
+    GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+    GOPS_TRY(nn_check(w));
+  }
   const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nsets, std::max<int64_t>(w.cfg.chunk, 1)));
   GOPS_TRY(ensure_push(w, chunk));
   for (int64_t c0 = 0; c0 < nsets; c0 += chunk) {
@@ -1547,7 +1554,7 @@ Status warm_loss_grad(WarmModel &w, double damping, int64_t nsets, const int64_t
   GOPS_TRY(nn_backward(w));
   GOPS_CUDA_TRY(cudaMemcpyAsync(grad, w.grad, sizeof(float) * kPCount, cudaMemcpyDeviceToHost, s));
   GOPS_CUDA_TRY(cudaStreamSynchronize(s));
-  return Status::ok();
+  return nn_check(w);
 }
 
 Status warm_push_one(WarmModel &w, double damping, const int32_t *seeds, int64_t nseeds, double *local, double *mix,

@@ -63,6 +63,8 @@ struct WarmModel {
   float *du = nullptr;             // n: dL/du
   float *cw = nullptr;             // r: sum of w per cluster
   float *grad = nullptr;           // kPCount
+  int *tc_err_h = nullptr;         // pinned, mapped: set by a tensor-core GEMM whose handshake wait ran out
+  int *tc_err_d = nullptr;         // the same flag, device address
   float *part = nullptr;           // GEMM / reduction partials
   int64_t part_cap = 0;
   bool weights_fresh = false;      // w/cw computed for the current parameters
@@ -107,6 +109,9 @@ Status nn_forward(WarmModel &w);
 // gradient of the parameters from du (dL/du), into w.grad
 Status nn_backward(WarmModel &w);
 Status nn_adam(WarmModel &w, float lr);
+// error when a tensor-core GEMM of the network reported a failed handshake
+// (read after a stream synchronisation)
+Status nn_check(const WarmModel &w);
 
 }  // namespace gops
 

@@ -6,16 +6,19 @@
 //   u  = H2 w3 + b3,  w = exp(u)                    per-node weight
 //
 // Activations and the GEMM operands are BF16; every product accumulates in
-// FP32 on the tensor cores (mma.sync m16n8k16).  At these shapes (K, N <=
-// 256, M = n) the GEMMs move far more bytes than they multiply, so they are
-// bound by HBM, not by the tensor pipe.  The backward pass runs the same two
-// GEMM forms: row tiles (dX = dY W^T) and a reduction over rows
-// (dW = X^T dY) with per-CTA partials summed in a fixed order, so gradients
-// are bit-reproducible.
+// FP32 on the tensor cores.  At these shapes (K, N <= 256, M = n) the GEMMs
+// move far more bytes than they multiply, so they are bound by HBM, not by
+// the tensor pipe.  The two large row-tile GEMMs -- layer 2 (K = 256, with
+// the bias, ReLU and head fused) and the input gradient dX = dH2 W2^T (N =
+// 256) -- run on tcgen05 with TMA-fed operands (warm_tc.cu).  Layer 1 (K = 48,
+// not a multiple of the 64-column swizzled k-block) and the weight gradients
+// (dW = X^T dY, a reduction over the rows with per-CTA partials summed in a
+// fixed order, so gradients are bit-reproducible) use mma.sync m16n8k16.
 #include <cmath>
 #include <vector>
 
 #include "warm.cuh"
+#include "warm_tc.cuh"
 
 namespace gops {
 
@@ -37,27 +40,18 @@ constexpr int kBM = 64;    // rows per tile (row-tile GEMM)
 constexpr int kBN = 128;   // output columns per CTA
 constexpr int kGT = 256;   // threads per GEMM CTA (8 warps: 2 along M x 4 along N)
 
-enum { EPI_RELU = 0, EPI_LAYER2 = 1, EPI_STORE = 2 };
-
-struct EpiArgs {
-  bf16 *out;           // M x ld (bf16)
-  int ld;
-  const float *bias;   // EPI_LAYER2: b2
-  const float *head;   // EPI_LAYER2: w3 (kBN) and b3 (head[kBN])
-  float *w;            // EPI_LAYER2: exp(u)
-};
-
-// Y[M x 128-tile] = [Xa | Xb] (M x K) . Bt^T, Bt = [Ntot][K] row-major (the
-// B operand in the mma "col" layout).  blockIdx.y selects the 128-column
-// tile.  Persistent over row tiles; Bt's tile is staged once per CTA.
-template <int K, int EPI>
+// out[M x 128-tile] = relu([Xa | Xb] (M x K) . Bt^T) (BF16, row stride ld),
+// Bt = [Ntot][K] row-major (the B operand in the mma "col" layout).
+// blockIdx.y selects the 128-column tile.  Persistent over row tiles; Bt's
+// tile is staged once per CTA.  Layer 1 (K = 48).
+template <int K>
 __global__ void __launch_bounds__(kGT) gemm_rows(const bf16 *__restrict__ xa, int ka, const bf16 *__restrict__ xb,
-                                                 const bf16 *__restrict__ bt, int64_t M, EpiArgs e) {
+                                                 const bf16 *__restrict__ bt, int64_t M, bf16 *__restrict__ out,
+                                                 int ld) {
   constexpr int LD = K + 8;  // padded row (bf16): conflict-free fragment loads
   extern __shared__ __align__(16) unsigned char smem_raw[];
   bf16 *Bs = reinterpret_cast<bf16 *>(smem_raw);  // [kBN][LD]
   bf16 *Xs = Bs + kBN * LD;                       // [kBM][LD]
-  __shared__ float red[kBM][4];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int wm = wid & 1, wn = wid >> 1;
   const int g = lane >> 2, t4 = lane & 3;
@@ -114,7 +108,6 @@ __global__ void __launch_bounds__(kGT) gemm_rows(const bf16 *__restrict__ xa, in
     }
     // epilogue: element (row, col) of acc[a][b][q]:
     //   row = wm*32 + a*16 + g + (q >= 2 ? 8 : 0), col = wn*32 + b*8 + 2*t4 + (q & 1)
-    float hs[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // EPI_LAYER2: partial head dot per owned row
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
@@ -124,43 +117,10 @@ __global__ void __launch_bounds__(kGT) gemm_rows(const bf16 *__restrict__ xa, in
           const int rl = wm * 32 + a * 16 + g + hq * 8;
           const int col = wn * 32 + b * 8 + 2 * t4;
           const int64_t row = row0 + rl;
-          float v0 = acc[a][b][hq * 2], v1 = acc[a][b][hq * 2 + 1];
-          if constexpr (EPI == EPI_LAYER2) {
-            v0 += e.bias[col];
-            v1 += e.bias[col + 1];
-          }
-          if constexpr (EPI != EPI_STORE) {
-            v0 = fmaxf(v0, 0.f);
-            v1 = fmaxf(v1, 0.f);
-          }
-          const __nv_bfloat162 pv = __floats2bfloat162_rn(v0, v1);
-          if constexpr (EPI == EPI_LAYER2) {
-            // the head reads the stored (rounded) activations
-            const float2 r2 = __bfloat1622float2(pv);
-            hs[a][hq] = fmaf(r2.x, e.head[col], fmaf(r2.y, e.head[col + 1], hs[a][hq]));
-          }
-          if (row < M)
-            *reinterpret_cast<__nv_bfloat162 *>(&e.out[row * e.ld + (int64_t)nt * kBN + col]) = pv;
+          const __nv_bfloat162 pv =
+              __floats2bfloat162_rn(fmaxf(acc[a][b][hq * 2], 0.f), fmaxf(acc[a][b][hq * 2 + 1], 0.f));
+          if (row < M) *reinterpret_cast<__nv_bfloat162 *>(&out[row * ld + (int64_t)nt * kBN + col]) = pv;
         }
-    if constexpr (EPI == EPI_LAYER2) {
-#pragma unroll
-      for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int hq = 0; hq < 2; ++hq) {
-          float v = hs[a][hq];
-          v += __shfl_xor_sync(0xffffffffu, v, 1);
-          v += __shfl_xor_sync(0xffffffffu, v, 2);
-          if (t4 == 0) red[wm * 32 + a * 16 + g + hq * 8][wn] = v;
-        }
-      __syncthreads();
-      if (tid < kBM) {
-        const int64_t row = row0 + tid;
-        // fixed summation order over the four column groups
-        float u = ((red[tid][0] + red[tid][1]) + (red[tid][2] + red[tid][3])) + e.head[kBN];
-        u = fminf(fmaxf(u, -20.f), 20.f);
-        if (row < M) e.w[row] = expf(u);
-      }
-    }
   }
 }
 
@@ -408,17 +368,17 @@ int gemm_ctas(const WarmModel &w, int64_t rows) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)w.ctx->num_sms * 2));
 }
 
-template <int K, int EPI>
-Status launch_rows(WarmModel &w, const bf16 *xa, int ka, const bf16 *xb, const bf16 *bt, int ntiles,
-                   const EpiArgs &e) {
+template <int K>
+Status launch_rows(WarmModel &w, const bf16 *xa, int ka, const bf16 *xb, const bf16 *bt, int ntiles, bf16 *out,
+                   int ld) {
   const size_t smem = sizeof(bf16) * (size_t)(kBN + kBM) * (K + 8);
   static bool attr = false;  // per instantiation
   if (!attr) {
-    GOPS_CUDA_TRY(cudaFuncSetAttribute(gemm_rows<K, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GOPS_CUDA_TRY(cudaFuncSetAttribute(gemm_rows<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
   dim3 grid(gemm_ctas(w, w.n), ntiles);
-  gemm_rows<K, EPI><<<grid, kGT, smem, w.ctx->stream>>>(xa, ka, xb, bt, w.n, e);
+  gemm_rows<K><<<grid, kGT, smem, w.ctx->stream>>>(xa, ka, xb, bt, w.n, out, ld);
   GOPS_CUDA_TRY(cudaGetLastError());
   return Status::ok();
 }
@@ -460,6 +420,16 @@ Status nn_alloc(WarmModel &w) {
   const int64_t heads = (n + kHeadRows - 1) / kHeadRows;
   w.part_cap = std::max<int64_t>((int64_t)w.ctx->num_sms * 2 * 2 * kWH * kBN, heads * (2 * kWH + 1));
   GOPS_CUDA_TRY(cudaMalloc(&w.part, sizeof(float) * w.part_cap));
+  GOPS_CUDA_TRY(cudaHostAlloc(&w.tc_err_h, sizeof(int), cudaHostAllocMapped));
+  *w.tc_err_h = 0;
+  GOPS_CUDA_TRY(cudaHostGetDevicePointer(&w.tc_err_d, w.tc_err_h, 0));
+  return Status::ok();
+}
+
+Status nn_check(const WarmModel &w) {
+  const int code = w.tc_err_h ? *(volatile int *)w.tc_err_h : 0;
+  if (code) return Status{GOPS_ERR_CUDA, "warm start: a tensor-core GEMM handshake timed out (stage " +
+                                             std::to_string(code) + ")"};
   return Status::ok();
 }
 
@@ -493,12 +463,11 @@ Status nn_refresh_bf16(WarmModel &w) {
 
 Status nn_forward(WarmModel &w) {
   cudaStream_t s = w.ctx->stream;
-  EpiArgs e1{w.h1, kWH, nullptr, nullptr, nullptr};
-  GOPS_TRY((launch_rows<kWIn, EPI_RELU>(w, w.x1, kWIn, nullptr, w.w1t, 1, e1)));
+  GOPS_TRY(launch_rows<kWIn>(w, w.x1, kWIn, nullptr, w.w1t, 1, w.h1, kWH));
   agg_in_128<<<blocks_for(w.n, 8, w.ctx->num_sms * 16), 256, 0, s>>>(w.in_rp, w.in_col, w.inv_in, w.h1, w.n, w.a1);
   GOPS_CUDA_TRY(cudaGetLastError());
-  EpiArgs e2{w.h2, kWH, w.params + kPB2, w.params + kPW3, w.w};
-  GOPS_TRY((launch_rows<2 * kWH, EPI_LAYER2>(w, w.h1, kWH, w.a1, w.w2t, 1, e2)));
+  const TcEpi e2{w.h2, kWH, w.params + kPB2, w.params + kPW3, w.w};
+  GOPS_TRY(tc_layer2(w.ctx, w.h1, w.a1, w.w2t, w.n, e2, w.tc_err_d));
   cluster_sums<<<blocks_for(w.r, 8, 1024), 256, 0, s>>>(w.members, w.cl_off, w.r, w.w, w.cw);
   GOPS_CUDA_TRY(cudaGetLastError());
   w.weights_fresh = true;
@@ -515,8 +484,8 @@ Status nn_backward(WarmModel &w) {
   sum_parts<<<2, 256, 0, s>>>(w.part, std::max<int64_t>(heads, 1), 2 * kWH + 1, 2 * kWH + 1, w.grad + kPB2);
   GOPS_CUDA_TRY(cudaGetLastError());
   GOPS_TRY(launch_reduce<2 * kWH>(w, w.h1, kWH, w.a1, w.g2, w.grad + kPW2));
-  EpiArgs e{w.gx, 2 * kWH, nullptr, nullptr, nullptr};
-  GOPS_TRY((launch_rows<kWH, EPI_STORE>(w, w.g2, kWH, nullptr, w.w2, 2, e)));
+  const TcEpi e{w.gx, 2 * kWH, nullptr, nullptr, nullptr};
+  GOPS_TRY(tc_input_grad(w.ctx, w.g2, w.w2, w.n, e, w.tc_err_d));
   h1_backward<<<blocks_for(w.n, 8, w.ctx->num_sms * 16), 256, 0, s>>>(w.out_rp, w.out_col, w.inv_in, w.gx, w.h1,
                                                                        w.n, w.g2);
   GOPS_CUDA_TRY(cudaGetLastError());

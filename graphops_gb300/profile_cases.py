@@ -15,6 +15,10 @@ cases:
              bench's k-tile): spmm_mixed and spmm_f32
   centrality Katz, eigenvector centrality and HITS on R-MAT scale 21
   topk       top-100 of a 2 M-entry FP64 score vector and of 128 FP32 rows
+  warm       the warm start's network on a stochastic block model (n = 500,000):
+             three loss / gradient evaluations of 16 sets, each one forward
+             (layer 1, aggregation, the tcgen05 layer 2) and one backward
+             (the tcgen05 input gradient, the weight-gradient reductions)
 """
 from __future__ import annotations
 
@@ -84,8 +88,21 @@ def case_topk():
         top_k_rows_device(rows.data_ptr(), 128, n, 100, ctx=ctx)
 
 
+def case_warm():
+    from . import _native, gen, warm
+    g = gen.sbm(500000, 64, 1.2, 16.0, 4.0, seed=3)
+    dg = _native.DeviceGraph.from_csr(g.row_ptr, g.col)
+    model = warm.WarmStart(dg, g.row_ptr, g.col, warm.default_config(clusters=72))
+    sp, si = gen.seed_sets(g, 16, 1, 32, seed=11)
+    rng = np.random.default_rng(5)
+    t = rng.random((16, g.n), dtype=np.float32)
+    t /= t.sum(axis=1, keepdims=True)
+    for _ in range(3):
+        model.loss_grad(0.85, sp, si, t)
+
+
 CASES = {"pagerank": case_pagerank, "upload": case_upload, "batched": case_batched,
-         "centrality": case_centrality, "topk": case_topk}
+         "centrality": case_centrality, "topk": case_topk, "warm": case_warm}
 
 
 def main(argv):

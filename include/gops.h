@@ -89,6 +89,18 @@ int gops_abi_version(void);
  * (GOPS_ERR_OOM from the call that needed it), until called with count < 0.
  * Lets tests drive every allocation-failure path without a GPU fault. */
 int gops_debug_fail_allocations_after(int64_t count);
+/* Test hook (no reference counterpart): one call of the warm start's
+ * tensor-core row-tile GEMM (tcgen05, TMA-fed) on caller device buffers, all
+ * BF16 row-major but bias/head/w (FP32).  Synchronous.
+ *   mode 0 (layer 2): out[m][128] = relu([xa | xb] bt^T + bias) with xa, xb
+ *     m x 128 and bt 128 x 256; w[i] = exp(clamp(out[i] . head[0:128] +
+ *     head[128], -20, 20)) from the rounded out row.
+ *   mode 1 (input gradient): out[m][256] = xa bt^T, xa m x 128, bt 256 x 128;
+ *     xb, bias, head and w are not used.
+ * err: a device int, set nonzero when a handshake wait in the kernel ran out
+ * (the kernel then winds down instead of hanging). */
+int gops_debug_tc_gemm(gops_ctx *ctx, int mode, const void *xa, const void *xb, const void *bt, int64_t m, void *out,
+                       const float *bias, const float *head, float *w, int *err);
 int gops_ctx_create(int device, gops_ctx **out);
 void gops_ctx_destroy(gops_ctx *ctx);
 const char *gops_last_error(const gops_ctx *ctx);

@@ -26,6 +26,7 @@ constexpr int kCThreads = 256;
 constexpr int kSub = 8;  // lanes per row
 constexpr int kCBlocks = 1024;
 constexpr int64_t kLong = 2048;    // rows with more edges are summed in chunks, a block each
+constexpr int64_t kLight = 8;      // rows with fewer edges are summed by one lane each
 constexpr int64_t kChunkE = 8192;  // edges per chunk
 
 // sum over the kSub lanes of this lane's group.  The mask names the group
@@ -75,18 +76,29 @@ struct SumOp {  // HITS: y[v] = sum over the row's edges (no self term); sum y^2
 
 // Rows with at most kLong edges: kSub lanes per row, four gathers in flight
 // per lane (each lane adds its edges e, e + kSub, ... in order).  Longer rows
-// are skipped here and summed in chunks (chunk_sums / long_rows).  x has
+// are skipped here and summed in chunks (chunk_sums / long_rows).  The four
+// row groups of a warp run together until the longest of their rows ends, so
+// rows are taken in non-increasing degree class: the in-edge CSR's rows
+// already are (relabelled by in-degree); the out-adjacency, in the caller's
+// node order, goes through a row order sorted by degree class.  x has
 // n + 1 entries when the rows are the padded in-edge CSR (x[n] = 0 for the
 // padding edges).  part[b * kSlots + j]: this block's global sums.
+// Rows are taken in the order `order` lists them (n_rows of them) or, with
+// order == nullptr, as 0..n_rows-1; the first n_heavy (the rows with at least
+// kLight edges, long ones included, which are skipped) by kSub-lane groups,
+// the rest (fewer than kLight edges: most rows of a power-law graph) by one
+// lane each, which adds the row's edges in order.
 template <class Op>
 __global__ void __launch_bounds__(kCThreads) short_rows(const int64_t *__restrict__ rp, const int32_t *__restrict__ col,
-                                                        int64_t n, Op op, const double *__restrict__ x,
+                                                        const int32_t *__restrict__ order, int64_t n_heavy,
+                                                        int64_t n_rows, Op op, const double *__restrict__ x,
                                                         double *__restrict__ y, double *__restrict__ part) {
   __shared__ double sh[kCThreads];
   const int lane = threadIdx.x & (kSub - 1);
   const int64_t groups = (int64_t)gridDim.x * (kCThreads / kSub);
   double acc[2] = {0.0, 0.0};
-  for (int64_t v = (int64_t)blockIdx.x * (kCThreads / kSub) + threadIdx.x / kSub; v < n; v += groups) {
+  for (int64_t i = (int64_t)blockIdx.x * (kCThreads / kSub) + threadIdx.x / kSub; i < n_heavy; i += groups) {
+    const int64_t v = order ? (int64_t)order[i] : i;
     const int64_t eb = rp[v], ee = rp[v + 1];
     if (ee - eb > kLong) continue;  // a long row: chunk_sums / long_rows
     double s = 0.0;
@@ -106,6 +118,25 @@ __global__ void __launch_bounds__(kCThreads) short_rows(const int64_t *__restric
       y[v] = yv;
       op.add(x[v], yv, acc);
     }
+  }
+  for (int64_t i = n_heavy + (int64_t)blockIdx.x * kCThreads + threadIdx.x; i < n_rows;
+       i += (int64_t)gridDim.x * kCThreads) {
+    const int64_t v = order ? (int64_t)order[i] : i;
+    const int64_t eb = rp[v], ee = rp[v + 1];
+    double s = 0.0;
+    int64_t e = eb;
+    for (; e + 4 <= ee; e += 4) {
+      const int32_t c0 = col[e], c1 = col[e + 1], c2 = col[e + 2], c3 = col[e + 3];
+      const double g0 = x[c0], g1 = x[c1], g2 = x[c2], g3 = x[c3];
+      s += g0;
+      s += g1;
+      s += g2;
+      s += g3;
+    }
+    for (; e < ee; ++e) s += x[col[e]];
+    const double yv = op.y(x[v], s);
+    y[v] = yv;
+    op.add(x[v], yv, acc);
   }
   for (int j = 0; j < Op::kSlots; ++j) block_part(acc[j], sh, part, Op::kSlots, j);
 }
@@ -278,12 +309,82 @@ struct LongPlan {
   int32_t *rows = nullptr, *task_row = nullptr;
   int64_t *first = nullptr;
   double *cpart = nullptr;
+  // rows of at most kLong edges by degree class, heaviest first (nullptr:
+  // the rows are already in that order)
+  int32_t *order = nullptr;
+  int64_t n_short = 0;
+  // leading rows (in the pull's order) with at least kLight edges
+  int64_t n_heavy = 0;
   ~LongPlan() {
-    cudaFree(rows); cudaFree(task_row); cudaFree(first); cudaFree(cpart);
+    cudaFree(rows); cudaFree(task_row); cudaFree(first); cudaFree(cpart); cudaFree(order);
   }
 };
 
-Status build_long_plan(cudaStream_t s, const int64_t *rp, int64_t n, LongPlan &lp) {
+// key of row v for the row order: 12 - (degree class) for rows of at most
+// kLong edges (class 0: no edge, c: 2^(c-1) <= degree < 2^c, so 0 for
+// degree kLong), 15 for long rows, which sort last and are left out
+__global__ void row_class_keys(const int64_t *rp, int64_t n, uint32_t *key) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t d = rp[v + 1] - rp[v];
+    const int cls = d == 0 ? 0 : 64 - __clzll((unsigned long long)d);
+    key[v] = d > kLong ? 15u : (uint32_t)(12 - cls);
+  }
+}
+
+static_assert(kLong == 2048, "row_class_keys: degree classes 0..12 for rows of at most kLong edges");
+static_assert(kLight == 8, "the light rows (degree < kLight) are the degree classes 0..3");
+
+// *count += rows with lo <= degree <= hi
+__global__ void count_rows(const int64_t *rp, int64_t n, int64_t lo, int64_t hi, unsigned long long *count) {
+  unsigned long long c = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t d = rp[v + 1] - rp[v];
+    c += d >= lo && d <= hi;
+  }
+  c = __reduce_add_sync(0xffffffffu, (unsigned)c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+Status count_rows_host(cudaStream_t s, const int64_t *rp, int64_t n, int64_t lo, int64_t hi, int64_t *out) {
+  unsigned long long *d = nullptr;
+  GOPS_CUDA_TRY(cudaMalloc(&d, sizeof(unsigned long long)));
+  struct Free {
+    unsigned long long *p;
+    ~Free() { cudaFree(p); }
+  } fd{d};
+  GOPS_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(unsigned long long), s));
+  count_rows<<<blocks_for(n, 256, 4096), 256, 0, s>>>(rp, n, lo, hi, d);
+  GOPS_CUDA_TRY(cudaGetLastError());
+  unsigned long long h = 0;
+  GOPS_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+  GOPS_CUDA_TRY(cudaStreamSynchronize(s));
+  *out = (int64_t)h;
+  return Status::ok();
+}
+
+// lp.order: the rows of at most kLong edges, stably sorted by degree class
+// (heaviest first; one 4-bit radix pass)
+Status build_row_order(cudaStream_t s, const int64_t *rp, int64_t n, LongPlan &lp) {
+  uint32_t *buf = nullptr;
+  GOPS_CUDA_TRY(cudaMalloc(&buf, sizeof(uint32_t) * 4 * n));
+  struct Free {
+    uint32_t *p;
+    ~Free() { cudaFree(p); }
+  } fb{buf};
+  uint32_t *key_in = buf, *k = buf + n, *v = buf + 2 * n, *k2 = buf + 3 * n;
+  GOPS_CUDA_TRY(cudaMalloc(&lp.order, sizeof(int32_t) * n));
+  uint32_t *v2 = reinterpret_cast<uint32_t *>(lp.order);
+  row_class_keys<<<blocks_for(n, 256, 4096), 256, 0, s>>>(rp, n, key_in);
+  GOPS_CUDA_TRY(cudaGetLastError());
+  bool alt = false;
+  GOPS_TRY(radix_sort_index_u32(key_in, k, v, k2, v2, n, 4, &alt, s));
+  if (!alt) GOPS_CUDA_TRY(cudaMemcpyAsync(lp.order, v, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+  GOPS_CUDA_TRY(cudaStreamSynchronize(s));  // buf is freed on return
+  lp.n_short = n - lp.n_long;
+  return Status::ok();
+}
+
+Status build_long_plan_rows(cudaStream_t s, const int64_t *rp, int64_t n, LongPlan &lp) {
   int64_t *pos = nullptr;
   GOPS_CUDA_TRY(cudaMalloc(&pos, sizeof(int64_t) * (n + 1)));
   struct Free {
@@ -311,6 +412,15 @@ Status build_long_plan(cudaStream_t s, const int64_t *rp, int64_t n, LongPlan &l
   return Status::ok();
 }
 
+// The long-row plan of a CSR, and with `ordered` the row order of its other rows.
+// The in-edge CSR's rows are in non-increasing degree (long rows first, which
+// the heavy loop skips); the ordered rows leave the long ones out.
+Status build_long_plan(cudaStream_t s, const int64_t *rp, int64_t n, LongPlan &lp, bool ordered) {
+  GOPS_TRY(build_long_plan_rows(s, rp, n, lp));
+  if (ordered) GOPS_TRY(build_row_order(s, rp, n, lp));
+  return count_rows_host(s, rp, n, kLight, ordered ? kLong : INT64_MAX, &lp.n_heavy);
+}
+
 // Blocks of part[] one pull writes: the short-row blocks, then the long-row blocks.
 int pull_blocks(int64_t n, const LongPlan &lp) {
   return grid_rows(n) + (lp.n_long ? (int)ceil_div<int64_t>(lp.n_long, kCThreads) : 0);
@@ -322,7 +432,7 @@ template <class Op>
 int pull(cudaStream_t s, const int64_t *rp, const int32_t *col, int64_t n, const LongPlan &lp, Op op,
          const double *x, double *y, double *part) {
   const int nb = grid_rows(n);
-  short_rows<Op><<<nb, kCThreads, 0, s>>>(rp, col, n, op, x, y, part);
+  short_rows<Op><<<nb, kCThreads, 0, s>>>(rp, col, lp.order, lp.n_heavy, lp.order ? lp.n_short : n, op, x, y, part);
   if (lp.n_long == 0) return 1;
   chunk_sums<<<(unsigned)lp.n_chunks, kCThreads, 0, s>>>(rp, col, lp.rows, lp.first, lp.task_row, x, lp.cpart);
   long_rows<Op><<<(unsigned)ceil_div<int64_t>(lp.n_long, kCThreads), kCThreads, 0, s>>>(
@@ -340,7 +450,7 @@ Status katz_run(Ctx *ctx, const Graph *g, const gops_katz_config *cfg, double *s
   cudaStream_t s = ctx->stream;
   Bufs b;
   LongPlan lp;
-  GOPS_TRY(build_long_plan(s, g->in_rp, n, lp));
+  GOPS_TRY(build_long_plan(s, g->in_rp, n, lp, false));
   const int nb = pull_blocks(n, lp);
   GOPS_CUDA_TRY(cudaMalloc(&b.x, sizeof(double) * (n + 1)));
   GOPS_CUDA_TRY(cudaMalloc(&b.y, sizeof(double) * (n + 1)));
@@ -396,7 +506,7 @@ Status eigenvector_run(Ctx *ctx, const Graph *g, uint64_t max_iterations, double
   cudaStream_t s = ctx->stream;
   Bufs b;
   LongPlan lp;
-  GOPS_TRY(build_long_plan(s, g->out_rp, n, lp));
+  GOPS_TRY(build_long_plan(s, g->out_rp, n, lp, true));
   const int nb = pull_blocks(n, lp);
   const int nbs = blocks_for(n, 256, kCBlocks);
   GOPS_CUDA_TRY(cudaMalloc(&b.x, sizeof(double) * n));
@@ -465,8 +575,8 @@ Status hits_run(Ctx *ctx, const Graph *g, uint64_t max_iterations, double tolera
     }
   } h;
   LongPlan lpi, lpo;
-  GOPS_TRY(build_long_plan(s, g->in_rp, n, lpi));
-  GOPS_TRY(build_long_plan(s, g->out_rp, n, lpo));
+  GOPS_TRY(build_long_plan(s, g->in_rp, n, lpi, false));
+  GOPS_TRY(build_long_plan(s, g->out_rp, n, lpo, true));
   const int nbi = pull_blocks(n, lpi), nbo = pull_blocks(n, lpo), nbs = blocks_for(n, 256, kCBlocks);
   const int nb = std::max(nbi, nbo);
   GOPS_CUDA_TRY(cudaMalloc(&h.hub, sizeof(double) * n));

@@ -5,7 +5,8 @@
 // (repeats count), normalised as src/ppr.rs:104-109 does -- an empty set gives
 // the uniform vector.  Sets run in waves of KT columns, KT = 32 * CPL with
 // CPL (columns per lane) 1, 2 or 4.  Per wave the library keeps row-major
-// (n+1) x KT blocks (relabelled node order) of the gathered step vector, the
+// (n+1) x KT blocks (relabelled node order) of the gathered step vector (FP32,
+// plus a BF16 block of low words for the double-float phase), the
 // double-float accumulator and the FP32 tail -- the residual form of the
 // single solve (csrc/pagerank.cu), column by column:
 //   r_1 = F(x_0) - x_0,  r_{k+1} = A r_k,  x_k = x_0 + sum r,  diff_k = ||r_k||_1
@@ -40,6 +41,8 @@
 // a chunk of kChunkSteps steps is captured once as a CUDA graph and replayed
 // for every chunk of every wave; the host polls a pinned copy of the wave
 // record after each replay, with one chunk queued ahead.
+#include <cuda_bf16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -118,8 +121,8 @@ struct BatchState {
   int32_t n_big = 0, n_big_tasks = 0, n_blocks = 0;
   int32_t *big_first = nullptr, *big_task_row = nullptr, *blk_first = nullptr;
   // wave workspace, kt_cap columns
-  float2 *gdf[2] = {nullptr, nullptr};
-  float *gf[2] = {nullptr, nullptr};
+  __nv_bfloat16 *glo[2] = {nullptr, nullptr};  // low words of the double-float gathered blocks (BF16)
+  float *gf[2] = {nullptr, nullptr};           // gathered blocks: FP32, the double-float high words
   float2 *acc = nullptr;
   float *tail = nullptr;
   float2 *lpart = nullptr;   // base-block sums of chunked rows (n_blocks x kt_cap)
@@ -170,9 +173,9 @@ static void free_plan(BatchState *b) {
 }
 
 static void free_blocks(BatchState *b) {
-  cudaFree(b->gdf[0]); cudaFree(b->gdf[1]); cudaFree(b->gf[0]); cudaFree(b->gf[1]);
+  cudaFree(b->glo[0]); cudaFree(b->glo[1]); cudaFree(b->gf[0]); cudaFree(b->gf[1]);
   cudaFree(b->acc); cudaFree(b->tail);
-  b->gdf[0] = b->gdf[1] = nullptr;
+  b->glo[0] = b->glo[1] = nullptr;
   b->gf[0] = b->gf[1] = nullptr;
   b->acc = nullptr;
   b->tail = nullptr;
@@ -214,7 +217,7 @@ struct StepParams {
   const int32_t *big_first, *big_task_row, *blk_first;
   const int32_t *prow, *pslot;
   const float2 *pval;
-  float2 *gdf[2];
+  __nv_bfloat16 *glo[2];
   float *gf[2];
   float2 *acc;
   float *tail;
@@ -344,6 +347,44 @@ __device__ __forceinline__ void st_dv(float2 *a, const DV<CPL> &r) {
   }
 }
 
+// Low words of CPL double-float entries, kept as BF16 (the high words are
+// the FP32 block): loaded as one 8-, 4- or 2-byte read, widened exactly.
+template <int CPL>
+__device__ __forceinline__ void ld_lo(const __nv_bfloat16 *a, float (&lo)[CPL]) {
+  const unsigned short *h = reinterpret_cast<const unsigned short *>(a);
+  if constexpr (CPL == 1) {
+    lo[0] = __uint_as_float((uint32_t)__ldg(h) << 16);
+  } else if constexpr (CPL == 2) {
+    const uint32_t t = __ldg(reinterpret_cast<const unsigned int *>(h));
+    lo[0] = __uint_as_float(t << 16);
+    lo[1] = __uint_as_float(t & 0xFFFF0000u);
+  } else {
+    const uint2 t = __ldg(reinterpret_cast<const uint2 *>(h));
+    lo[0] = __uint_as_float(t.x << 16);
+    lo[1] = __uint_as_float(t.x & 0xFFFF0000u);
+    lo[2] = __uint_as_float(t.y << 16);
+    lo[3] = __uint_as_float(t.y & 0xFFFF0000u);
+  }
+}
+
+__device__ __forceinline__ uint32_t bf16_bits(float v) {
+  const __nv_bfloat16 b = __float2bfloat16_rn(v);
+  return (uint32_t)*reinterpret_cast<const unsigned short *>(&b);
+}
+
+template <int CPL>
+__device__ __forceinline__ void st_lo(__nv_bfloat16 *a, const DV<CPL> &r) {
+  unsigned short *h = reinterpret_cast<unsigned short *>(a);
+  if constexpr (CPL == 1) {
+    *h = (unsigned short)bf16_bits(r.v[0].lo);
+  } else if constexpr (CPL == 2) {
+    *reinterpret_cast<unsigned int *>(h) = bf16_bits(r.v[0].lo) | (bf16_bits(r.v[1].lo) << 16);
+  } else {
+    *reinterpret_cast<uint2 *>(h) = make_uint2(bf16_bits(r.v[0].lo) | (bf16_bits(r.v[1].lo) << 16),
+                                               bf16_bits(r.v[2].lo) | (bf16_bits(r.v[3].lo) << 16));
+  }
+}
+
 // FP32 step of one column (shared by both kernels, with explicit roundings
 // so that the two compute the same bits): r = d (s + dsum * red).
 __device__ __forceinline__ float f32_step(float s, float dsum, float red, float d) {
@@ -415,7 +456,10 @@ __device__ __forceinline__ FV<CPL> f32_block(const StepParams &p, int in, int kt
 
 // ---------------------------------------------------------------------------
 // The mixed step (some active column still in its double-float phase).
-// Every lane gathers its 8-byte (hi, lo) entries of the double-float block.
+// Every lane gathers its double-float entries: the high words from the FP32
+// block and the low words from the BF16 low-word block (6 bytes per entry;
+// a stored value keeps 24 + 8 significant bits, far more than the FP32
+// phase's sums, while the gathers move 3/4 of full double-float's bytes).
 // A column in its double-float phase adds them in double-float arithmetic; a
 // column already in its FP32 phase adds only the hi words in FP32 (its sum
 // kept in the hi word), which is exactly what the FP32 step computes from the
@@ -459,9 +503,21 @@ __device__ __forceinline__ void mix_add(MixSum<CPL> &s, const MixSum<CPL> &t) {
 }
 
 template <int CPL>
+__device__ __forceinline__ DV<CPL> gather_dv(const float *ghi, const __nv_bfloat16 *glo, int64_t off) {
+  const FV<CPL> h = ld_fv<CPL>(ghi + off);
+  float lo[CPL];
+  ld_lo<CPL>(glo + off, lo);
+  DV<CPL> r;
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) r.v[q] = {h.v[q], lo[q]};
+  return r;
+}
+
+template <int CPL>
 __device__ __forceinline__ MixSum<CPL> mix_block(const StepParams &p, int in, int kt, int eb, int ee, int lane) {
   constexpr int U = CPL == 4 ? 4 : 8;
-  const float2 *gb = p.gdf[in] + lane * CPL;
+  const float *ghi = p.gf[in] + lane * CPL;
+  const __nv_bfloat16 *glo = p.glo[in] + lane * CPL;
   MixSum<CPL> s = mix_zero<CPL>();
   for (int e = eb; e < ee; e += U) {  // ee - eb is a multiple of 4
     int32_t u[U];
@@ -476,7 +532,7 @@ __device__ __forceinline__ MixSum<CPL> mix_block(const StepParams &p, int in, in
     DV<CPL> g[U];
 #pragma unroll
     for (int q = 0; q < U; ++q)
-      if (q < 4 || ok2) g[q] = ld_dv<CPL>(gb + (int64_t)u[q] * kt, true);
+      if (q < 4 || ok2) g[q] = gather_dv<CPL>(ghi, glo, (int64_t)u[q] * kt);
 #pragma unroll
     for (int q = 0; q < U; ++q)
       if (q < 4 || ok2) mix_add<CPL>(s, g[q]);
@@ -612,7 +668,7 @@ __device__ __forceinline__ void mix_epilogue(const StepParams &p, const WaveScal
   }
   st_dv<CPL>(p.acc + i, an);
   if (ln.fmask) st_fv<CPL>(p.tail + i, tn);
-  st_dv<CPL>(p.gdf[out] + i, g);
+  st_lo<CPL>(p.glo[out] + i, g);
   st_fv<CPL>(p.gf[out] + i, gh);
 }
 
@@ -873,7 +929,7 @@ __global__ void __launch_bounds__(kBThreads) batch_init(StepParams p) {
     const int64_t v = i / kt;
     const int c = (int)(i - v * kt);
     if (v == p.n) {
-      p.gdf[0][i] = p.gdf[1][i] = make_float2(0.f, 0.f);
+      p.glo[0][i] = p.glo[1][i] = __float2bfloat16_rn(0.f);
       p.gf[0][i] = p.gf[1][i] = 0.f;
       continue;
     }
@@ -883,7 +939,7 @@ __global__ void __launch_bounds__(kBThreads) batch_init(StepParams p) {
     p.acc[i] = make_float2(x0.hi, x0.lo);
     p.tail[i] = 0.f;
     const df g = dg > 0.f ? df_div_f(x0, dg) : df{0.f, 0.f};
-    p.gdf[0][i] = make_float2(g.hi, g.lo);
+    p.glo[0][i] = __float2bfloat16_rn(g.lo);
     p.gf[0][i] = g.hi;
     if (dg == 0.f && col_ok) {
       const long long t = fx_of(x0.hi, wc.fx_scale) + fx_of(x0.lo, wc.fx_scale);
@@ -917,7 +973,7 @@ __global__ void __launch_bounds__(kBThreads) batch_init_x0(StepParams p, const f
   if (blockIdx.x == 0 && wid == 0) {  // padding row: gathers of padded edges read zeros
     for (int c = lane; c < kt; c += 32) {
       const int64_t i = p.n * kt + c;
-      p.gdf[0][i] = p.gdf[1][i] = make_float2(0.f, 0.f);
+      p.glo[0][i] = p.glo[1][i] = __float2bfloat16_rn(0.f);
       p.gf[0][i] = p.gf[1][i] = 0.f;
     }
   }
@@ -944,7 +1000,7 @@ __global__ void __launch_bounds__(kBThreads) batch_init_x0(StepParams p, const f
       p.acc[i] = make_float2(xv.hi, xv.lo);
       p.tail[i] = 0.f;
       const df g = dg > 0.f ? df_div_f(xv, dg) : df{0.f, 0.f};
-      p.gdf[0][i] = make_float2(g.hi, g.lo);
+      p.glo[0][i] = __float2bfloat16_rn(g.lo);
       p.gf[0][i] = g.hi;
       if (dg == 0.f) dang += fx_of(xv.hi, wc.fx_scale);
     }
@@ -1057,8 +1113,8 @@ __global__ void __launch_bounds__(256) prow_from_sorted(const int32_t *rows, int
 // ---------------------------------------------------------------------------
 int cpl_index(int cpl) { return cpl == 1 ? 0 : (cpl == 2 ? 1 : 2); }
 
-size_t block_bytes_per_col(int64_t n) {  // gdf x2, gf x2, acc, tail
-  return (size_t)(n + 1) * (2 * sizeof(float2) + 2 * sizeof(float) + sizeof(float2) + sizeof(float));
+size_t block_bytes_per_col(int64_t n) {  // glo x2, gf x2, acc, tail
+  return (size_t)(n + 1) * (2 * sizeof(__nv_bfloat16) + 2 * sizeof(float) + sizeof(float2) + sizeof(float));
 }
 
 Status batch_prepare_impl(Ctx *ctx, Graph *g);
@@ -1162,8 +1218,8 @@ Status ensure_tile(Ctx *ctx, Graph *g, int cpl, int chunk) {
     GOPS_CUDA_TRY(cudaStreamSynchronize(s));
     free_blocks(b);
     const size_t blk = (size_t)(n + 1) * kt;
-    GOPS_CUDA_TRY(cudaMalloc(&b->gdf[0], sizeof(float2) * blk));
-    GOPS_CUDA_TRY(cudaMalloc(&b->gdf[1], sizeof(float2) * blk));
+    GOPS_CUDA_TRY(cudaMalloc(&b->glo[0], sizeof(__nv_bfloat16) * blk));
+    GOPS_CUDA_TRY(cudaMalloc(&b->glo[1], sizeof(__nv_bfloat16) * blk));
     GOPS_CUDA_TRY(cudaMalloc(&b->gf[0], sizeof(float) * blk));
     GOPS_CUDA_TRY(cudaMalloc(&b->gf[1], sizeof(float) * blk));
     GOPS_CUDA_TRY(cudaMalloc(&b->acc, sizeof(float2) * blk));
@@ -1213,8 +1269,8 @@ StepParams step_params(const Graph *g, const BatchState *b) {
   p.prow = b->prow;
   p.pslot = b->pslot;
   p.pval = b->pval;
-  p.gdf[0] = b->gdf[0];
-  p.gdf[1] = b->gdf[1];
+  p.glo[0] = b->glo[0];
+  p.glo[1] = b->glo[1];
   p.gf[0] = b->gf[0];
   p.gf[1] = b->gf[1];
   p.acc = b->acc;

@@ -111,3 +111,57 @@ def test_edge_list_checks():
     e = go.DeviceGraph.from_edges(5, np.zeros(0, np.int32), np.zeros(0, np.int32))
     s, it, _, conv = e.pagerank_run(go.PageRankConfig())
     assert np.allclose(s, 0.2) and conv  # no edges: every node dangling, uniform
+
+
+def _pair_weight(u, v):
+    """A weight per (source, target) pair, so parallel edges carry equal weights
+    (the adapter's newest-edge rule then changes nothing); some negative, some
+    NaN (both count as 0)."""
+    h = (u.astype(np.int64) * 2654435761 + v.astype(np.int64) * 40503) % 1000003
+    w = 0.1 + (h % 1000) / 1111.0
+    w = np.where(h % 13 == 0, -w, w)
+    return np.where(h % 29 == 0, np.nan, w)
+
+
+def test_chunked_weight_upload_matches_the_one_chunk_build():
+    """Over 4 M edges gops_graph_upload copies the weights in chunks of whole
+    rows and turns each chunk into transition weights as it lands;
+    gops_graph_from_edges builds the same out-adjacency with its weights
+    already on the device (one chunk).  The graph has rows of every size
+    class (1-7 entries: a lane each; 8-256: an 8-lane group; 257-3,000 and a
+    hub row with more than half of the edges: a block each, the hub leaving a
+    chunk empty), rows whose weights are all zero (dangling by weight),
+    negative and NaN weights, and rows without edges.  The two builds give
+    bit-identical weighted solves, and match the oracle's restatement."""
+    from oracle import port
+    rng = np.random.default_rng(12)
+    n = 400_000
+    deg = np.zeros(n, np.int64)
+    idx = rng.permutation(n)
+    deg[idx[:250_000]] = rng.integers(1, 8, 250_000)
+    deg[idx[250_000:270_000]] = rng.integers(8, 257, 20_000)
+    deg[idx[270_000:270_300]] = rng.integers(257, 3001, 300)
+    hub = n // 2
+    deg[hub] = 4_200_000
+    rp = np.zeros(n + 1, np.int64)
+    rp[1:] = np.cumsum(deg)
+    m = int(rp[-1])
+    assert m >= 1 << 22 and deg[hub] > m // 2
+    row = np.repeat(np.arange(n, dtype=np.int64), deg)
+    col = rng.integers(0, n, m).astype(np.int32)
+    w = _pair_weight(row, col.astype(np.int64))
+    for u in idx[1000:1400]:  # light and mid rows whose weights are all zero
+        w[rp[u]:rp[u + 1]] = 0.0
+    # the raw edge list whose newest-first walk is this CSR: each row reversed
+    rev = rp[row] + rp[row + 1] - 1 - np.arange(m, dtype=np.int64)
+    src_raw, dst_raw, w_raw = row.astype(np.int32), col[rev], w[rev]
+    conf = go.PageRankConfig(0.85, 1000, 1e-9)
+    chunked = go.DeviceGraph.from_csr(rp, col, w)
+    one = go.DeviceGraph.from_edges(n, src_raw, dst_raw, w_raw)
+    a = chunked.pagerank_weighted_run(conf)
+    b = one.pagerank_weighted_run(conf)
+    assert np.array_equal(a[0], b[0]) and a[1:] == b[1:]
+    ref = port.pagerank_weighted_run(rp, col, w, 0.85, 1000, 1e-9)
+    assert np.abs(a[0] - ref[0]).sum() <= 1e-7 and abs(a[1] - ref[1]) <= 1
+    again = go.DeviceGraph.from_csr(rp, col, w).pagerank_weighted_run(conf)
+    assert np.array_equal(a[0], again[0])

@@ -122,35 +122,15 @@ Status upload_impl(Ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *c
   if (e == cudaSuccess && w) e = dev_malloc_async((void **)&d_w, sizeof(double) * (m > 0 ? m : 1), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_rp, row_ptr, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(d_col, col, sizeof(int32_t) * m, cudaMemcpyHostToDevice, s);
-  // the weights (the largest array) follow on the copy stream, in chunks of
-  // whole rows of about equal size, while the checks, the edge sort and the
-  // structure of the build, which do not read them, run on the main stream;
-  // the build turns each chunk into transition weights as it lands
+  // the weights (the largest array) follow on the copy stream while the
+  // checks and the edge sort, which do not read them, run on the main stream
   bool w_async = false;
-  WeightArrival wa;
   if (e == cudaSuccess && w && m > 0) {
-    wa.chunks = m >= kWeightChunkMinEdges ? kWeightChunks : 1;
-    wa.row_start[0] = 0;
-    for (int c = 1; c < wa.chunks; ++c)  // first row starting at or after edge c * m / chunks
-      wa.row_start[c] = std::lower_bound(row_ptr, row_ptr + n + 1, m * c / wa.chunks) - row_ptr;
-    wa.row_start[wa.chunks] = n;
-    // edge bounds of the chunks, clamped into [0, m] and non-decreasing, so
-    // the copies cover exactly the m weights even before the device check of
-    // row_ptr has run (an invalid row_ptr fails that check; nothing is built)
-    int64_t eb[kWeightChunks + 1];
-    eb[0] = 0;
-    for (int c = 1; c < wa.chunks; ++c)
-      eb[c] = std::min(m, std::max(eb[c - 1], row_ptr[wa.row_start[c]]));
-    eb[wa.chunks] = m;
     e = cudaEventRecord(ctx->copy_ev[0], s);  // after d_w's allocation and the column copy
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[0], 0);
-    for (int c = 0; c < wa.chunks && e == cudaSuccess; ++c) {
-      const int64_t e0 = eb[c], e1 = eb[c + 1];
-      if (e1 > e0)
-        e = cudaMemcpyAsync(d_w + e0, w + e0, sizeof(double) * (e1 - e0), cudaMemcpyHostToDevice, ctx->copy_stream);
-      if (e == cudaSuccess) e = cudaEventRecord(ctx->copy_ev[1 + c], ctx->copy_stream);
-      wa.ready[c] = ctx->copy_ev[1 + c];
-    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_w, w, sizeof(double) * m, cudaMemcpyHostToDevice, ctx->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->copy_ev[1], ctx->copy_stream);
     w_async = e == cudaSuccess;
   }
   if (e != cudaSuccess) st = fail(e, "graph upload");
@@ -171,10 +151,10 @@ Status upload_impl(Ctx *ctx, int64_t n, const int64_t *row_ptr, const int32_t *c
     if (e != cudaSuccess) st = fail(e, "graph upload");
     else if (flags[0]) st = Status{GOPS_ERR_INVALID, "row_ptr must be non-decreasing"};
     else if (flags[1]) st = Status{GOPS_ERR_INVALID, "neighbor index out of range"};
-    else st = graph_build_from_out_csr_device(ctx, g, d_rp, d_col, d_w, w_async ? &wa : nullptr);
+    else st = graph_build_from_out_csr_device(ctx, g, d_rp, d_col, d_w, w_async ? ctx->copy_ev[1] : nullptr);
   }
   // every path: the main stream passes the weight copy before d_w is freed
-  if (w_async) cudaStreamWaitEvent(s, ctx->copy_ev[wa.chunks], 0);
+  if (w_async) cudaStreamWaitEvent(s, ctx->copy_ev[1], 0);
   if (st.code == GOPS_OK) {  // kept: the out-adjacency drives eigenvector centrality
     g->out_rp = d_rp;
     g->out_col = d_col;
@@ -215,8 +195,7 @@ int gops_ctx_create(int device, gops_ctx **out) {
   if (e == cudaSuccess) e = cudaMallocHost((void **)&x.host_state, sizeof(SolveState));
   for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&x.ev[i]);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x.copy_stream, cudaStreamNonBlocking);
-  for (int i = 0; i < 1 + kWeightChunks && e == cudaSuccess; ++i)
-    e = cudaEventCreateWithFlags(&x.copy_ev[i], cudaEventDisableTiming);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&x.copy_ev[i], cudaEventDisableTiming);
   if (e != cudaSuccess) {
     gops_ctx_destroy(c);
     return e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA;
@@ -240,7 +219,7 @@ void gops_ctx_destroy(gops_ctx *ctx) {
   for (int i = 0; i < 4; ++i)
     if (x.ev[i]) cudaEventDestroy(x.ev[i]);
   if (x.copy_stream) cudaStreamSynchronize(x.copy_stream);
-  for (int i = 0; i < 1 + kWeightChunks; ++i)
+  for (int i = 0; i < 2; ++i)
     if (x.copy_ev[i]) cudaEventDestroy(x.copy_ev[i]);
   if (x.copy_stream) cudaStreamDestroy(x.copy_stream);
   if (x.host_state) cudaFreeHost(x.host_state);

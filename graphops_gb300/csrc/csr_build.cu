@@ -25,26 +25,26 @@ namespace gops {
 
 namespace {
 
-// Per out-row u: out-degree and the source id of every entry (the structure
-// pass, before the weights have arrived):
+// Per out-row u: out-degree, source id of every entry, and (weighted) the
+// transition weight max(w,0) / sum_u max(w,0) in FP32 with the weighted-
+// dangling bit, in three passes that keep FP64 instructions (issued at a
+// small fraction of the FP32 rate on this GPU) to one add per entry, one
+// divide per row and one multiply and conversion per entry:
 //  out_row_sums      rows of at most kRowBig entries (nearly all: R-MAT rows
 //                    average ~16): an 8-lane group per row in a persistent
-//                    grid; longer rows are listed in big[1..big[0]]
-//  out_row_sums_big  the listed rows (hubs, up to ~1e5 entries), a block per row
-// and (weighted) the transition weight max(w,0) / sum_u max(w,0) in FP32 with
-// the weighted-dangling bit, computed chunk by chunk as the weight upload
-// lands: the rows of each chunk, sorted by size class before the first
-// chunk arrives, go to one lane (fewer than kLightW entries: most rows of a
-// power-law graph), an 8-lane group, or a block (more than kRowBig); each
-// reads its row's weights, takes the FP64 sum in a fixed order, and writes
-// every entry's FP32 weight in entry order (coalesced); after the last chunk
-// one pass gathers them into the in-edge CSR through the entry id that the
-// structure scatter recorded at every position (e_at).  FP64 instructions
-// (issued at a small fraction of the FP32 rate on this GPU) stay at one add
-// per entry, one divide per row and one multiply and conversion per entry.
+//                    grid, the FP64 sum in a fixed order per group (the
+//                    shuffles name the group only: groups of a warp run
+//                    different numbers of rows); longer rows are listed in
+//                    big[1..big[0]] (list order varies, per-row results do not)
+//  out_row_sums_big  the listed rows (hubs, up to ~1e5 entries), a block per
+//                    row, a fixed-order block sum
+//  row_inverse       a thread per row: rowsum -> 1/rowsum (0 for an empty or
+//                    zero-weight row) and the dangling bits, a word per warp
+//  edge_weights      a thread per entry: (float)(max(w,0) * inverse of its row),
+//                    stored beside the entry's source so that the in-CSR
+//                    scatter gathers both with one 8-byte load
 constexpr int kRowLanes = 8;
 constexpr int64_t kRowBig = 256;
-constexpr int64_t kLightW = 8;
 
 // max(w, 0), 0 for NaN (the maximum ignores a NaN operand), from the bits
 __device__ __forceinline__ double clamp_weight(double w) {
@@ -53,125 +53,84 @@ __device__ __forceinline__ double clamp_weight(double w) {
   return neg_or_nan ? 0.0 : w;
 }
 
-// Structure pass: out-degree, sources, the list of long rows.
-__global__ void out_row_sums(int64_t n, const int64_t *__restrict__ rp, uint32_t *__restrict__ src,
-                             float *__restrict__ deg_f, uint32_t *__restrict__ big) {
+// Two calls: the structure pass (w == nullptr: out-degree, sources, the list
+// of long rows), which needs no weights and runs while they are still being
+// copied, then the sums pass (w set: row sums only).
+__global__ void out_row_sums(int64_t n, const int64_t *__restrict__ rp, const double *__restrict__ w,
+                             uint32_t *__restrict__ src, float *__restrict__ deg_f,
+                             double *__restrict__ rowsum, uint32_t *__restrict__ big) {
   const int lane = threadIdx.x & (kRowLanes - 1);
+  const unsigned gmask = ((1u << kRowLanes) - 1u) << ((threadIdx.x & 31) & ~(kRowLanes - 1));
   const int64_t groups = (int64_t)gridDim.x * (blockDim.x / kRowLanes);
   for (int64_t u = (int64_t)blockIdx.x * (blockDim.x / kRowLanes) + threadIdx.x / kRowLanes; u < n; u += groups) {
     const int64_t b = rp[u], e = rp[u + 1];
     if (e - b > kRowBig) {  // the whole group skips: same row
-      if (lane == 0) big[1 + atomicAdd(&big[0], 1u)] = (uint32_t)u;
+      if (!w && lane == 0) big[1 + atomicAdd(&big[0], 1u)] = (uint32_t)u;
       continue;
     }
-    if (lane == 0) deg_f[u] = (float)(e - b);
-    for (int64_t i = b + lane; i < e; i += kRowLanes) src[i] = (uint32_t)u;
+    if (!w) {
+      if (lane == 0) deg_f[u] = (float)(e - b);
+      for (int64_t i = b + lane; i < e; i += kRowLanes) src[i] = (uint32_t)u;
+    } else {
+      double s = 0.0;
+      for (int64_t i = b + lane; i < e; i += kRowLanes) s += clamp_weight(w[i]);
+#pragma unroll
+      for (int o = kRowLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, kRowLanes);
+      if (lane == 0) rowsum[u] = s;
+    }
   }
 }
 
-__global__ void __launch_bounds__(256) out_row_sums_big(const int64_t *__restrict__ rp, uint32_t *__restrict__ src,
-                                                         float *__restrict__ deg_f, const uint32_t *__restrict__ big) {
+__global__ void __launch_bounds__(256) out_row_sums_big(const int64_t *__restrict__ rp,
+                                                         const double *__restrict__ w, uint32_t *__restrict__ src,
+                                                         float *__restrict__ deg_f, double *__restrict__ rowsum,
+                                                         const uint32_t *__restrict__ big) {
+  __shared__ double sh[256];
   const uint32_t nbig = big[0];
   for (uint32_t k = blockIdx.x; k < nbig; k += gridDim.x) {  // uniform per block
     const int64_t u = big[1 + k];
     const int64_t b = rp[u], e = rp[u + 1];
-    if (threadIdx.x == 0) deg_f[u] = (float)(e - b);
-    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) src[i] = (uint32_t)u;
-  }
-}
-
-// ---- transition weights, chunk by chunk ----
-struct ChunkRows {
-  int64_t start[kWeightChunks + 1];
-  int chunks;
-};
-
-// key[v] = 4 * (v's weight chunk) + size class (0: more than kRowBig
-// entries, 1: kLightW..kRowBig, 2: fewer than kLightW); counts[key] += 1
-__global__ void weight_row_keys(const int64_t *rp, int64_t n, ChunkRows cr, uint32_t *key, unsigned *counts) {
-  __shared__ unsigned sc[4 * kWeightChunks];
-  for (int i = threadIdx.x; i < 4 * kWeightChunks; i += blockDim.x) sc[i] = 0;
-  __syncthreads();
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    int c = 0;
-    while (c + 1 < cr.chunks && v >= cr.start[c + 1]) ++c;
-    const int64_t d = rp[v + 1] - rp[v];
-    const uint32_t k = 4u * (uint32_t)c + (d > kRowBig ? 0u : d >= kLightW ? 1u : 2u);
-    key[v] = k;
-    atomicAdd(&sc[k], 1u);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < 4 * kWeightChunks; i += blockDim.x)
-    if (sc[i]) atomicAdd(&counts[i], sc[i]);
-}
-
-__device__ __forceinline__ float transition_weight(double wc, double inv) {
-  return __double_as_longlong(wc) > 0 ? (float)(wc * inv) : 0.0f;
-}
-
-// rows[0..count): fewer than kLightW entries, one lane each; the sum in entry order
-__global__ void weights_light(const uint32_t *__restrict__ rows, int64_t count, const int64_t *__restrict__ rp,
-                              const double *__restrict__ w, float *__restrict__ val,
-                              uint32_t *__restrict__ dmask) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t u = rows[i];
-    const int64_t b = rp[u], e = rp[u + 1];
+    if (!w) {  // structure pass
+      if (threadIdx.x == 0) deg_f[u] = (float)(e - b);
+      for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) src[i] = (uint32_t)u;
+      continue;
+    }
     double s = 0.0;
-    for (int64_t j = b; j < e; ++j) s += clamp_weight(w[j]);
-    const bool dang = !(s > 0.0);
-    const double inv = dang ? 0.0 : 1.0 / s;
-    if (dang) atomicOr(&dmask[u >> 5], 1u << (u & 31));
-    for (int64_t j = b; j < e; ++j) val[j] = transition_weight(clamp_weight(w[j]), inv);
-  }
-}
-
-// rows[0..count): kLightW..kRowBig entries, an 8-lane group each; the sum per
-// lane in entry order, then a fixed xor tree (the shuffles name the group
-// only: groups of a warp run different numbers of rows)
-__global__ void weights_mid(const uint32_t *__restrict__ rows, int64_t count, const int64_t *__restrict__ rp,
-                            const double *__restrict__ w, float *__restrict__ val,
-                            uint32_t *__restrict__ dmask) {
-  const int lane = threadIdx.x & (kRowLanes - 1);
-  const unsigned gmask = ((1u << kRowLanes) - 1u) << ((threadIdx.x & 31) & ~(kRowLanes - 1));
-  const int64_t groups = (int64_t)gridDim.x * (blockDim.x / kRowLanes);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x / kRowLanes) + threadIdx.x / kRowLanes; i < count;
-       i += groups) {
-    const int64_t u = rows[i];
-    const int64_t b = rp[u], e = rp[u + 1];
-    double s = 0.0;
-    for (int64_t j = b + lane; j < e; j += kRowLanes) s += clamp_weight(w[j]);
-#pragma unroll
-    for (int o = kRowLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, kRowLanes);
-    const bool dang = !(s > 0.0);
-    const double inv = dang ? 0.0 : 1.0 / s;
-    if (dang && lane == 0) atomicOr(&dmask[u >> 5], 1u << (u & 31));
-    for (int64_t j = b + lane; j < e; j += kRowLanes) val[j] = transition_weight(clamp_weight(w[j]), inv);
-  }
-}
-
-// rows[0..count): more than kRowBig entries, a block each; the sum per thread
-// in entry order, then a fixed tree
-__global__ void __launch_bounds__(256) weights_big(const uint32_t *__restrict__ rows, int64_t count,
-                                                   const int64_t *__restrict__ rp, const double *__restrict__ w,
-                                                   float *__restrict__ val, uint32_t *__restrict__ dmask) {
-  __shared__ double sh[256];
-  for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {  // uniform per block
-    const int64_t u = rows[i];
-    const int64_t b = rp[u], e = rp[u + 1];
-    double s = 0.0;
-    for (int64_t j = b + threadIdx.x; j < e; j += blockDim.x) s += clamp_weight(w[j]);
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) s += clamp_weight(w[i]);
     sh[threadIdx.x] = s;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
       if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
       __syncthreads();
     }
-    const double tot = sh[0];
-    __syncthreads();  // sh is rewritten by the next row
-    const bool dang = !(tot > 0.0);
-    const double inv = dang ? 0.0 : 1.0 / tot;
-    if (dang && threadIdx.x == 0) atomicOr(&dmask[u >> 5], 1u << (u & 31));
-    for (int64_t j = b + threadIdx.x; j < e; j += blockDim.x) val[j] = transition_weight(clamp_weight(w[j]), inv);
+    if (threadIdx.x == 0) rowsum[u] = sh[0];
+    __syncthreads();
+  }
+}
+
+// Rows 32*j .. 32*j+31 are one warp's: dmask word j is written whole.
+__global__ void row_inverse(int64_t n, double *__restrict__ rowsum, uint32_t *__restrict__ dmask) {
+  const int64_t words = (n + 31) / 32;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < words * 32;
+       u += (int64_t)gridDim.x * blockDim.x) {  // uniform per warp: words * 32 rounds up
+    bool dang = false;
+    if (u < n) {
+      const double s = rowsum[u];
+      dang = !(s > 0.0);
+      rowsum[u] = dang ? 0.0 : 1.0 / s;
+    }
+    const unsigned bits = __ballot_sync(0xffffffffu, dang);
+    if ((threadIdx.x & 31) == 0) dmask[u >> 5] = bits;
+  }
+}
+
+__global__ void edge_weights(int64_t m, const double *__restrict__ w, const uint32_t *__restrict__ src,
+                             const double *__restrict__ inv, uint2 *__restrict__ src_val) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const double wc = clamp_weight(w[i]);
+    const uint32_t u = src[i];
+    const float v = __double_as_longlong(wc) > 0 ? (float)(wc * inv[u]) : 0.0f;
+    src_val[i] = make_uint2(u, __float_as_uint(v));
   }
 }
 
@@ -234,36 +193,23 @@ __global__ void permute_dmask(const int32_t *perm, int64_t n, const uint32_t *ol
 }
 
 // Sorted position i holds edge O[i] into node K[i]; it lands in relabelled
-// row inv_perm[K[i]] at the same offset within the row.  e_at (weighted
-// graphs): the out-entry id at every in-edge CSR position (padding positions
-// keep kNoEntry), through which the weights are gathered once they exist.
-constexpr uint32_t kNoEntry = 0xFFFFFFFFu;
+// row inv_perm[K[i]] at the same offset within the row.
 __global__ void scatter_edges(const uint32_t *K, const uint32_t *O, int64_t m, const int64_t *rp_old,
                               const int32_t *inv_perm, const int64_t *rp_new, const uint32_t *src,
-                              int32_t *in_col, uint32_t *e_at) {
+                              const uint2 *src_val, int32_t *in_col, float *in_val) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
        i += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t v = K[i];
     const int64_t pos = rp_new[inv_perm[v]] + (i - rp_old[v]);
     const uint32_t e = O[i];
-    in_col[pos] = inv_perm[src[e]];
-    if (e_at) e_at[pos] = e;
+    if (src_val) {  // weighted: source and weight in one load
+      const uint2 sv = src_val[e];
+      in_col[pos] = inv_perm[sv.x];
+      in_val[pos] = __uint_as_float(sv.y);
+    } else {
+      in_col[pos] = inv_perm[src[e]];
+    }
   }
-}
-
-// in_val[p] = the transition weight of the entry at in-edge position p (0 at padding)
-__global__ void gather_weights(const uint32_t *__restrict__ e_at, int64_t count, const float *__restrict__ val,
-                               float *__restrict__ in_val) {
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < count; p += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t e = e_at[p];
-    in_val[p] = e == kNoEntry ? 0.0f : val[e];
-  }
-}
-
-__global__ void fill_u32(uint32_t *a, int64_t count, uint32_t v) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
-       i += (int64_t)gridDim.x * blockDim.x)
-    a[i] = v;
 }
 
 __global__ void pad_degrees(int64_t *deg, int64_t n, int align) {
@@ -416,7 +362,7 @@ void graph_free_device(Graph &g) {
 
 Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_rp,
                                        const int32_t *d_out_col, const double *d_w,
-                                       const WeightArrival *wa) {
+                                       cudaEvent_t w_ready) {
   cudaStream_t s = ctx->stream;
   const int64_t n = g->n, m = g->m;
   g->weighted = d_w != nullptr;
@@ -424,19 +370,18 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   uint32_t *src = nullptr, *keys = nullptr, *vals = nullptr, *keys2 = nullptr, *vals2 = nullptr;
   uint32_t *nk = nullptr, *nv = nullptr, *nk2 = nullptr, *nv2 = nullptr, *dmask_old = nullptr;
   float *deg_old = nullptr;
-  float *val = nullptr;     // transition weights in out-entry order (weighted)
-  uint32_t *e_at = nullptr; // out-entry id per in-edge position (weighted)
+  uint2 *src_val = nullptr;
   int64_t *rp_old = nullptr, *new_deg = nullptr, *small = nullptr;
   int32_t *inv_perm = nullptr;
-  unsigned *maxdeg = nullptr, *wcounts = nullptr;
-  uint32_t *wkey = nullptr;
+  unsigned *maxdeg = nullptr;
   uint32_t *bigrows = nullptr;
+  double *rowsum = nullptr;
   auto cleanup = [&]() {
     free_async(src, s); free_async(keys, s); free_async(vals, s); free_async(keys2, s);
     free_async(vals2, s); free_async(nk, s); free_async(nv, s); free_async(nk2, s);
-    free_async(nv2, s); free_async(dmask_old, s); free_async(val, s); free_async(e_at, s); free_async(deg_old, s);
+    free_async(nv2, s); free_async(dmask_old, s); free_async(src_val, s); free_async(deg_old, s);
     free_async(rp_old, s); free_async(new_deg, s); free_async(small, s); free_async(inv_perm, s);
-    free_async(maxdeg, s); free_async(bigrows, s); free_async(wcounts, s); free_async(wkey, s);
+    free_async(maxdeg, s); free_async(bigrows, s); free_async(rowsum, s);
   };
 #define BUILD_TRY(expr)                                                                     \
   do {                                                                                      \
@@ -464,7 +409,8 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(cudaMemsetAsync(g->dmask_w, 0, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(dev_malloc_async((void **)&dmask_old, sizeof(uint32_t) * nwords, s));
     BUILD_TRY(cudaMemsetAsync(dmask_old, 0, sizeof(uint32_t) * nwords, s));
-    BUILD_TRY(dev_malloc_async((void **)&val, sizeof(float) * mm, s));
+    BUILD_TRY(dev_malloc_async((void **)&src_val, sizeof(uint2) * mm, s));
+    BUILD_TRY(dev_malloc_async((void **)&rowsum, sizeof(double) * nn, s));
   }
   // K1: stable sort of edge ids by destination
   BUILD_TRY(dev_malloc_async((void **)&keys, sizeof(uint32_t) * mm, s));
@@ -484,9 +430,9 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     const int64_t nbig_cap = std::min<int64_t>(n, m / (kRowBig + 1)) + 1;
     BUILD_TRY(dev_malloc_async((void **)&bigrows, sizeof(uint32_t) * nbig_cap, s));
     BUILD_TRY(cudaMemsetAsync(bigrows, 0, sizeof(uint32_t), s));
-    out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(n, d_out_rp, src, deg_old,
-                                                                                  bigrows);
-    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, src, deg_old, bigrows);
+    out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
+        n, d_out_rp, nullptr, src, deg_old, rowsum, bigrows);
+    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, nullptr, src, deg_old, rowsum, bigrows);
     BUILD_TRY(cudaGetLastError());
   }
   BUILD_TRY(dev_malloc_async((void **)&rp_old, sizeof(int64_t) * (n + 1), s));
@@ -537,12 +483,22 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   }
   if (g->weighted) {
     BUILD_TRY(dev_malloc_async(&g->in_val, sizeof(float) * ms, s));
-    BUILD_TRY(dev_malloc_async((void **)&e_at, sizeof(uint32_t) * ms, s));
-    fill_u32<<<grid_for((int64_t)ms, 256), 256, 0, s>>>(e_at, (int64_t)ms, kNoEntry);
+    BUILD_TRY(cudaMemsetAsync(g->in_val, 0, sizeof(float) * ms, s));
+  }
+  // the weights: everything above ran while they were being copied
+  if (w_ready) BUILD_TRY(cudaStreamWaitEvent(s, w_ready, 0));
+  if (d_w && n > 0) {
+    out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
+        n, d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+    row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(n, rowsum, dmask_old);
+    if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, s>>>(m, d_w, src, rowsum, src_val);
+    permute_dmask<<<(unsigned)ceil_div<int64_t>(n, 256), 256, 0, s>>>(g->perm, n, dmask_old, g->dmask_w);
     BUILD_TRY(cudaGetLastError());
   }
-  if (m > 0) {  // the in-edge structure (and e_at): no weights read
-    scatter_edges<<<grid_for(m, 256), 256, 0, s>>>(K, O, m, rp_old, inv_perm, g->in_rp, src, g->in_col, e_at);
+  if (m > 0) {
+    scatter_edges<<<grid_for(m, 256), 256, 0, s>>>(K, O, m, rp_old, inv_perm, g->in_rp, src, src_val,
+                                                   g->in_col, g->in_val);
     BUILD_TRY(cudaGetLastError());
   }
   // plan: degree classes over the (non-increasing) relabelled degrees
@@ -600,48 +556,6 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   for (int i = 0; i < pl.n_segs; ++i) pl.segs[i].task_begin += pl.n_hub_tasks;
   if (task + pl.n_hub_tasks >= INT32_MAX) { cleanup(); return Status{GOPS_ERR_INVALID, "graph too large"}; }
   pl.n_tasks = (int32_t)(task + pl.n_hub_tasks);
-  // the transition weights: everything above ran while the weights were
-  // being copied; each chunk's rows run as soon as the chunk has landed
-  if (d_w && n > 0) {
-    WeightArrival one;
-    one.row_start[1] = n;
-    const WeightArrival &w_in = wa ? *wa : one;
-    ChunkRows cr{};
-    cr.chunks = w_in.chunks;
-    for (int c = 0; c <= w_in.chunks; ++c) cr.start[c] = w_in.row_start[c];
-    BUILD_TRY(dev_malloc_async((void **)&wcounts, sizeof(unsigned) * 4 * kWeightChunks, s));
-    BUILD_TRY(cudaMemsetAsync(wcounts, 0, sizeof(unsigned) * 4 * kWeightChunks, s));
-    BUILD_TRY(dev_malloc_async((void **)&wkey, sizeof(uint32_t) * nn, s));
-    // rows by (chunk, size class); the node-sort buffers (nk, nv, nk2, nv2;
-    // n entries each) are free again after the plan
-    weight_row_keys<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(d_out_rp, n, cr, wkey, wcounts);
-    BUILD_TRY(cudaGetLastError());
-    bool alt = false;
-    BUILD_ST(radix_sort_index_u32(wkey, nk, nv, nk2, nv2, n, 4, &alt, s));
-    const uint32_t *order = alt ? nv2 : nv;
-    unsigned cnt[4 * kWeightChunks];
-    BUILD_TRY(cudaMemcpyAsync(cnt, wcounts, sizeof(cnt), cudaMemcpyDeviceToHost, s));
-    BUILD_TRY(cudaStreamSynchronize(s));
-    int64_t off = 0;
-    for (int c = 0; c < w_in.chunks; ++c) {
-      if (w_in.ready[c]) BUILD_TRY(cudaStreamWaitEvent(s, w_in.ready[c], 0));
-      const int64_t nbig = cnt[4 * c], nmid = cnt[4 * c + 1], nlight = cnt[4 * c + 2];
-      if (nbig)
-        weights_big<<<(unsigned)std::min<int64_t>(nbig, ctx->num_sms * 8), 256, 0, s>>>(
-            order + off, nbig, d_out_rp, d_w, val, dmask_old);
-      if (nmid)
-        weights_mid<<<blocks_for(nmid, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
-            order + off + nbig, nmid, d_out_rp, d_w, val, dmask_old);
-      if (nlight)
-        weights_light<<<blocks_for(nlight, 256, ctx->num_sms * 8), 256, 0, s>>>(
-            order + off + nbig + nmid, nlight, d_out_rp, d_w, val, dmask_old);
-      BUILD_TRY(cudaGetLastError());
-      off += nbig + nmid + nlight;
-    }
-    permute_dmask<<<(unsigned)ceil_div<int64_t>(n, 256), 256, 0, s>>>(g->perm, n, dmask_old, g->dmask_w);
-    gather_weights<<<grid_for(m_stored + 64, 256), 256, 0, s>>>(e_at, m_stored + 64, val, g->in_val);
-    BUILD_TRY(cudaGetLastError());
-  }
   BUILD_TRY(cudaStreamSynchronize(s));
   cleanup();
   return Status::ok();

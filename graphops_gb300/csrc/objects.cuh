@@ -57,11 +57,6 @@ struct Workspace {
   struct SolveState *state = nullptr;   // device-side run record
 };
 
-// chunks of the weight upload of gops_graph_upload (whole out-rows each):
-// the transition weights of chunk c are computed while chunk c + 1 is in flight
-constexpr int kWeightChunks = 4;
-constexpr int64_t kWeightChunkMinEdges = int64_t(1) << 22;  // smaller graphs: one chunk
-
 struct SolveState {
   unsigned long long iterations;
   unsigned long long f32_from;  // first step run in the FP32 phase (0: none)
@@ -103,12 +98,10 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   SolveState *host_state = nullptr;  // pinned
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  // a second stream for the weight upload, which overlaps the input checks,
-  // the edge sort and the structure of the build in gops_graph_upload;
-  // copy_ev[0] orders it after the column copy, copy_ev[1 + c] marks weight
-  // chunk c on the device
+  // a second stream for the weight upload, which overlaps the input checks
+  // and the edge sort of gops_graph_upload; copy_ev orders it against stream
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t copy_ev[1 + kWeightChunks] = {};
+  cudaEvent_t copy_ev[2] = {nullptr, nullptr};
   // optional per-launch timing of the iteration kernels (gops_ctx_set_timing)
   bool timing = false;
   std::vector<cudaEvent_t> tev;
@@ -128,19 +121,11 @@ Status solve_plain_in_workspace(Ctx *ctx, Graph *g, const gops_config *cfg, Work
 // a device with its first context, released with its last
 Status noalloc_attach(int device);
 void noalloc_detach(int device);
-// How the weights reach the device: `chunks` runs of whole out-rows, chunk c
-// = rows [row_start[c], row_start[c+1]), complete after event ready[c]
-// (nullptr: already on the device).  The build reads a chunk's weights only
-// after its event, and everything that needs no weights before the first.
-struct WeightArrival {
-  int chunks = 1;
-  int64_t row_start[kWeightChunks + 1] = {};
-  cudaEvent_t ready[kWeightChunks] = {};
-};
-// wa == nullptr: the weights (if any) are on the device already.
+// w_ready (optional): an event after which d_w is complete; the build
+// orders its first read of d_w after it.
 Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_rp,
                                        const int32_t *d_out_col, const double *d_w,
-                                       const WeightArrival *wa = nullptr);
+                                       cudaEvent_t w_ready = nullptr);
 Status workspace_ensure(Ctx *ctx, Graph *g);
 void workspace_free(Workspace &ws);
 void graph_free_device(Graph &g);

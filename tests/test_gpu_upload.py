@@ -123,16 +123,16 @@ def _pair_weight(u, v):
     return np.where(h % 29 == 0, np.nan, w)
 
 
-def test_chunked_weight_upload_matches_the_one_chunk_build():
-    """Over 4 M edges gops_graph_upload copies the weights in chunks of whole
-    rows and turns each chunk into transition weights as it lands;
-    gops_graph_from_edges builds the same out-adjacency with its weights
-    already on the device (one chunk).  The graph has rows of every size
-    class (1-7 entries: a lane each; 8-256: an 8-lane group; 257-3,000 and a
-    hub row with more than half of the edges: a block each, the hub leaving a
-    chunk empty), rows whose weights are all zero (dangling by weight),
-    negative and NaN weights, and rows without edges.  The two builds give
-    bit-identical weighted solves, and match the oracle's restatement."""
+def test_large_weighted_upload_matches_the_edge_list_build():
+    """gops_graph_upload (weights copied on the second stream while the edge
+    sort runs) against gops_graph_from_edges (the same out-adjacency built
+    on the device from the raw edge list, weights already there), over 4 M
+    edges: rows of 1-7 entries, 8-256 entries (an 8-lane group each in the
+    row-sum pass), 257-3,000 entries and a hub row with more than half of the
+    edges (a block each), rows whose weights are all zero (dangling by
+    weight), negative and NaN weights, and rows without edges.  The two
+    builds give bit-identical weighted solves, and match the oracle's
+    restatement."""
     from oracle import port
     rng = np.random.default_rng(12)
     n = 400_000

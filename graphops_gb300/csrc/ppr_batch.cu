@@ -67,6 +67,10 @@ constexpr double kBTheta = 1e-1;      // double-float phase while some column ha
 // 2; a column started from s (no judge, or a learned set over the push
 // budget) keeps the cold threshold, whatever its wave
 constexpr double kBThetaWarm = 5e-1;
+// first step that skips the rows without in-edges (WaveScalars::skip_from):
+// both gathered blocks have been written with their exact zeros by steps 2
+// and 3, also after a caller's start vector (step 1 writes x0's residual)
+constexpr int kSkipFrom = 4;
 
 struct ColState {
   unsigned long long iterations;
@@ -99,6 +103,15 @@ struct WaveScalars {
   unsigned long long max_iter;
   int has_x0;
   int kt;  // columns of the wave's blocks (row stride)
+  // From step skip_from on, rows without in-edges (rows [n_nz, n)) are
+  // skipped but for the n_srow rows listed in srow (those of them that seed
+  // a set of the wave): with no in-edge and no personalization their step
+  // residual is exactly 0 from step 2 on, and everything the step would write
+  // for them (tail, both gathered blocks, the double-float accumulator)
+  // already holds that value once steps 2 and 3 have written both blocks.
+  // A wave with a uniform column (empty seed set) skips nothing.
+  int skip_from;
+  int n_srow;
 };
 struct WaveConst {
   WaveScalars s;
@@ -136,7 +149,9 @@ struct BatchState {
   int32_t *pslot = nullptr;   // seed entries of the wave: column slot
   float2 *pval = nullptr;     //   and normalised weight (double-float)
   int32_t *prows_sorted = nullptr;
+  int32_t *srow = nullptr;    // the wave's seeded rows without in-edges (pcap entries)
   int64_t pcap = 0;
+  int32_t n_nz = 0;           // rows with an in-edge: rows [0, n_nz) (in-degree order)
   float *x0 = nullptr;        // warm-start vectors of the wave (set-major, original order)
   float *out = nullptr;       // results of the wave (set-major, original order)
   int64_t x0_cols = 0, out_cols = 0;
@@ -191,7 +206,8 @@ void batch_free(Graph &g) {
   free_plan(b);
   free_blocks(b);
   cudaFree(b->sums); cudaFree(b->cols); cudaFree(b->wave); cudaFree(b->wc); cudaFree(b->prow);
-  cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted); cudaFree(b->x0); cudaFree(b->out);
+  cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted); cudaFree(b->srow); cudaFree(b->x0);
+  cudaFree(b->out);
   cudaFree(b->d_inv_perm);
   if (b->hstage[0]) cudaFreeHost(b->hstage[0]);
   if (b->hstage[1]) cudaFreeHost(b->hstage[1]);
@@ -217,6 +233,8 @@ struct StepParams {
   const int32_t *big_first, *big_task_row, *blk_first;
   const int32_t *prow, *pslot;
   const float2 *pval;
+  int32_t n_nz;
+  const int32_t *srow;
   __nv_bfloat16 *glo[2];
   float *gf[2];
   float2 *acc;
@@ -809,7 +827,9 @@ __global__ void __launch_bounds__(kBThreads) spmm_f32(StepParams p) {
   const int kt = wc.kt;
   LaneAcc<CPL> a(&bl1[wid][lane * CPL], &bdg[wid][lane * CPL], &bbad[wid][lane]);
   const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
-  const int64_t nwt = p.n_big_tasks + (p.n - p.n_big);
+  const bool skip = k >= (unsigned long long)wc.skip_from;
+  const int64_t nreg = (skip ? (int64_t)p.n_nz : p.n) - p.n_big;  // regular rows taken in order
+  const int64_t nwt = p.n_big_tasks + nreg + (skip ? wc.n_srow : 0);
   for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
     if (w < p.n_big_tasks) {
       int h, first, nch, b0, nb, cs, ce, rb;
@@ -834,7 +854,8 @@ __global__ void __launch_bounds__(kBThreads) spmm_f32(StepParams p) {
         f32_epilogue<CPL, L2H>(p, wc, h, all, bi, ln, out, a, lane);
       }
     } else if (ln.any) {
-      const int64_t v = p.n_big + (w - p.n_big_tasks);
+      const int64_t r = w - p.n_big_tasks;
+      const int64_t v = r < nreg ? p.n_big + r : (int64_t)__ldg(&p.srow[r - nreg]);
       const BIn<CPL> bi = b_in<CPL, L2H>(p, wc, v, lane, ln, false, true);
       const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
       // canonical row sum: base blocks from eb, added in order
@@ -860,7 +881,9 @@ __global__ void __launch_bounds__(kBThreads, 2) spmm_mixed(StepParams p) {
   const int kt = wc.kt;
   LaneAcc<CPL> a(&bl1[wid][lane * CPL], &bdg[wid][lane * CPL], &bbad[wid][lane]);
   const int64_t nwarps = (int64_t)gridDim.x * kBWarps;
-  const int64_t nwt = p.n_big_tasks + (p.n - p.n_big);
+  const bool skip = k >= (unsigned long long)wc.skip_from;
+  const int64_t nreg = (skip ? (int64_t)p.n_nz : p.n) - p.n_big;  // regular rows taken in order
+  const int64_t nwt = p.n_big_tasks + nreg + (skip ? wc.n_srow : 0);
   for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
     if (w < p.n_big_tasks) {
       int h, first, nch, b0, nb, cs, ce, rb;
@@ -888,7 +911,8 @@ __global__ void __launch_bounds__(kBThreads, 2) spmm_mixed(StepParams p) {
         mix_epilogue<CPL>(p, wc, h, all, bi, ln, out, k, a, lane);
       }
     } else if (ln.any) {
-      const int64_t v = p.n_big + (w - p.n_big_tasks);
+      const int64_t r = w - p.n_big_tasks;
+      const int64_t v = r < nreg ? p.n_big + r : (int64_t)__ldg(&p.srow[r - nreg]);
       const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, true, ln.fmask != 0);
       const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
       MixSum<CPL> tot = mix_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane);
@@ -1131,6 +1155,17 @@ Status batch_prepare(Ctx *ctx, Graph *g) {
   return st;
 }
 
+// out[0] += rows with an in-edge, out[1] = min(out[1], first row without one)
+__global__ void nonempty_rows(const int64_t *rp, int64_t n, unsigned long long *out) {
+  unsigned long long c = 0, first = ~0ull;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    if (rp[v + 1] > rp[v]) ++c;
+    else if ((unsigned long long)v < first) first = (unsigned long long)v;
+  }
+  if (c) atomicAdd(&out[0], c);
+  if (first != ~0ull) atomicMin(&out[1], first);
+}
+
 Status batch_prepare_impl(Ctx *ctx, Graph *g) {
   cudaStream_t s = ctx->stream;
   BatchState *b = new BatchState();
@@ -1146,6 +1181,22 @@ Status batch_prepare_impl(Ctx *ctx, Graph *g) {
   GOPS_CUDA_TRY(cudaMalloc(&b->wave, sizeof(WaveState)));
   GOPS_CUDA_TRY(cudaMalloc(&b->wc, sizeof(WaveConst)));
   GOPS_CUDA_TRY(cudaMalloc(&b->prow, sizeof(int32_t) * (n + 1)));
+  // rows with an in-edge: a prefix of the in-degree order (if the count and
+  // the first empty row disagree, nothing is skipped)
+  {
+    unsigned long long *d = nullptr, h[2] = {0, ~0ull};
+    GOPS_CUDA_TRY(cudaMalloc(&d, sizeof(h)));
+    cudaError_t e = cudaMemcpyAsync(d, h, sizeof(h), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && n > 0) {
+      nonempty_rows<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(g->in_rp, n, d);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d);
+    GOPS_CUDA_TRY(e);
+    b->n_nz = (int32_t)(h[1] == h[0] ? h[0] : (unsigned long long)n);
+  }
   // host copy of the relabelling, inverted
   std::vector<int32_t> perm((size_t)n);
   GOPS_CUDA_TRY(cudaMemcpyAsync(perm.data(), g->perm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
@@ -1239,13 +1290,14 @@ Status ensure_entries(BatchState *b, int64_t e, cudaStream_t st) {
   if (e <= b->pcap) return Status::ok();
   GOPS_CUDA_TRY(cudaStreamSynchronize(st));  // earlier waves may still read the old arrays
   free_graphs(b);                            // the captured chunks name the old arrays
-  cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted);
-  b->pslot = nullptr; b->pval = nullptr; b->prows_sorted = nullptr;
+  cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted); cudaFree(b->srow);
+  b->pslot = nullptr; b->pval = nullptr; b->prows_sorted = nullptr; b->srow = nullptr;
   b->pcap = 0;  // a failed allocation below leaves no capacity claimed
   const int64_t cap = std::max<int64_t>(e, 4096);
   GOPS_CUDA_TRY(cudaMalloc(&b->pslot, sizeof(int32_t) * cap));
   GOPS_CUDA_TRY(cudaMalloc(&b->pval, sizeof(float2) * cap));
   GOPS_CUDA_TRY(cudaMalloc(&b->prows_sorted, sizeof(int32_t) * cap));
+  GOPS_CUDA_TRY(cudaMalloc(&b->srow, sizeof(int32_t) * cap));
   b->pcap = cap;
   return Status::ok();
 }
@@ -1269,6 +1321,8 @@ StepParams step_params(const Graph *g, const BatchState *b) {
   p.prow = b->prow;
   p.pslot = b->pslot;
   p.pval = b->pval;
+  p.n_nz = b->n_nz;
+  p.srow = b->srow;
   p.glo[0] = b->glo[0];
   p.glo[1] = b->glo[1];
   p.gf[0] = b->gf[0];
@@ -1366,6 +1420,8 @@ void fill_wave_const(WaveScalars &w, const gops_config *cfg, int64_t n, int kt, 
   w.ncols = ncols;
   w.has_x0 = has_x0 ? 1 : 0;
   w.kt = kt;
+  w.skip_from = INT32_MAX;  // set per wave by its caller
+  w.n_srow = 0;
   // fixed-point range: a start of L1 norm up to wmax keeps every partial
   // sum far below 2^63; larger or non-finite starts are flagged by the
   // nonfinite counter and the column does not converge
@@ -1620,8 +1676,9 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   // wave w+1 while wave w runs on the device.
   struct HostWave {
     int ncols = 0;
+    bool uniform = false;  // some column has the uniform personalization
     std::vector<ColState> cols;
-    std::vector<int32_t> erow, eslot;
+    std::vector<int32_t> erow, eslot, srow;
     std::vector<float2> eval;
   } hw[2];
   auto prep = [&](HostWave &h, int64_t set0) {
@@ -1633,18 +1690,25 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       h.cols[c] = ColState{0, 0.0, c < h.ncols ? 0 : 1, 0, 0, 0, r1,
                            x0 && std::isfinite(r1) ? kBThetaWarm : kBTheta};
     }
+    h.uniform = false;
     for (int c = 0; c < h.ncols; ++c) {
       const int64_t a0 = seed_ptr[order[set0 + c]], a1 = seed_ptr[order[set0 + c] + 1];
-      if (a1 == a0) { h.cols[c].uniform = 1; continue; }  // sum <= 0: uniform (src/ppr.rs:108)
+      if (a1 == a0) {  // sum <= 0: uniform (src/ppr.rs:108)
+        h.cols[c].uniform = 1;
+        h.uniform = true;
+        continue;
+      }
       const double inv = 1.0 / (double)(a1 - a0);
       for (int64_t k = a0; k < a1; ++k) ent[{b->inv_perm[(size_t)seed_idx[k]], c}] += inv;
     }
-    h.erow.clear(); h.eslot.clear(); h.eval.clear();
-    for (const auto &kv : ent) {
-      h.erow.push_back(kv.first.first);
+    h.erow.clear(); h.eslot.clear(); h.eval.clear(); h.srow.clear();
+    for (const auto &kv : ent) {  // by row, then column
+      const int32_t r = kv.first.first;
+      h.erow.push_back(r);
       h.eslot.push_back(kv.first.second);
       const df w = df_from_double(kv.second);
       h.eval.push_back(make_float2(w.hi, w.lo));
+      if (r >= b->n_nz && (h.srow.empty() || h.srow.back() != r)) h.srow.push_back(r);
     }
   };
   // per-column records of every wave stay on the device until the end
@@ -1685,6 +1749,11 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       w.xcol[c] = x0 && !x0_on_device ? c : sid;
       w.ocol[c] = scores && !scores_on_device ? c : sid;
     }
+    w.s.skip_from = h.uniform ? INT32_MAX : kSkipFrom;
+    w.s.n_srow = (int)h.srow.size();
+    if (!h.srow.empty())
+      GOPS_CUDA_TRY(cudaMemcpyAsync(b->srow, h.srow.data(), sizeof(int32_t) * h.srow.size(), cudaMemcpyHostToDevice,
+                                    st));
     const int64_t ne = (int64_t)h.erow.size();
     if (ne) {
       GOPS_CUDA_TRY(cudaMemcpyAsync(b->prows_sorted, h.erow.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, st));

@@ -176,3 +176,48 @@ def test_every_tile_gives_the_same_bits():
     assert cost_l2 > 0 and l2 == (cost_l2 < cost[cost > 0].min())
     r = go.ppr_batch(dg, conf, sp, si)
     assert np.array_equal(r.scores, first[0].scores)
+
+
+def test_rows_without_in_edges_skipped_bit_for_bit():
+    """From step 4 a wave skips the rows without in-edges that seed none of
+    its sets (their step residual is exactly 0 from step 2 on); a wave with
+    an empty seed set (uniform personalization) skips nothing.  The same 40
+    sets -- many seeded on rows without in-edges, some solved from caller
+    start vectors -- in one wave alone, and in one wave with an empty set
+    added, give the same bits, and match the oracle."""
+    g = gen.rmat(14, 8, seed=31)
+    n = g.n
+    indeg = np.bincount(np.asarray(g.col), minlength=n)
+    outdeg = np.diff(np.asarray(g.row_ptr))
+    no_in = np.nonzero((indeg == 0) & (outdeg > 0))[0]
+    rng = np.random.default_rng(5)
+    sets = []
+    for i in range(40):
+        k = int(rng.integers(1, 9))
+        s = list(rng.choice(no_in, size=min(k, len(no_in)), replace=False)) if i % 2 == 0 else []
+        s += list(rng.integers(0, n, size=k))
+        sets.append([int(v) for v in s])
+    sp, si = go.seed_sets_to_csr(sets)
+    sp_u, si_u = go.seed_sets_to_csr(sets + [[]])
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    dg.set_batch_tile(64, 256, False)
+    conf = go.PageRankConfig(0.85, 1000, 1e-7)
+    a = go.ppr_batch(dg, conf, sp, si)
+    b = go.ppr_batch(dg, conf, sp_u, si_u)
+    assert np.array_equal(a.scores, b.scores[:40])
+    assert np.array_equal(a.iterations, b.iterations[:40]) and a.converged.all()
+    # the skipping steps ran (a set seeded only on nodes without edges is its
+    # own fixed point and stops after one step)
+    assert (a.iterations >= 6).sum() >= 30
+    ref, its = port.ppr_many(g.row_ptr, g.col, sp, si, 0.85, 1000, 1e-7, threads=8)
+    assert np.abs(a.scores.astype(np.float64) - ref).sum(axis=1).max() <= L1_TARGET
+    assert np.array_equal(a.iterations, its.astype(np.int64))
+    # caller start vectors (every entry nonzero, rows without in-edges included)
+    x0 = np.full((40, n), 1.0 / n, dtype=np.float32)
+    x0_u = np.full((41, n), 1.0 / n, dtype=np.float32)
+    c = go.ppr_batch(dg, conf, sp, si, x0=x0)
+    d = go.ppr_batch(dg, conf, sp_u, si_u, x0=x0_u)
+    assert np.array_equal(c.scores, d.scores[:40])
+    assert np.array_equal(c.iterations, d.iterations[:40])
+    # another start: each result within d/(1-d) tol of the fixed point, like the oracle's
+    assert np.abs(c.scores.astype(np.float64) - ref).sum(axis=1).max() <= 1e-6

@@ -380,6 +380,9 @@ def batch_roofline(g, st, kt):
                                    "frac": round(achg / peak, 4) if achg else None,
                                    "note": "8(N+1) + 4m + 8Nk + 4mk: every in-edge gathers its source's k-tile row"},
             "df_phase_mean_ms": round(st.df_ms / max(1, st.df_launches), 5), "df_launches": int(st.df_launches),
+            "note": "the formula counts every row; from step 4 the step skips the rows without in-edges "
+                    "that seed none of the wave's sets (their entries are exact zeros already), so it "
+                    "moves fewer bytes than the formula names",
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"}
 
 

@@ -68,9 +68,12 @@ constexpr double kBTheta = 1e-1;      // double-float phase while some column ha
 // budget) keeps the cold threshold, whatever its wave
 constexpr double kBThetaWarm = 5e-1;
 // first step that skips the rows without in-edges (WaveScalars::skip_from):
-// both gathered blocks have been written with their exact zeros by steps 2
-// and 3, also after a caller's start vector (step 1 writes x0's residual)
-constexpr int kSkipFrom = 4;
+// from a cold start the initialisation writes their zeros into gathered
+// block 0 (and the accumulator and tail) and step 1 into block 1; after a
+// caller's start vector step 1 writes its residual -x0, so steps 2 and 3
+// write the zeros into both blocks first
+constexpr int kSkipFromCold = 2;
+constexpr int kSkipFromWarm = 4;
 
 struct ColState {
   unsigned long long iterations;
@@ -106,10 +109,11 @@ struct WaveScalars {
   // From step skip_from on, rows without in-edges (rows [n_nz, n)) are
   // skipped but for the n_srow rows listed in srow (those of them that seed
   // a set of the wave): with no in-edge and no personalization their step
-  // residual is exactly 0 from step 2 on, and everything the step would write
-  // for them (tail, both gathered blocks, the double-float accumulator)
-  // already holds that value once steps 2 and 3 have written both blocks.
-  // A wave with a uniform column (empty seed set) skips nothing.
+  // residual is exactly 0 (from step 1 from a cold start, from step 2 after
+  // a caller's start vector), and everything the step would write for them
+  // (tail, both gathered blocks, the double-float accumulator) already holds
+  // that value once both blocks have been written with it.  A wave with a
+  // uniform column (empty seed set) skips nothing.
   int skip_from;
   int n_srow;
 };
@@ -1749,7 +1753,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
       w.xcol[c] = x0 && !x0_on_device ? c : sid;
       w.ocol[c] = scores && !scores_on_device ? c : sid;
     }
-    w.s.skip_from = h.uniform ? INT32_MAX : kSkipFrom;
+    w.s.skip_from = h.uniform ? INT32_MAX : x0 ? kSkipFromWarm : kSkipFromCold;
     w.s.n_srow = (int)h.srow.size();
     if (!h.srow.empty())
       GOPS_CUDA_TRY(cudaMemcpyAsync(b->srow, h.srow.data(), sizeof(int32_t) * h.srow.size(), cudaMemcpyHostToDevice,

@@ -1159,15 +1159,20 @@ Status batch_prepare(Ctx *ctx, Graph *g) {
   return st;
 }
 
-// out[0] += rows with an in-edge, out[1] = min(out[1], first row without one)
+// out[0] += rows with an in-edge, out[1] = min(out[1], first row without
+// one); rows are below 2^31, so the warp reductions run on 32 bits
 __global__ void nonempty_rows(const int64_t *rp, int64_t n, unsigned long long *out) {
-  unsigned long long c = 0, first = ~0ull;
+  unsigned c = 0, first = ~0u;
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
     if (rp[v + 1] > rp[v]) ++c;
-    else if ((unsigned long long)v < first) first = (unsigned long long)v;
+    else if ((unsigned)v < first) first = (unsigned)v;
   }
-  if (c) atomicAdd(&out[0], c);
-  if (first != ~0ull) atomicMin(&out[1], first);
+  c = __reduce_add_sync(0xffffffffu, c);
+  first = __reduce_min_sync(0xffffffffu, first);
+  if ((threadIdx.x & 31) == 0) {
+    if (c) atomicAdd(&out[0], (unsigned long long)c);
+    if (first != ~0u) atomicMin(&out[1], (unsigned long long)first);
+  }
 }
 
 Status batch_prepare_impl(Ctx *ctx, Graph *g) {

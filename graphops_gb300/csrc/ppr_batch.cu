@@ -506,13 +506,28 @@ __device__ __forceinline__ MixSum<CPL> mix_zero() {
   return r;
 }
 
+// One gathered entry into a base block's sums: the high words with an exact
+// two-sum (Knuth), its error and the entry's low word into an FP32 low word
+// that is renormalised once per base block (mix_normalize), 8 instead of
+// 11 FP32 operations per double-float column; the low sum of a 256-edge
+// block keeps the result to about 2^-32 of its largest term, the precision
+// of the stored (BF16) low words themselves.
 template <int CPL>
 __device__ __forceinline__ void mix_add(MixSum<CPL> &s, const DV<CPL> &g) {
 #pragma unroll
   for (int q = 0; q < CPL; ++q) {
-    s.d.v[q] = df_add(s.d.v[q], g.v[q]);
+    const df t = two_sum(s.d.v[q].hi, g.v[q].hi);
+    s.d.v[q] = {t.hi, __fadd_rn(s.d.v[q].lo, __fadd_rn(t.lo, g.v[q].lo))};
     s.f.v[q] += g.v[q].hi;
   }
+}
+
+// the base block's double-float sums back to (hi, lo) with |lo| <= ulp(hi)/2
+// (a full two-sum: the high sum may have cancelled below the low one)
+template <int CPL>
+__device__ __forceinline__ void mix_normalize(MixSum<CPL> &s) {
+#pragma unroll
+  for (int q = 0; q < CPL; ++q) s.d.v[q] = two_sum(s.d.v[q].hi, s.d.v[q].lo);
 }
 
 template <int CPL>
@@ -559,6 +574,7 @@ __device__ __forceinline__ MixSum<CPL> mix_block(const StepParams &p, int in, in
     for (int q = 0; q < U; ++q)
       if (q < 4 || ok2) mix_add<CPL>(s, g[q]);
   }
+  mix_normalize<CPL>(s);
   return s;
 }
 

@@ -221,6 +221,10 @@ void gops_ctx_destroy(gops_ctx *ctx) {
   if (x.copy_stream) cudaStreamSynchronize(x.copy_stream);
   for (int i = 0; i < 2; ++i)
     if (x.copy_ev[i]) cudaEventDestroy(x.copy_ev[i]);
+  for (int i = 0; i < 2; ++i) {
+    if (x.hstage[i]) cudaFreeHost(x.hstage[i]);
+    if (x.sev[i]) cudaEventDestroy(x.sev[i]);
+  }
   if (x.copy_stream) cudaStreamDestroy(x.copy_stream);
   if (x.host_state) cudaFreeHost(x.host_state);
   for (cudaEvent_t e : x.tev) cudaEventDestroy(e);

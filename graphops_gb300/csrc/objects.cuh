@@ -102,6 +102,12 @@ struct Ctx {
   // and the edge sort of gops_graph_upload; copy_ev orders it against stream
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_ev[2] = {nullptr, nullptr};
+  // pinned host staging of the batched path's result blocks (two waves in
+  // flight), kept across calls and graphs: pinning is slow next to a solve;
+  // sev[q] follows the copy into hstage[q]
+  float *hstage[2] = {nullptr, nullptr};
+  size_t hstage_bytes = 0;
+  cudaEvent_t sev[2] = {nullptr, nullptr};
   // optional per-launch timing of the iteration kernels (gops_ctx_set_timing)
   bool timing = false;
   std::vector<cudaEvent_t> tev;

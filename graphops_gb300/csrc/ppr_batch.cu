@@ -159,9 +159,6 @@ struct BatchState {
   float *x0 = nullptr;        // warm-start vectors of the wave (set-major, original order)
   float *out = nullptr;       // results of the wave (set-major, original order)
   int64_t x0_cols = 0, out_cols = 0;
-  float *hstage[2] = {nullptr, nullptr};  // pinned host copies of two waves' results
-  size_t hstage_bytes = 0;
-  cudaEvent_t sev[2] = {nullptr, nullptr};  // after each pinned copy
   WaveState *hwave = nullptr;             // pinned: two polled copies of the wave record
   cudaEvent_t wev[2] = {nullptr, nullptr};
   std::vector<int32_t> inv_perm;  // host: original id -> relabelled row
@@ -213,10 +210,6 @@ void batch_free(Graph &g) {
   cudaFree(b->pslot); cudaFree(b->pval); cudaFree(b->prows_sorted); cudaFree(b->srow); cudaFree(b->x0);
   cudaFree(b->out);
   cudaFree(b->d_inv_perm);
-  if (b->hstage[0]) cudaFreeHost(b->hstage[0]);
-  if (b->hstage[1]) cudaFreeHost(b->hstage[1]);
-  for (cudaEvent_t e : b->sev)
-    if (e) cudaEventDestroy(e);
   if (b->hwave) cudaFreeHost(b->hwave);
   for (cudaEvent_t e : b->wev)
     if (e) cudaEventDestroy(e);
@@ -1642,20 +1635,21 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   // the next wave (two buffers; a buffer's scatter is joined before reuse)
   const size_t block_bytes = sizeof(float) * (size_t)KT * (size_t)n;
   const bool staged = scores && !scores_on_device && block_bytes <= (size_t(1) << 31);
-  if (staged && b->hstage_bytes < block_bytes) {
-    for (auto &h : b->hstage)
+  // the context's pinned staging, grown when a wave's block does not fit
+  if (staged && ctx->hstage_bytes < block_bytes) {
+    for (auto &h : ctx->hstage)
       if (h) {
         cudaFreeHost(h);
         h = nullptr;
       }
-    b->hstage_bytes = 0;
-    GOPS_CUDA_TRY(cudaMallocHost(&b->hstage[0], block_bytes));
-    GOPS_CUDA_TRY(cudaMallocHost(&b->hstage[1], block_bytes));
-    b->hstage_bytes = block_bytes;
-    if (!b->sev[0]) {
-      GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->sev[0], cudaEventDisableTiming));
-      GOPS_CUDA_TRY(cudaEventCreateWithFlags(&b->sev[1], cudaEventDisableTiming));
-    }
+    ctx->hstage_bytes = 0;
+    GOPS_CUDA_TRY(cudaMallocHost(&ctx->hstage[0], block_bytes));
+    GOPS_CUDA_TRY(cudaMallocHost(&ctx->hstage[1], block_bytes));
+    ctx->hstage_bytes = block_bytes;
+  }
+  if (staged && !ctx->sev[0]) {
+    GOPS_CUDA_TRY(cudaEventCreateWithFlags(&ctx->sev[0], cudaEventDisableTiming));
+    GOPS_CUDA_TRY(cudaEventCreateWithFlags(&ctx->sev[1], cudaEventDisableTiming));
   }
   constexpr int kScatterThreads = 4;
   struct Scatter {
@@ -1685,8 +1679,8 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   int pend_copy_q = -1;  // the last wave whose block went to a pinned buffer
   auto start_scatter = [&]() -> Status {
     if (pend.set0 < 0) return Status::ok();
-    GOPS_CUDA_TRY(cudaEventSynchronize(b->sev[pend.q]));
-    const float *src = b->hstage[pend.q];
+    GOPS_CUDA_TRY(cudaEventSynchronize(ctx->sev[pend.q]));
+    const float *src = ctx->hstage[pend.q];
     const int ncols_p = pend.ncols;
     const std::vector<int64_t> ids(order.begin() + pend.set0, order.begin() + pend.set0 + ncols_p);
     for (int t = 0; t < kScatterThreads; ++t)
@@ -1897,7 +1891,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     if (scores) {
       float *outw = scores_on_device ? scores : b->out;
       // the previous wave's pinned copy (on the copy stream) has read b->out
-      if (staged && pend_copy_q >= 0) GOPS_CUDA_TRY(cudaStreamWaitEvent(st, b->sev[pend_copy_q], 0));
+      if (staged && pend_copy_q >= 0) GOPS_CUDA_TRY(cudaStreamWaitEvent(st, ctx->sev[pend_copy_q], 0));
       batch_finalize_t<<<blocks_for(ceil_div<int64_t>(n, kTile) * (KT / kTile), kBWarps, ctx->num_sms * 8), kBThreads,
                          0, st>>>(p, outw, b->d_inv_perm);
       GOPS_CUDA_TRY(cudaGetLastError());
@@ -1909,9 +1903,9 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
         scatter.join(q);  // the scatter of two waves ago read this buffer
         GOPS_CUDA_TRY(cudaEventRecord(ctx->copy_ev[0], st));
         GOPS_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[0], 0));
-        GOPS_CUDA_TRY(cudaMemcpyAsync(b->hstage[q], b->out, sizeof(float) * (size_t)ncols * n,
+        GOPS_CUDA_TRY(cudaMemcpyAsync(ctx->hstage[q], b->out, sizeof(float) * (size_t)ncols * n,
                                       cudaMemcpyDeviceToHost, ctx->copy_stream));
-        GOPS_CUDA_TRY(cudaEventRecord(b->sev[q], ctx->copy_stream));
+        GOPS_CUDA_TRY(cudaEventRecord(ctx->sev[q], ctx->copy_stream));
         pend_copy_q = q;
         ctx->stats.d2h_bytes += sizeof(float) * (size_t)ncols * n;
         pend.set0 = set0;

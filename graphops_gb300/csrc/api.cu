@@ -196,6 +196,7 @@ int gops_ctx_create(int device, gops_ctx **out) {
   for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&x.ev[i]);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x.copy_stream, cudaStreamNonBlocking);
   for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&x.copy_ev[i], cudaEventDisableTiming);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&x.build_ev[i], cudaEventDisableTiming);
   if (e != cudaSuccess) {
     gops_ctx_destroy(c);
     return e == cudaErrorMemoryAllocation ? GOPS_ERR_OOM : GOPS_ERR_CUDA;
@@ -221,6 +222,8 @@ void gops_ctx_destroy(gops_ctx *ctx) {
   if (x.copy_stream) cudaStreamSynchronize(x.copy_stream);
   for (int i = 0; i < 2; ++i)
     if (x.copy_ev[i]) cudaEventDestroy(x.copy_ev[i]);
+  for (int i = 0; i < 2; ++i)
+    if (x.build_ev[i]) cudaEventDestroy(x.build_ev[i]);
   for (int i = 0; i < 2; ++i) {
     if (x.hstage[i]) cudaFreeHost(x.hstage[i]);
     if (x.sev[i]) cudaEventDestroy(x.sev[i]);

@@ -376,7 +376,11 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   unsigned *maxdeg = nullptr;
   uint32_t *bigrows = nullptr;
   double *rowsum = nullptr;
+  // weight passes queued on the copy stream (the main stream waits for them
+  // before any buffer they use is freed)
+  bool copy_side = false;
   auto cleanup = [&]() {
+    if (copy_side) cudaStreamWaitEvent(s, ctx->build_ev[1], 0);
     free_async(src, s); free_async(keys, s); free_async(vals, s); free_async(keys2, s);
     free_async(vals2, s); free_async(nk, s); free_async(nv, s); free_async(nk2, s);
     free_async(nv2, s); free_async(dmask_old, s); free_async(src_val, s); free_async(deg_old, s);
@@ -435,6 +439,23 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, nullptr, src, deg_old, rowsum, bigrows);
     BUILD_TRY(cudaGetLastError());
   }
+  // The weight passes need the weights, the structure pass and nothing of
+  // the relabelling: with the weights arriving on the copy stream they run
+  // there as soon as both are done, beside the main stream's relabelling.
+  if (w_ready && d_w && n > 0) {
+    cudaStream_t cs = ctx->copy_stream;
+    BUILD_TRY(cudaEventRecord(ctx->build_ev[0], s));
+    BUILD_TRY(cudaStreamWaitEvent(cs, ctx->build_ev[0], 0));
+    BUILD_TRY(cudaStreamWaitEvent(cs, w_ready, 0));
+    copy_side = true;
+    out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, cs>>>(
+        n, d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, cs>>>(d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+    row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, cs>>>(n, rowsum, dmask_old);
+    if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, cs>>>(m, d_w, src, rowsum, src_val);
+    BUILD_TRY(cudaGetLastError());
+    BUILD_TRY(cudaEventRecord(ctx->build_ev[1], cs));
+  }
   BUILD_TRY(dev_malloc_async((void **)&rp_old, sizeof(int64_t) * (n + 1), s));
   rp_from_sorted<<<grid_for(m + 1, 256), 256, 0, s>>>(K, m, n, rp_old);
   BUILD_TRY(cudaGetLastError());
@@ -486,13 +507,19 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(cudaMemsetAsync(g->in_val, 0, sizeof(float) * ms, s));
   }
   // the weights: everything above ran while they were being copied
-  if (w_ready) BUILD_TRY(cudaStreamWaitEvent(s, w_ready, 0));
+  if (copy_side) {
+    BUILD_TRY(cudaStreamWaitEvent(s, ctx->build_ev[1], 0));
+  } else {
+    if (w_ready) BUILD_TRY(cudaStreamWaitEvent(s, w_ready, 0));
+    if (d_w && n > 0) {
+      out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
+          n, d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+      out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, d_w, src, deg_old, rowsum, bigrows);
+      row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(n, rowsum, dmask_old);
+      if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, s>>>(m, d_w, src, rowsum, src_val);
+    }
+  }
   if (d_w && n > 0) {
-    out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
-        n, d_out_rp, d_w, src, deg_old, rowsum, bigrows);
-    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, d_w, src, deg_old, rowsum, bigrows);
-    row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(n, rowsum, dmask_old);
-    if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, s>>>(m, d_w, src, rowsum, src_val);
     permute_dmask<<<(unsigned)ceil_div<int64_t>(n, 256), 256, 0, s>>>(g->perm, n, dmask_old, g->dmask_w);
     BUILD_TRY(cudaGetLastError());
   }

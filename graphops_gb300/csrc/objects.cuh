@@ -102,6 +102,10 @@ struct Ctx {
   // and the edge sort of gops_graph_upload; copy_ev orders it against stream
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_ev[2] = {nullptr, nullptr};
+  // the graph build's hand-over to and from the copy stream: build_ev[0]
+  // after its structure pass (main stream), build_ev[1] after the weight
+  // passes that run on the copy stream once the weights have arrived
+  cudaEvent_t build_ev[2] = {nullptr, nullptr};
   // pinned host staging of the batched path's result blocks (two waves in
   // flight), kept across calls and graphs: pinning is slow next to a solve;
   // sev[q] follows the copy into hstage[q]

@@ -504,14 +504,15 @@ __device__ __forceinline__ MixSum<CPL> mix_zero() {
 // that is renormalised once per base block (mix_normalize), 8 instead of
 // 11 FP32 operations per double-float column; the low sum of a 256-edge
 // block keeps the result to about 2^-32 of its largest term, the precision
-// of the stored (BF16) low words themselves.
-template <int CPL>
+// of the stored (BF16) low words themselves.  WANT_F: some column of the
+// wave is in its FP32 phase and needs the FP32 sum of the high words.
+template <int CPL, bool WANT_F>
 __device__ __forceinline__ void mix_add(MixSum<CPL> &s, const DV<CPL> &g) {
 #pragma unroll
   for (int q = 0; q < CPL; ++q) {
     const df t = two_sum(s.d.v[q].hi, g.v[q].hi);
     s.d.v[q] = {t.hi, __fadd_rn(s.d.v[q].lo, __fadd_rn(t.lo, g.v[q].lo))};
-    s.f.v[q] += g.v[q].hi;
+    if constexpr (WANT_F) s.f.v[q] += g.v[q].hi;
   }
 }
 
@@ -543,7 +544,7 @@ __device__ __forceinline__ DV<CPL> gather_dv(const float *ghi, const __nv_bfloat
   return r;
 }
 
-template <int CPL>
+template <int CPL, bool WANT_F>
 __device__ __forceinline__ MixSum<CPL> mix_block(const StepParams &p, int in, int kt, int eb, int ee, int lane) {
   constexpr int U = CPL == 4 ? 4 : 8;
   const float *ghi = p.gf[in] + lane * CPL;
@@ -565,7 +566,7 @@ __device__ __forceinline__ MixSum<CPL> mix_block(const StepParams &p, int in, in
       if (q < 4 || ok2) g[q] = gather_dv<CPL>(ghi, glo, (int64_t)u[q] * kt);
 #pragma unroll
     for (int q = 0; q < U; ++q)
-      if (q < 4 || ok2) mix_add<CPL>(s, g[q]);
+      if (q < 4 || ok2) mix_add<CPL, WANT_F>(s, g[q]);
   }
   mix_normalize<CPL>(s);
   return s;
@@ -897,6 +898,16 @@ __global__ void __launch_bounds__(kBThreads, 2) spmm_mixed(StepParams p) {
   const bool skip = k >= (unsigned long long)wc.skip_from;
   const int64_t nreg = (skip ? (int64_t)p.n_nz : p.n) - p.n_big;  // regular rows taken in order
   const int64_t nwt = p.n_big_tasks + nreg + (skip ? wc.n_srow : 0);
+  // At 4 columns per lane the FP32 sums of the high words are kept only when
+  // some column is in its FP32 phase (the same for every warp: they read the
+  // same column records); narrower tiles keep one variant, within their
+  // register budget.
+  const bool want_f = __any_sync(0xffffffffu, ln.fmask != 0u);
+  auto block_sum = [&](int b0_, int b1_) {
+    if constexpr (CPL == 4)
+      if (!want_f) return mix_block<CPL, false>(p, in, kt, b0_, b1_, lane);
+    return mix_block<CPL, true>(p, in, kt, b0_, b1_, lane);
+  };
   for (int64_t w = (int64_t)blockIdx.x * kBWarps + wid; w < nwt; w += nwarps) {
     if (w < p.n_big_tasks) {
       int h, first, nch, b0, nb, cs, ce, rb;
@@ -904,7 +915,7 @@ __global__ void __launch_bounds__(kBThreads, 2) spmm_mixed(StepParams p) {
       if (ln.any)
         for (int b = cs; b < ce; b += kBase) {
           // per column: the double-float sum, or the FP32 sum as (s, 0)
-          const MixSum<CPL> s = mix_block<CPL>(p, in, kt, b, min(ce, b + kBase), lane);
+          const MixSum<CPL> s = block_sum(b, min(ce, b + kBase));
           DV<CPL> pk;
 #pragma unroll
           for (int q = 0; q < CPL; ++q) pk.v[q] = ((ln.fmask >> q) & 1u) ? df{s.f.v[q], 0.0f} : s.d.v[q];
@@ -928,8 +939,8 @@ __global__ void __launch_bounds__(kBThreads, 2) spmm_mixed(StepParams p) {
       const int64_t v = r < nreg ? p.n_big + r : (int64_t)__ldg(&p.srow[r - nreg]);
       const BIn<CPL> bi = b_in<CPL>(p, wc, v, lane, ln, true, ln.fmask != 0);
       const int eb = (int)__ldg(&p.rp[v]), ee = (int)__ldg(&p.rp[v + 1]);
-      MixSum<CPL> tot = mix_block<CPL>(p, in, kt, eb, min(ee, eb + kBase), lane);
-      for (int b = eb + kBase; b < ee; b += kBase) mix_add<CPL>(tot, mix_block<CPL>(p, in, kt, b, min(ee, b + kBase), lane));
+      MixSum<CPL> tot = block_sum(eb, min(ee, eb + kBase));
+      for (int b = eb + kBase; b < ee; b += kBase) mix_add<CPL>(tot, block_sum(b, min(ee, b + kBase)));
       mix_epilogue<CPL>(p, wc, v, tot, bi, ln, out, k, a, lane);
     }
   }

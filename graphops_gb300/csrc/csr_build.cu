@@ -25,21 +25,22 @@ namespace gops {
 
 namespace {
 
-// Per out-row u: out-degree, source id of every entry, and (weighted) the
-// transition weight max(w,0) / sum_u max(w,0) in FP32 with the weighted-
-// dangling bit, in three passes that keep FP64 instructions (issued at a
-// small fraction of the FP32 rate on this GPU) to one add per entry, one
-// divide per row and one multiply and conversion per entry:
-//  out_row_sums      rows of at most kRowBig entries (nearly all: R-MAT rows
-//                    average ~16): an 8-lane group per row in a persistent
-//                    grid, the FP64 sum in a fixed order per group (the
-//                    shuffles name the group only: groups of a warp run
-//                    different numbers of rows); longer rows are listed in
-//                    big[1..big[0]] (list order varies, per-row results do not)
-//  out_row_sums_big  the listed rows (hubs, up to ~1e5 entries), a block per
-//                    row, a fixed-order block sum
-//  row_inverse       a thread per row: rowsum -> 1/rowsum (0 for an empty or
-//                    zero-weight row) and the dangling bits, a word per warp
+// Per out-row u: out-degree and the source id of every entry (the structure
+// pass, before the weights have arrived), then (weighted) the transition
+// weight max(w,0) / sum_u max(w,0) in FP32 with the weighted-dangling bit.
+// FP64 instructions issue at a small fraction of the FP32 rate on this GPU,
+// so the weight passes keep them to one add per entry, one divide per row and
+// one multiply and conversion per entry:
+//  out_rows          structure pass, rows of at most kRowBig entries (nearly
+//                    all: R-MAT rows average ~16): an 8-lane group per row in
+//                    a persistent grid; longer rows are listed in
+//                    big[1..big[0]] (list order varies, results do not)
+//  out_rows_big      structure pass, the listed rows (hubs), a block per row
+//  row_sums_tiles    the sums over the entry array in 256-entry warp tiles
+//                    (every lane sums 8 consecutive entries in order), pieces
+//                    of a row joined across lanes and tiles in a fixed order
+//  row_finish        a thread per row: the row's pieces -> sum -> 1/sum (0 for
+//                    an empty or zero-weight row) and the dangling bits
 //  edge_weights      a thread per entry: (float)(max(w,0) * inverse of its row),
 //                    stored beside the entry's source so that the in-CSR
 //                    scatter gathers both with one 8-byte load
@@ -53,69 +54,156 @@ __device__ __forceinline__ double clamp_weight(double w) {
   return neg_or_nan ? 0.0 : w;
 }
 
-// Two calls: the structure pass (w == nullptr: out-degree, sources, the list
-// of long rows), which needs no weights and runs while they are still being
-// copied, then the sums pass (w set: row sums only).
-__global__ void out_row_sums(int64_t n, const int64_t *__restrict__ rp, const double *__restrict__ w,
-                             uint32_t *__restrict__ src, float *__restrict__ deg_f,
-                             double *__restrict__ rowsum, uint32_t *__restrict__ big) {
+__global__ void out_rows(int64_t n, const int64_t *__restrict__ rp, uint32_t *__restrict__ src,
+                         float *__restrict__ deg_f, uint32_t *__restrict__ big) {
   const int lane = threadIdx.x & (kRowLanes - 1);
-  const unsigned gmask = ((1u << kRowLanes) - 1u) << ((threadIdx.x & 31) & ~(kRowLanes - 1));
   const int64_t groups = (int64_t)gridDim.x * (blockDim.x / kRowLanes);
   for (int64_t u = (int64_t)blockIdx.x * (blockDim.x / kRowLanes) + threadIdx.x / kRowLanes; u < n; u += groups) {
     const int64_t b = rp[u], e = rp[u + 1];
     if (e - b > kRowBig) {  // the whole group skips: same row
-      if (!w && lane == 0) big[1 + atomicAdd(&big[0], 1u)] = (uint32_t)u;
+      if (lane == 0) big[1 + atomicAdd(&big[0], 1u)] = (uint32_t)u;
       continue;
     }
-    if (!w) {
-      if (lane == 0) deg_f[u] = (float)(e - b);
-      for (int64_t i = b + lane; i < e; i += kRowLanes) src[i] = (uint32_t)u;
-    } else {
-      double s = 0.0;
-      for (int64_t i = b + lane; i < e; i += kRowLanes) s += clamp_weight(w[i]);
-#pragma unroll
-      for (int o = kRowLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, kRowLanes);
-      if (lane == 0) rowsum[u] = s;
-    }
+    if (lane == 0) deg_f[u] = (float)(e - b);
+    for (int64_t i = b + lane; i < e; i += kRowLanes) src[i] = (uint32_t)u;
   }
 }
 
-__global__ void __launch_bounds__(256) out_row_sums_big(const int64_t *__restrict__ rp,
-                                                         const double *__restrict__ w, uint32_t *__restrict__ src,
-                                                         float *__restrict__ deg_f, double *__restrict__ rowsum,
-                                                         const uint32_t *__restrict__ big) {
-  __shared__ double sh[256];
+__global__ void __launch_bounds__(256) out_rows_big(const int64_t *__restrict__ rp, uint32_t *__restrict__ src,
+                                                     float *__restrict__ deg_f, const uint32_t *__restrict__ big) {
   const uint32_t nbig = big[0];
-  for (uint32_t k = blockIdx.x; k < nbig; k += gridDim.x) {  // uniform per block
+  for (uint32_t k = blockIdx.x; k < nbig; k += gridDim.x) {
     const int64_t u = big[1 + k];
     const int64_t b = rp[u], e = rp[u + 1];
-    if (!w) {  // structure pass
-      if (threadIdx.x == 0) deg_f[u] = (float)(e - b);
-      for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) src[i] = (uint32_t)u;
-      continue;
-    }
-    double s = 0.0;
-    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) s += clamp_weight(w[i]);
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) rowsum[u] = sh[0];
-    __syncthreads();
+    if (threadIdx.x == 0) deg_f[u] = (float)(e - b);
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) src[i] = (uint32_t)u;
   }
+}
+
+// The sums pass.  Warp tile t holds entries [256 t, 256 t + 256), lane l the
+// 8 from 256 t + 8 l.  A lane adds its entries in order, row by row (src
+// gives each entry's row); a row begun and ended in the lane is written to
+// rowsum.  A row that crosses lanes is joined by a segmented scan over the
+// lanes (left to right): the lane where it ends adds the scan's carry from
+// the left to its own first piece.  A row that crosses the tile's ends
+// leaves its pieces for row_finish: tcarry[t] = the part in tile t of the
+// tile's last row, when that row continues past the tile (a tile inside one
+// row: the tile's sum), thead[t] = the part in tile t of the tile's first
+// row, when that row began before the tile and ends in it.  One FP64 add per
+// entry and a few per tile; the order is fixed by the tiling.
+constexpr int kSumItems = 8;
+constexpr int kSumTile = 32 * kSumItems;
+constexpr uint32_t kNoRow = 0xFFFFFFFFu;
+
+__global__ void __launch_bounds__(256) row_sums_tiles(int64_t m, const uint32_t *__restrict__ src,
+                                                       const double *__restrict__ w, int vec,
+                                                       double *__restrict__ rowsum, double *__restrict__ tcarry,
+                                                       double *__restrict__ thead) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t t = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int64_t T = t * kSumTile;
+  if (T >= m) return;  // the whole warp
+  const int64_t i0 = T + (int64_t)lane * kSumItems;
+  uint32_t r[kSumItems];
+  double x[kSumItems];
+  if (vec && i0 + kSumItems <= m) {  // 16-byte aligned: i0 is a multiple of 8
+    const uint4 a = __ldg(reinterpret_cast<const uint4 *>(src + i0));
+    const uint4 b = __ldg(reinterpret_cast<const uint4 *>(src + i0 + 4));
+    r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+    r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+#pragma unroll
+    for (int q = 0; q < kSumItems / 2; ++q) {
+      const double2 d = __ldg(reinterpret_cast<const double2 *>(w + i0) + q);
+      x[2 * q] = d.x;
+      x[2 * q + 1] = d.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kSumItems; ++k) {
+      const bool ok = i0 + k < m;
+      r[k] = ok ? __ldg(src + i0 + k) : kNoRow;
+      x[k] = ok ? __ldg(w + i0 + k) : 0.0;
+    }
+  }
+  // the rows of the entries on either side of the lane's run
+  uint32_t prev = __shfl_up_sync(full, r[kSumItems - 1], 1);
+  uint32_t next = __shfl_down_sync(full, r[0], 1);
+  if (lane == 0) prev = T > 0 ? __ldg(src + T - 1) : kNoRow;
+  if (lane == 31) next = T + kSumTile < m ? __ldg(src + T + kSumTile) : kNoRow;
+  const bool first_cont = r[0] == prev;  // the first entry continues a row from the left
+  double seg = 0.0, head = 0.0, tail = 0.0;
+  bool head_done = false;  // the first piece continues from the left and ends its row here
+  bool pass = false;       // the lane's last piece is its first and continues on both sides
+#pragma unroll
+  for (int k = 0; k < kSumItems; ++k) {
+    const double v = clamp_weight(x[k]);
+    const bool seg_first = k == 0 || r[k] != r[k - 1];
+    seg = seg_first ? v : seg + v;
+    const bool seg_end = k == kSumItems - 1 || r[k + 1] != r[k];
+    if (seg_end) {
+      const bool row_end = k < kSumItems - 1 || next != r[k];
+      // this piece is the lane's first (from entry 0) and continues from the left
+      bool from_left = first_cont;
+#pragma unroll
+      for (int j = 1; j <= k; ++j) from_left = from_left && r[j] == r[0];
+      if (row_end && !from_left) {
+        if (r[k] != kNoRow) rowsum[r[k]] = seg;
+      } else if (row_end) {
+        head = seg;
+        head_done = true;
+      } else {  // k is the lane's last entry: the piece continues to the right
+        tail = seg;
+        pass = from_left;
+      }
+    }
+  }
+  // segmented inclusive scan over the lanes: a lane passes the carry from its
+  // left on only when its one piece continues on both sides
+  double sc = tail;
+  bool fl = lane == 0 || !pass;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double so = __shfl_up_sync(full, sc, o);
+    const int fo = __shfl_up_sync(full, (int)fl, o);
+    if (lane >= o) {
+      if (!fl) sc = so + sc;
+      fl = fl || fo;
+    }
+  }
+  double carry = __shfl_up_sync(full, sc, 1);
+  if (lane == 0) carry = 0.0;
+  const bool tile_cont = __shfl_sync(full, (int)first_cont, 0) != 0;  // tile's first row began before it
+  const uint32_t tile_row = __shfl_sync(full, r[0], 0);
+  if (head_done) {
+    const double tot = carry + head;
+    if (tile_cont && r[0] == tile_row) thead[t] = tot;
+    else rowsum[r[0]] = tot;
+  }
+  if (lane == 31 && r[kSumItems - 1] != kNoRow && next == r[kSumItems - 1]) tcarry[t] = sc;
 }
 
 // Rows 32*j .. 32*j+31 are one warp's: dmask word j is written whole.
-__global__ void row_inverse(int64_t n, double *__restrict__ rowsum, uint32_t *__restrict__ dmask) {
+__global__ void row_finish(int64_t n, const int64_t *__restrict__ rp, const double *__restrict__ tcarry,
+                           const double *__restrict__ thead, double *__restrict__ rowsum,
+                           uint32_t *__restrict__ dmask) {
   const int64_t words = (n + 31) / 32;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < words * 32;
        u += (int64_t)gridDim.x * blockDim.x) {  // uniform per warp: words * 32 rounds up
     bool dang = false;
     if (u < n) {
-      const double s = rowsum[u];
+      const int64_t b = rp[u], e = rp[u + 1];
+      double s = 0.0;
+      if (e > b) {
+        const int64_t t0 = b / kSumTile, t1 = (e - 1) / kSumTile;
+        if (t0 == t1) {
+          s = rowsum[u];
+        } else {  // the tiles' pieces in order
+          s = tcarry[t0];
+          for (int64_t q = t0 + 1; q < t1; ++q) s += tcarry[q];
+          s += thead[t1];
+        }
+      }
       dang = !(s > 0.0);
       rowsum[u] = dang ? 0.0 : 1.0 / s;
     }
@@ -218,10 +306,30 @@ __global__ void pad_degrees(int64_t *deg, int64_t n, int align) {
     deg[i] = (deg[i] + align - 1) / align * align;
 }
 
-__global__ void fill_i32(int32_t *a, int64_t count, int32_t v) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
-       i += (int64_t)gridDim.x * blockDim.x)
-    a[i] = v;
+// Slots of the relabelled in-CSR that no edge fills: the padding of row i
+// (md - sorted_keys[i] edges in a run rounded up to kRowAlign slots) and the
+// kTailSlots slots past the last row, read by vector loads: source n (whose
+// gathered value is 0) and weight 0.
+constexpr int64_t kTailSlots = 64;
+
+__global__ void pad_slots(const uint32_t *sorted_keys, const unsigned *maxdeg, const int64_t *in_rp, int64_t n,
+                          int32_t *in_col, float *in_val) {
+  const unsigned md = *maxdeg;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n + kTailSlots;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b, e;
+    if (i < n) {
+      b = in_rp[i] + (int64_t)(md - sorted_keys[i]);
+      e = in_rp[i + 1];
+    } else {
+      b = in_rp[n] + (i - n);
+      e = b + 1;
+    }
+    for (int64_t j = b; j < e; ++j) {
+      in_col[j] = (int32_t)n;
+      if (in_val) in_val[j] = 0.0f;
+    }
+  }
 }
 
 // out[j] = number of relabelled rows with in-degree >= thr[j] (degrees are
@@ -375,7 +483,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   int32_t *inv_perm = nullptr;
   unsigned *maxdeg = nullptr;
   uint32_t *bigrows = nullptr;
-  double *rowsum = nullptr;
+  double *rowsum = nullptr, *tcarry = nullptr, *thead = nullptr;
   // weight passes queued on the copy stream (the main stream waits for them
   // before any buffer they use is freed)
   bool copy_side = false;
@@ -386,6 +494,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     free_async(nv2, s); free_async(dmask_old, s); free_async(src_val, s); free_async(deg_old, s);
     free_async(rp_old, s); free_async(new_deg, s); free_async(small, s); free_async(inv_perm, s);
     free_async(maxdeg, s); free_async(bigrows, s); free_async(rowsum, s);
+    free_async(tcarry, s); free_async(thead, s);
   };
 #define BUILD_TRY(expr)                                                                     \
   do {                                                                                      \
@@ -434,11 +543,24 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     const int64_t nbig_cap = std::min<int64_t>(n, m / (kRowBig + 1)) + 1;
     BUILD_TRY(dev_malloc_async((void **)&bigrows, sizeof(uint32_t) * nbig_cap, s));
     BUILD_TRY(cudaMemsetAsync(bigrows, 0, sizeof(uint32_t), s));
-    out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
-        n, d_out_rp, nullptr, src, deg_old, rowsum, bigrows);
-    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, nullptr, src, deg_old, rowsum, bigrows);
+    out_rows<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(n, d_out_rp, src, deg_old, bigrows);
+    out_rows_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, src, deg_old, bigrows);
     BUILD_TRY(cudaGetLastError());
   }
+  // the weight passes' per-tile pieces of rows that cross a tile's ends
+  const int64_t wtiles = ceil_div<int64_t>(m, kSumTile);
+  if (d_w && m > 0) {
+    BUILD_TRY(dev_malloc_async((void **)&tcarry, sizeof(double) * wtiles, s));
+    BUILD_TRY(dev_malloc_async((void **)&thead, sizeof(double) * wtiles, s));
+  }
+  auto weight_passes = [&](cudaStream_t st) {
+    if (m > 0) {
+      const int vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(d_w)) & 15) == 0;
+      row_sums_tiles<<<(unsigned)ceil_div<int64_t>(wtiles, 8), 256, 0, st>>>(m, src, d_w, vec, rowsum, tcarry, thead);
+    }
+    row_finish<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, st>>>(n, d_out_rp, tcarry, thead, rowsum, dmask_old);
+    if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, st>>>(m, d_w, src, rowsum, src_val);
+  };
   // The weight passes need the weights, the structure pass and nothing of
   // the relabelling: with the weights arriving on the copy stream they run
   // there as soon as both are done, beside the main stream's relabelling.
@@ -448,11 +570,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(cudaStreamWaitEvent(cs, ctx->build_ev[0], 0));
     BUILD_TRY(cudaStreamWaitEvent(cs, w_ready, 0));
     copy_side = true;
-    out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, cs>>>(
-        n, d_out_rp, d_w, src, deg_old, rowsum, bigrows);
-    out_row_sums_big<<<ctx->num_sms * 4, 256, 0, cs>>>(d_out_rp, d_w, src, deg_old, rowsum, bigrows);
-    row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, cs>>>(n, rowsum, dmask_old);
-    if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, cs>>>(m, d_w, src, rowsum, src_val);
+    weight_passes(cs);
     BUILD_TRY(cudaGetLastError());
     BUILD_TRY(cudaEventRecord(ctx->build_ev[1], cs));
   }
@@ -471,7 +589,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   unsigned md = 0;
   uint32_t *SK = nk, *SV = nv;
   if (n > 0) {
-    max_indeg<<<grid_for(n, 256), 256, 0, s>>>(rp_old, n, maxdeg);
+    max_indeg<<<blocks_for(n, 256, ctx->num_sms * 4), 256, 0, s>>>(rp_old, n, maxdeg);
     node_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(rp_old, n, maxdeg, nk, nv);
     BUILD_TRY(cudaGetLastError());
     BUILD_TRY(cudaMemcpyAsync(&md, maxdeg, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
@@ -494,29 +612,19 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
   BUILD_TRY(cudaMemcpyAsync(&m_stored, g->in_rp + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   BUILD_TRY(cudaStreamSynchronize(s));
   g->m_stored = m_stored;
-  const size_t ms = (size_t)std::max<int64_t>(m_stored, 1) + 64;  // +64: vector loads past the end
+  const size_t ms = (size_t)m_stored + kTailSlots;  // vector loads past the end
   BUILD_TRY(dev_malloc_async(&g->in_col, sizeof(int32_t) * ms, s));
-  if (kRowAlign > 1) {
-    fill_i32<<<grid_for((int64_t)ms, 256), 256, 0, s>>>(g->in_col, (int64_t)ms, (int32_t)n);
-    BUILD_TRY(cudaGetLastError());
-  } else {
-    BUILD_TRY(cudaMemsetAsync(g->in_col, 0, sizeof(int32_t) * ms, s));
-  }
-  if (g->weighted) {
-    BUILD_TRY(dev_malloc_async(&g->in_val, sizeof(float) * ms, s));
-    BUILD_TRY(cudaMemsetAsync(g->in_val, 0, sizeof(float) * ms, s));
-  }
+  if (g->weighted) BUILD_TRY(dev_malloc_async(&g->in_val, sizeof(float) * ms, s));
+  // the slots that no edge fills (the scatter writes the others)
+  pad_slots<<<grid_for(n + kTailSlots, 256), 256, 0, s>>>(SK, maxdeg, g->in_rp, n, g->in_col, g->in_val);
+  BUILD_TRY(cudaGetLastError());
   // the weights: everything above ran while they were being copied
   if (copy_side) {
     BUILD_TRY(cudaStreamWaitEvent(s, ctx->build_ev[1], 0));
   } else {
     if (w_ready) BUILD_TRY(cudaStreamWaitEvent(s, w_ready, 0));
     if (d_w && n > 0) {
-      out_row_sums<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(
-          n, d_out_rp, d_w, src, deg_old, rowsum, bigrows);
-      out_row_sums_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, d_w, src, deg_old, rowsum, bigrows);
-      row_inverse<<<blocks_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(n, rowsum, dmask_old);
-      if (m > 0) edge_weights<<<blocks_for(m, 256, ctx->num_sms * 8), 256, 0, s>>>(m, d_w, src, rowsum, src_val);
+      weight_passes(s);
     }
   }
   if (d_w && n > 0) {

@@ -142,18 +142,28 @@ __global__ void __launch_bounds__(kSortThreads, 3) radix_downsweep(const uint32_
   const int64_t tbase = (int64_t)blockIdx.x * kSortTile;
   const int64_t wbase = tbase + (int64_t)w * kPerWarp;
   const unsigned lt_mask = (1u << lane) - 1u;
-  uint32_t k[kChunks];
-  unsigned pk[kChunks];  // each item's peers (same digit) in its 32-item chunk
-  // (a)
+  uint32_t k[kChunks], v[kChunks];
+  // (a) all of the warp's key loads go out before any ranking, and the value
+  // loads right after it, so that their latencies overlap (the ranking's
+  // warp barriers would otherwise keep one chunk's load in flight at a time)
+#pragma unroll
+  for (int c = 0; c < kChunks; ++c) {
+    const int64_t idx = wbase + c * kWarp + lane;
+    k[c] = idx < n ? __ldg(keys + idx) : 0u;
+  }
 #pragma unroll
   for (int c = 0; c < kChunks; ++c) {
     const int64_t idx = wbase + c * kWarp + lane;
     const bool valid = idx < n;
-    k[c] = valid ? keys[idx] : 0u;
     const unsigned dig = valid ? ((k[c] >> shift) & 0xFF) : 0x100u;
-    pk[c] = __match_any_sync(0xffffffffu, dig);
-    if (valid && lane == __ffs(pk[c]) - 1) wcnt[w][dig] += __popc(pk[c]);
+    const unsigned peers = __match_any_sync(0xffffffffu, dig);  // same digit in the 32-item chunk
+    if (valid && lane == __ffs(peers) - 1) wcnt[w][dig] += __popc(peers);
     __syncwarp();
+  }
+#pragma unroll
+  for (int c = 0; c < kChunks; ++c) {
+    const int64_t idx = wbase + c * kWarp + lane;
+    v[c] = vals ? (idx < n ? __ldg(vals + idx) : 0u) : (uint32_t)idx;  // no vals: the input position
   }
   __syncthreads();
   // (b) thread d owns digit d (kSortThreads == kRadix)
@@ -181,18 +191,18 @@ __global__ void __launch_bounds__(kSortThreads, 3) radix_downsweep(const uint32_
     gdelta[d] = offs[(int64_t)d * tiles + blockIdx.x] - loc;
   }
   __syncthreads();
-  // (c)
+  // (c) the peers are found again (cheaper than keeping 16 masks live)
 #pragma unroll
   for (int c = 0; c < kChunks; ++c) {
     const int64_t idx = wbase + c * kWarp + lane;
     const bool valid = idx < n;
     const unsigned dig = valid ? ((k[c] >> shift) & 0xFF) : 0x100u;
-    const unsigned peers = pk[c];
+    const unsigned peers = __match_any_sync(0xffffffffu, dig);
     const uint32_t pos = valid ? wcnt[w][dig] + __popc(peers & lt_mask) : 0u;
     __syncwarp();
     if (valid) {
       skeys[pos] = k[c];
-      svals[pos] = vals ? vals[idx] : (uint32_t)idx;  // no vals: the input position
+      svals[pos] = v[c];
       if (lane == __ffs(peers) - 1) wcnt[w][dig] += __popc(peers);
     }
     __syncwarp();

@@ -127,10 +127,11 @@ def test_large_weighted_upload_matches_the_edge_list_build():
     """gops_graph_upload (weights copied on the second stream while the edge
     sort runs) against gops_graph_from_edges (the same out-adjacency built
     on the device from the raw edge list, weights already there), over 4 M
-    edges: rows of 1-7 entries, 8-256 entries (an 8-lane group each in the
-    row-sum pass), 257-3,000 entries and a hub row with more than half of the
-    edges (a block each), rows whose weights are all zero (dangling by
-    weight), negative and NaN weights, and rows without edges.  The two
+    edges: rows of 1-7 entries (within one lane's 8 entries of the row-sum
+    pass, or across two), 8-256 entries (across lanes and 256-entry tiles),
+    257-3,000 entries and a hub row with more than half of the edges (across
+    many tiles), rows whose weights are all zero (dangling by weight),
+    negative and NaN weights, and rows without edges.  The two
     builds give bit-identical weighted solves, and match the oracle's
     restatement."""
     from oracle import port

@@ -32,8 +32,8 @@ namespace {
 // so the weight passes keep them to one add per entry, one divide per row and
 // one multiply and conversion per entry:
 //  out_rows          structure pass, rows of at most kRowBig entries (nearly
-//                    all: R-MAT rows average ~16): an 8-lane group per row in
-//                    a persistent grid; longer rows are listed in
+//                    all: R-MAT rows average ~16): an 8-lane group per row;
+//                    longer rows are listed in
 //                    big[1..big[0]] (list order varies, results do not)
 //  out_rows_big      structure pass, the listed rows (hubs), a block per row
 //  row_sums_tiles    the sums over the entry array in 256-entry warp tiles
@@ -222,13 +222,20 @@ __global__ void edge_weights(int64_t m, const double *__restrict__ w, const uint
   }
 }
 
-// rp[v] = first position i of the sorted destination keys K with K[i] >= v.
+// rp[v] = first position i of the sorted destination keys K with K[i] >= v
+// (v = 0..n): a binary search per node, so that no thread writes a long run
+// of rows without in-edges (the searches of neighbouring nodes share their
+// first probes in cache).
 __global__ void rp_from_sorted(const uint32_t *K, int64_t m, int64_t n, int64_t *rp) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= m;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t prev = i == 0 ? -1 : (int64_t)K[i - 1];
-    const int64_t cur = i == m ? n : (int64_t)K[i];
-    for (int64_t v = prev + 1; v <= cur; ++v) rp[v] = i;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v <= n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = m;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)__ldg(&K[mid]) < v) lo = mid + 1;
+      else hi = mid;
+    }
+    rp[v] = lo;
   }
 }
 
@@ -543,7 +550,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     const int64_t nbig_cap = std::min<int64_t>(n, m / (kRowBig + 1)) + 1;
     BUILD_TRY(dev_malloc_async((void **)&bigrows, sizeof(uint32_t) * nbig_cap, s));
     BUILD_TRY(cudaMemsetAsync(bigrows, 0, sizeof(uint32_t), s));
-    out_rows<<<blocks_for(n, 256 / kRowLanes, ctx->num_sms * 8), 256, 0, s>>>(n, d_out_rp, src, deg_old, bigrows);
+    out_rows<<<grid_for(n, 256 / kRowLanes), 256, 0, s>>>(n, d_out_rp, src, deg_old, bigrows);
     out_rows_big<<<ctx->num_sms * 4, 256, 0, s>>>(d_out_rp, src, deg_old, bigrows);
     BUILD_TRY(cudaGetLastError());
   }
@@ -575,7 +582,7 @@ Status graph_build_from_out_csr_device(Ctx *ctx, Graph *g, const int64_t *d_out_
     BUILD_TRY(cudaEventRecord(ctx->build_ev[1], cs));
   }
   BUILD_TRY(dev_malloc_async((void **)&rp_old, sizeof(int64_t) * (n + 1), s));
-  rp_from_sorted<<<grid_for(m + 1, 256), 256, 0, s>>>(K, m, n, rp_old);
+  rp_from_sorted<<<grid_for(n + 1, 256), 256, 0, s>>>(K, m, n, rp_old);
   BUILD_TRY(cudaGetLastError());
   // K2: relabel by in-degree, descending (stable: ties keep id order)
   BUILD_TRY(dev_malloc_async((void **)&maxdeg, sizeof(unsigned), s));
@@ -790,7 +797,7 @@ Status edges_to_out_csr_device(Ctx *ctx, int64_t n, int64_t m, const int32_t *d_
   EDGE_ST(radix_sort_index_u32(kin, k1, v1, k2, v2, m, bits, &alt, s));
   const uint32_t *rows = alt ? k2 : k1;
   const uint32_t *pos_rev = alt ? v2 : v1;
-  rp_from_sorted<<<grid_for(m + 1, 256), 256, 0, s>>>(rows, m, n, *d_rp);
+  rp_from_sorted<<<grid_for(n + 1, 256), 256, 0, s>>>(rows, m, n, *d_rp);
   EDGE_TRY(cudaGetLastError());
   if (d_w) {
     EDGE_TRY(dev_malloc_async((void **)&wraw, sizeof(double) * mm, s));

@@ -107,18 +107,39 @@ constexpr int kSortTile = kSortWarps * kPerWarp;
 constexpr int kRadix = 256;
 static_assert(kSortThreads == kRadix, "the downsweep gives each thread one digit");
 
+// Per tile: the count of every digit, in per-warp counters (a skewed digit's
+// additions spread over eight addresses), from 16-byte loads of a full tile.
 __global__ void radix_upsweep(const uint32_t *keys, int64_t n, int shift, uint32_t *hist,
-                              int64_t tiles) {
-  __shared__ uint32_t cnt[kRadix];
-  for (int i = threadIdx.x; i < kRadix; i += kSortThreads) cnt[i] = 0;
+                              int64_t tiles, int vec) {
+  __shared__ uint32_t wc[kSortWarps][kRadix];
+  for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) (&wc[0][0])[i] = 0;
   __syncthreads();
+  const int w = threadIdx.x >> 5;
   const int64_t base = (int64_t)blockIdx.x * kSortTile;
-  for (int i = threadIdx.x; i < kSortTile; i += kSortThreads) {
-    int64_t idx = base + i;
-    if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & 0xFF], 1u);
+  if (vec && base + kSortTile <= n) {
+    constexpr int kQuads = kSortTile / (4 * kSortThreads);
+    uint4 q[kQuads];
+#pragma unroll
+    for (int j = 0; j < kQuads; ++j) q[j] = __ldg(reinterpret_cast<const uint4 *>(keys + base) + threadIdx.x + j * kSortThreads);
+#pragma unroll
+    for (int j = 0; j < kQuads; ++j) {
+      atomicAdd(&wc[w][(q[j].x >> shift) & 0xFF], 1u);
+      atomicAdd(&wc[w][(q[j].y >> shift) & 0xFF], 1u);
+      atomicAdd(&wc[w][(q[j].z >> shift) & 0xFF], 1u);
+      atomicAdd(&wc[w][(q[j].w >> shift) & 0xFF], 1u);
+    }
+  } else {
+    for (int i = threadIdx.x; i < kSortTile; i += kSortThreads) {
+      const int64_t idx = base + i;
+      if (idx < n) atomicAdd(&wc[w][(keys[idx] >> shift) & 0xFF], 1u);
+    }
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < kRadix; d += kSortThreads) hist[(int64_t)d * tiles + blockIdx.x] = cnt[d];
+  const int d = threadIdx.x;  // kSortThreads == kRadix
+  uint32_t t = 0;
+#pragma unroll
+  for (int ww = 0; ww < kSortWarps; ++ww) t += wc[ww][d];
+  hist[(int64_t)d * tiles + blockIdx.x] = t;
 }
 
 // Per tile: (a) warp-private digit counts (the tile's keys stay in
@@ -259,7 +280,8 @@ Status radix_sort_impl(const uint32_t *keys_in, const uint32_t *vals_in, uint32_
   const uint32_t *k_in = keys_in, *v_in = vals_in;
   Status st;
   for (int shift = 0; shift < key_bits; shift += 8) {
-    radix_upsweep<<<(unsigned)tiles, kSortThreads, 0, s>>>(k_in, n, shift, hist, tiles);
+    const int vec = (reinterpret_cast<uintptr_t>(k_in) & 15) == 0;
+    radix_upsweep<<<(unsigned)tiles, kSortThreads, 0, s>>>(k_in, n, shift, hist, tiles, vec);
     st = exclusive_scan_u32(hist, hist, tiles * kRadix, s);
     if (st.code != GOPS_OK) break;
     radix_downsweep<<<(unsigned)tiles, kSortThreads, 0, s>>>(k_in, v_in, bk[cur ^ 1], bv[cur ^ 1], n, shift,

@@ -11,6 +11,8 @@ cases:
              iterate_kernel (double-float and FP32 steps), init / finalize
   upload     the out-CSR upload and device build of that graph (radix sort,
              scatter_edges, the per-row weight passes)
+  upload22   the same for an R-MAT scale 22 graph (4 M nodes, ~65 M edges),
+             uploaded from pinned host arrays three times
   batched    batched PPR on R-MAT scale 20, one wave of 128 seed sets (the
              bench's k-tile): spmm_mixed and spmm_f32
   centrality Katz, eigenvector centrality and HITS on R-MAT scale 21
@@ -49,6 +51,20 @@ def case_upload():
     w = g.weight.astype(np.float64)
     for _ in range(3):
         _native.DeviceGraph.from_csr(g.row_ptr, g.col, w).close()
+
+
+def case_upload22():
+    """An R-MAT 22 graph with FP64 weights (the bench's weighted PageRank
+    sizes) uploaded from pinned host arrays three times."""
+    import torch
+    from . import _native
+    g = _rmat(22, weighted=True, seed=22)
+    rp = torch.from_numpy(g.row_ptr).pin_memory().numpy()
+    col = torch.from_numpy(g.col).pin_memory().numpy()
+    w = torch.from_numpy(g.weight.astype(np.float64)).pin_memory().numpy()
+    for _ in range(3):
+        _native.DeviceGraph.from_csr(rp, col, w).close()
+        torch.cuda.synchronize()
 
 
 def case_batched():
@@ -101,7 +117,7 @@ def case_warm():
         model.loss_grad(0.85, sp, si, t)
 
 
-CASES = {"pagerank": case_pagerank, "upload": case_upload, "batched": case_batched,
+CASES = {"pagerank": case_pagerank, "upload": case_upload, "upload22": case_upload22, "batched": case_batched,
          "centrality": case_centrality, "topk": case_topk, "warm": case_warm}
 
 

@@ -198,6 +198,17 @@ def default_context() -> Context:
     return c
 
 
+def score_buffer(out, nsets: int, n: int):
+    """The batched calls' score destination: out=True a new array, False
+    none, or the caller's own array (checked: float32, C-contiguous,
+    shape (nsets, n))."""
+    if isinstance(out, np.ndarray):
+        if out.dtype != np.float32 or out.shape != (nsets, n) or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float32 array of shape (nsets, n)")
+        return out
+    return np.empty((nsets, n), dtype=np.float32) if out else None
+
+
 class DeviceGraph:
     """A graph resident on the device (a gops_graph)."""
 
@@ -276,12 +287,15 @@ class DeviceGraph:
 
     def ppr_batch(self, cfg, seed_ptr, seed_idx, x0=None, out=True):
         """Batched PPR over seed sets (CSR: seed_ptr[nsets+1], seed_idx).
-        Returns (scores float32 [nsets, n] or None, runs as a structured array)."""
+        out: True (a new array), False (no scores) or the caller's C-contiguous
+        float32 array of shape (nsets, n), e.g. a page-locked one, which the
+        library fills by DMA without staging.
+        Returns (scores float32 [nsets, n] or None, iterations, diff_l1, converged)."""
         sp = np.ascontiguousarray(seed_ptr, dtype=np.int64)
         si = np.ascontiguousarray(seed_idx, dtype=np.int32)
         ns = int(sp.shape[0]) - 1
         c = Config(float(cfg.damping), int(cfg.max_iterations), float(cfg.tolerance))
-        scores = np.empty((ns, self.n), dtype=np.float32) if out else None
+        scores = score_buffer(out, ns, self.n)
         xx = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float32)
         if xx is not None and xx.shape != (ns, self.n):
             raise ValueError("x0 must have shape (nsets, n)")

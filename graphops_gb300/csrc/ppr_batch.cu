@@ -1645,7 +1645,23 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
   // host threads scatter its columns to the sets' rows while the GPU runs
   // the next wave (two buffers; a buffer's scatter is joined before reuse)
   const size_t block_bytes = sizeof(float) * (size_t)KT * (size_t)n;
-  const bool staged = scores && !scores_on_device && block_bytes <= (size_t(1) << 31);
+  // a page-locked host destination takes every set's row by DMA straight
+  // from the wave's block, on the copy stream (no staging, no host copy)
+  bool direct = false;
+  if (scores && !scores_on_device) {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, scores) == cudaSuccess) direct = pa.type == cudaMemoryTypeHost;
+    else cudaGetLastError();  // not a pointer CUDA knows: pageable
+  }
+  // copies still in flight into the caller's array end before any return
+  struct CopyGuard {
+    cudaStream_t s;
+    bool on;
+    ~CopyGuard() {
+      if (on) cudaStreamSynchronize(s);
+    }
+  } copy_guard{ctx->copy_stream, direct};
+  const bool staged = scores && !scores_on_device && !direct && block_bytes <= (size_t(1) << 31);
   // the context's pinned staging, grown when a wave's block does not fit
   if (staged && ctx->hstage_bytes < block_bytes) {
     for (auto &h : ctx->hstage)
@@ -1658,7 +1674,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     GOPS_CUDA_TRY(cudaMallocHost(&ctx->hstage[1], block_bytes));
     ctx->hstage_bytes = block_bytes;
   }
-  if (staged && !ctx->sev[0]) {
+  if ((staged || direct) && !ctx->sev[0]) {
     GOPS_CUDA_TRY(cudaEventCreateWithFlags(&ctx->sev[0], cudaEventDisableTiming));
     GOPS_CUDA_TRY(cudaEventCreateWithFlags(&ctx->sev[1], cudaEventDisableTiming));
   }
@@ -1901,13 +1917,24 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
     // ---- results of the wave
     if (scores) {
       float *outw = scores_on_device ? scores : b->out;
-      // the previous wave's pinned copy (on the copy stream) has read b->out
-      if (staged && pend_copy_q >= 0) GOPS_CUDA_TRY(cudaStreamWaitEvent(st, ctx->sev[pend_copy_q], 0));
+      // the previous wave's copies (on the copy stream) have read b->out
+      if ((staged || direct) && pend_copy_q >= 0) GOPS_CUDA_TRY(cudaStreamWaitEvent(st, ctx->sev[pend_copy_q], 0));
       batch_finalize_t<<<blocks_for(ceil_div<int64_t>(n, kTile) * (KT / kTile), kBWarps, ctx->num_sms * 8), kBThreads,
                          0, st>>>(p, outw, b->d_inv_perm);
       GOPS_CUDA_TRY(cudaGetLastError());
       ++launches;
-      if (staged) {
+      if (direct) {
+        // one copy per set into the caller's page-locked array, on the copy
+        // stream, overlapping the next wave's steps
+        GOPS_CUDA_TRY(cudaEventRecord(ctx->copy_ev[0], st));
+        GOPS_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[0], 0));
+        for (int c = 0; c < ncols; ++c)
+          GOPS_CUDA_TRY(cudaMemcpyAsync(scores + order[set0 + c] * n, b->out + (size_t)c * n, sizeof(float) * (size_t)n,
+                                        cudaMemcpyDeviceToHost, ctx->copy_stream));
+        GOPS_CUDA_TRY(cudaEventRecord(ctx->sev[0], ctx->copy_stream));
+        pend_copy_q = 0;
+        ctx->stats.d2h_bytes += sizeof(float) * (size_t)ncols * n;
+      } else if (staged) {
         // the copy to the pinned buffer runs on the copy stream, overlapping
         // the next wave's steps
         const int q = (int)((set0 / KT) & 1);
@@ -1933,6 +1960,7 @@ Status ppr_batch(Ctx *ctx, Graph *g, const gops_config *cfg, int64_t nsets, cons
                                   cudaMemcpyDeviceToDevice, st));
   }
   GOPS_TRY(start_scatter());  // the last wave's block
+  if (direct && pend_copy_q >= 0) GOPS_CUDA_TRY(cudaStreamWaitEvent(st, ctx->sev[0], 0));
   std::vector<ColState> cols_res((size_t)nwaves * KT);
   GOPS_CUDA_TRY(cudaMemcpyAsync(cols_res.data(), cols_all, sizeof(ColState) * cols_res.size(), cudaMemcpyDeviceToHost,
                                 st));

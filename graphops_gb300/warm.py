@@ -28,7 +28,7 @@ from typing import Optional
 import numpy as np
 
 from . import _native
-from ._native import Config, Run, WarmConfig, WarmStats, ptr
+from ._native import Config, Run, WarmConfig, WarmStats, ptr, score_buffer
 
 PARAMS, COUPLING, CLUSTERS, FEATURES, CODE, WEIGHT = range(6)
 
@@ -233,10 +233,12 @@ class WarmStart:
                                                       ptr(si), ctypes.c_void_p(x0_device_ptr), ptr(r1)))
         return r1[:ns]
 
-    def ppr_batch(self, cfg, seed_ptr, seed_idx, scores: bool = True) -> LearnedRun:
+    def ppr_batch(self, cfg, seed_ptr, seed_idx, scores=True) -> LearnedRun:
+        """scores: True (a new array), False (none) or the caller's float32
+        (nsets, n) array, as DeviceGraph.ppr_batch's out."""
         sp, si, ns = _sets(seed_ptr, seed_idx)
         c = _cfg(cfg)
-        out = np.empty((ns, self.n), dtype=np.float32) if scores else None
+        out = score_buffer(scores, ns, self.n)
         runs = (Run * max(ns, 1))()
         rej = np.zeros(max(ns, 1), dtype=np.int32)
         self.ctx.check(self.ctx._l.gops_ppr_batch_learned(self.ctx.handle, self.graph.handle, self.handle,

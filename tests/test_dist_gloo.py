@@ -95,7 +95,11 @@ class _FakeDeviceGraph:
         import numpy as np
         ns = len(sp) - 1
         _FakeDeviceGraph.seen.append(tuple(int(x) for x in si[:64]))
-        s = np.zeros((ns, self.n), np.float32) if out else None
+        if isinstance(out, np.ndarray):  # the caller's array
+            out[:] = 0.0
+            s = out
+        else:
+            s = np.zeros((ns, self.n), np.float32) if out else None
         return s, np.full(ns, 11, np.int64), np.zeros(ns), np.ones(ns, bool)
 
     def batch_tile(self):
@@ -109,6 +113,10 @@ def _batch_worker(rank, port, results):
     import bench
     from graphops_gb300 import _native
     _native.DeviceGraph = _FakeDeviceGraph
+    # page-locked host buffers need a GPU: plain arrays stand in for them
+    import numpy as np
+    bench.pinned_copy = np.ascontiguousarray
+    bench.pinned_empty = lambda shape: np.empty(shape, np.float32)
     r, ws = bench.dist_init(SimpleNamespace(impl="reference"))
     a = SimpleNamespace(impl="gb300", batch_scale=10, batch_sets=64, no_cpu=True)
     out = bench.run_batch(a, _FakeCtx(r), r, ws)

@@ -221,3 +221,26 @@ def test_rows_without_in_edges_skipped_bit_for_bit():
     assert np.array_equal(c.iterations, d.iterations[:40])
     # another start: each result within d/(1-d) tol of the fixed point, like the oracle's
     assert np.abs(c.scores.astype(np.float64) - ref).sum(axis=1).max() <= 1e-6
+
+
+def test_caller_score_arrays():
+    """out = the caller's array: a page-locked one is filled by DMA straight
+    from each wave's block (one copy per set, on the copy stream), a pageable
+    one through the pinned staging; both hold the bits of a new array, over
+    three waves whose sets run in size order."""
+    torch = pytest.importorskip("torch")
+    g = gen.rmat(12, 16, seed=4)
+    sp, si = gen.seed_sets(g, 70, 1, 64, seed=2)
+    dg = go.DeviceGraph.from_csr(g.row_ptr, g.col)
+    conf = go.PageRankConfig(0.85, 1000, 1e-7)
+    new = dg.ppr_batch(conf, sp, si)[0]
+    pinned = torch.empty((70, g.n), dtype=torch.float32).pin_memory().numpy()
+    pinned.fill(np.nan)
+    got = dg.ppr_batch(conf, sp, si, out=pinned)[0]
+    assert got is pinned and np.array_equal(pinned, new)
+    pageable = np.full((70, g.n), np.nan, dtype=np.float32)
+    assert np.array_equal(dg.ppr_batch(conf, sp, si, out=pageable)[0], new)
+    with pytest.raises(ValueError, match="float32 array of shape"):
+        dg.ppr_batch(conf, sp, si, out=np.empty((70, g.n), np.float64))
+    with pytest.raises(ValueError, match="float32 array of shape"):
+        dg.ppr_batch(conf, sp, si, out=np.empty((69, g.n), np.float32))

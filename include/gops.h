@@ -192,7 +192,10 @@ int gops_personalized_pagerank_run(gops_ctx *ctx, const gops_graph *g, const gop
  * x0 (optional, nsets*n floats, set-major, original node order) replaces the
  * start vector p by a caller-supplied one (a warm start, such as the learned
  * one); the iteration and its stopping rule are unchanged.
- * scores (optional): nsets*n floats, set-major, original node order (FP32).
+ * scores (optional): nsets*n floats, set-major, original node order (FP32);
+ * page-locked host memory (cudaHostAlloc, cudaHostRegister) is written by
+ * DMA from each wave's block while the next wave runs, other host memory
+ * through the context's pinned staging buffers and a host copy.
  * runs (optional): nsets run records. */
 int gops_ppr_batch(gops_ctx *ctx, const gops_graph *g, const gops_config *cfg, int64_t nsets,
                    const int64_t *seed_ptr, const int32_t *seed_idx, const float *x0,

@@ -203,3 +203,18 @@ def test_ctypes_signatures_match_the_header():
         else:
             assert res is SCALARS[ret.replace("const ", "").strip()] or \
                 ctypes.sizeof(res) == ctypes.sizeof(SCALARS[ret.strip()]), name
+
+
+def test_score_buffer_arguments():
+    """The batched calls' destination: True a new (nsets, n) float32 array,
+    False none, a caller's array used as it is when it is C-contiguous float32
+    of that shape, and anything else refused before the library is called."""
+    a = _native.score_buffer(True, 3, 5)
+    assert a.shape == (3, 5) and a.dtype == np.float32
+    assert _native.score_buffer(False, 3, 5) is None
+    mine = np.empty((3, 5), np.float32)
+    assert _native.score_buffer(mine, 3, 5) is mine
+    for bad in (np.empty((3, 5), np.float64), np.empty((2, 5), np.float32),
+                np.empty((5, 3), np.float32).T):
+        with pytest.raises(ValueError, match="float32 array of shape"):
+            _native.score_buffer(bad, 3, 5)

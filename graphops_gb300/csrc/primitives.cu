@@ -164,9 +164,10 @@ __global__ void __launch_bounds__(kSortThreads, 3) radix_downsweep(const uint32_
   const int64_t wbase = tbase + (int64_t)w * kPerWarp;
   const unsigned lt_mask = (1u << lane) - 1u;
   uint32_t k[kChunks], v[kChunks];
-  // (a) all of the warp's key loads go out before any ranking, and the value
-  // loads right after it, so that their latencies overlap (the ranking's
-  // warp barriers would otherwise keep one chunk's load in flight at a time)
+  // (a) all of the warp's key loads go out before the digit counting, and the
+  // value loads after it (in flight during (b)), so that their latencies
+  // overlap: the counting's warp barriers would otherwise keep one chunk's
+  // load in flight at a time
 #pragma unroll
   for (int c = 0; c < kChunks; ++c) {
     const int64_t idx = wbase + c * kWarp + lane;
